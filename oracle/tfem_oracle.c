@@ -1,0 +1,923 @@
+/*
+ * CPU oracle for the implicit corotational tetrahedral FEM step.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the checker that the CUDA path is
+ * compared against; only tests/, __graft_entry__.smoke() and the CPU-baseline
+ * leg of bench.py may load it. The product (sofa_gb300/) never calls it.
+ *
+ * It restates, in plain C and in the reference's operation order, the CPU
+ * path of SOFA v26.06 (file:line citations are paths inside that project):
+ *
+ *   TetrahedronFEMForceField   Sofa/Component/SolidMechanics/FEM/Elastic/src/
+ *                              sofa/component/solidmechanics/fem/elastic/
+ *                              TetrahedronFEMForceField.inl (cited as TFEM.inl)
+ *   polar decomposition        Sofa/framework/Helper/src/sofa/helper/decompose.inl
+ *   3x3 norms                  Sofa/framework/Type/src/sofa/type/Mat.h:1056-1080
+ *   UniformMass                Sofa/Component/Mass/src/sofa/component/mass/UniformMass.inl
+ *   DiagonalMass (tet lumping) Sofa/Component/Mass/src/sofa/component/mass/DiagonalMass.inl
+ *   FixedProjectiveConstraint  Sofa/Component/Constraint/Projective/src/sofa/component/
+ *                              constraint/projective/FixedProjectiveConstraint.inl
+ *   CGLinearSolver             Sofa/Component/LinearSolver/Iterative/src/sofa/component/
+ *                              linearsolver/iterative/CGLinearSolver.inl (+ .cpp)
+ *   EulerImplicitSolver        Sofa/Component/ODESolver/Backward/src/sofa/component/
+ *                              odesolver/backward/EulerImplicitSolver.cpp
+ *   MechanicalObject vOps      Sofa/Component/StateContainer/src/sofa/component/
+ *                              statecontainer/MechanicalObject.inl
+ *
+ * It is compiled with -ffp-contract=off so that every a*b+c rounds twice, as
+ * the reference does on a target without fused multiply-add; the results are
+ * then identical on x86-64 and aarch64.
+ *
+ * The multi-threaded mode (orc_set_threads > 1) follows the MultiThreading
+ * plugin's ParallelTetrahedronFEMForceField (thread-local force buffers merged
+ * after the element loop, applications/plugins/MultiThreading/src/
+ * MultiThreading/component/solidmechanics/fem/elastic/
+ * ParallelTetrahedronFEMForceField.inl:53-124); its sums are reordered, so it
+ * is used for timing, not as the parity reference.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_SMALL 0
+#define ORC_LARGE 1
+#define ORC_POLAR 2
+
+/* ------------------------------------------------------------------------- */
+/* small fixed-size helpers                                                   */
+/* ------------------------------------------------------------------------- */
+
+/* Vec::norm2 then sqrt, Vec::normalizeWithNorm with the default epsilon
+ * threshold (Sofa/framework/Type/src/sofa/type/Vec.h:496-562). */
+static void vec_normalize(double v[3])
+{
+    double n2 = v[0] * v[0];
+    n2 += v[1] * v[1];
+    n2 += v[2] * v[2];
+    double n = sqrt(n2);
+    if (n > 2.220446049250313e-16) {
+        v[0] /= n;
+        v[1] /= n;
+        v[2] /= n;
+    }
+}
+
+/* type::cross (Vec.h:775-780) */
+static void vec_cross(const double a[3], const double b[3], double r[3])
+{
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* Vec dot (Vec::operator*(Vec), Vec.h:406-412): left to right. */
+static double vec_dot(const double a[3], const double b[3])
+{
+    double r = a[0] * b[0];
+    r += a[1] * b[1];
+    r += a[2] * b[2];
+    return r;
+}
+
+/* Mat * Vec (Mat.h:577-587): r(i) = m(i,0)v0; r(i) += m(i,1)v1; ... */
+static void mat_vec(const double m[9], const double v[3], double r[3])
+{
+    for (int i = 0; i < 3; ++i) {
+        double s = m[3 * i + 0] * v[0];
+        s += m[3 * i + 1] * v[1];
+        s += m[3 * i + 2] * v[2];
+        r[i] = s;
+    }
+}
+
+static void mat_transpose(const double m[9], double t[9])
+{
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) t[3 * i + j] = m[3 * j + i];
+}
+
+/* oneNorm / infNorm of a 3x3 (Mat.h:1056-1080). */
+static double mat_one_norm(const double a[9])
+{
+    double norm = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        double s = fabs(a[0 * 3 + i]) + fabs(a[1 * 3 + i]) + fabs(a[2 * 3 + i]);
+        if (s > norm) norm = s;
+    }
+    return norm;
+}
+
+static double mat_inf_norm(const double a[9])
+{
+    double norm = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        double s = fabs(a[i * 3 + 0]) + fabs(a[i * 3 + 1]) + fabs(a[i * 3 + 2]);
+        if (s > norm) norm = s;
+    }
+    return norm;
+}
+
+/* Higham's scaled Newton iteration for the orthogonal polar factor, as in
+ * Decompose<double>::polarDecomposition(M, Q) (decompose.inl:672-723) with
+ * the FP64 tolerance 1e-8 (decompose.h:384-387). M and Q are row-major 3x3.
+ * Returns the determinant of the last iterate. */
+double orc_polar(const double M[9], double Q[9])
+{
+    double Mk[9], Ek[9], Madj[9];
+    double det = 0.0, M_one, M_inf, E_one;
+    const double tol = 1e-8;
+    mat_transpose(M, Mk);
+    M_one = mat_one_norm(Mk);
+    M_inf = mat_inf_norm(Mk);
+    do {
+        vec_cross(&Mk[3], &Mk[6], &Madj[0]);
+        vec_cross(&Mk[6], &Mk[0], &Madj[3]);
+        vec_cross(&Mk[0], &Mk[3], &Madj[6]);
+        det = Mk[0] * Madj[0] + Mk[1] * Madj[1] + Mk[2] * Madj[2];
+        if (det == 0.0) break;
+        double adj_one = mat_one_norm(Madj);
+        double adj_inf = mat_inf_norm(Madj);
+        double gamma = sqrt(sqrt((adj_one * adj_inf) / (M_one * M_inf)) / fabs(det));
+        double g1 = gamma * 0.5;
+        double g2 = 0.5 / (gamma * det);
+        for (int i = 0; i < 9; ++i) {
+            Ek[i] = Mk[i];
+            Mk[i] = Mk[i] * g1 + Madj[i] * g2;
+            Ek[i] -= Mk[i];
+        }
+        E_one = mat_one_norm(Ek);
+        M_one = mat_one_norm(Mk);
+        M_inf = mat_inf_norm(Mk);
+    } while (E_one > M_one * tol);
+    mat_transpose(Mk, Q);
+    return det;
+}
+
+/* computeRotationLarge (TFEM.inl:755-778): rows of R are the unit edge
+ * ab, the in-plane unit vector and the normal. */
+static void rotation_large(const double* pa, const double* pb, const double* pc, double R[9])
+{
+    double ex[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+    vec_normalize(ex);
+    double ey[3] = {pc[0] - pa[0], pc[1] - pa[1], pc[2] - pa[2]};
+    double ez[3];
+    vec_cross(ex, ey, ez);
+    vec_normalize(ez);
+    vec_cross(ez, ex, ey);
+    for (int k = 0; k < 3; ++k) {
+        R[0 + k] = ex[k];
+        R[3 + k] = ey[k];
+        R[6 + k] = ez[k];
+    }
+}
+
+/* peudo_determinant_for_coef (TFEM.inl:211-215); m = [m00 m01 m02; m10 m11 m12]. */
+static double pdet(double m00, double m01, double m02, double m10, double m11, double m12)
+{
+    return m01 * m12 - m11 * m02 - m00 * m12 + m10 * m02 + m00 * m11 - m10 * m01;
+}
+
+/* computeStrainDisplacement (TFEM.inl:134-209). The 12x6 J has three
+ * distinct values per node i, stored as J3[3i+0] = J(3i,0) = J(3i+1,3) =
+ * J(3i+2,5), J3[3i+1] = J(3i,3) = J(3i+1,1) = J(3i+2,4) and J3[3i+2] =
+ * J(3i,5) = J(3i+1,4) = J(3i+2,2). */
+static void strain_displacement(const double* a, const double* b, const double* c, const double* d,
+                                double J3[12])
+{
+    J3[0] = -pdet(b[1], c[1], d[1], b[2], c[2], d[2]);
+    J3[1] = pdet(b[0], c[0], d[0], b[2], c[2], d[2]);
+    J3[2] = -pdet(b[0], c[0], d[0], b[1], c[1], d[1]);
+
+    J3[3] = pdet(c[1], d[1], a[1], c[2], d[2], a[2]);
+    J3[4] = -pdet(c[0], d[0], a[0], c[2], d[2], a[2]);
+    J3[5] = pdet(c[0], d[0], a[0], c[1], d[1], a[1]);
+
+    J3[6] = -pdet(d[1], a[1], b[1], d[2], a[2], b[2]);
+    J3[7] = pdet(d[0], a[0], b[0], d[2], a[2], b[2]);
+    J3[8] = -pdet(d[0], a[0], b[0], d[1], a[1], b[1]);
+
+    J3[9] = pdet(a[1], b[1], c[1], a[2], b[2], c[2]);
+    J3[10] = -pdet(a[0], b[0], c[0], a[2], b[2], c[2]);
+    J3[11] = pdet(a[0], b[0], c[0], a[1], b[1], c[1]);
+}
+
+/* computeForce (TFEM.inl:293-415 without plasticity, and :417-521 with
+ * `fact`): F = J K J^T D using only J's non-zero pattern, in the
+ * reference's term order. K3 = {K(0,0), K(0,1), K(3,3)}. fact is applied to
+ * K J^T D when use_fact is set. */
+static void compute_force(double F[12], const double D[12], const double K3[3], const double J3[12],
+                          int use_fact, double fact)
+{
+#define JA(i) J3[3 * (i) + 0]
+#define JB(i) J3[3 * (i) + 1]
+#define JC(i) J3[3 * (i) + 2]
+    double JtD[6], KJtD[6];
+    JtD[0] = JA(0) * D[0] + JA(1) * D[3] + JA(2) * D[6] + JA(3) * D[9];
+    JtD[1] = JB(0) * D[1] + JB(1) * D[4] + JB(2) * D[7] + JB(3) * D[10];
+    JtD[2] = JC(0) * D[2] + JC(1) * D[5] + JC(2) * D[8] + JC(3) * D[11];
+    JtD[3] = JB(0) * D[0] + JA(0) * D[1] + JB(1) * D[3] + JA(1) * D[4] + JB(2) * D[6] + JA(2) * D[7] +
+             JB(3) * D[9] + JA(3) * D[10];
+    JtD[4] = JC(0) * D[1] + JB(0) * D[2] + JC(1) * D[4] + JB(1) * D[5] + JC(2) * D[7] + JB(2) * D[8] +
+             JC(3) * D[10] + JB(3) * D[11];
+    JtD[5] = JC(0) * D[0] + JA(0) * D[2] + JC(1) * D[3] + JA(1) * D[5] + JC(2) * D[6] + JA(2) * D[8] +
+             JC(3) * D[9] + JA(3) * D[11];
+
+    const double k0 = K3[0], k1 = K3[1], k2 = K3[2];
+    KJtD[0] = k0 * JtD[0] + k1 * JtD[1] + k1 * JtD[2];
+    KJtD[1] = k1 * JtD[0] + k0 * JtD[1] + k1 * JtD[2];
+    KJtD[2] = k1 * JtD[0] + k1 * JtD[1] + k0 * JtD[2];
+    KJtD[3] = k2 * JtD[3];
+    KJtD[4] = k2 * JtD[4];
+    KJtD[5] = k2 * JtD[5];
+    if (use_fact)
+        for (int i = 0; i < 6; ++i) KJtD[i] *= fact;
+
+    for (int i = 0; i < 4; ++i) {
+        F[3 * i + 0] = JA(i) * KJtD[0] + JB(i) * KJtD[3] + JC(i) * KJtD[5];
+        F[3 * i + 1] = JB(i) * KJtD[1] + JA(i) * KJtD[3] + JC(i) * KJtD[4];
+        F[3 * i + 2] = JC(i) * KJtD[2] + JB(i) * KJtD[4] + JA(i) * KJtD[5];
+    }
+#undef JA
+#undef JB
+#undef JC
+}
+
+/* ------------------------------------------------------------------------- */
+/* thread pool (one parallel region at a time)                               */
+/* ------------------------------------------------------------------------- */
+
+static int g_threads = 1;
+
+void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int orc_get_threads(void) { return g_threads; }
+
+typedef void (*orc_task_fn)(void* ctx, int tid, int nthreads);
+typedef struct {
+    orc_task_fn fn;
+    void* ctx;
+    int tid, n;
+} orc_task;
+
+static void* orc_task_main(void* p)
+{
+    orc_task* t = (orc_task*)p;
+    t->fn(t->ctx, t->tid, t->n);
+    return NULL;
+}
+
+static void parallel_run(orc_task_fn fn, void* ctx, int n)
+{
+    if (n <= 1) {
+        fn(ctx, 0, 1);
+        return;
+    }
+    pthread_t th[256];
+    orc_task tk[256];
+    if (n > 256) n = 256;
+    for (int t = 0; t < n; ++t) {
+        tk[t].fn = fn;
+        tk[t].ctx = ctx;
+        tk[t].tid = t;
+        tk[t].n = n;
+        if (t > 0) pthread_create(&th[t], NULL, orc_task_main, &tk[t]);
+    }
+    fn(ctx, 0, n);
+    for (int t = 1; t < n; ++t) pthread_join(th[t], NULL);
+}
+
+static void chunk(long total, int tid, int n, long* b, long* e)
+{
+    long per = (total + n - 1) / n;
+    *b = per * tid;
+    *e = *b + per;
+    if (*b > total) *b = total;
+    if (*e > total) *e = total;
+}
+
+/* ------------------------------------------------------------------------- */
+/* TetrahedronFEMForceField                                                   */
+/* ------------------------------------------------------------------------- */
+
+typedef struct orc_fem {
+    int n_nodes, n_tets, method;
+    int32_t* tets;     /* 4 per element */
+    double* rest;      /* initialPoints, 3 per node */
+    double* K3;        /* 3 per element */
+    double* J3;        /* 12 per element */
+    double* R0t;       /* _initialRotations, 9 per element */
+    double* rot;       /* rotations (= R^T), 9 per element */
+    double* rest_rot;  /* _rotatedInitialElements, 12 per element */
+    double rest_volume;
+    double* tl_buf;    /* thread-local force buffers for the threaded mode */
+    int tl_threads;
+} orc_fem;
+
+/* BaseLinearElasticityFEMForceField::getYoungModulusInElement /
+ * getPoissonRatioInElement (BaseLinearElasticityFEMForceField.inl:114-144):
+ * the per-element entry when the vector is long enough, else entry 0. */
+static double per_element(const double* v, int n, int e, int n_tets)
+{
+    return (n >= n_tets && n > e) ? v[e] : v[0];
+}
+
+orc_fem* orc_fem_create(int n_nodes, const double* rest, int n_tets, const int32_t* tets,
+                        const double* young, int n_young, const double* poisson, int n_poisson,
+                        const double* lsf, int n_lsf, int method)
+{
+    orc_fem* m = (orc_fem*)calloc(1, sizeof(orc_fem));
+    m->n_nodes = n_nodes;
+    m->n_tets = n_tets;
+    m->method = method;
+    m->tets = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)n_tets);
+    memcpy(m->tets, tets, sizeof(int32_t) * 4 * (size_t)n_tets);
+    m->rest = (double*)malloc(sizeof(double) * 3 * (size_t)n_nodes);
+    memcpy(m->rest, rest, sizeof(double) * 3 * (size_t)n_nodes);
+    m->K3 = (double*)calloc(3 * (size_t)n_tets, sizeof(double));
+    m->J3 = (double*)calloc(12 * (size_t)n_tets, sizeof(double));
+    m->R0t = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
+    m->rot = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
+    m->rest_rot = (double*)calloc(12 * (size_t)n_tets, sizeof(double));
+
+    for (int e = 0; e < n_tets; ++e) {
+        const int32_t* t = &tets[4 * e];
+        const double *pa = &rest[3 * t[0]], *pb = &rest[3 * t[1]], *pc = &rest[3 * t[2]],
+                     *pd = &rest[3 * t[3]];
+        /* computeMaterialStiffness (TFEM.inl:256-291) */
+        double E = per_element(young, n_young, e, n_tets);
+        double nu = per_element(poisson, n_poisson, e, n_tets);
+        double f = (n_lsf > 0) ? lsf[(size_t)e * (size_t)n_lsf / (size_t)n_tets] : 1.0;
+        E = f * E;
+        double s = (E * (1 - nu)) / ((1 + nu) * (1 - 2 * nu));
+        double k0 = 1.0, k1 = nu / (1 - nu), k2 = (1 - 2 * nu) / (2 * (1 - nu));
+        k0 *= s;
+        k1 *= s;
+        k2 *= s;
+        /* geometry::Tetrahedron::volume (Geometry/.../Tetrahedron.h:55-83) */
+        double ea[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+        double eb[3] = {pc[0] - pa[0], pc[1] - pa[1], pc[2] - pa[2]};
+        double ec[3] = {pd[0] - pa[0], pd[1] - pa[1], pd[2] - pa[2]};
+        double cr[3];
+        vec_cross(ea, eb, cr);
+        double vol = fabs(vec_dot(cr, ec) / 6.0);
+        m->rest_volume += vol;
+        k0 /= vol * 36;
+        k1 /= vol * 36;
+        k2 /= vol * 36;
+        m->K3[3 * e + 0] = k0;
+        m->K3[3 * e + 1] = k1;
+        m->K3[3 * e + 2] = k2;
+
+        double* rr = &m->rest_rot[12 * e];
+        if (method == ORC_SMALL) {
+            /* initSmall (TFEM.inl:526-532) */
+            strain_displacement(pa, pb, pc, pd, &m->J3[12 * e]);
+            for (int i = 0; i < 9; ++i) m->R0t[9 * e + i] = m->rot[9 * e + i] = (i % 4 == 0);
+        } else {
+            double R[9];
+            if (method == ORC_LARGE) {
+                /* initLarge (TFEM.inl:835-868) */
+                rotation_large(pa, pb, pc, R);
+            } else {
+                /* initPolar (TFEM.inl:993-1023) */
+                double A[9] = {ea[0], ea[1], ea[2], eb[0], eb[1], eb[2], ec[0], ec[1], ec[2]};
+                orc_polar(A, R);
+            }
+            mat_transpose(R, &m->R0t[9 * e]);
+            memcpy(&m->rot[9 * e], &m->R0t[9 * e], sizeof(double) * 9);
+            mat_vec(R, pa, &rr[0]);
+            mat_vec(R, pb, &rr[3]);
+            mat_vec(R, pc, &rr[6]);
+            mat_vec(R, pd, &rr[9]);
+            if (method == ORC_LARGE) {
+                for (int i = 1; i < 4; ++i)
+                    for (int k = 0; k < 3; ++k) rr[3 * i + k] -= rr[k];
+                rr[0] = rr[1] = rr[2] = 0.0;
+            }
+            strain_displacement(&rr[0], &rr[3], &rr[6], &rr[9], &m->J3[12 * e]);
+        }
+    }
+    return m;
+}
+
+void orc_fem_destroy(orc_fem* m)
+{
+    if (!m) return;
+    free(m->tets);
+    free(m->rest);
+    free(m->K3);
+    free(m->J3);
+    free(m->R0t);
+    free(m->rot);
+    free(m->rest_rot);
+    free(m->tl_buf);
+    free(m);
+}
+
+/* Element e's contribution to addForce, added into f (TFEM.inl:534-623 small,
+ * :870-986 large, :1025-1079 polar). Also stores rotations[e]. */
+static void element_force(orc_fem* m, int e, const double* p, double* f)
+{
+    const int32_t* t = &m->tets[4 * e];
+    const double* K3 = &m->K3[3 * e];
+    const double* J3 = &m->J3[12 * e];
+    const double* rr = &m->rest_rot[12 * e];
+    double D[12], F[12];
+    if (m->method == ORC_SMALL) {
+        const double* ip = m->rest;
+        const int a = t[0];
+        D[0] = D[1] = D[2] = 0.0;
+        for (int i = 1; i < 4; ++i)
+            for (int k = 0; k < 3; ++k)
+                D[3 * i + k] = ip[3 * t[i] + k] - ip[3 * a + k] - p[3 * t[i] + k] + p[3 * a + k];
+        compute_force(F, D, K3, J3, 0, 0.0);
+        for (int i = 0; i < 4; ++i)
+            for (int k = 0; k < 3; ++k) f[3 * t[i] + k] += F[3 * i + k];
+        return;
+    }
+    double R[9], def[12];
+    if (m->method == ORC_LARGE) {
+        rotation_large(&p[3 * t[0]], &p[3 * t[1]], &p[3 * t[2]], R);
+    } else {
+        const double *p0 = &p[3 * t[0]], *p1 = &p[3 * t[1]], *p2 = &p[3 * t[2]], *p3 = &p[3 * t[3]];
+        double A[9] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], p2[0] - p0[0], p2[1] - p0[1],
+                       p2[2] - p0[2], p3[0] - p0[0], p3[1] - p0[1], p3[2] - p0[2]};
+        orc_polar(A, R);
+    }
+    double* rot = &m->rot[9 * e];
+    mat_transpose(R, rot);
+    for (int i = 0; i < 4; ++i) mat_vec(R, &p[3 * t[i]], &def[3 * i]);
+    if (m->method == ORC_LARGE) {
+        def[3] -= def[0];
+        def[6] -= def[0];
+        def[7] -= def[1];
+        def[9] -= def[0];
+        def[10] -= def[1];
+        def[11] -= def[2];
+        D[0] = D[1] = D[2] = 0.0;
+        D[3] = rr[3] - def[3];
+        D[4] = D[5] = 0.0;
+        D[6] = rr[6] - def[6];
+        D[7] = rr[7] - def[7];
+        D[8] = 0.0;
+        D[9] = rr[9] - def[9];
+        D[10] = rr[10] - def[10];
+        D[11] = rr[11] - def[11];
+    } else {
+        for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
+    }
+    compute_force(F, D, K3, J3, 0, 0.0);
+    for (int i = 0; i < 4; ++i) {
+        double r3[3];
+        mat_vec(rot, &F[3 * i], r3);
+        f[3 * t[i] + 0] += r3[0];
+        f[3 * t[i] + 1] += r3[1];
+        f[3 * t[i] + 2] += r3[2];
+    }
+}
+
+/* applyStiffnessSmall / applyStiffnessCorotational (TFEM.inl:721-749,
+ * 1193-1237): df -= R K (R^T dx) * fact for element e. */
+static void element_dforce(const orc_fem* m, int e, const double* x, double* df, double fact)
+{
+    const int32_t* t = &m->tets[4 * e];
+    const double* K3 = &m->K3[3 * e];
+    const double* J3 = &m->J3[12 * e];
+    double X[12], F[12];
+    if (m->method == ORC_SMALL) {
+        for (int i = 0; i < 4; ++i)
+            for (int k = 0; k < 3; ++k) X[3 * i + k] = x[3 * t[i] + k];
+        compute_force(F, X, K3, J3, 1, fact);
+        for (int i = 0; i < 4; ++i)
+            for (int k = 0; k < 3; ++k) df[3 * t[i] + k] += -F[3 * i + k];
+        return;
+    }
+    const double* r = &m->rot[9 * e]; /* rotations[i] = R^T */
+    for (int i = 0; i < 4; ++i) {
+        const double* xi = &x[3 * t[i]];
+        for (int k = 0; k < 3; ++k) X[3 * i + k] = r[0 * 3 + k] * xi[0] + r[1 * 3 + k] * xi[1] + r[2 * 3 + k] * xi[2];
+    }
+    compute_force(F, X, K3, J3, 1, fact);
+    for (int i = 0; i < 4; ++i) {
+        double* fi = &df[3 * t[i]];
+        for (int k = 0; k < 3; ++k)
+            fi[k] -= r[k * 3 + 0] * F[3 * i + 0] + r[k * 3 + 1] * F[3 * i + 1] + r[k * 3 + 2] * F[3 * i + 2];
+    }
+}
+
+typedef struct {
+    orc_fem* m;
+    const double* in;
+    double* out;
+    double fact;
+    int dforce;
+} fem_job;
+
+static void fem_job_run(void* ctx, int tid, int n)
+{
+    fem_job* j = (fem_job*)ctx;
+    long b, e;
+    chunk(j->m->n_tets, tid, n, &b, &e);
+    double* buf = j->m->tl_buf + (size_t)tid * 3 * (size_t)j->m->n_nodes;
+    memset(buf, 0, sizeof(double) * 3 * (size_t)j->m->n_nodes);
+    for (long i = b; i < e; ++i) {
+        if (j->dforce)
+            element_dforce(j->m, (int)i, j->in, buf, j->fact);
+        else
+            element_force(j->m, (int)i, j->in, buf);
+    }
+}
+
+typedef struct {
+    orc_fem* m;
+    double* out;
+    int nt;
+} merge_job;
+
+static void merge_job_run(void* ctx, int tid, int n)
+{
+    merge_job* j = (merge_job*)ctx;
+    long b, e;
+    long len = 3L * j->m->n_nodes;
+    chunk(len, tid, n, &b, &e);
+    for (int t = 0; t < j->nt; ++t) {
+        const double* buf = j->m->tl_buf + (size_t)t * (size_t)len;
+        for (long i = b; i < e; ++i) j->out[i] += buf[i];
+    }
+}
+
+static void fem_threaded(orc_fem* m, const double* in, double* out, double fact, int dforce)
+{
+    int nt = g_threads;
+    if (m->tl_threads < nt) {
+        free(m->tl_buf);
+        m->tl_buf = (double*)malloc(sizeof(double) * 3 * (size_t)m->n_nodes * (size_t)nt);
+        m->tl_threads = nt;
+    }
+    fem_job j = {m, in, out, fact, dforce};
+    parallel_run(fem_job_run, &j, nt);
+    merge_job mj = {m, out, nt};
+    parallel_run(merge_job_run, &mj, nt);
+}
+
+/* addForce (TFEM.inl:1548-1604): f += internal forces at positions x. */
+void orc_fem_add_force(orc_fem* m, const double* x, double* f)
+{
+    if (g_threads > 1) {
+        fem_threaded(m, x, f, 0.0, 0);
+        return;
+    }
+    for (int e = 0; e < m->n_tets; ++e) element_force(m, e, x, f);
+}
+
+/* addDForce (TFEM.inl:1606-1636): df += -kFactor K dx. */
+void orc_fem_add_dforce(orc_fem* m, const double* dx, double* df, double kfactor)
+{
+    if (g_threads > 1) {
+        fem_threaded(m, dx, df, kfactor, 1);
+        return;
+    }
+    for (int e = 0; e < m->n_tets; ++e) element_dforce(m, e, dx, df, kfactor);
+}
+
+/* Element data for the known-answer tests: out[0:9] initial rotation (R0^T),
+ * out[9:18] current rotation (R^T), out[18:30] rotated rest coordinates,
+ * out[30:33] K(0,0), K(0,1), K(3,3), out[33:45] the 12 distinct J values. */
+void orc_fem_element(const orc_fem* m, int e, double* out)
+{
+    memcpy(out, &m->R0t[9 * e], 9 * sizeof(double));
+    memcpy(out + 9, &m->rot[9 * e], 9 * sizeof(double));
+    memcpy(out + 18, &m->rest_rot[12 * e], 12 * sizeof(double));
+    memcpy(out + 30, &m->K3[3 * e], 3 * sizeof(double));
+    memcpy(out + 33, &m->J3[12 * e], 12 * sizeof(double));
+}
+
+double orc_fem_rest_volume(const orc_fem* m) { return m->rest_volume; }
+
+/* ------------------------------------------------------------------------- */
+/* Scene: MechanicalObject + mass + force fields + projective constraint,    */
+/* integrated by EulerImplicitSolver with CGLinearSolver<GraphScattered>.    */
+/* ------------------------------------------------------------------------- */
+
+typedef struct orc_scene {
+    int n;               /* nodes */
+    orc_fem* fem;        /* borrowed, may be NULL */
+    int mass_kind;       /* 0: UniformMass, 1: DiagonalMass */
+    double vertex_mass;  /* UniformMass vertexMass */
+    double* node_mass;   /* DiagonalMass per-node masses */
+    double g[3];
+    int* fixed;
+    int n_fixed;
+    int fix_all;
+    double* ext;         /* MechanicalObject externalForce, may be NULL */
+    /* optional isotropic anchor springs: f -= k (x - anchor) (test helper) */
+    double spring_k;
+    double* anchor;
+    int mass_first;      /* component order in the node: mass before the FEM */
+    /* EulerImplicitSolver data */
+    double dt, rs, rm, vdamping;
+    /* CGLinearSolver data */
+    int cg_iters;
+    double cg_tol, cg_threshold;
+    long time_step_count;
+    /* state + solver vectors */
+    double *x, *v, *f, *b, *xs, *p, *q, *r;
+    /* statistics of the last solve */
+    int last_iters;
+    double last_err;
+} orc_scene;
+
+orc_scene* orc_scene_create(orc_fem* fem, int n_nodes, int mass_kind, double vertex_mass,
+                            const double* node_mass, const double* gravity, const int32_t* fixed,
+                            int n_fixed, int fix_all, double dt, double rs, double rm, double vdamping,
+                            int cg_iters, double cg_tol, double cg_threshold, int mass_first)
+{
+    orc_scene* s = (orc_scene*)calloc(1, sizeof(orc_scene));
+    size_t n3 = 3 * (size_t)n_nodes;
+    s->n = n_nodes;
+    s->fem = fem;
+    s->mass_kind = mass_kind;
+    s->vertex_mass = vertex_mass;
+    if (mass_kind == 1) {
+        s->node_mass = (double*)malloc(sizeof(double) * (size_t)n_nodes);
+        memcpy(s->node_mass, node_mass, sizeof(double) * (size_t)n_nodes);
+    }
+    memcpy(s->g, gravity, sizeof(double) * 3);
+    s->n_fixed = n_fixed;
+    s->fixed = (int*)malloc(sizeof(int) * (size_t)(n_fixed > 0 ? n_fixed : 1));
+    for (int i = 0; i < n_fixed; ++i) s->fixed[i] = fixed[i];
+    s->fix_all = fix_all;
+    s->dt = dt;
+    s->rs = rs;
+    s->rm = rm;
+    s->vdamping = vdamping;
+    s->cg_iters = cg_iters;
+    s->cg_tol = cg_tol;
+    s->cg_threshold = cg_threshold;
+    s->mass_first = mass_first;
+    s->x = (double*)calloc(n3, sizeof(double));
+    s->v = (double*)calloc(n3, sizeof(double));
+    s->f = (double*)calloc(n3, sizeof(double));
+    s->b = (double*)calloc(n3, sizeof(double));
+    s->xs = (double*)calloc(n3, sizeof(double));
+    s->p = (double*)calloc(n3, sizeof(double));
+    s->q = (double*)calloc(n3, sizeof(double));
+    s->r = (double*)calloc(n3, sizeof(double));
+    if (fem) memcpy(s->x, fem->rest, sizeof(double) * n3);
+    return s;
+}
+
+void orc_scene_destroy(orc_scene* s)
+{
+    if (!s) return;
+    free(s->node_mass);
+    free(s->fixed);
+    free(s->ext);
+    free(s->anchor);
+    free(s->x);
+    free(s->v);
+    free(s->f);
+    free(s->b);
+    free(s->xs);
+    free(s->p);
+    free(s->q);
+    free(s->r);
+    free(s);
+}
+
+void orc_scene_set_state(orc_scene* s, const double* x, const double* v)
+{
+    size_t n3 = 3 * (size_t)s->n;
+    if (x) memcpy(s->x, x, sizeof(double) * n3);
+    if (v) memcpy(s->v, v, sizeof(double) * n3);
+}
+
+void orc_scene_get_state(const orc_scene* s, double* x, double* v)
+{
+    size_t n3 = 3 * (size_t)s->n;
+    if (x) memcpy(x, s->x, sizeof(double) * n3);
+    if (v) memcpy(v, s->v, sizeof(double) * n3);
+}
+
+void orc_scene_set_external_force(orc_scene* s, const double* fext)
+{
+    size_t n3 = 3 * (size_t)s->n;
+    if (!s->ext) s->ext = (double*)malloc(sizeof(double) * n3);
+    memcpy(s->ext, fext, sizeof(double) * n3);
+}
+
+void orc_scene_set_springs(orc_scene* s, double k, const double* anchor)
+{
+    size_t n3 = 3 * (size_t)s->n;
+    s->spring_k = k;
+    if (!s->anchor) s->anchor = (double*)malloc(sizeof(double) * n3);
+    memcpy(s->anchor, anchor, sizeof(double) * n3);
+}
+
+int orc_scene_last_iterations(const orc_scene* s) { return s->last_iters; }
+double orc_scene_last_error(const orc_scene* s) { return s->last_err; }
+
+/* UniformMass::addForce (UniformMass.inl:471-496) / DiagonalMass::addForce
+ * (DiagonalMass.inl:1393-1413): f += m g. */
+static void mass_add_force(const orc_scene* s, double* f)
+{
+    if (s->mass_kind == 0) {
+        double mg[3] = {s->g[0] * s->vertex_mass, s->g[1] * s->vertex_mass, s->g[2] * s->vertex_mass};
+        for (int i = 0; i < s->n; ++i)
+            for (int k = 0; k < 3; ++k) f[3 * i + k] += mg[k];
+    } else {
+        for (int i = 0; i < s->n; ++i)
+            for (int k = 0; k < 3; ++k) f[3 * i + k] += s->g[k] * s->node_mass[i];
+    }
+}
+
+/* UniformMass::addMDx (UniformMass.inl:403-419) / DiagonalMass::addMDx
+ * (DiagonalMass.inl:536-559): res += factor M dx. */
+static void mass_add_mdx(const orc_scene* s, double* res, const double* dx, double factor)
+{
+    if (s->mass_kind == 0) {
+        double m = s->vertex_mass;
+        if (factor != 1.0) m *= factor;
+        for (long i = 0; i < 3L * s->n; ++i) res[i] += dx[i] * m;
+    } else if (factor == 1.0) {
+        for (int i = 0; i < s->n; ++i)
+            for (int k = 0; k < 3; ++k) res[3 * i + k] += dx[3 * i + k] * s->node_mass[i];
+    } else {
+        for (int i = 0; i < s->n; ++i)
+            for (int k = 0; k < 3; ++k) res[3 * i + k] += (dx[3 * i + k] * s->node_mass[i]) * factor;
+    }
+}
+
+static void spring_add_force(const orc_scene* s, const double* x, double* f)
+{
+    if (s->spring_k == 0.0) return;
+    for (long i = 0; i < 3L * s->n; ++i) f[i] += -s->spring_k * (x[i] - s->anchor[i]);
+}
+
+static void spring_add_dforce(const orc_scene* s, const double* dx, double* df, double kf)
+{
+    if (s->spring_k == 0.0) return;
+    for (long i = 0; i < 3L * s->n; ++i) df[i] += -s->spring_k * dx[i] * kf;
+}
+
+/* FixedProjectiveConstraint::projectResponse (FixedProjectiveConstraint.inl:184-207). */
+static void project_response(const orc_scene* s, double* res)
+{
+    if (s->fix_all) {
+        memset(res, 0, sizeof(double) * 3 * (size_t)s->n);
+        return;
+    }
+    for (int i = 0; i < s->n_fixed; ++i) {
+        int j = s->fixed[i];
+        if (j >= 0 && j < s->n) res[3 * j] = res[3 * j + 1] = res[3 * j + 2] = 0.0;
+    }
+}
+
+/* MechanicalObject::vDot (MechanicalObject.inl:2334-2356). */
+static double vdot(const double* a, const double* b, int n)
+{
+    double r = 0.0;
+    for (int i = 0; i < n; ++i) r += vec_dot(&a[3 * i], &b[3 * i]);
+    return r;
+}
+
+/* addMBKdx with the forcefield order of the node: mass (Mass::addMBKdx,
+ * Mass.inl:94-104) and the FEM (BaseForceField::addMBKdx,
+ * BaseForceField.cpp:38-47). The force fields' own Rayleigh coefficients are
+ * zero in every scene here, so kFactorIncludingRayleighDamping = k and
+ * mFactorIncludingRayleighDamping = m (MechanicalParams.h:62-64). */
+static void add_mbkdx(orc_scene* s, double* df, const double* dx, double mf, double kf)
+{
+    if (s->mass_first) {
+        if (mf != 0.0) mass_add_mdx(s, df, dx, mf);
+        if (kf != 0.0 && s->fem) orc_fem_add_dforce(s->fem, dx, df, kf);
+    } else {
+        if (kf != 0.0 && s->fem) orc_fem_add_dforce(s->fem, dx, df, kf);
+        if (mf != 0.0) mass_add_mdx(s, df, dx, mf);
+    }
+    if (kf != 0.0) spring_add_dforce(s, dx, df, kf);
+}
+
+/* GraphScatteredMatrix::apply (GraphScatteredTypes.cpp:33-45):
+ * q = (mF M + kF K) p, then projected. */
+static void matvec(orc_scene* s, double* q, const double* p, double mf, double kf)
+{
+    memset(q, 0, sizeof(double) * 3 * (size_t)s->n);
+    add_mbkdx(s, q, p, mf, kf);
+    project_response(s, q);
+}
+
+/* CGLinearSolver::solve (CGLinearSolver.inl:72-315) with the GraphScattered
+ * cgstep_beta / cgstep_alpha (CGLinearSolver.cpp:40-63), warmStart off. */
+static void cg_solve(orc_scene* s, double mf, double kf)
+{
+    const int n = s->n;
+    const long n3 = 3L * n;
+    double *x = s->xs, *b = s->b, *p = s->p, *q = s->q, *r = s->r;
+    double rho, rho_1 = 0.0, alpha, beta;
+    memset(x, 0, sizeof(double) * (size_t)n3);
+    memcpy(r, b, sizeof(double) * (size_t)n3);
+    const double normb = sqrt(vdot(b, b, n));
+    int nb_iter = 0, n_matvec = 0;
+    s->last_err = 0.0;
+    if (normb != 0.0) {
+        for (nb_iter = 1; nb_iter <= s->cg_iters; nb_iter++) {
+            rho = vdot(r, r, n);
+            const double err = sqrt(rho) / normb;
+            s->last_err = err;
+            if (err <= s->cg_tol) {
+                if (!(nb_iter == 1 && s->time_step_count == 0)) break;
+            }
+            if (nb_iter == 1) {
+                memcpy(p, r, sizeof(double) * (size_t)n3);
+            } else {
+                beta = rho / rho_1;
+                /* vOp_avf (MechanicalObject.inl:1999-2013): p *= beta; p += r */
+                if (beta == 1.0)
+                    for (long i = 0; i < n3; ++i) p[i] += r[i];
+                else
+                    for (long i = 0; i < n3; ++i) {
+                        p[i] *= beta;
+                        p[i] += r[i];
+                    }
+            }
+            matvec(s, q, p, mf, kf);
+            n_matvec++;
+            const double den = vdot(p, q, n);
+            if (den != 0.0) {
+                if (fabs(den) <= s->cg_threshold) {
+                    if (!(nb_iter == 1 && s->time_step_count == 0)) break;
+                }
+                alpha = rho / den;
+                /* vOp_v_inc_bf (MechanicalObject.inl:2018-2032), alpha != 1 */
+                for (long i = 0; i < n3; ++i) x[i] += p[i] * alpha;
+                for (long i = 0; i < n3; ++i) r[i] += q[i] * -alpha;
+            } else {
+                break;
+            }
+            rho_1 = rho;
+        }
+    }
+    s->time_step_count++;
+    s->last_iters = n_matvec;
+}
+
+/* computeForce (MappingGraphMechanicalOperations.cpp:41-92): f = 0,
+ * f += externalForce, f += sum of the force fields' addForce. */
+static void scene_compute_force(orc_scene* s)
+{
+    const long n3 = 3L * s->n;
+    memset(s->f, 0, sizeof(double) * (size_t)n3);
+    if (s->ext)
+        for (long i = 0; i < n3; ++i) s->f[i] += s->ext[i];
+    if (s->mass_first) {
+        mass_add_force(s, s->f);
+        if (s->fem) orc_fem_add_force(s->fem, s->x, s->f);
+    } else {
+        if (s->fem) orc_fem_add_force(s->fem, s->x, s->f);
+        mass_add_force(s, s->f);
+    }
+    spring_add_force(s, s->x, s->f);
+}
+
+/* One EulerImplicitSolver::solve (EulerImplicitSolver.cpp:83-341) in its
+ * second-order, non-trapezoidal form, followed by the animation loop's
+ * projectPositionAndVelocity (no-op for FixedProjectiveConstraint with
+ * activate_projectVelocity off). */
+static void euler_step(orc_scene* s)
+{
+    const long n3 = 3L * s->n;
+    const double h = s->dt;
+    scene_compute_force(s);
+    /* b = f; b += (-rm M + (h + rs) K) v; b *= h; project(b) */
+    memcpy(s->b, s->f, sizeof(double) * (size_t)n3);
+    add_mbkdx(s, s->b, s->v, -s->rm, h * 1.0 + s->rs);
+    for (long i = 0; i < n3; ++i) s->b[i] *= h;
+    project_response(s, s->b);
+    /* setSystemMBKMatrix: mF = 1 + h rm, bF = -h, kF = -h (h + rs) */
+    const double mf = 1 + 1.0 * h * s->rm;
+    const double kf = -1.0 * h * (1.0 * h + s->rs);
+    cg_solve(s, mf, kf);
+    /* vMultiOp fast path (MechanicalObject.inl:2206-2240): v += dv; x += v h */
+    for (long i = 0; i < n3; ++i) {
+        s->v[i] += s->xs[i];
+        s->x[i] += s->v[i] * h;
+    }
+    if (s->vdamping != 0.0) {
+        const double d = exp(-h * s->vdamping);
+        for (long i = 0; i < n3; ++i) s->v[i] *= d;
+    }
+}
+
+void orc_scene_step(orc_scene* s, int n_steps)
+{
+    for (int i = 0; i < n_steps; ++i) euler_step(s);
+}
+
+/* Exposed pieces of the step for per-call parity checks. */
+void orc_scene_compute_force(orc_scene* s, double* f_out)
+{
+    scene_compute_force(s);
+    if (f_out) memcpy(f_out, s->f, sizeof(double) * 3 * (size_t)s->n);
+}
