@@ -1,0 +1,395 @@
+"""Benchmark of the implicit corotational tet-FEM step on GB300.
+
+Default workload (N=1): the single large cantilever beam, 64x64x257 nodes
+(1,052,672 nodes, 5,080,320 tetrahedra), spacing 0.5, interior jitter
+0.05*spacing, 5-tet split, E=5000, nu=0.45, method=polar, total mass 1,
+gravity -9.81 y, z=0 fixed, dt=0.01, Rayleigh 0.1/0.1, CG 50 iterations,
+tolerance 1e-7, threshold 1e-9 (the reference default threshold 1e-5 is
+replaced by 1e-9, as the workload's CG tolerance is 1e-7). The inputs are
+seeded synthetic meshes; no dataset is involved.
+
+A "step" is one EulerImplicitSolver step of that beam. `value` is
+tet-steps/s of the mixed-precision path (FP32 element math and solver
+vectors, FP64 dots and state) with the mesh and state resident in HBM,
+timed with CUDA events on the scene's stream. `e2e` is the same metric
+through the C ABI with the state uploaded from pinned host memory and the
+positions read back every step. The plain FP64 path, the position error of
+mixed vs FP64 after 100 steps, the addDForce roofline and a CPU baseline
+(the CPU oracle, multi-threaded, bounded sample) are reported beside it.
+
+--impl reference times the reference's CPU algorithm (the oracle port; the
+reference itself cannot be built here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = dict(n=(64, 64, 257), spacing=0.5, jitter=0.05, seed=0, young=5000.0, poisson=0.45, method="polar",
+              dt=0.01, rs=0.1, rm=0.1, cg_iterations=50, cg_tolerance=1e-7, cg_threshold=1e-9, total_mass=1.0,
+              gravity=(0.0, -9.81, 0.0))
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", default=None, help="override node grid, e.g. 32,32,129")
+    ap.add_argument("--error-steps", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-error", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: build the mixed scene, run warm-up + steps, print a short line")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_mesh(cfg):
+    from sofa_gb300 import topology as topo
+
+    return topo.beam(cfg["n"], spacing=cfg["spacing"], jitter=cfg["jitter"], seed=cfg["seed"], split=5)
+
+
+def make_scene(capi, mesh, cfg, precision):
+    fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, cfg["young"], cfg["poisson"], cfg["method"], precision)
+    return capi.Scene(fem, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"], rayleigh_mass=cfg["rm"],
+                      cg_iterations=cfg["cg_iterations"], cg_tolerance=cfg["cg_tolerance"],
+                      cg_threshold=cfg["cg_threshold"], gravity=cfg["gravity"],
+                      vertex_mass=cfg["total_mass"] / mesh.n_nodes, fixed=mesh.fixed)
+
+
+def time_steps(torch, scene, steps, warmup):
+    stream = torch.cuda.ExternalStream(scene.stream)
+    scene.step(warmup)
+    scene.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    scene.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def time_add_dforce(torch, capi, scene, mesh, reps=20):
+    """Average duration of one addDForce call (element + gather kernels) on
+    the scene's stream, from CUDA events."""
+    fem = scene.fem
+    dt = torch.float32 if fem.precision == "mixed" else torch.float64
+    g = torch.Generator(device="cuda").manual_seed(0)
+    dx = torch.randn((mesh.n_nodes, 3), dtype=dt, device="cuda", generator=g) * 1e-3
+    df = torch.zeros((mesh.n_nodes, 3), dtype=dt, device="cuda")
+    stream = torch.cuda.ExternalStream(scene.stream)
+    torch.cuda.synchronize()
+    for _ in range(3):
+        fem.add_dforce(dx.data_ptr(), df.data_ptr(), -1e-3, stream=scene.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fem.add_dforce(dx.data_ptr(), df.data_ptr(), -1e-3, stream=scene.stream)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def adddforce_bytes(n_tets, n_nodes, p_e, p_v):
+    """Algorithmic bytes of one addDForce call: per element 16 B indices,
+    9 p_e rotation, 15 p_e (12 J + 3 K), 16 B of gather slots; per node
+    3 p_v read (dx) and 3 p_v written (df); 4 (N+1) B row pointers."""
+    return n_tets * (16 + 9 * p_e + 15 * p_e + 16) + n_nodes * (6 * p_v) + 4 * (n_nodes + 1)
+
+
+def e2e_steps(torch, capi, scene, mesh, steps):
+    """Through the C ABI with host buffers: each step uploads the state from
+    pinned host memory, steps once and reads the positions back."""
+    n3 = (mesh.n_nodes, 3)
+    xh = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
+    vh = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
+    x0, v0 = scene.state()
+    xh[:] = x0
+    vh[:] = v0
+    scene.set_state(xh, vh)
+    scene.step(1)
+    scene.state()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        scene.set_state(xh, vh)
+        scene.step(1)
+        xr, _ = scene.state()
+    t1 = time.perf_counter()
+    return t1 - t0, 2 * xh.nbytes, 2 * xh.nbytes  # set_state copies x and v; get_state reads x and v
+
+
+def cpu_baseline(mesh, cfg, threads, steps=1):
+    from oracle import pyoracle
+
+    pyoracle.set_threads(threads)
+    fem = pyoracle.OracleFEM(mesh.positions, mesh.tetrahedra, cfg["young"], cfg["poisson"], cfg["method"])
+    sc = pyoracle.OracleScene(fem, vertex_mass=cfg["total_mass"] / mesh.n_nodes, gravity=cfg["gravity"],
+                              fixed=mesh.fixed, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"],
+                              rayleigh_mass=cfg["rm"], cg_iterations=cfg["cg_iterations"],
+                              cg_tolerance=cfg["cg_tolerance"], cg_threshold=cfg["cg_threshold"])
+    t0 = time.perf_counter()
+    sc.step(steps)
+    dt = time.perf_counter() - t0
+    return mesh.n_tets * steps / dt, dt
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, cfg, rank):
+    if rank != 0:
+        return 0
+    mesh = make_mesh(cfg)
+    threads = host_threads()
+    from oracle import pyoracle
+
+    pyoracle.build()
+    pyoracle.set_threads(threads)
+    fem = pyoracle.OracleFEM(mesh.positions, mesh.tetrahedra, cfg["young"], cfg["poisson"], cfg["method"])
+    sc = pyoracle.OracleScene(fem, vertex_mass=cfg["total_mass"] / mesh.n_nodes, gravity=cfg["gravity"],
+                              fixed=mesh.fixed, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"],
+                              rayleigh_mass=cfg["rm"], cg_iterations=cfg["cg_iterations"],
+                              cg_tolerance=cfg["cg_tolerance"], cg_threshold=cfg["cg_threshold"])
+    sc.step(args.warmup)
+    t0 = time.perf_counter()
+    sc.step(args.steps)
+    dt = time.perf_counter() - t0
+    value = mesh.n_tets * args.steps / dt
+    line = {
+        "metric": "tet-steps/s", "value": value, "unit": "tet-steps/s", "impl": "reference", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(cfg, mesh),
+        "cpu_baseline": {"value": value, "unit": "tet-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps of the workload after {args.warmup} warm-up steps, "
+                                   "FP64 CPU oracle (restatement of the reference CPU path) with thread-local "
+                                   "force buffers"},
+        "e2e": {"value": value, "unit": "tet-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(cfg, mesh):
+    return {"workload": f"single cantilever beam {cfg['n'][0]}x{cfg['n'][1]}x{cfg['n'][2]} nodes, "
+                        f"{mesh.n_tets} tets, method={cfg['method']}, CG {cfg['cg_iterations']}/"
+                        f"{cfg['cg_tolerance']:g}",
+            "n_nodes": mesh.n_nodes, "n_tets": mesh.n_tets, "method": cfg["method"],
+            "cg_iterations": cfg["cg_iterations"], "cg_tolerance": cfg["cg_tolerance"], "dt": cfg["dt"],
+            "l2": "inputs larger than L2 (element data ~0.6 GB FP32, 1.2 GB FP64 vs 129 MB L2)",
+            "parallelism": "replicas"}
+
+
+def main():
+    args = parse()
+    cfg = dict(CONFIG)
+    if args.n:
+        cfg["n"] = tuple(int(v) for v in args.n.split(","))
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, cfg, rank)
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from sofa_gb300 import build, capi
+
+    build.build()
+    capi.load()
+    mesh = make_mesh(cfg)
+    E, N = mesh.n_tets, mesh.n_nodes
+    hbm_peak, peak_kind = peaks()
+
+    mixed = make_scene(capi, mesh, cfg, "mixed")
+    mixed.step(1)
+    mixed.sync()
+    if args.profile:
+        t = time_steps(torch, mixed, args.steps, args.warmup)
+        print(json.dumps({"profile_run": True, "n_tets": E, "ms_per_step": t / max(args.steps, 1) * 1e3}))
+        return 0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_mixed = time_steps(torch, mixed, args.steps, args.warmup)
+    iters_mixed, res_mixed = mixed.sync()
+    t_all = torch.tensor([t_mixed], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_all, op=torch.distributed.ReduceOp.MAX)
+    t_max = float(t_all.item())
+    value = world * E * args.steps / t_max
+
+    # addDForce roofline on the mixed path
+    t_df = time_add_dforce(torch, capi, mixed, mesh)
+    alg = adddforce_bytes(E, N, 4, 4)
+    achieved = alg / t_df / 1e9
+
+    # end to end through the C ABI with host buffers
+    e2e_t, h2d, d2h = e2e_steps(torch, capi, mixed, mesh, max(2, min(args.steps, 10)))
+    e2e_steps_n = max(2, min(args.steps, 10))
+    e2e_value = world * E * e2e_steps_n / e2e_t
+
+    # plain FP64 path (reference rounding and FMA variants)
+    plain = {}
+    for prec in ("fp64_fma", "fp64"):
+        sc = make_scene(capi, mesh, cfg, prec)
+        sc.step(1)
+        sc.sync()
+        k = max(2, min(args.steps, 5))
+        t = time_steps(torch, sc, k, 1)
+        plain[prec] = {"tet_steps_per_s": E * k / t, "ms_per_step": t / k * 1e3}
+        sc.close()
+
+    # position error of mixed vs FP64 after error-steps steps
+    err = None
+    if not args.no_error and rank == 0:
+        ref = make_scene(capi, mesh, cfg, "fp64_fma")
+        ref.step(args.error_steps)
+        xr, _ = ref.state()
+        ref.close()
+        mx = make_scene(capi, mesh, cfg, "mixed")
+        mx.step(args.error_steps)
+        xm, _ = mx.state()
+        mx.close()
+        d = np.linalg.norm(xr - mesh.positions)
+        err = {"steps": args.error_steps, "rel_l2_position": float(np.linalg.norm(xm - xr) / np.linalg.norm(xr)),
+               "rel_l2_displacement": float(np.linalg.norm(xm - xr) / d) if d > 0 else None,
+               "target_uses": "rel_l2_position", "reference": "GPU FP64 (FMA) run of the same workload"}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        threads = host_threads()
+        v, dt = cpu_baseline(mesh, cfg, threads, steps=1)
+        cpu = {"value": v, "unit": "tet-steps/s", "cores": threads, "kind": "port",
+               "sample": f"1 full step of the workload ({E} tets, CG {cfg['cg_iterations']}), FP64 CPU oracle "
+                         f"with {threads} threads, {dt:.1f} s"}
+
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("adddforce_mixed_bytes_per_call")
+        except Exception:
+            traffic = None
+
+    launches_per_step = 5 + 3 * cfg["cg_iterations"]
+    line = {
+        "metric": "tet-steps/s", "value": value, "unit": "tet-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 dots and state)", "data": "synthetic",
+        "config": workload_config(cfg, mesh),
+        "cg_iterations_last_step": iters_mixed, "cg_residual_last_step": res_mixed,
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64": value / max(p["tet_steps_per_s"] for p in plain.values()),
+        "position_error": err,
+        "roofline": {"kernel": "addDForce (element + gather kernels, mixed)", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg,
+                     "avg_launch_ms": t_df * 1e3},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "tet-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,179 @@
+/*
+ * sofa_gb300.h -- C ABI of the GB300-native implicit tetrahedral-FEM step.
+ *
+ * The library replaces, for one GPU, the hot path of SOFA's soft-body step:
+ * TetrahedronFEMForceField (method small/large/polar) integrated by
+ * EulerImplicitSolver with a matrix-free CGLinearSolver, UniformMass (or a
+ * lumped per-node mass) and FixedProjectiveConstraint. Reference files are
+ * cited by their path inside the SOFA source tree (v26.06).
+ *
+ * Conventions (shared by every entry point):
+ *  - Every function returns an int status: SGB_OK (0) or a negative
+ *    SGB_ERR_* code; sgb_last_error() gives a message for the calling
+ *    thread. Nothing aborts the process. (Error style of
+ *    applications/projects/SofaPhysicsAPI/src/SofaPhysicsAPI/SofaPhysicsAPI.h:55-59.)
+ *  - Node vectors are arrays of xyz triples (Vec3 AoS, as
+ *    Sofa/framework/DefaultType/src/sofa/defaulttype/VecTypes.h).
+ *    Tetrahedra are 4 int32 node indices each.
+ *  - Pointers named *_dev are device pointers; *_host are host pointers.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = the handle's own
+ *    stream). Calls are stream-ordered and return without synchronising
+ *    unless stated.
+ *  - A handle may be used by one host thread at a time.
+ */
+#ifndef SOFA_GB300_H
+#define SOFA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGB_OK 0
+#define SGB_ERR_INVALID_ARGUMENT -1
+#define SGB_ERR_CUDA -2
+#define SGB_ERR_OUT_OF_MEMORY -3
+#define SGB_ERR_NOT_SUPPORTED -4
+#define SGB_ERR_NUMERICAL -5   /* a non-finite value was met in the CG solve */
+#define SGB_ERR_BUDGET -6      /* admission refused: HBM budget exceeded */
+#define SGB_ERR_NOT_FOUND -7
+
+/* TetrahedronFEMForceField Data "method"
+ * (TetrahedronFEMForceField.inl:45): small, large (QR frame), polar. */
+#define SGB_METHOD_SMALL 0
+#define SGB_METHOD_LARGE 1
+#define SGB_METHOD_POLAR 2
+
+/* Precision of the element math and solver vectors.
+ *  FP64       FP64 everywhere, rounding like the reference CPU code (no FMA,
+ *             the reference's term and summation order per node).
+ *  MIXED      FP32 rotation, stiffness apply and vector updates; FP64 dot
+ *             products, norms and x/v state accumulation.
+ *  FP64_FMA   FP64 with fused multiply-add (faster, within rounding). */
+#define SGB_PRECISION_FP64 0
+#define SGB_PRECISION_MIXED 1
+#define SGB_PRECISION_FP64_FMA 2
+
+const char* sgb_last_error(void);
+const char* sgb_version(void);
+
+/* ------------------------------------------------------------------ */
+/* TetrahedronFEMForceField                                            */
+/* ------------------------------------------------------------------ */
+typedef struct sgb_tfem sgb_tfem_t;
+
+/* Creates the force field on a mesh and runs its init/reinit on the GPU:
+ * per-element material stiffness (TetrahedronFEMForceField.inl:256-291),
+ * strain-displacement matrix (:134-209) and initial rotation plus rotated
+ * rest coordinates (initLarge :835-868, initPolar :993-1023, initSmall
+ * :526-532); builds the node->(element,corner) gather table.
+ * young/poisson have 1 or n_tets entries (entry e, else entry 0, as
+ * BaseLinearElasticityFEMForceField.inl:114-132); values out of range
+ * (E < 0, nu outside [0, 0.5)) are replaced by 5000 / 0.45 with a warning
+ * readable through sgb_last_error(), as
+ * BaseLinearElasticityFEMForceField.inl:53-85 does. local_stiffness_factor
+ * may be NULL (n_lsf = 0). Replaces the reference's reinit path feeding
+ * TetrahedronFEMForceFieldCuda3f_addForce
+ * (applications/plugins/SofaCUDA/Component/src/SofaCUDA/component/
+ * solidmechanics/fem/elastic/CudaTetrahedronFEMForceField.cu:39-40). */
+int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_host, int n_tets,
+                    const int32_t* tetrahedra_host, const double* young, int n_young, const double* poisson,
+                    int n_poisson, const double* local_stiffness_factor, int n_lsf, int method, int precision);
+int sgb_tfem_destroy(sgb_tfem_t* fem);
+
+/* addForce (TetrahedronFEMForceField.inl:1548-1604; SofaCUDA
+ * TetrahedronFEMForceFieldCuda3d_addForce, CudaTetrahedronFEMForceField.cu:49):
+ * f += internal forces at positions x; updates the element rotations used by
+ * the next sgb_tfem_add_dforce. x is FP64 for every precision; f is FP64
+ * (FP64 handles) -- use sgb_tfem_add_force_f32 for MIXED handles. */
+int sgb_tfem_add_force(sgb_tfem_t* fem, const double* x_dev, double* f_dev, void* stream);
+int sgb_tfem_add_force_f32(sgb_tfem_t* fem, const double* x_dev, float* f_dev, void* stream);
+
+/* addDForce (TetrahedronFEMForceField.inl:1606-1636; SofaCUDA
+ * TetrahedronFEMForceFieldCuda3d_addDForce, CudaTetrahedronFEMForceField.cu:50):
+ * df += -kfactor K dx with the rotations of the last add_force. kfactor is
+ * mparams->kFactorIncludingRayleighDamping(rayleighStiffness). */
+int sgb_tfem_add_dforce(sgb_tfem_t* fem, const double* dx_dev, double* df_dev, double kfactor, void* stream);
+int sgb_tfem_add_dforce_f32(sgb_tfem_t* fem, const float* dx_dev, float* df_dev, float kfactor, void* stream);
+
+/* Per-element rotations in the reference's convention: rotations[e] = R^T,
+ * 9 doubles row-major per element (TetrahedronFEMForceField.h
+ * getActualTetraRotation / getInitialTetraRotation). Synchronous. */
+int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* initial_rotations_host);
+
+/* Sizes and device footprint of the force field. */
+int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method, int* precision,
+                  size_t* device_bytes);
+
+/* ------------------------------------------------------------------ */
+/* Scene: MechanicalObject + mass + FEM + fixed constraint, advanced by */
+/* EulerImplicitSolver + CGLinearSolver<GraphScattered>.                */
+/* ------------------------------------------------------------------ */
+typedef struct sgb_scene sgb_scene_t;
+
+typedef struct sgb_scene_params {
+    /* EulerImplicitSolver Data (EulerImplicitSolver.cpp:40-51) */
+    double dt;
+    double rayleigh_stiffness;
+    double rayleigh_mass;
+    double vdamping;
+    /* CGLinearSolver Data (CGLinearSolver.inl:34-46): iterations, tolerance, threshold */
+    int cg_iterations;
+    double cg_tolerance;
+    double cg_threshold;
+    /* context gravity */
+    double gravity[3];
+    /* UniformMass vertexMass (UniformMass.inl:153-340); ignored when node_masses is given */
+    double vertex_mass;
+    /* optional lumped per-node masses (DiagonalMass-style), host, n_nodes entries, or NULL */
+    const double* node_masses_host;
+    /* FixedProjectiveConstraint indices / fixAll (FixedProjectiveConstraint.inl:39-48);
+     * out-of-range indices are dropped, as checkIndices (:130-160) does */
+    const int32_t* fixed_host;
+    int n_fixed;
+    int fix_all;
+    /* 1: the mass component precedes the force field in the node (its
+     * forces are accumulated first), 0: after it */
+    int mass_first;
+    /* 1: dot products summed serially in node order, as
+     * MechanicalObject::vDot does (bit-identical to the reference with
+     * SGB_PRECISION_FP64; slow on large meshes) */
+    int serial_dots;
+} sgb_scene_params;
+
+/* Fills params with the reference Data defaults: dt 0.01, Rayleigh 0, CG
+ * 25 / 1e-5 / 1e-5, gravity (0,-9.81,0), vertex mass 1, mass first. */
+void sgb_scene_params_default(sgb_scene_params* params);
+
+/* Creates a scene on a force field; the scene takes ownership of `fem`.
+ * Positions start at the rest positions, velocities at zero. */
+int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params* params);
+int sgb_scene_destroy(sgb_scene_t* scene);
+
+/* Advances n_steps implicit Euler steps (DefaultAnimationLoop::step,
+ * Sofa/framework/Simulation/Core/src/sofa/simulation/DefaultAnimationLoop.cpp:273-325).
+ * Stream-ordered; the step is recorded once as a CUDA graph and replayed. */
+int sgb_scene_step(sgb_scene_t* scene, int n_steps);
+
+/* Waits for the scene's stream and reports the last CG solve: iterations
+ * run, last relative residual |r|/|b|, and SGB_ERR_NUMERICAL if a
+ * non-finite value was met. */
+int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual);
+
+/* State access (FP64). get_* synchronise; set_* are stream-ordered. */
+int sgb_scene_get_state(sgb_scene_t* scene, double* x_host, double* v_host);
+int sgb_scene_set_state(sgb_scene_t* scene, const double* x_host, const double* v_host);
+/* MechanicalObject externalForce (accumulateForce, MechanicalObject.inl:1357-1376). */
+int sgb_scene_set_external_force(sgb_scene_t* scene, const double* fext_host);
+/* Device pointers of the FP64 state (n_nodes x 3), valid for the scene's lifetime. */
+int sgb_scene_state_device(sgb_scene_t* scene, double** x_dev, double** v_dev);
+/* The scene's stream (cudaStream_t as void*). */
+void* sgb_scene_stream(sgb_scene_t* scene);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SOFA_GB300_H */

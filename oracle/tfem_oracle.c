@@ -314,12 +314,13 @@ typedef struct orc_fem {
     int tl_threads;
 } orc_fem;
 
-/* BaseLinearElasticityFEMForceField::getYoungModulusInElement /
- * getPoissonRatioInElement (BaseLinearElasticityFEMForceField.inl:114-144):
- * the per-element entry when the vector is long enough, else entry 0. */
+/* BaseLinearElasticityFEMForceField::getVecRealInElement
+ * (BaseLinearElasticityFEMForceField.inl:114-144): entry e when the vector is
+ * longer than e, else entry 0. */
 static double per_element(const double* v, int n, int e, int n_tets)
 {
-    return (n >= n_tets && n > e) ? v[e] : v[0];
+    (void)n_tets;
+    return (n > e) ? v[e] : v[0];
 }
 
 orc_fem* orc_fem_create(int n_nodes, const double* rest, int n_tets, const int32_t* tets,

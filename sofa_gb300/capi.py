@@ -1,0 +1,280 @@
+"""ctypes binding of libsofa_gb300.so (the C ABI declared in include/sofa_gb300.h).
+
+This is plumbing for Python callers (tests, benchmarks, notebooks): every
+numeric operation runs in the CUDA library. Loading fails loudly when the
+library has not been built -- there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsofa_gb300.so")
+
+SGB_OK = 0
+ERRORS = {
+    -1: "invalid argument",
+    -2: "CUDA error",
+    -3: "out of device memory",
+    -4: "not supported",
+    -5: "non-finite value in the CG solve",
+    -6: "HBM budget exceeded",
+    -7: "not found",
+}
+METHODS = {"small": 0, "large": 1, "polar": 2}
+PRECISIONS = {"fp64": 0, "mixed": 1, "fp64_fma": 2}
+
+
+class SgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SceneParams(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_double),
+        ("rayleigh_stiffness", ctypes.c_double),
+        ("rayleigh_mass", ctypes.c_double),
+        ("vdamping", ctypes.c_double),
+        ("cg_iterations", ctypes.c_int),
+        ("cg_tolerance", ctypes.c_double),
+        ("cg_threshold", ctypes.c_double),
+        ("gravity", ctypes.c_double * 3),
+        ("vertex_mass", ctypes.c_double),
+        ("node_masses_host", ctypes.POINTER(ctypes.c_double)),
+        ("fixed_host", ctypes.POINTER(ctypes.c_int32)),
+        ("n_fixed", ctypes.c_int),
+        ("fix_all", ctypes.c_int),
+        ("mass_first", ctypes.c_int),
+        ("serial_dots", ctypes.c_int),
+    ]
+
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+
+def load():
+    """Load the CUDA library (it must have been built with sofa_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m sofa_gb300.build` "
+                          "(this package has no CPU implementation)")
+    lib = ctypes.CDLL(LIB_PATH)
+    c_int, c_double, c_float = ctypes.c_int, ctypes.c_double, ctypes.c_float
+    sig = {
+        "sgb_last_error": (ctypes.c_char_p, []),
+        "sgb_version": (ctypes.c_char_p, []),
+        "sgb_tfem_create": (c_int, [ctypes.POINTER(_vp), c_int, _dp, c_int, _ip, _dp, c_int, _dp, c_int, _dp, c_int,
+                                    c_int, c_int]),
+        "sgb_tfem_destroy": (c_int, [_vp]),
+        "sgb_tfem_add_force": (c_int, [_vp, _vp, _vp, _vp]),
+        "sgb_tfem_add_force_f32": (c_int, [_vp, _vp, _vp, _vp]),
+        "sgb_tfem_add_dforce": (c_int, [_vp, _vp, _vp, c_double, _vp]),
+        "sgb_tfem_add_dforce_f32": (c_int, [_vp, _vp, _vp, c_float, _vp]),
+        "sgb_tfem_get_rotations": (c_int, [_vp, _dp, _dp]),
+        "sgb_tfem_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                  ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_size_t)]),
+        "sgb_scene_params_default": (None, [ctypes.POINTER(SceneParams)]),
+        "sgb_scene_create": (c_int, [ctypes.POINTER(_vp), _vp, ctypes.POINTER(SceneParams)]),
+        "sgb_scene_destroy": (c_int, [_vp]),
+        "sgb_scene_step": (c_int, [_vp, c_int]),
+        "sgb_scene_sync": (c_int, [_vp, ctypes.POINTER(c_int), _dp]),
+        "sgb_scene_get_state": (c_int, [_vp, _dp, _dp]),
+        "sgb_scene_set_state": (c_int, [_vp, _dp, _dp]),
+        "sgb_scene_set_external_force": (c_int, [_vp, _dp]),
+        "sgb_scene_state_device": (c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+        "sgb_scene_stream": (_vp, [_vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error():
+    return load().sgb_last_error().decode()
+
+
+def check(rc):
+    if rc != SGB_OK:
+        raise SgbError(rc, last_error())
+    return rc
+
+
+def _d(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_ip)
+
+
+class TetrahedronFEM:
+    """Handle of sgb_tfem_t: a TetrahedronFEMForceField on one mesh, on the GPU."""
+
+    def __init__(self, rest_positions, tetrahedra, young=5000.0, poisson=0.45, method="large", precision="fp64",
+                 local_stiffness_factor=None):
+        lib = load()
+        pos, ppos = _d(np.asarray(rest_positions).reshape(-1, 3))
+        tets, ptets = _i(np.asarray(tetrahedra).reshape(-1, 4))
+        y, py = _d(np.atleast_1d(young))
+        nu, pnu = _d(np.atleast_1d(poisson))
+        if local_stiffness_factor is not None:
+            lsf, plsf = _d(np.atleast_1d(local_stiffness_factor))
+            nl = lsf.size
+        else:
+            plsf, nl = _dp(), 0
+        h = _vp()
+        check(lib.sgb_tfem_create(ctypes.byref(h), pos.shape[0], ppos, tets.shape[0], ptets, py, y.size, pnu,
+                                  nu.size, plsf, nl, METHODS[method], PRECISIONS[precision]))
+        self.warnings = last_error()
+        self._h = h
+        self.n_nodes = pos.shape[0]
+        self.n_tets = tets.shape[0]
+        self.method = method
+        self.precision = precision
+        self._owned = True
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_owned", False) and self._h:
+            load().sgb_tfem_destroy(self._h)
+        self._h = None
+        self._owned = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_force(self, x_dev, f_dev, stream=None):
+        """f += F(x); device pointers (ints). f is FP64 (fp64 handles) or FP32 (mixed)."""
+        lib = load()
+        if self.precision == "mixed":
+            check(lib.sgb_tfem_add_force_f32(self._h, x_dev, f_dev, stream))
+        else:
+            check(lib.sgb_tfem_add_force(self._h, x_dev, f_dev, stream))
+
+    def add_dforce(self, dx_dev, df_dev, kfactor, stream=None):
+        """df += -kfactor K dx; device pointers (ints)."""
+        lib = load()
+        if self.precision == "mixed":
+            check(lib.sgb_tfem_add_dforce_f32(self._h, dx_dev, df_dev, float(kfactor), stream))
+        else:
+            check(lib.sgb_tfem_add_dforce(self._h, dx_dev, df_dev, float(kfactor), stream))
+
+    def rotations(self):
+        r = np.zeros((self.n_tets, 3, 3))
+        r0 = np.zeros((self.n_tets, 3, 3))
+        check(load().sgb_tfem_get_rotations(self._h, r.ctypes.data_as(_dp), r0.ctypes.data_as(_dp)))
+        return r, r0
+
+    def device_bytes(self):
+        b = ctypes.c_size_t()
+        check(load().sgb_tfem_info(self._h, None, None, None, None, ctypes.byref(b)))
+        return b.value
+
+
+class Scene:
+    """Handle of sgb_scene_t: mesh + mass + FEM + fixed nodes advanced by
+    EulerImplicitSolver / CGLinearSolver on the GPU."""
+
+    def __init__(self, fem: TetrahedronFEM, dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0,
+                 cg_iterations=25, cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0),
+                 vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
+                 serial_dots=False):
+        lib = load()
+        p = SceneParams()
+        lib.sgb_scene_params_default(ctypes.byref(p))
+        p.dt = dt
+        p.rayleigh_stiffness = rayleigh_stiffness
+        p.rayleigh_mass = rayleigh_mass
+        p.vdamping = vdamping
+        p.cg_iterations = int(cg_iterations)
+        p.cg_tolerance = cg_tolerance
+        p.cg_threshold = cg_threshold
+        for k in range(3):
+            p.gravity[k] = float(gravity[k])
+        if vertex_mass is None:
+            # UniformMass: vertexMass = totalMass / N (UniformMass.inl:337)
+            vertex_mass = (1.0 if total_mass is None else float(total_mass)) / fem.n_nodes
+        p.vertex_mass = float(vertex_mass)
+        self._nm = None
+        if node_masses is not None:
+            self._nm, p.node_masses_host = _d(node_masses)
+        self._fixed, p.fixed_host = _i(np.asarray(fixed, dtype=np.int32).reshape(-1) if len(fixed) else
+                                       np.zeros(1, np.int32))
+        p.n_fixed = len(fixed)
+        p.fix_all = int(fix_all)
+        p.mass_first = int(mass_first)
+        p.serial_dots = int(serial_dots)
+        h = _vp()
+        check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
+        fem._owned = False  # the scene owns the force field now
+        self.fem = fem
+        self._h = h
+        self.n_nodes = fem.n_nodes
+        self.params = p
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().sgb_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n=1):
+        check(load().sgb_scene_step(self._h, int(n)))
+
+    def sync(self):
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        check(load().sgb_scene_sync(self._h, ctypes.byref(it), ctypes.byref(res)))
+        return it.value, res.value
+
+    def state(self):
+        x = np.zeros((self.n_nodes, 3))
+        v = np.zeros((self.n_nodes, 3))
+        check(load().sgb_scene_get_state(self._h, x.ctypes.data_as(_dp), v.ctypes.data_as(_dp)))
+        return x, v
+
+    def set_state(self, x=None, v=None):
+        xa, px = _d(np.asarray(x).reshape(-1, 3)) if x is not None else (None, _dp())
+        va, pv = _d(np.asarray(v).reshape(-1, 3)) if v is not None else (None, _dp())
+        check(load().sgb_scene_set_state(self._h, px, pv))
+
+    def set_external_force(self, fext):
+        a, p = _d(np.asarray(fext).reshape(-1, 3))
+        check(load().sgb_scene_set_external_force(self._h, p))
+
+    def state_device(self):
+        x = _vp()
+        v = _vp()
+        check(load().sgb_scene_state_device(self._h, ctypes.byref(x), ctypes.byref(v)))
+        return x.value, v.value
+
+    @property
+    def stream(self):
+        return load().sgb_scene_stream(self._h)

@@ -1,0 +1,570 @@
+// C ABI of the GB300 tetrahedral-FEM library: handle management, input
+// validation, the node->slot gather table, scene orchestration and CUDA
+// graph capture. Kernels live in tfem_impl.cuh (one instance per precision).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sofa_gb300.h"
+#include "sgb_internal.h"
+#include "variants.h"
+
+using namespace sgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return (e == cudaErrorMemoryAllocation) ? SGB_ERR_OUT_OF_MEMORY : SGB_ERR_CUDA;
+}
+
+#define SGB_CUDA_TRY(expr)                                   \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return cuda_fail(_e, #expr);  \
+    } while (0)
+
+template <typename T>
+int dev_alloc(T** p, size_t count, size_t* acc)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if (acc) *acc += sizeof(T) * count;
+    return SGB_OK;
+}
+
+int dev_alloc_bytes(void** p, size_t bytes, size_t* acc)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if (acc) *acc += bytes;
+    return SGB_OK;
+}
+
+}  // namespace
+
+struct sgb_tfem {
+    TfemMesh m;
+    const VariantOps* ops = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string warnings;
+};
+
+struct sgb_scene {
+    Scene s;
+    sgb_tfem* fem = nullptr;
+    const VariantOps* ops = nullptr;
+    double* dot_terms = nullptr;
+    int serial_dots = 0;
+    int mass_first = 1;
+};
+
+namespace sgb {
+const VariantOps* variant_for(int precision)
+{
+    switch (precision) {
+        case SGB_PRECISION_FP64: return &ops_fp64_exact;
+        case SGB_PRECISION_MIXED: return &ops_mixed;
+        case SGB_PRECISION_FP64_FMA: return &ops_fp64_fast;
+        default: return nullptr;
+    }
+}
+}  // namespace sgb
+
+static void free_mesh(TfemMesh& m)
+{
+    cudaFree(m.tets);
+    cudaFree(m.rot);
+    cudaFree(m.K);
+    cudaFree(m.J);
+    cudaFree(m.rest);
+    cudaFree(m.R0);
+    cudaFree(m.rest_pos);
+    cudaFree(m.rowptr);
+    cudaFree(m.slots);
+    cudaFree(m.eforce);
+    m = TfemMesh();
+}
+
+// Node -> (element*4 + corner) table, each row in increasing slot order so
+// a node sums its element terms in the reference's element-loop order.
+static void build_csr(int N, int E, const int32_t* tets, std::vector<int>& rowptr, std::vector<int>& slots,
+                      int& max_valence)
+{
+    rowptr.assign((size_t)N + 1, 0);
+    for (size_t i = 0; i < (size_t)E * 4; ++i) rowptr[(size_t)tets[i] + 1]++;
+    max_valence = 0;
+    for (int n = 0; n < N; ++n) {
+        max_valence = std::max(max_valence, rowptr[(size_t)n + 1]);
+        rowptr[(size_t)n + 1] += rowptr[n];
+    }
+    slots.resize((size_t)E * 4);
+    std::vector<int> pos(rowptr.begin(), rowptr.end() - 1);
+    for (size_t i = 0; i < (size_t)E * 4; ++i) slots[(size_t)pos[tets[i]]++] = (int)i;
+}
+
+extern "C" {
+
+const char* sgb_last_error(void) { return g_last_error.c_str(); }
+
+const char* sgb_version(void) { return "sofa_gb300 0.1 (sm_103a)"; }
+
+int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_host, int n_tets,
+                    const int32_t* tetrahedra_host, const double* young, int n_young, const double* poisson,
+                    int n_poisson, const double* local_stiffness_factor, int n_lsf, int method, int precision)
+{
+    if (!out) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: out is NULL");
+    *out = nullptr;
+    if (n_nodes <= 0 || !rest_positions_host)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: the mesh needs at least one node");
+    if (n_tets < 0 || (n_tets > 0 && !tetrahedra_host))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: invalid tetrahedra");
+    if (method < SGB_METHOD_SMALL || method > SGB_METHOD_POLAR)
+        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_tfem_create: method must be small, large or polar (svd is not supported)");
+    const VariantOps* ops = variant_for(precision);
+    if (!ops) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: unknown precision");
+    if ((size_t)n_tets * 12 > (size_t)0x7fffffff)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: too many tetrahedra for one mesh");
+    for (size_t i = 0; i < (size_t)n_tets * 4; ++i)
+        if (tetrahedra_host[i] < 0 || tetrahedra_host[i] >= n_nodes)
+            return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: tetrahedron node index out of range");
+    for (size_t i = 0; i < (size_t)n_nodes * 3; ++i)
+        if (!std::isfinite(rest_positions_host[i]))
+            return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: non-finite rest position");
+    if (n_lsf < 0 || (n_lsf > 0 && !local_stiffness_factor))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: invalid localStiffnessFactor");
+
+    std::string warn;
+    // BaseLinearElasticityFEMForceField::checkYoungModulus / checkPoissonRatio
+    std::vector<double> E_h, nu_h;
+    if (young && n_young > 0) E_h.assign(young, young + n_young);
+    if (poisson && n_poisson > 0) nu_h.assign(poisson, poisson + n_poisson);
+    if (E_h.empty()) {
+        E_h.push_back(5000.0);
+        warn += "youngModulus empty, using 5000; ";
+    }
+    if (nu_h.empty()) {
+        nu_h.push_back(0.45);
+        warn += "poissonRatio empty, using 0.45; ";
+    }
+    for (double& y : E_h)
+        if (!(y >= 0)) {
+            warn += "negative youngModulus replaced by 5000; ";
+            y = 5000.0;
+        }
+    for (double& p : nu_h)
+        if (!(p >= 0 && p < 0.5)) {
+            warn += "poissonRatio outside [0,0.5) replaced by 0.45; ";
+            p = 0.45;
+        }
+
+    sgb_tfem* h = new sgb_tfem();
+    TfemMesh& m = h->m;
+    h->ops = ops;
+    m.n_nodes = n_nodes;
+    m.n_tets = n_tets;
+    m.method = method;
+    m.precision = precision;
+    m.real_size = ops->real_size;
+    m.young_h = E_h;
+    m.poisson_h = nu_h;
+    int rc = SGB_OK;
+    std::vector<int> rowptr, slots;
+    build_csr(n_nodes, n_tets, tetrahedra_host, rowptr, slots, m.max_valence);
+    const size_t rs = ops->real_size, E = (size_t)n_tets;
+    size_t* acc = &m.device_bytes;
+    double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr, *d_vol = nullptr;
+    cudaError_t ce;
+    ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        rc = cuda_fail(ce, "cudaStreamCreate");
+        goto fail_out;
+    }
+    if ((rc = dev_alloc(&m.tets, E, acc)) || (rc = dev_alloc_bytes(&m.rot, rs * 9 * E, acc)) ||
+        (rc = dev_alloc_bytes(&m.R0, rs * 9 * E, acc)) || (rc = dev_alloc_bytes(&m.K, rs * 3 * E, acc)) ||
+        (rc = dev_alloc_bytes(&m.J, rs * 12 * E, acc)) || (rc = dev_alloc_bytes(&m.rest, rs * 12 * E, acc)) ||
+        (rc = dev_alloc_bytes(&m.eforce, rs * 12 * E, acc)) || (rc = dev_alloc(&m.rest_pos, 3 * (size_t)n_nodes, acc)) ||
+        (rc = dev_alloc(&m.rowptr, (size_t)n_nodes + 1, acc)) || (rc = dev_alloc(&m.slots, 4 * E, acc)))
+        goto fail_out;
+    if ((rc = dev_alloc(&d_y, E_h.size(), nullptr)) || (rc = dev_alloc(&d_p, nu_h.size(), nullptr)) ||
+        (rc = dev_alloc(&d_l, (size_t)std::max(n_lsf, 1), nullptr)) || (rc = dev_alloc(&d_vol, E, nullptr)))
+        goto fail_out;
+    if ((ce = cudaMemcpyAsync(m.tets, tetrahedra_host, sizeof(int4) * E, cudaMemcpyHostToDevice, h->stream)) ||
+        (ce = cudaMemcpyAsync(m.rest_pos, rest_positions_host, sizeof(double) * 3 * n_nodes, cudaMemcpyHostToDevice,
+                              h->stream)) ||
+        (ce = cudaMemcpyAsync(m.rowptr, rowptr.data(), sizeof(int) * rowptr.size(), cudaMemcpyHostToDevice,
+                              h->stream)) ||
+        (!slots.empty() && (ce = cudaMemcpyAsync(m.slots, slots.data(), sizeof(int) * slots.size(),
+                                                 cudaMemcpyHostToDevice, h->stream))) ||
+        (ce = cudaMemcpyAsync(d_y, E_h.data(), sizeof(double) * E_h.size(), cudaMemcpyHostToDevice, h->stream)) ||
+        (ce = cudaMemcpyAsync(d_p, nu_h.data(), sizeof(double) * nu_h.size(), cudaMemcpyHostToDevice, h->stream))) {
+        rc = cuda_fail(ce, "cudaMemcpyAsync");
+        goto fail_out;
+    }
+    if (n_lsf > 0 && (ce = cudaMemcpyAsync(d_l, local_stiffness_factor, sizeof(double) * n_lsf,
+                                           cudaMemcpyHostToDevice, h->stream))) {
+        rc = cuda_fail(ce, "cudaMemcpyAsync");
+        goto fail_out;
+    }
+    ops->init(&m, d_y, (int)E_h.size(), d_p, (int)nu_h.size(), d_l, n_lsf, d_vol, h->stream);
+    if ((ce = cudaGetLastError()) != cudaSuccess) {
+        rc = cuda_fail(ce, "init kernel launch");
+        goto fail_out;
+    }
+    {
+        std::vector<double> vol(E);
+        if (E) {
+            ce = cudaMemcpyAsync(vol.data(), d_vol, sizeof(double) * E, cudaMemcpyDeviceToHost, h->stream);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+            if (ce != cudaSuccess) {
+                rc = cuda_fail(ce, "init");
+                goto fail_out;
+            }
+        }
+        size_t degenerate = 0;
+        double total = 0.0;
+        for (double v : vol) {
+            total += v;
+            if (!(v > 0)) degenerate++;
+        }
+        m.rest_volume = total;
+        if (degenerate) warn += std::to_string(degenerate) + " degenerate (zero-volume) tetrahedra; ";
+    }
+    cudaFree(d_y);
+    cudaFree(d_p);
+    cudaFree(d_l);
+    cudaFree(d_vol);
+    h->warnings = warn;
+    g_last_error = warn;
+    *out = h;
+    return SGB_OK;
+fail_out:
+    cudaFree(d_y);
+    cudaFree(d_p);
+    cudaFree(d_l);
+    cudaFree(d_vol);
+    free_mesh(m);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return rc;
+}
+
+int sgb_tfem_destroy(sgb_tfem_t* fem)
+{
+    if (!fem) return SGB_OK;
+    cudaStreamSynchronize(fem->stream);
+    free_mesh(fem->m);
+    cudaStreamDestroy(fem->stream);
+    delete fem;
+    return SGB_OK;
+}
+
+static cudaStream_t pick(sgb_tfem_t* fem, void* stream)
+{
+    return stream ? (cudaStream_t)stream : fem->stream;
+}
+
+int sgb_tfem_add_force(sgb_tfem_t* fem, const double* x_dev, double* f_dev, void* stream)
+{
+    if (!fem || !x_dev || !f_dev) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_force: NULL argument");
+    if (fem->m.real_size != sizeof(double))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_force: MIXED handle, use sgb_tfem_add_force_f32");
+    fem->ops->add_force(&fem->m, x_dev, f_dev, pick(fem, stream));
+    SGB_CUDA_TRY(cudaGetLastError());
+    return SGB_OK;
+}
+
+int sgb_tfem_add_force_f32(sgb_tfem_t* fem, const double* x_dev, float* f_dev, void* stream)
+{
+    if (!fem || !x_dev || !f_dev) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_force_f32: NULL argument");
+    if (fem->m.real_size != sizeof(float))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_force_f32: FP64 handle, use sgb_tfem_add_force");
+    fem->ops->add_force(&fem->m, x_dev, f_dev, pick(fem, stream));
+    SGB_CUDA_TRY(cudaGetLastError());
+    return SGB_OK;
+}
+
+int sgb_tfem_add_dforce(sgb_tfem_t* fem, const double* dx_dev, double* df_dev, double kfactor, void* stream)
+{
+    if (!fem || !dx_dev || !df_dev) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_dforce: NULL argument");
+    if (fem->m.real_size != sizeof(double))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_dforce: MIXED handle, use sgb_tfem_add_dforce_f32");
+    fem->ops->add_dforce(&fem->m, dx_dev, df_dev, kfactor, pick(fem, stream));
+    SGB_CUDA_TRY(cudaGetLastError());
+    return SGB_OK;
+}
+
+int sgb_tfem_add_dforce_f32(sgb_tfem_t* fem, const float* dx_dev, float* df_dev, float kfactor, void* stream)
+{
+    if (!fem || !dx_dev || !df_dev) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_dforce_f32: NULL argument");
+    if (fem->m.real_size != sizeof(float))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_dforce_f32: FP64 handle, use sgb_tfem_add_dforce");
+    fem->ops->add_dforce(&fem->m, dx_dev, df_dev, (double)kfactor, pick(fem, stream));
+    SGB_CUDA_TRY(cudaGetLastError());
+    return SGB_OK;
+}
+
+int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* initial_rotations_host)
+{
+    if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_get_rotations: NULL handle");
+    const size_t E = (size_t)fem->m.n_tets, rs = fem->m.real_size;
+    std::vector<unsigned char> buf(rs * 9 * std::max<size_t>(E, 1));
+    void* src[2] = {fem->m.rot, fem->m.R0};
+    double* dst[2] = {rotations_host, initial_rotations_host};
+    SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
+    for (int w = 0; w < 2; ++w) {
+        if (!dst[w] || E == 0) continue;
+        SGB_CUDA_TRY(cudaMemcpy(buf.data(), src[w], rs * 9 * E, cudaMemcpyDeviceToHost));
+        for (size_t e = 0; e < E; ++e)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    // stored: rows of R, SoA; reference convention: R^T row-major
+                    size_t k = (size_t)(3 * j + i) * E + e;
+                    double v = (rs == 8) ? ((double*)buf.data())[k] : (double)((float*)buf.data())[k];
+                    dst[w][9 * e + 3 * i + j] = v;
+                }
+    }
+    return SGB_OK;
+}
+
+int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method, int* precision, size_t* device_bytes)
+{
+    if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_info: NULL handle");
+    if (n_nodes) *n_nodes = fem->m.n_nodes;
+    if (n_tets) *n_tets = fem->m.n_tets;
+    if (method) *method = fem->m.method;
+    if (precision) *precision = fem->m.precision;
+    if (device_bytes) *device_bytes = fem->m.device_bytes;
+    return SGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// scene
+// ---------------------------------------------------------------------------
+
+void sgb_scene_params_default(sgb_scene_params* p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 0.01;
+    p->cg_iterations = 25;
+    p->cg_tolerance = 1e-5;
+    p->cg_threshold = 1e-5;
+    p->gravity[1] = -9.81;
+    p->vertex_mass = 1.0;
+    p->mass_first = 1;
+}
+
+static void free_scene(sgb_scene* sc)
+{
+    Scene& s = sc->s;
+    if (s.graph) cudaGraphExecDestroy(s.graph);
+    cudaFree(s.x);
+    cudaFree(s.v);
+    cudaFree(s.node_mass);
+    cudaFree(s.fixed);
+    cudaFree(s.ext);
+    cudaFree(s.f);
+    cudaFree(s.b);
+    cudaFree(s.xs);
+    cudaFree(s.p);
+    cudaFree(s.q);
+    cudaFree(s.r);
+    cudaFree(s.cg);
+    cudaFree(sc->dot_terms);
+    if (s.cg_h) cudaFreeHost(s.cg_h);
+}
+
+int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params* params)
+{
+    if (!out || !fem || !params) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: NULL argument");
+    *out = nullptr;
+    const sgb_scene_params& P = *params;
+    if (!(P.dt > 0) || P.cg_iterations < 0 || !(P.cg_tolerance >= 0) || !(P.cg_threshold >= 0))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: invalid solver parameters");
+    if (P.n_fixed < 0 || (P.n_fixed > 0 && !P.fixed_host))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: invalid fixed indices");
+    sgb_scene* sc = new sgb_scene();
+    Scene& s = sc->s;
+    const int N = fem->m.n_nodes;
+    const size_t rs = fem->m.real_size;
+    s.mesh = &fem->m;
+    s.n = N;
+    s.prm.dt = P.dt;
+    s.prm.rayleigh_stiffness = P.rayleigh_stiffness;
+    s.prm.rayleigh_mass = P.rayleigh_mass;
+    s.prm.vdamping = P.vdamping;
+    s.prm.cg_iterations = P.cg_iterations;
+    s.prm.cg_tolerance = P.cg_tolerance;
+    s.prm.cg_threshold = P.cg_threshold;
+    for (int k = 0; k < 3; ++k) s.prm.gravity[k] = P.gravity[k];
+    s.prm.vertex_mass = P.vertex_mass;
+    s.stream = fem->stream;
+    sc->fem = fem;
+    sc->ops = fem->ops;
+    sc->serial_dots = P.serial_dots;
+    sc->mass_first = P.mass_first;
+    size_t* acc = &s.device_bytes;
+    int rc;
+    std::vector<uint8_t> fixed((size_t)N, 0);
+    if (P.fix_all)
+        std::fill(fixed.begin(), fixed.end(), 1);
+    else
+        for (int i = 0; i < P.n_fixed; ++i)
+            if (P.fixed_host[i] >= 0 && P.fixed_host[i] < N) fixed[(size_t)P.fixed_host[i]] = 1;
+    cudaError_t ce;
+    if ((rc = dev_alloc(&s.x, 3 * (size_t)N, acc)) || (rc = dev_alloc(&s.v, 3 * (size_t)N, acc)) ||
+        (rc = dev_alloc(&s.fixed, (size_t)N, acc)) || (rc = dev_alloc_bytes(&s.f, rs * 3 * N, acc)) ||
+        (rc = dev_alloc_bytes(&s.b, rs * 3 * N, acc)) || (rc = dev_alloc_bytes(&s.xs, rs * 3 * N, acc)) ||
+        (rc = dev_alloc_bytes(&s.p, rs * 3 * N, acc)) || (rc = dev_alloc_bytes(&s.q, rs * 3 * N, acc)) ||
+        (rc = dev_alloc_bytes(&s.r, rs * 3 * N, acc)) || (rc = dev_alloc(&s.cg, 1, acc)))
+        goto fail_out;
+    if (P.node_masses_host && (rc = dev_alloc(&s.node_mass, (size_t)N, acc))) goto fail_out;
+    if (P.serial_dots && (rc = dev_alloc(&sc->dot_terms, (size_t)N, acc))) goto fail_out;
+    if ((ce = cudaMallocHost((void**)&s.cg_h, sizeof(CgScalars))) != cudaSuccess) {
+        rc = cuda_fail(ce, "cudaMallocHost");
+        goto fail_out;
+    }
+    if ((ce = cudaMemcpyAsync(s.x, fem->m.rest_pos, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s.stream)) ||
+        (ce = cudaMemsetAsync(s.v, 0, sizeof(double) * 3 * N, s.stream)) ||
+        (ce = cudaMemsetAsync(s.p, 0, rs * 3 * N, s.stream)) || (ce = cudaMemsetAsync(s.xs, 0, rs * 3 * N, s.stream)) ||
+        (ce = cudaMemsetAsync(s.cg, 0, sizeof(CgScalars), s.stream)) ||
+        (ce = cudaMemcpyAsync(s.fixed, fixed.data(), (size_t)N, cudaMemcpyHostToDevice, s.stream))) {
+        rc = cuda_fail(ce, "scene init copy");
+        goto fail_out;
+    }
+    if (P.node_masses_host &&
+        (ce = cudaMemcpyAsync(s.node_mass, P.node_masses_host, sizeof(double) * N, cudaMemcpyHostToDevice, s.stream))) {
+        rc = cuda_fail(ce, "scene init copy");
+        goto fail_out;
+    }
+    if ((ce = cudaStreamSynchronize(s.stream)) != cudaSuccess) {
+        rc = cuda_fail(ce, "scene init");
+        goto fail_out;
+    }
+    *out = sc;
+    return SGB_OK;
+fail_out:
+    free_scene(sc);
+    delete sc;
+    return rc;
+}
+
+int sgb_scene_destroy(sgb_scene_t* scene)
+{
+    if (!scene) return SGB_OK;
+    cudaStreamSynchronize(scene->s.stream);
+    free_scene(scene);
+    sgb_tfem_destroy(scene->fem);
+    delete scene;
+    return SGB_OK;
+}
+
+int sgb_scene_step(sgb_scene_t* scene, int n_steps)
+{
+    if (!scene || n_steps < 0) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_step: invalid argument");
+    Scene& s = scene->s;
+    if (!s.graph_valid) {
+        cudaGraph_t g;
+        SGB_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+        scene->ops->scene_step(&s, scene->dot_terms, scene->mass_first, s.stream);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(s.stream, &g);
+        if (le != cudaSuccess) return cuda_fail(le, "scene step launch");
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&s.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+        s.graph_valid = true;
+    }
+    for (int i = 0; i < n_steps; ++i) SGB_CUDA_TRY(cudaGraphLaunch(s.graph, s.stream));
+    return SGB_OK;
+}
+
+int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual)
+{
+    if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_sync: NULL scene");
+    Scene& s = scene->s;
+    SGB_CUDA_TRY(cudaMemcpyAsync(s.cg_h, s.cg, offsetof(CgScalars, partials), cudaMemcpyDeviceToHost, s.stream));
+    SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    if (cg_iterations) *cg_iterations = s.cg_h->iters;
+    if (cg_residual) *cg_residual = s.cg_h->last_err;
+    if (s.cg_h->status & 1) return fail(SGB_ERR_NUMERICAL, "non-finite value in the CG solve");
+    return SGB_OK;
+}
+
+int sgb_scene_get_state(sgb_scene_t* scene, double* x_host, double* v_host)
+{
+    if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_get_state: NULL scene");
+    Scene& s = scene->s;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s.n;
+    if (x_host) SGB_CUDA_TRY(cudaMemcpyAsync(x_host, s.x, bytes, cudaMemcpyDeviceToHost, s.stream));
+    if (v_host) SGB_CUDA_TRY(cudaMemcpyAsync(v_host, s.v, bytes, cudaMemcpyDeviceToHost, s.stream));
+    SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return SGB_OK;
+}
+
+int sgb_scene_set_state(sgb_scene_t* scene, const double* x_host, const double* v_host)
+{
+    if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_set_state: NULL scene");
+    Scene& s = scene->s;
+    const size_t bytes = sizeof(double) * 3 * (size_t)s.n;
+    if (x_host) SGB_CUDA_TRY(cudaMemcpyAsync(s.x, x_host, bytes, cudaMemcpyHostToDevice, s.stream));
+    if (v_host) SGB_CUDA_TRY(cudaMemcpyAsync(s.v, v_host, bytes, cudaMemcpyHostToDevice, s.stream));
+    SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return SGB_OK;
+}
+
+int sgb_scene_set_external_force(sgb_scene_t* scene, const double* fext_host)
+{
+    if (!scene || !fext_host) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_set_external_force: NULL argument");
+    Scene& s = scene->s;
+    const size_t n3 = 3 * (size_t)s.n, rs = s.mesh->real_size;
+    if (!s.ext) {
+        int rc = dev_alloc_bytes(&s.ext, rs * n3, &s.device_bytes);
+        if (rc) return rc;
+        s.graph_valid = false;  // the force gather reads ext: re-record the step
+        if (s.graph) {
+            cudaGraphExecDestroy(s.graph);
+            s.graph = nullptr;
+        }
+    }
+    if (rs == sizeof(double)) {
+        SGB_CUDA_TRY(cudaMemcpyAsync(s.ext, fext_host, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
+    } else {
+        std::vector<float> tmp(n3);
+        for (size_t i = 0; i < n3; ++i) tmp[i] = (float)fext_host[i];
+        SGB_CUDA_TRY(cudaMemcpyAsync(s.ext, tmp.data(), sizeof(float) * n3, cudaMemcpyHostToDevice, s.stream));
+        SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    }
+    SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return SGB_OK;
+}
+
+int sgb_scene_state_device(sgb_scene_t* scene, double** x_dev, double** v_dev)
+{
+    if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_state_device: NULL scene");
+    if (x_dev) *x_dev = scene->s.x;
+    if (v_dev) *v_dev = scene->s.v;
+    return SGB_OK;
+}
+
+void* sgb_scene_stream(sgb_scene_t* scene) { return scene ? (void*)scene->s.stream : nullptr; }
+
+}  // extern "C"

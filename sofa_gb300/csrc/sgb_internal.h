@@ -1,0 +1,115 @@
+// Internal data structures of the GB300 tetrahedral-FEM library. Device
+// buffers are owned by the library; every pointer below is device memory
+// unless its name ends in _h.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace sgb {
+
+enum Method { METHOD_SMALL = 0, METHOD_LARGE = 1, METHOD_POLAR = 2 };
+enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+// Blocks used by every node-parallel kernel that produces a dot product: the
+// per-block partial sums live in a fixed-size array and the last block to
+// finish reduces them in index order, so a dot product is bit-reproducible.
+constexpr int kNodeBlock = 256;
+constexpr int kMaxNodeBlocks = 152 * 8;
+constexpr int kElemBlock = 128;
+
+// Structure-of-arrays view of the per-element data. Arrays of width W are
+// stored as W rows of n_tets entries (value k of element e at [k*n_tets+e]),
+// so a warp's loads of one value are contiguous.
+template <typename R>
+struct ElemView {
+    const int4* tets;  // node indices a,b,c,d
+    R* rot;            // 9 rows: current rotation R (rows x,y,z of the element frame)
+    const R* K;        // 3 rows: K(0,0), K(0,1), K(3,3) of the 6x6 material stiffness / (36 V)
+    const R* J;        // 12 rows: the distinct values of the 12x6 strain-displacement matrix
+    const R* rest;     // 12 rows: rotated rest coordinates (method dependent, see tfem.cu)
+    int n_tets;
+    int method;
+};
+
+// Node -> (element*4 + corner) incidence in CSR form, each row sorted by slot.
+struct NodeCSR {
+    const int* rowptr;  // n_nodes + 1
+    const int* slots;   // 4 * n_tets
+};
+
+struct TfemMesh {
+    int n_nodes = 0, n_tets = 0, method = METHOD_LARGE, precision = PREC_FP64;
+    size_t real_size = 8;
+    // element data (real type = double for FP64, float for mixed)
+    int4* tets = nullptr;
+    void* rot = nullptr;
+    void* K = nullptr;
+    void* J = nullptr;
+    void* rest = nullptr;
+    void* R0 = nullptr;       // initial rotation rows (for the rotation getter)
+    double* rest_pos = nullptr;  // rest positions (FP64, n_nodes*3), used by method=small
+    int* rowptr = nullptr;
+    int* slots = nullptr;
+    int max_valence = 0;
+    void* eforce = nullptr;   // scratch: 12 reals per element (corner forces)
+    double rest_volume = 0.0;
+    std::vector<double> young_h, poisson_h;  // as given (for inspection)
+    size_t device_bytes = 0;
+};
+
+// Device-side scalar state of one CG solve plus the reduction scratch.
+struct CgScalars {
+    double normb;
+    double rho, rho_prev, den, alpha, beta;
+    double last_err;
+    long long time_step_count;
+    int done;
+    int iters;
+    int status;  // bit 0: non-finite value seen
+    int pad;
+    unsigned int ticket;
+    unsigned int pad2;
+    double partials[kMaxNodeBlocks];
+};
+
+struct SceneParams {
+    double dt = 0.01, rayleigh_stiffness = 0.0, rayleigh_mass = 0.0, vdamping = 0.0;
+    int cg_iterations = 25;
+    double cg_tolerance = 1e-5, cg_threshold = 1e-5;
+    double gravity[3] = {0.0, -9.81, 0.0};
+    double vertex_mass = 1.0;
+};
+
+struct Scene {
+    TfemMesh* mesh = nullptr;
+    bool owns_mesh = false;
+    SceneParams prm;
+    int n = 0;
+    // state (always FP64)
+    double* x = nullptr;
+    double* v = nullptr;
+    // per-node data
+    double* node_mass = nullptr;   // optional per-node masses (DiagonalMass-style), else uniform
+    uint8_t* fixed = nullptr;      // 1 = projected to zero
+    void* ext = nullptr;           // optional external force (real type)
+    // solver vectors (real type of the mesh precision)
+    void* f = nullptr;
+    void* b = nullptr;
+    void* xs = nullptr;
+    void* p = nullptr;
+    void* q = nullptr;
+    void* r = nullptr;
+    CgScalars* cg = nullptr;
+    CgScalars* cg_h = nullptr;  // pinned mirror for reads
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    int graph_steps = 0;
+    size_t device_bytes = 0;
+};
+
+}  // namespace sgb

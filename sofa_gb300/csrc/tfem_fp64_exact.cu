@@ -1,0 +1,7 @@
+// FP64 kernels compiled without FMA contraction (-fmad=false): each a*b+c
+// rounds twice, as the reference CPU code does.
+#define SGB_NS sgb_fp64_exact
+#define SGB_REAL double
+#define SGB_TABLE ops_fp64_exact
+#define SGB_VARIANT_NAME "fp64"
+#include "variant_def.cuh"

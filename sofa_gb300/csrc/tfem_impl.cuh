@@ -1,0 +1,876 @@
+// Kernels of one precision variant of the tetrahedral-FEM implicit step.
+//
+// This header is compiled three times, each time inside its own namespace
+// (SGB_NS):
+//   tfem_fp64_exact.cu  R = double, no FMA contraction (-fmad=false): the
+//                       element math, node gathers and vector updates round
+//                       exactly like the reference's CPU code, so with
+//                       serial dot products a whole step is bit-identical to
+//                       it;
+//   tfem_fp64_fast.cu   R = double with FMA contraction;
+//   tfem_mixed.cu       R = float element math and solver vectors, FP64 state
+//                       (positions, velocities) and FP64 dot products.
+//
+// Data flow of one addForce / addDForce (reference: Sofa/Component/
+// SolidMechanics/FEM/Elastic/src/sofa/component/solidmechanics/fem/elastic/
+// TetrahedronFEMForceField.inl:1548-1636, "TFEM.inl"):
+//   element kernel   one thread per tetrahedron: rotation, strain, K J^T,
+//                    the four corner forces R^T F into `eforce` (12 reals);
+//   gather kernel    one thread per node: sums its (element, corner) slots
+//                    from the node->slot CSR in element order, no atomics.
+// The solver kernels fuse the mass term, the fixed-node projection, the CG
+// vector updates and the dot products into the gathers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "sgb_internal.h"
+#include "tfem_math.cuh"
+
+#ifndef SGB_NS
+#error "define SGB_NS before including tfem_impl.cuh"
+#endif
+
+namespace SGB_NS {
+using namespace sgb;
+
+template <typename R>
+using is_mixed = std::is_same<R, float>;
+
+__device__ __forceinline__ void ld3(const double* p, long long i, double o[3])
+{
+    o[0] = p[3 * i];
+    o[1] = p[3 * i + 1];
+    o[2] = p[3 * i + 2];
+}
+__device__ __forceinline__ void ld3(const float* p, long long i, float o[3])
+{
+    o[0] = p[3 * i];
+    o[1] = p[3 * i + 1];
+    o[2] = p[3 * i + 2];
+}
+
+// ------------------------------------------------------------------------
+// initialisation: per-element K, J, initial rotation and rotated rest
+// coordinates, computed in FP64 (computeMaterialStiffness TFEM.inl:256-291,
+// initSmall/initLarge/initPolar TFEM.inl:526-532, 835-868, 993-1023) and
+// stored in R.
+// ------------------------------------------------------------------------
+template <typename R>
+__global__ void k_init_elements(const double* __restrict__ rest_pos, const int4* __restrict__ tets, int E,
+                                int method, const double* __restrict__ young, int n_young,
+                                const double* __restrict__ poisson, int n_poisson, const double* __restrict__ lsf,
+                                int n_lsf, R* K, R* J, R* rest, R* rot, R* R0, double* vol)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const int4 t = tets[e];
+    double pa[3], pb[3], pc[3], pd[3];
+    ld3(rest_pos, t.x, pa);
+    ld3(rest_pos, t.y, pb);
+    ld3(rest_pos, t.z, pc);
+    ld3(rest_pos, t.w, pd);
+    // getVecRealInElement (BaseLinearElasticityFEMForceField.inl:114-132)
+    double Ey = (n_young > e) ? young[e] : young[0];
+    double nu = (n_poisson > e) ? poisson[e] : poisson[0];
+    double f = (n_lsf > 0) ? lsf[(size_t)e * (size_t)n_lsf / (size_t)E] : 1.0;
+    Ey = f * Ey;
+    double s = (Ey * (1 - nu)) / ((1 + nu) * (1 - 2 * nu));
+    double k0 = 1.0, k1 = nu / (1 - nu), k2 = (1 - 2 * nu) / (2 * (1 - nu));
+    k0 *= s;
+    k1 *= s;
+    k2 *= s;
+    double ea[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+    double eb[3] = {pc[0] - pa[0], pc[1] - pa[1], pc[2] - pa[2]};
+    double ec[3] = {pd[0] - pa[0], pd[1] - pa[1], pd[2] - pa[2]};
+    double cr[3];
+    cross3(ea, eb, cr);
+    double dt = cr[0] * ec[0];
+    dt += cr[1] * ec[1];
+    dt += cr[2] * ec[2];
+    double v = fabs(dt / 6.0);
+    vol[e] = v;
+    k0 /= v * 36;
+    k1 /= v * 36;
+    k2 /= v * 36;
+    const size_t En = (size_t)E;
+    K[0 * En + e] = (R)k0;
+    K[1 * En + e] = (R)k1;
+    K[2 * En + e] = (R)k2;
+
+    double Jd[12], rr[12];
+    double Rm[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (method == METHOD_SMALL) {
+        strain_displacement(pa, pb, pc, pd, Jd);
+        for (int i = 0; i < 12; ++i) rr[i] = 0.0;
+    } else {
+        if (method == METHOD_LARGE) {
+            rotation_large(ea, eb, Rm);
+        } else {
+            double A[9] = {ea[0], ea[1], ea[2], eb[0], eb[1], eb[2], ec[0], ec[1], ec[2]};
+            polar3(A, Rm, 1000);
+        }
+        const double* P[4] = {pa, pb, pc, pd};
+        for (int i = 0; i < 4; ++i)
+            for (int k = 0; k < 3; ++k) {
+                double acc = Rm[3 * k] * P[i][0];
+                acc += Rm[3 * k + 1] * P[i][1];
+                acc += Rm[3 * k + 2] * P[i][2];
+                rr[3 * i + k] = acc;
+            }
+        if (method == METHOD_LARGE) {
+            for (int i = 1; i < 4; ++i)
+                for (int k = 0; k < 3; ++k) rr[3 * i + k] -= rr[k];
+            rr[0] = rr[1] = rr[2] = 0.0;
+        }
+        strain_displacement(&rr[0], &rr[3], &rr[6], &rr[9], Jd);
+        if (method == METHOD_POLAR && is_mixed<R>::value) {
+            // mixed precision drops the rigid translation (J's columns sum to
+            // zero): keep rest coordinates relative to node a
+            for (int i = 1; i < 4; ++i)
+                for (int k = 0; k < 3; ++k) rr[3 * i + k] -= rr[k];
+            rr[0] = rr[1] = rr[2] = 0.0;
+        }
+    }
+    for (int i = 0; i < 12; ++i) J[(size_t)i * En + e] = (R)Jd[i];
+    for (int i = 0; i < 12; ++i) rest[(size_t)i * En + e] = (R)rr[i];
+    for (int i = 0; i < 9; ++i) {
+        rot[(size_t)i * En + e] = (R)Rm[i];
+        R0[(size_t)i * En + e] = (R)Rm[i];
+    }
+}
+
+// ------------------------------------------------------------------------
+// element kernels
+// ------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void load_elem_KJ(const ElemView<R>& ev, int e, R K[3], R J[12])
+{
+    const size_t En = (size_t)ev.n_tets;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
+}
+
+template <typename R>
+__device__ __forceinline__ void store_eforce(R* eforce, int e, const R c[12])
+{
+    R* o = eforce + (size_t)e * 12;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) o[i] = c[i];
+}
+
+// addForce element part: accumulateForceSmall / Large / Polar
+// (TFEM.inl:534-623, 870-986, 1025-1079). Writes rotations and the corner
+// forces R^T F (method=small: F).
+template <typename R, int METHOD>
+__global__ void __launch_bounds__(kElemBlock) k_elem_force(ElemView<R> ev, const double* __restrict__ x,
+                                                           const double* __restrict__ rest_pos,
+                                                           R* __restrict__ eforce)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ev.n_tets) return;
+    const size_t En = (size_t)ev.n_tets;
+    const int4 t = ev.tets[e];
+    double p[4][3];
+    ld3(x, t.x, p[0]);
+    ld3(x, t.y, p[1]);
+    ld3(x, t.z, p[2]);
+    ld3(x, t.w, p[3]);
+    R K[3], J[12];
+    load_elem_KJ(ev, e, K, J);
+    R D[12], F[12], c[12];
+    if (METHOD == METHOD_SMALL) {
+        double q[4][3];
+        ld3(rest_pos, t.x, q[0]);
+        ld3(rest_pos, t.y, q[1]);
+        ld3(rest_pos, t.z, q[2]);
+        ld3(rest_pos, t.w, q[3]);
+        D[0] = D[1] = D[2] = R(0);
+#pragma unroll
+        for (int i = 1; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) D[3 * i + k] = (R)(q[i][k] - q[0][k] - p[i][k] + p[0][k]);
+        element_force_nofact(F, D, K, J);
+#pragma unroll
+        for (int i = 0; i < 12; ++i) c[i] = F[i];
+        store_eforce(eforce, e, c);
+        return;
+    }
+    R Rm[9];
+    R rr[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) rr[i] = ev.rest[i * En + e];
+    if (!is_mixed<R>::value) {
+        // FP64: the reference's formulation on absolute positions
+        R eab[3] = {R(p[1][0] - p[0][0]), R(p[1][1] - p[0][1]), R(p[1][2] - p[0][2])};
+        R eac[3] = {R(p[2][0] - p[0][0]), R(p[2][1] - p[0][1]), R(p[2][2] - p[0][2])};
+        if (METHOD == METHOD_LARGE) {
+            rotation_large(eab, eac, Rm);
+        } else {
+            R ead[3] = {R(p[3][0] - p[0][0]), R(p[3][1] - p[0][1]), R(p[3][2] - p[0][2])};
+            R A[9] = {eab[0], eab[1], eab[2], eac[0], eac[1], eac[2], ead[0], ead[1], ead[2]};
+            polar3(A, Rm);
+        }
+        R def[12];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                R acc = Rm[3 * k] * (R)p[i][0];
+                acc += Rm[3 * k + 1] * (R)p[i][1];
+                acc += Rm[3 * k + 2] * (R)p[i][2];
+                def[3 * i + k] = acc;
+            }
+        if (METHOD == METHOD_LARGE) {
+            def[3] -= def[0];
+            def[6] -= def[0];
+            def[7] -= def[1];
+            def[9] -= def[0];
+            def[10] -= def[1];
+            def[11] -= def[2];
+            D[0] = D[1] = D[2] = D[4] = D[5] = D[8] = R(0);
+            D[3] = rr[3] - def[3];
+            D[6] = rr[6] - def[6];
+            D[7] = rr[7] - def[7];
+            D[9] = rr[9] - def[9];
+            D[10] = rr[10] - def[10];
+            D[11] = rr[11] - def[11];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
+        }
+    } else {
+        // mixed: edges are formed in FP64 and rounded once, the element math
+        // runs in FP32 on positions relative to node a
+        R ed[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ed[i][k] = (R)(p[i + 1][k] - p[0][k]);
+        if (METHOD == METHOD_LARGE) {
+            rotation_large(ed[0], ed[1], Rm);
+        } else {
+            R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
+            polar3(A, Rm);
+        }
+        D[0] = D[1] = D[2] = R(0);
+#pragma unroll
+        for (int i = 1; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                R d = Rm[3 * k] * ed[i - 1][0] + Rm[3 * k + 1] * ed[i - 1][1] + Rm[3 * k + 2] * ed[i - 1][2];
+                D[3 * i + k] = rr[3 * i + k] - d;
+            }
+        if (METHOD == METHOD_LARGE) D[4] = D[5] = D[8] = R(0);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) ev.rot[i * En + e] = Rm[i];
+    element_force_nofact(F, D, K, J);
+    // f[node] += rotations[e] * F_node, rotations[e] = R^T
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            R acc = Rm[k] * F[3 * i];
+            acc += Rm[3 + k] * F[3 * i + 1];
+            acc += Rm[6 + k] * F[3 * i + 2];
+            c[3 * i + k] = acc;
+        }
+    store_eforce(eforce, e, c);
+}
+
+// Direction of the CG step for the matvec element pass. DIR 0: the input
+// vector itself; DIR 1: p = r (first iteration); DIR 2: p = p_old*beta + r
+// (vOp_avf, Sofa/Component/StateContainer/src/sofa/component/statecontainer/
+// MechanicalObject.inl:1999-2013).
+template <typename R>
+__device__ __forceinline__ R cg_dir(R r, R pold, R beta)
+{
+    R t = pold * beta;
+    return t + r;
+}
+
+// addDForce element part: applyStiffnessSmall / applyStiffnessCorotational
+// (TFEM.inl:721-749, 1193-1237). Writes the corner terms R K (R^T dx) fact
+// that the gather subtracts.
+template <typename R, typename VIN, int METHOD, int DIR>
+__global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, const VIN* __restrict__ dx,
+                                                            const R* __restrict__ pold, const CgScalars* cg,
+                                                            R fact, R* __restrict__ eforce)
+{
+    if (DIR != 0 && cg->done) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ev.n_tets) return;
+    const size_t En = (size_t)ev.n_tets;
+    const int4 t = ev.tets[e];
+    const int node[4] = {t.x, t.y, t.z, t.w};
+    R xin[4][3];
+    R beta = R(0);
+    if (DIR == 2) beta = (R)cg->beta;
+    VIN v0[3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        VIN v3[3];
+        ld3(dx, node[i], v3);
+        if (DIR == 2) {
+            R po[3];
+            ld3(pold, node[i], po);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xin[i][k] = cg_dir((R)v3[k], po[k], beta);
+        } else if (is_mixed<R>::value && !std::is_same<VIN, R>::value) {
+            // FP64 input (velocities): form the differences to node a in
+            // FP64 before rounding to FP32
+            if (i == 0) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) v0[k] = v3[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xin[i][k] = (R)(v3[k] - v0[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xin[i][k] = (R)v3[k];
+        }
+    }
+    if (is_mixed<R>::value && METHOD != METHOD_SMALL) {
+        // FP32: J^T annihilates rigid translations (each column of J sums to
+        // zero over the four nodes), so work on values relative to node a;
+        // smooth CG directions then keep their strain bits
+#pragma unroll
+        for (int i = 3; i >= 0; --i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xin[i][k] -= xin[0][k];
+    }
+    R K[3], J[12];
+    load_elem_KJ(ev, e, K, J);
+    R X[12], F[12], c[12];
+    if (METHOD == METHOD_SMALL) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) X[3 * i + k] = xin[i][k];
+        element_force(F, X, K, J, fact);
+#pragma unroll
+        for (int i = 0; i < 12; ++i) c[i] = F[i];
+        store_eforce(eforce, e, c);
+        return;
+    }
+    R Rm[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            R acc = Rm[3 * k] * xin[i][0];
+            acc += Rm[3 * k + 1] * xin[i][1];
+            acc += Rm[3 * k + 2] * xin[i][2];
+            X[3 * i + k] = acc;
+        }
+    element_force(F, X, K, J, fact);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            R acc = Rm[k] * F[3 * i];
+            acc += Rm[3 + k] * F[3 * i + 1];
+            acc += Rm[6 + k] * F[3 * i + 2];
+            c[3 * i + k] = acc;
+        }
+    store_eforce(eforce, e, c);
+}
+
+// ------------------------------------------------------------------------
+// node-centric gathers
+// ------------------------------------------------------------------------
+
+// out[n] += sum (ADD) or out[n] -= each term (SUB), terms in element order:
+// the reference's serial scatter, restated per node.
+template <typename R, typename VO, bool SUB>
+__global__ void __launch_bounds__(kNodeBlock) k_gather_accumulate(NodeCSR csr, const R* __restrict__ eforce,
+                                                                  VO* __restrict__ out, int N)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R a0 = (R)out[3 * (size_t)n], a1 = (R)out[3 * (size_t)n + 1], a2 = (R)out[3 * (size_t)n + 2];
+        const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            if (SUB) {
+                a0 -= c[0];
+                a1 -= c[1];
+                a2 -= c[2];
+            } else {
+                a0 += c[0];
+                a1 += c[1];
+                a2 += c[2];
+            }
+        }
+        out[3 * (size_t)n] = (VO)a0;
+        out[3 * (size_t)n + 1] = (VO)a1;
+        out[3 * (size_t)n + 2] = (VO)a2;
+    }
+}
+
+// ---- deterministic dot products -----------------------------------------
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block in a fixed tree; the result is valid in thread 0.
+__device__ __forceinline__ double block_sum(double v)
+{
+    __shared__ double red[kNodeBlock / 32];
+    __syncthreads();
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (wid == 0) {
+        r = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// Vec3 dot in the reference order ((x x' + y y') + z z'), FP64.
+template <typename A, typename B>
+__device__ __forceinline__ double dot3(const A a[3], const B b[3])
+{
+    double r = (double)a[0] * (double)b[0];
+    r += (double)a[1] * (double)b[1];
+    r += (double)a[2] * (double)b[2];
+    return r;
+}
+
+enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2 };
+
+struct SolveConsts {
+    double tol, threshold;
+    int it;  // CG iteration this kernel belongs to (1-based)
+};
+
+// Last-block finish of a dot product: every block writes its partial; the
+// last block to arrive (integer ticket) adds the partials in block order and
+// applies the CG bookkeeping of CGLinearSolver::solve
+// (Sofa/Component/LinearSolver/Iterative/src/sofa/component/linearsolver/
+// iterative/CGLinearSolver.inl:102-272). With `terms` non-null the sum is
+// instead the serial node-order sum of per-node terms, as MechanicalObject::vDot
+// (MechanicalObject.inl:2334-2356) computes it.
+template <int FIN>
+__device__ void finish_dot(double local, CgScalars* cg, const double* terms, int N, SolveConsts sc)
+{
+    __shared__ int is_last;
+    double bsum = block_sum(local);
+    if (threadIdx.x == 0) {
+        cg->partials[blockIdx.x] = bsum;
+        __threadfence();
+        unsigned t = atomicAdd(&cg->ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double total;
+    if (terms) {
+        total = 0.0;
+        if (threadIdx.x == 0)
+            for (int i = 0; i < N; ++i) total += __ldcg(&terms[i]);
+    } else {
+        double v = 0.0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) v += __ldcg(&cg->partials[i]);
+        total = block_sum(v);
+    }
+    if (threadIdx.x != 0) return;
+    cg->ticket = 0;
+    if (!isfinite(total)) {
+        cg->status |= 1;
+        cg->done = 1;
+        return;
+    }
+    const bool first_of_first = (sc.it == 1 && cg->time_step_count == 0);
+    if (FIN == FIN_RHS) {
+        // x = 0; r = b; normb = |b|; iteration 1 starts with rho = r.r
+        cg->rho = total;
+        cg->normb = sqrt(total);
+        cg->iters = 0;
+        cg->last_err = 0.0;
+        if (cg->normb == 0.0) {
+            cg->done = 1;
+        } else {
+            double err = sqrt(total) / cg->normb;
+            cg->last_err = err;
+            cg->done = (err <= sc.tol && !first_of_first) ? 1 : 0;
+        }
+    } else if (FIN == FIN_DEN) {
+        cg->den = total;
+        if (total != 0.0) {
+            if (fabs(total) <= sc.threshold && !first_of_first) {
+                cg->done = 1;
+            } else {
+                cg->alpha = cg->rho / total;
+            }
+        } else {
+            cg->done = 1;
+        }
+    } else {
+        cg->rho_prev = cg->rho;
+        cg->rho = total;
+        cg->iters = sc.it;
+        cg->beta = total / cg->rho_prev;
+        double err = sqrt(total) / cg->normb;
+        cg->last_err = err;
+        if (err <= sc.tol) cg->done = 1;
+    }
+}
+
+struct MassArgs {
+    const double* node_mass;  // per-node masses, or null for a uniform vertex mass
+    double vertex_mass;
+    double g[3];
+};
+
+// computeForce of the scene (MappingGraphMechanicalOperations.cpp:41-92):
+// f = ext + (mass m g and FEM forces in component order).
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_gather_force(NodeCSR csr, const R* __restrict__ eforce,
+                                                             const R* __restrict__ ext, MassArgs ma,
+                                                             int mass_first, R* __restrict__ f, int N)
+{
+    // UniformMass::addForce: mg = g * vertexMass (UniformMass.inl:471-496)
+    const R mg0 = (R)(ma.g[0] * ma.vertex_mass), mg1 = (R)(ma.g[1] * ma.vertex_mass),
+            mg2 = (R)(ma.g[2] * ma.vertex_mass);
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R a0 = R(0), a1 = R(0), a2 = R(0);
+        if (ext) {
+            a0 += ext[3 * (size_t)n];
+            a1 += ext[3 * (size_t)n + 1];
+            a2 += ext[3 * (size_t)n + 2];
+        }
+        R m0 = mg0, m1 = mg1, m2 = mg2;
+        if (ma.node_mass) {
+            const double m = ma.node_mass[n];
+            m0 = (R)(ma.g[0] * m);
+            m1 = (R)(ma.g[1] * m);
+            m2 = (R)(ma.g[2] * m);
+        }
+        if (mass_first) {
+            a0 += m0;
+            a1 += m1;
+            a2 += m2;
+        }
+        const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            a0 += c[0];
+            a1 += c[1];
+            a2 += c[2];
+        }
+        if (!mass_first) {
+            a0 += m0;
+            a1 += m1;
+            a2 += m2;
+        }
+        f[3 * (size_t)n] = a0;
+        f[3 * (size_t)n + 1] = a1;
+        f[3 * (size_t)n + 2] = a2;
+    }
+}
+
+// res += factor M dx for one node (UniformMass::addMDx UniformMass.inl:403-419,
+// DiagonalMass::addMDx DiagonalMass.inl:536-559).
+template <typename R>
+__device__ __forceinline__ void add_mdx(R a[3], const R d[3], const MassArgs& ma, double factor, R mm_uniform, int n)
+{
+    if (ma.node_mass) {
+        const R m = (R)ma.node_mass[n];
+        if (factor == 1.0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] += d[k] * m;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] += (d[k] * m) * (R)factor;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a[k] += d[k] * mm_uniform;
+    }
+}
+
+// Right-hand side of EulerImplicitSolver (EulerImplicitSolver.cpp:130-163):
+// b = h (f + (-rm M + (h+rs) K) v), projected; then the CG start r = b,
+// x = 0 and the dot b.b.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R* __restrict__ eforce,
+                                                           const R* __restrict__ f, const double* __restrict__ v,
+                                                           MassArgs ma, double mfac, int mass_first, double h,
+                                                           const uint8_t* __restrict__ fixed, R* __restrict__ b,
+                                                           R* __restrict__ r, R* __restrict__ xs, CgScalars* cg,
+                                                           double* terms, int N, SolveConsts sc)
+{
+    const R mm = (R)(mfac != 1.0 ? ma.vertex_mass * mfac : ma.vertex_mass);
+    const R hr = (R)h;
+    double local = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) cg->done = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R a[3] = {f[3 * (size_t)n], f[3 * (size_t)n + 1], f[3 * (size_t)n + 2]};
+        R vv[3] = {(R)v[3 * (size_t)n], (R)v[3 * (size_t)n + 1], (R)v[3 * (size_t)n + 2]};
+        if (mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+        const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            a[0] -= c[0];
+            a[1] -= c[1];
+            a[2] -= c[2];
+        }
+        if (!mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a[k] *= hr;
+        if (fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            b[3 * (size_t)n + k] = a[k];
+            r[3 * (size_t)n + k] = a[k];
+            xs[3 * (size_t)n + k] = R(0);
+        }
+        double d = dot3(a, a);
+        if (terms) terms[n] = d;
+        local += d;
+    }
+    finish_dot<FIN_RHS>(local, cg, terms, N, sc);
+}
+
+// q = A p for GraphScatteredMatrix::apply (GraphScatteredTypes.cpp:33-45):
+// q = mF M p - (K p terms), projected; also stores the direction p and
+// the dot p.q.
+template <typename R, int DIR>
+__global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const R* __restrict__ eforce,
+                                                              const R* __restrict__ r, R* __restrict__ p,
+                                                              MassArgs ma, double mf, int mass_first,
+                                                              const uint8_t* __restrict__ fixed,
+                                                              R* __restrict__ q, CgScalars* cg, double* terms,
+                                                              int N, SolveConsts sc)
+{
+    if (cg->done) return;
+    const R mm = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    const R beta = (DIR == 2) ? (R)cg->beta : R(0);
+    double local = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R pp[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            R rv = r[3 * (size_t)n + k];
+            pp[k] = (DIR == 2) ? cg_dir(rv, p[3 * (size_t)n + k], beta) : rv;
+        }
+        R a[3] = {R(0), R(0), R(0)};
+        if (mass_first) add_mdx(a, pp, ma, mf, mm, n);
+        const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            a[0] -= c[0];
+            a[1] -= c[1];
+            a[2] -= c[2];
+        }
+        if (!mass_first) add_mdx(a, pp, ma, mf, mm, n);
+        if (fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            p[3 * (size_t)n + k] = pp[k];
+            q[3 * (size_t)n + k] = a[k];
+        }
+        double d = dot3(pp, a);
+        if (terms) terms[n] = d;
+        local += d;
+    }
+    finish_dot<FIN_DEN>(local, cg, terms, N, sc);
+}
+
+// cgstep_alpha (CGLinearSolver.cpp:47-63): x += alpha p; r += -alpha q; then
+// rho = r.r for the next iteration.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_cg_update(R* __restrict__ xs, R* __restrict__ r,
+                                                          const R* __restrict__ p, const R* __restrict__ q,
+                                                          CgScalars* cg, double* terms, int N, SolveConsts sc)
+{
+    if (cg->done) return;
+    const R alpha = (R)cg->alpha;
+    const R nalpha = -alpha;
+    double local = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R rr[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const size_t i = 3 * (size_t)n + k;
+            R t = p[i] * alpha;
+            xs[i] = xs[i] + t;
+            R u = q[i] * nalpha;
+            rr[k] = r[i] + u;
+            r[i] = rr[k];
+        }
+        double d = dot3(rr, rr);
+        if (terms) terms[n] = d;
+        local += d;
+    }
+    finish_dot<FIN_RHO>(local, cg, terms, N, sc);
+}
+
+// Euler update (MechanicalObject::vMultiOp fast path, MechanicalObject.inl:
+// 2206-2240): v += dv; x += v h; optional v *= exp(-h vdamping).
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict__ x, double* __restrict__ v,
+                                                             const R* __restrict__ xs, double h, double vdamp,
+                                                             CgScalars* cg, int N)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const size_t i = 3 * (size_t)n + k;
+            double vv = v[i] + (double)xs[i];
+            double t = vv * h;
+            x[i] = x[i] + t;
+            if (vdamp != 1.0) vv *= vdamp;
+            v[i] = vv;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cg->time_step_count += 1;
+}
+
+// ------------------------------------------------------------------------
+// host launchers
+// ------------------------------------------------------------------------
+inline int node_grid(int N)
+{
+    int g = (N + kNodeBlock - 1) / kNodeBlock;
+    if (g > kMaxNodeBlocks) g = kMaxNodeBlocks;
+    return g < 1 ? 1 : g;
+}
+inline int elem_grid(int E) { return (E + kElemBlock - 1) / kElemBlock; }
+
+template <typename R>
+ElemView<R> view(TfemMesh* m)
+{
+    ElemView<R> ev;
+    ev.tets = m->tets;
+    ev.rot = (R*)m->rot;
+    ev.K = (const R*)m->K;
+    ev.J = (const R*)m->J;
+    ev.rest = (const R*)m->rest;
+    ev.n_tets = m->n_tets;
+    ev.method = m->method;
+    return ev;
+}
+
+template <typename R>
+void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson, int np, const double* lsf, int nl,
+                 double* vol, cudaStream_t s)
+{
+    if (m->n_tets == 0) return;
+    k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
+        m->rest_pos, m->tets, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K, (R*)m->J,
+        (R*)m->rest, (R*)m->rot, (R*)m->R0, vol);
+}
+
+template <typename R>
+void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
+{
+    if (m->n_tets == 0) return;
+    ElemView<R> ev = view<R>(m);
+    const int g = elem_grid(m->n_tets);
+    if (m->method == METHOD_SMALL)
+        k_elem_force<R, METHOD_SMALL><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+    else if (m->method == METHOD_LARGE)
+        k_elem_force<R, METHOD_LARGE><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+    else
+        k_elem_force<R, METHOD_POLAR><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+}
+
+template <typename R, typename VIN, int DIR>
+void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScalars* cg, R fact, cudaStream_t s)
+{
+    if (m->n_tets == 0) return;
+    ElemView<R> ev = view<R>(m);
+    const int g = elem_grid(m->n_tets);
+    if (m->method == METHOD_SMALL)
+        k_elem_dforce<R, VIN, METHOD_SMALL, DIR><<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce);
+    else
+        k_elem_dforce<R, VIN, METHOD_LARGE, DIR><<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce);
+}
+
+// Public per-call operations (the drop-in for
+// TetrahedronFEMForceFieldCuda3{f,d}_addForce / _addDForce).
+template <typename R, typename VO>
+void api_add_force(TfemMesh* m, const double* x, VO* f, cudaStream_t s)
+{
+    launch_elem_force<R>(m, x, s);
+    NodeCSR csr{m->rowptr, m->slots};
+    k_gather_accumulate<R, VO, false><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f,
+                                                                                   m->n_nodes);
+}
+
+template <typename R>
+void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
+{
+    launch_elem_dforce<R, R, 0>(m, dx, nullptr, nullptr, kfactor, s);
+    NodeCSR csr{m->rowptr, m->slots};
+    k_gather_accumulate<R, R, true><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, df,
+                                                                                 m->n_nodes);
+}
+
+// One implicit Euler step of a scene (EulerImplicitSolver::solve,
+// Sofa/Component/ODESolver/Backward/src/sofa/component/odesolver/backward/
+// EulerImplicitSolver.cpp:83-341) as a fixed sequence of launches: the CG
+// loop is unrolled to `iterations` and the kernels after convergence return
+// at once, so the step can be captured in a CUDA graph.
+template <typename R>
+void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
+{
+    TfemMesh* m = sc->mesh;
+    const int N = sc->n;
+    const SceneParams& P = sc->prm;
+    const double h = P.dt;
+    NodeCSR csr{m->rowptr, m->slots};
+    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const int ng = node_grid(N);
+    R* f = (R*)sc->f;
+    R* b = (R*)sc->b;
+    R* r = (R*)sc->r;
+    R* p = (R*)sc->p;
+    R* q = (R*)sc->q;
+    R* xs = (R*)sc->xs;
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1};
+    // f = F(x)
+    launch_elem_force<R>(m, sc->x, s);
+    k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
+    // b = h (f - (h+rs) K v - rm M v)
+    const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
+    launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)kf_rhs, s);
+    k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass, mass_first,
+                                              h, sc->fixed, b, r, xs, sc->cg, dot_terms, N, cons);
+    // CG on (mF M + kF K) dv = b
+    const double mf = 1 + 1.0 * h * P.rayleigh_mass;
+    const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    for (int it = 1; it <= P.cg_iterations; ++it) {
+        cons.it = it;
+        if (it == 1) {
+            launch_elem_dforce<R, R, 1>(m, r, p, sc->cg, (R)kf, s);
+            k_gather_matvec<R, 1><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf, mass_first,
+                                                            sc->fixed, q, sc->cg, dot_terms, N, cons);
+        } else {
+            launch_elem_dforce<R, R, 2>(m, r, p, sc->cg, (R)kf, s);
+            k_gather_matvec<R, 2><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf, mass_first,
+                                                            sc->fixed, q, sc->cg, dot_terms, N, cons);
+        }
+        k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons);
+    }
+    const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
+    k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);
+}
+
+}  // namespace SGB_NS

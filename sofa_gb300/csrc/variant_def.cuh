@@ -1,0 +1,29 @@
+// Instantiates tfem_impl.cuh for one real type and exports its table.
+// Expects SGB_NS, SGB_REAL and SGB_TABLE to be defined.
+#include "tfem_impl.cuh"
+#include "variants.h"
+
+namespace SGB_NS {
+static void v_init(TfemMesh* m, const double* y, int ny, const double* p, int np, const double* l, int nl,
+                   double* vol, cudaStream_t s)
+{
+    launch_init<SGB_REAL>(m, y, ny, p, np, l, nl, vol, s);
+}
+static void v_add_force(TfemMesh* m, const double* x, void* f, cudaStream_t s)
+{
+    api_add_force<SGB_REAL, SGB_REAL>(m, x, (SGB_REAL*)f, s);
+}
+static void v_add_dforce(TfemMesh* m, const void* dx, void* df, double k, cudaStream_t s)
+{
+    api_add_dforce<SGB_REAL>(m, (const SGB_REAL*)dx, (SGB_REAL*)df, (SGB_REAL)k, s);
+}
+static void v_scene_step(Scene* sc, double* terms, int mass_first, cudaStream_t s)
+{
+    scene_step<SGB_REAL>(sc, terms, mass_first, s);
+}
+}  // namespace SGB_NS
+
+namespace sgb {
+const VariantOps SGB_TABLE = {SGB_VARIANT_NAME, sizeof(SGB_REAL), SGB_NS::v_init, SGB_NS::v_add_force,
+                              SGB_NS::v_add_dforce, SGB_NS::v_scene_step};
+}

@@ -1,0 +1,25 @@
+// Function table of one precision variant of the kernels (tfem_impl.cuh).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sgb_internal.h"
+
+namespace sgb {
+
+struct VariantOps {
+    const char* name;
+    size_t real_size;
+    void (*init)(TfemMesh*, const double* young, int ny, const double* poisson, int np, const double* lsf, int nl,
+                 double* vol, cudaStream_t);
+    void (*add_force)(TfemMesh*, const double* x, void* f, cudaStream_t);
+    void (*add_dforce)(TfemMesh*, const void* dx, void* df, double kfactor, cudaStream_t);
+    void (*scene_step)(Scene*, double* dot_terms, int mass_first, cudaStream_t);
+};
+
+extern const VariantOps ops_fp64_exact;
+extern const VariantOps ops_fp64_fast;
+extern const VariantOps ops_mixed;
+
+const VariantOps* variant_for(int precision);
+
+}  // namespace sgb
