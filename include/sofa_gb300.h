@@ -107,6 +107,17 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
 int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method, int* precision,
                   size_t* device_bytes);
 
+/* Host-only check of the element ordering and patch layout the fused
+ * kernels use (no GPU needed): every (element, corner) gathered exactly once
+ * by one patch, one owner per node, partial-sum slots in patch order.
+ * stats (5 ints, may be NULL): patches, largest local node count, local
+ * nodes in total, nodes shared by several patches, partial-sum slots.
+ * Returns SGB_OK or SGB_ERR_NUMERICAL with the violated invariant in
+ * sgb_last_error(). No reference counterpart: it validates this library's
+ * own layout. */
+int sgb_patch_layout_check(int n_nodes, const double* rest_positions_host, int n_tets, const int32_t* tetrahedra_host,
+                           int elements_per_patch, int max_nodes_per_patch, int* stats);
+
 /* ------------------------------------------------------------------ */
 /* Scene: MechanicalObject + mass + FEM + fixed constraint, advanced by */
 /* EulerImplicitSolver + CGLinearSolver<GraphScattered>.                */

@@ -28,6 +28,7 @@ UNITS = {
     "tfem_fp64_fast.cu": ["-fmad=true"],
     "tfem_mixed.cu": ["-fmad=true"],
     "capi.cu": [],
+    "mesh_layout.cu": [],
 }
 
 

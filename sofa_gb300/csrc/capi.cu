@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/sofa_gb300.h"
+#include "mesh_layout.h"
 #include "sgb_internal.h"
 #include "variants.h"
 
@@ -99,24 +100,17 @@ static void free_mesh(TfemMesh& m)
     cudaFree(m.rowptr);
     cudaFree(m.slots);
     cudaFree(m.eforce);
+    cudaFree(m.elem_orig);
+    cudaFree(m.pl.elem_start);
+    cudaFree(m.pl.node_start);
+    cudaFree(m.pl.lnode_gid);
+    cudaFree(m.pl.lnode_info);
+    cudaFree(m.pl.lrow);
+    cudaFree(m.pl.lslots);
+    cudaFree(m.pl.lconn);
+    cudaFree(m.pl.bnd_rowptr);
+    cudaFree(m.pl.partials);
     m = TfemMesh();
-}
-
-// Node -> (element*4 + corner) table, each row in increasing slot order so
-// a node sums its element terms in the reference's element-loop order.
-static void build_csr(int N, int E, const int32_t* tets, std::vector<int>& rowptr, std::vector<int>& slots,
-                      int& max_valence)
-{
-    rowptr.assign((size_t)N + 1, 0);
-    for (size_t i = 0; i < (size_t)E * 4; ++i) rowptr[(size_t)tets[i] + 1]++;
-    max_valence = 0;
-    for (int n = 0; n < N; ++n) {
-        max_valence = std::max(max_valence, rowptr[(size_t)n + 1]);
-        rowptr[(size_t)n + 1] += rowptr[n];
-    }
-    slots.resize((size_t)E * 4);
-    std::vector<int> pos(rowptr.begin(), rowptr.end() - 1);
-    for (size_t i = 0; i < (size_t)E * 4; ++i) slots[(size_t)pos[tets[i]]++] = (int)i;
 }
 
 extern "C" {
@@ -185,8 +179,24 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     m.young_h = E_h;
     m.poisson_h = nu_h;
     int rc = SGB_OK;
+    // element storage order and patch layout (Morton-ordered patches) for
+    // the fused variants; the reference-rounding variant keeps the caller's
+    // element order
+    HostLayout L;
+    const int pe = ops->real_size == 4 ? 512 : 256;
+    if (ops->uses_patches && method != SGB_METHOD_SMALL && n_tets > 0) {
+        build_patch_layout(n_nodes, n_tets, tetrahedra_host, rest_positions_host, pe, 1024, L);
+    } else {
+        L.perm.resize((size_t)n_tets);
+        L.inv.resize((size_t)n_tets);
+        for (int e = 0; e < n_tets; ++e) L.perm[(size_t)e] = L.inv[(size_t)e] = e;
+    }
     std::vector<int> rowptr, slots;
-    build_csr(n_nodes, n_tets, tetrahedra_host, rowptr, slots, m.max_valence);
+    build_node_csr(n_nodes, n_tets, tetrahedra_host, L.inv, rowptr, slots, m.max_valence);
+    std::vector<int32_t> tets_store((size_t)n_tets * 4);
+    for (size_t s = 0; s < (size_t)n_tets; ++s)
+        for (int c = 0; c < 4; ++c) tets_store[4 * s + c] = tetrahedra_host[4 * (size_t)L.perm[s] + c];
+    m.perm_h = L.perm;
     const size_t rs = ops->real_size, E = (size_t)n_tets;
     size_t* acc = &m.device_bytes;
     double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr, *d_vol = nullptr;
@@ -200,12 +210,58 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
         (rc = dev_alloc_bytes(&m.R0, rs * 9 * E, acc)) || (rc = dev_alloc_bytes(&m.K, rs * 3 * E, acc)) ||
         (rc = dev_alloc_bytes(&m.J, rs * 12 * E, acc)) || (rc = dev_alloc_bytes(&m.rest, rs * 12 * E, acc)) ||
         (rc = dev_alloc_bytes(&m.eforce, rs * 12 * E, acc)) || (rc = dev_alloc(&m.rest_pos, 3 * (size_t)n_nodes, acc)) ||
-        (rc = dev_alloc(&m.rowptr, (size_t)n_nodes + 1, acc)) || (rc = dev_alloc(&m.slots, 4 * E, acc)))
+        (rc = dev_alloc(&m.rowptr, (size_t)n_nodes + 1, acc)) || (rc = dev_alloc(&m.slots, 4 * E, acc)) ||
+        (rc = dev_alloc(&m.elem_orig, E, acc)))
         goto fail_out;
+    if (!L.elem_start.empty()) {
+        PatchLayout& pl = m.pl;
+        pl.n_patches = (int)L.elem_start.size() - 1;
+        pl.pe = pe;
+        pl.max_lnodes = L.max_lnodes;
+        pl.n_partials = L.n_partials;
+        pl.n_lnodes = (int)L.lnode_gid.size();
+        pl.n_boundary = L.n_boundary;
+        if ((rc = dev_alloc(&pl.elem_start, L.elem_start.size(), acc)) ||
+            (rc = dev_alloc(&pl.node_start, L.node_start.size(), acc)) ||
+            (rc = dev_alloc(&pl.lnode_gid, L.lnode_gid.size(), acc)) ||
+            (rc = dev_alloc(&pl.lnode_info, L.lnode_info.size(), acc)) ||
+            (rc = dev_alloc(&pl.lrow, L.lrow.size(), acc)) || (rc = dev_alloc(&pl.lslots, L.lslots.size(), acc)) ||
+            (rc = dev_alloc(&pl.lconn, L.lconn.size(), acc)) ||
+            (rc = dev_alloc(&pl.bnd_rowptr, L.bnd_rowptr.size(), acc)) ||
+            (rc = dev_alloc_bytes(&pl.partials, rs * 3 * (size_t)std::max(L.n_partials, 1), acc)))
+            goto fail_out;
+        struct {
+            void* dst;
+            const void* src;
+            size_t bytes;
+        } up[] = {
+            {pl.elem_start, L.elem_start.data(), sizeof(int) * L.elem_start.size()},
+            {pl.node_start, L.node_start.data(), sizeof(int) * L.node_start.size()},
+            {pl.lnode_gid, L.lnode_gid.data(), sizeof(int) * L.lnode_gid.size()},
+            {pl.lnode_info, L.lnode_info.data(), sizeof(int) * L.lnode_info.size()},
+            {pl.lrow, L.lrow.data(), sizeof(int) * L.lrow.size()},
+            {pl.lslots, L.lslots.data(), sizeof(uint16_t) * L.lslots.size()},
+            {pl.lconn, L.lconn.data(), sizeof(ushort4) * L.lconn.size()},
+            {pl.bnd_rowptr, L.bnd_rowptr.data(), sizeof(int) * L.bnd_rowptr.size()},
+        };
+        for (auto& u : up) {
+            if (u.bytes == 0) continue;
+            if ((ce = cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) {
+                rc = cuda_fail(ce, "cudaMemcpyAsync");
+                goto fail_out;
+            }
+        }
+        m.patch_grid = ops->prepare(&m);
+        if ((ce = cudaGetLastError()) != cudaSuccess) {
+            rc = cuda_fail(ce, "patch kernel attributes");
+            goto fail_out;
+        }
+    }
     if ((rc = dev_alloc(&d_y, E_h.size(), nullptr)) || (rc = dev_alloc(&d_p, nu_h.size(), nullptr)) ||
         (rc = dev_alloc(&d_l, (size_t)std::max(n_lsf, 1), nullptr)) || (rc = dev_alloc(&d_vol, E, nullptr)))
         goto fail_out;
-    if ((ce = cudaMemcpyAsync(m.tets, tetrahedra_host, sizeof(int4) * E, cudaMemcpyHostToDevice, h->stream)) ||
+    if ((ce = cudaMemcpyAsync(m.tets, tets_store.data(), sizeof(int4) * E, cudaMemcpyHostToDevice, h->stream)) ||
+        (ce = cudaMemcpyAsync(m.elem_orig, L.perm.data(), sizeof(int) * E, cudaMemcpyHostToDevice, h->stream)) ||
         (ce = cudaMemcpyAsync(m.rest_pos, rest_positions_host, sizeof(double) * 3 * n_nodes, cudaMemcpyHostToDevice,
                               h->stream)) ||
         (ce = cudaMemcpyAsync(m.rowptr, rowptr.data(), sizeof(int) * rowptr.size(), cudaMemcpyHostToDevice,
@@ -331,14 +387,16 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
     for (int w = 0; w < 2; ++w) {
         if (!dst[w] || E == 0) continue;
         SGB_CUDA_TRY(cudaMemcpy(buf.data(), src[w], rs * 9 * E, cudaMemcpyDeviceToHost));
-        for (size_t e = 0; e < E; ++e)
+        for (size_t e = 0; e < E; ++e) {
+            const size_t o = (size_t)fem->m.perm_h[e];  // caller's element index
             for (int i = 0; i < 3; ++i)
                 for (int j = 0; j < 3; ++j) {
                     // stored: rows of R, SoA; reference convention: R^T row-major
                     size_t k = (size_t)(3 * j + i) * E + e;
                     double v = (rs == 8) ? ((double*)buf.data())[k] : (double)((float*)buf.data())[k];
-                    dst[w][9 * e + 3 * i + j] = v;
+                    dst[w][9 * o + 3 * i + j] = v;
                 }
+        }
     }
     return SGB_OK;
 }
@@ -357,6 +415,76 @@ int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method,
 // ---------------------------------------------------------------------------
 // scene
 // ---------------------------------------------------------------------------
+
+int sgb_patch_layout_check(int n_nodes, const double* rest_positions_host, int n_tets, const int32_t* tetrahedra_host,
+                           int elements_per_patch, int max_nodes_per_patch, int* stats)
+{
+    if (n_nodes <= 0 || n_tets < 0 || !rest_positions_host || (n_tets > 0 && !tetrahedra_host) ||
+        elements_per_patch < 1 || elements_per_patch > 16384 || max_nodes_per_patch < 4 ||
+        max_nodes_per_patch > 65535)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_patch_layout_check: invalid argument");
+    for (size_t i = 0; i < (size_t)n_tets * 4; ++i)
+        if (tetrahedra_host[i] < 0 || tetrahedra_host[i] >= n_nodes)
+            return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_patch_layout_check: node index out of range");
+    HostLayout L;
+    build_patch_layout(n_nodes, n_tets, tetrahedra_host, rest_positions_host, elements_per_patch,
+                       max_nodes_per_patch, L);
+    const int P = (int)L.elem_start.size() - 1;
+    // every (element, corner) is gathered exactly once, by the patch that
+    // holds the element, at the local node that is that corner's node
+    std::vector<int> seen((size_t)n_tets * 4, 0);
+    std::vector<int> owners((size_t)n_nodes, 0), touched((size_t)n_nodes, 0);
+    for (int p = 0; p < P; ++p) {
+        const int e0 = L.elem_start[p], e1 = L.elem_start[p + 1];
+        if (e1 - e0 > elements_per_patch || e1 <= e0) return fail(SGB_ERR_NUMERICAL, "patch element range");
+        const int n0 = L.node_start[p], n1 = L.node_start[p + 1];
+        if (n1 - n0 > max_nodes_per_patch) return fail(SGB_ERR_NUMERICAL, "patch node count");
+        for (int l = n0; l < n1; ++l) {
+            const int g = L.lnode_gid[(size_t)l];
+            if (l > n0 && g <= L.lnode_gid[(size_t)l - 1]) return fail(SGB_ERR_NUMERICAL, "local nodes not sorted");
+            touched[(size_t)g]++;
+            const int info = L.lnode_info[(size_t)l];
+            if (info < 0 || (info & 1)) owners[(size_t)g]++;
+            if (info >= 0) {
+                const int slot = info >> 1;
+                if (slot < L.bnd_rowptr[(size_t)g] || slot >= L.bnd_rowptr[(size_t)g + 1])
+                    return fail(SGB_ERR_NUMERICAL, "partial slot outside the node's range");
+            }
+            int prev = -1;
+            for (int s = L.lrow[(size_t)l]; s < L.lrow[(size_t)l + 1]; ++s) {
+                const int slot = L.lslots[(size_t)s];
+                const int le = slot >> 2, c = slot & 3;
+                if (le >= e1 - e0 || slot <= prev) return fail(SGB_ERR_NUMERICAL, "local slot order");
+                prev = slot;
+                const int st = e0 + le;
+                const int orig = L.perm[(size_t)st];
+                if (tetrahedra_host[4 * (size_t)orig + c] != g) return fail(SGB_ERR_NUMERICAL, "slot node mismatch");
+                const ushort4 lc = L.lconn[(size_t)st];
+                const int ln[4] = {lc.x, lc.y, lc.z, lc.w};
+                if (n0 + ln[c] != l) return fail(SGB_ERR_NUMERICAL, "local connectivity mismatch");
+                seen[4 * (size_t)orig + c]++;
+            }
+        }
+    }
+    int boundary = 0;
+    for (int n = 0; n < n_nodes; ++n) {
+        const int cnt = L.bnd_rowptr[(size_t)n + 1] - L.bnd_rowptr[(size_t)n];
+        if (touched[(size_t)n] > 0 && owners[(size_t)n] != 1) return fail(SGB_ERR_NUMERICAL, "node owner count");
+        if (touched[(size_t)n] > 1 ? cnt != touched[(size_t)n] : cnt != 0)
+            return fail(SGB_ERR_NUMERICAL, "partial slot count");
+        boundary += cnt > 0;
+    }
+    for (size_t i = 0; i < seen.size(); ++i)
+        if (seen[i] != 1) return fail(SGB_ERR_NUMERICAL, "element corner not gathered exactly once");
+    if (stats) {
+        stats[0] = P;
+        stats[1] = L.max_lnodes;
+        stats[2] = (int)L.lnode_gid.size();
+        stats[3] = boundary;
+        stats[4] = L.n_partials;
+    }
+    return SGB_OK;
+}
 
 void sgb_scene_params_default(sgb_scene_params* p)
 {
@@ -384,6 +512,7 @@ static void free_scene(sgb_scene* sc)
     cudaFree(s.b);
     cudaFree(s.xs);
     cudaFree(s.p);
+    cudaFree(s.p2);
     cudaFree(s.q);
     cudaFree(s.r);
     cudaFree(s.cg);
@@ -432,7 +561,8 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     if ((rc = dev_alloc(&s.x, 3 * (size_t)N, acc)) || (rc = dev_alloc(&s.v, 3 * (size_t)N, acc)) ||
         (rc = dev_alloc(&s.fixed, (size_t)N, acc)) || (rc = dev_alloc_bytes(&s.f, rs * 3 * N, acc)) ||
         (rc = dev_alloc_bytes(&s.b, rs * 3 * N, acc)) || (rc = dev_alloc_bytes(&s.xs, rs * 3 * N, acc)) ||
-        (rc = dev_alloc_bytes(&s.p, rs * 3 * N, acc)) || (rc = dev_alloc_bytes(&s.q, rs * 3 * N, acc)) ||
+        (rc = dev_alloc_bytes(&s.p, rs * 3 * N, acc)) || (rc = dev_alloc_bytes(&s.p2, rs * 3 * N, acc)) ||
+        (rc = dev_alloc_bytes(&s.q, rs * 3 * N, acc)) ||
         (rc = dev_alloc_bytes(&s.r, rs * 3 * N, acc)) || (rc = dev_alloc(&s.cg, 1, acc)))
         goto fail_out;
     if (P.node_masses_host && (rc = dev_alloc(&s.node_mass, (size_t)N, acc))) goto fail_out;
@@ -443,7 +573,8 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     }
     if ((ce = cudaMemcpyAsync(s.x, fem->m.rest_pos, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s.stream)) ||
         (ce = cudaMemsetAsync(s.v, 0, sizeof(double) * 3 * N, s.stream)) ||
-        (ce = cudaMemsetAsync(s.p, 0, rs * 3 * N, s.stream)) || (ce = cudaMemsetAsync(s.xs, 0, rs * 3 * N, s.stream)) ||
+        (ce = cudaMemsetAsync(s.p, 0, rs * 3 * N, s.stream)) || (ce = cudaMemsetAsync(s.p2, 0, rs * 3 * N, s.stream)) ||
+        (ce = cudaMemsetAsync(s.xs, 0, rs * 3 * N, s.stream)) ||
         (ce = cudaMemsetAsync(s.cg, 0, sizeof(CgScalars), s.stream)) ||
         (ce = cudaMemcpyAsync(s.fixed, fixed.data(), (size_t)N, cudaMemcpyHostToDevice, s.stream))) {
         rc = cuda_fail(ce, "scene init copy");

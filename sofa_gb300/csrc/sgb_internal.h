@@ -40,6 +40,40 @@ struct NodeCSR {
     const int* slots;   // 4 * n_tets
 };
 
+// Patch layout for the fused matvec: elements are stored in patch order
+// (Morton order of their centroids, cut into patches of at most `pe`
+// elements); each patch lists its nodes (local numbering), its elements'
+// corners in local numbering and, per local node, the (element, corner)
+// slots that touch it. A node touched by one patch is interior to it; a
+// node touched by several patches gets one partial-sum slot per patch and is
+// owned by the first of them.
+struct PatchView {
+    const int* elem_start;      // n_patches + 1, element storage positions
+    const int* node_start;      // n_patches + 1, offsets into the local-node arrays
+    const int* lnode_gid;       // global node id of each local node
+    const int* lnode_info;      // -1: interior; else 2*partial_slot + owner_bit
+    const int* lrow;            // per local node: range in lslots (global offsets), size total+1
+    const uint16_t* lslots;     // local element*4 + corner, sorted by local element
+    const ushort4* lconn;       // per element (storage order): local node indices
+    const int* bnd_rowptr;      // per global node: range of its partial slots (empty if interior)
+    int n_patches;
+    int pe;                     // elements per patch (shared-memory stride)
+    int max_lnodes;             // largest local node count of a patch
+};
+
+struct PatchLayout {
+    int* elem_start = nullptr;
+    int* node_start = nullptr;
+    int* lnode_gid = nullptr;
+    int* lnode_info = nullptr;
+    int* lrow = nullptr;
+    uint16_t* lslots = nullptr;
+    ushort4* lconn = nullptr;
+    int* bnd_rowptr = nullptr;
+    void* partials = nullptr;   // scratch: 3 reals per partial slot
+    int n_patches = 0, pe = 0, max_lnodes = 0, n_partials = 0, n_lnodes = 0, n_boundary = 0;
+};
+
 struct TfemMesh {
     int n_nodes = 0, n_tets = 0, method = METHOD_LARGE, precision = PREC_FP64;
     size_t real_size = 8;
@@ -53,8 +87,12 @@ struct TfemMesh {
     double* rest_pos = nullptr;  // rest positions (FP64, n_nodes*3), used by method=small
     int* rowptr = nullptr;
     int* slots = nullptr;
+    int* elem_orig = nullptr;      // original element index of each storage position
+    std::vector<int> perm_h;       // storage position -> original element index
+    PatchLayout pl;
     int max_valence = 0;
     void* eforce = nullptr;   // scratch: 12 reals per element (corner forces)
+    int patch_grid = 0;       // CTAs of the persistent patch kernels
     double rest_volume = 0.0;
     std::vector<double> young_h, poisson_h;  // as given (for inspection)
     size_t device_bytes = 0;
@@ -100,6 +138,7 @@ struct Scene {
     void* b = nullptr;
     void* xs = nullptr;
     void* p = nullptr;
+    void* p2 = nullptr;            // second CG direction buffer (patch path ping-pong)
     void* q = nullptr;
     void* r = nullptr;
     CgScalars* cg = nullptr;

@@ -4,4 +4,5 @@
 #define SGB_REAL double
 #define SGB_TABLE ops_fp64_exact
 #define SGB_VARIANT_NAME "fp64"
+#define SGB_USES_PATCHES 0
 #include "variant_def.cuh"

@@ -3,4 +3,5 @@
 #define SGB_REAL double
 #define SGB_TABLE ops_fp64_fast
 #define SGB_VARIANT_NAME "fp64_fma"
+#define SGB_USES_PATCHES 1
 #include "variant_def.cuh"

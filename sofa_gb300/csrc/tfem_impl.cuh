@@ -59,14 +59,16 @@ __device__ __forceinline__ void ld3(const float* p, long long i, float o[3])
 // stored in R.
 // ------------------------------------------------------------------------
 template <typename R>
-__global__ void k_init_elements(const double* __restrict__ rest_pos, const int4* __restrict__ tets, int E,
-                                int method, const double* __restrict__ young, int n_young,
-                                const double* __restrict__ poisson, int n_poisson, const double* __restrict__ lsf,
-                                int n_lsf, R* K, R* J, R* rest, R* rot, R* R0, double* vol)
+__global__ void k_init_elements(const double* __restrict__ rest_pos, const int4* __restrict__ tets,
+                                const int* __restrict__ elem_orig, int E, int method,
+                                const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
+                                int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest, R* rot,
+                                R* R0, double* vol)
 {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
-    const int4 t = tets[e];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= E) return;
+    const int e = elem_orig[s];  // material data is indexed by the caller's element order
+    const int4 t = tets[s];
     double pa[3], pb[3], pc[3], pd[3];
     ld3(rest_pos, t.x, pa);
     ld3(rest_pos, t.y, pb);
@@ -77,11 +79,11 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
     double nu = (n_poisson > e) ? poisson[e] : poisson[0];
     double f = (n_lsf > 0) ? lsf[(size_t)e * (size_t)n_lsf / (size_t)E] : 1.0;
     Ey = f * Ey;
-    double s = (Ey * (1 - nu)) / ((1 + nu) * (1 - 2 * nu));
+    double sc = (Ey * (1 - nu)) / ((1 + nu) * (1 - 2 * nu));
     double k0 = 1.0, k1 = nu / (1 - nu), k2 = (1 - 2 * nu) / (2 * (1 - nu));
-    k0 *= s;
-    k1 *= s;
-    k2 *= s;
+    k0 *= sc;
+    k1 *= sc;
+    k2 *= sc;
     double ea[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
     double eb[3] = {pc[0] - pa[0], pc[1] - pa[1], pc[2] - pa[2]};
     double ec[3] = {pd[0] - pa[0], pd[1] - pa[1], pd[2] - pa[2]};
@@ -91,14 +93,14 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
     dt += cr[1] * ec[1];
     dt += cr[2] * ec[2];
     double v = fabs(dt / 6.0);
-    vol[e] = v;
+    vol[s] = v;
     k0 /= v * 36;
     k1 /= v * 36;
     k2 /= v * 36;
     const size_t En = (size_t)E;
-    K[0 * En + e] = (R)k0;
-    K[1 * En + e] = (R)k1;
-    K[2 * En + e] = (R)k2;
+    K[0 * En + s] = (R)k0;
+    K[1 * En + s] = (R)k1;
+    K[2 * En + s] = (R)k2;
 
     double Jd[12], rr[12];
     double Rm[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -134,11 +136,11 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
             rr[0] = rr[1] = rr[2] = 0.0;
         }
     }
-    for (int i = 0; i < 12; ++i) J[(size_t)i * En + e] = (R)Jd[i];
-    for (int i = 0; i < 12; ++i) rest[(size_t)i * En + e] = (R)rr[i];
+    for (int i = 0; i < 12; ++i) J[(size_t)i * En + s] = (R)Jd[i];
+    for (int i = 0; i < 12; ++i) rest[(size_t)i * En + s] = (R)rr[i];
     for (int i = 0; i < 9; ++i) {
-        rot[(size_t)i * En + e] = (R)Rm[i];
-        R0[(size_t)i * En + e] = (R)Rm[i];
+        rot[(size_t)i * En + s] = (R)Rm[i];
+        R0[(size_t)i * En + s] = (R)Rm[i];
     }
 }
 
@@ -743,6 +745,216 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict_
 }
 
 // ------------------------------------------------------------------------
+// fused patch matvec: one CTA per patch of elements (persistent over
+// patches). Phase 0 loads the patch's nodal values into shared memory (and
+// forms the CG direction p); phase 1 computes every element's four corner
+// terms R K R^T (p_i - p_a) into shared memory; phase 2 sums, for each local
+// node, its (element, corner) slots in element order -- a deterministic
+// gather with no atomics. Nodes touched by this patch only are finished
+// here; nodes shared with other patches leave one partial sum per patch.
+// MODE 0: addDForce of the C ABI (df -= sum); MODE 1/2: CG matvec with p = r
+// (first iteration) or p = p_old*beta + r, q = mF M p - sum, projected, and
+// p^T A p from element energies plus the mass term.
+// ------------------------------------------------------------------------
+constexpr int kPatchThreads = 128;
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kPatchThreads) k_patch_matvec(PatchView pv, ElemView<R> ev,
+                                                                const R* __restrict__ rin, const R* __restrict__ pold,
+                                                                R* __restrict__ pnew, CgScalars* cg, R kf, MassArgs ma,
+                                                                double mf, const uint8_t* __restrict__ fixed,
+                                                                R* __restrict__ qout, R* __restrict__ partials,
+                                                                SolveConsts sc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* ef = reinterpret_cast<R*>(smem_raw);  // [12][pe]
+    R* lp = ef + 12 * pv.pe;                 // [max_lnodes][3]
+    if (MODE != 0 && cg->done) return;
+    const R beta = (MODE == 2) ? (R)cg->beta : R(0);
+    const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    const size_t En = (size_t)ev.n_tets;
+    double energy = 0.0;  // FP64 across patches; FP32 within one patch
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
+        R pen = R(0);
+        const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
+        const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+        // phase 0: nodal values of the patch
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int g = pv.lnode_gid[n0 + l];
+            R v[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const R rv = rin[3 * (size_t)g + k];
+                v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
+                lp[3 * l + k] = v[k];
+            }
+            if (MODE != 0) {
+                const int info = pv.lnode_info[n0 + l];
+                if (info < 0 || (info & 1)) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
+                }
+            }
+        }
+        __syncthreads();
+        // phase 1: element terms
+        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+            const size_t e = (size_t)(e0 + le);
+            const ushort4 c = pv.lconn[e];
+            const int ln[4] = {c.x, c.y, c.z, c.w};
+            R xr[4][3];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
+            // relative to node a: J^T annihilates translations
+#pragma unroll
+            for (int i = 3; i >= 0; --i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
+            R Rm[9], K[3], J[12];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
+#pragma unroll
+            for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
+            R X[12], F[12];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
+            element_force(F, X, K, J, kf);
+            R en = R(0);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const R ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
+                    ef[(3 * i + k) * pv.pe + le] = ck;
+                    en += xr[i][k] * ck;
+                }
+            if (MODE != 0) pen -= en;
+        }
+        __syncthreads();
+        // phase 2: per local node, its slots in element order
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int s0 = pv.lrow[n0 + l], s1 = pv.lrow[n0 + l + 1];
+            R a0 = R(0), a1 = R(0), a2 = R(0);
+            for (int s = s0; s < s1; ++s) {
+                const int slot = pv.lslots[s];
+                const int le = slot >> 2, cc = slot & 3;
+                a0 += ef[(3 * cc + 0) * pv.pe + le];
+                a1 += ef[(3 * cc + 1) * pv.pe + le];
+                a2 += ef[(3 * cc + 2) * pv.pe + le];
+            }
+            const int g = pv.lnode_gid[n0 + l];
+            const int info = pv.lnode_info[n0 + l];
+            if (info >= 0) {
+                R* o = partials + 3 * (size_t)(info >> 1);
+                o[0] = a0;
+                o[1] = a1;
+                o[2] = a2;
+            }
+            if (MODE == 0) {
+                if (info < 0) {
+                    qout[3 * (size_t)g] -= a0;
+                    qout[3 * (size_t)g + 1] -= a1;
+                    qout[3 * (size_t)g + 2] -= a2;
+                }
+            } else if (info < 0 || (info & 1)) {
+                const R p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
+                const R mm = ma.node_mass ? (R)(ma.node_mass[g] * mf) : mmu;
+                pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
+                if (info < 0) {
+                    R q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
+                    if (fixed[g]) q0 = q1 = q2 = R(0);
+                    qout[3 * (size_t)g] = q0;
+                    qout[3 * (size_t)g + 1] = q1;
+                    qout[3 * (size_t)g + 2] = q2;
+                }
+            }
+        }
+        energy += (double)pen;
+        __syncthreads();
+    }
+    if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
+}
+
+// C ABI addDForce, second pass: nodes shared by several patches subtract
+// their partial sums in patch order.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restrict__ bnd_rowptr,
+                                                            const R* __restrict__ partials, R* __restrict__ df, int N)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
+        if (b0 == b1) continue;
+        R a0 = R(0), a1 = R(0), a2 = R(0);
+        for (int b = b0; b < b1; ++b) {
+            a0 += partials[3 * (size_t)b];
+            a1 += partials[3 * (size_t)b + 1];
+            a2 += partials[3 * (size_t)b + 2];
+        }
+        df[3 * (size_t)n] -= a0;
+        df[3 * (size_t)n + 1] -= a1;
+        df[3 * (size_t)n + 2] -= a2;
+    }
+}
+
+// CG update after a patch matvec: completes q on shared nodes (mass term
+// minus the patches' partial sums, projected), then x += alpha p,
+// r += -alpha q and rho = r.r.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_cg_update_patch(R* __restrict__ xs, R* __restrict__ r,
+                                                                const R* __restrict__ p, const R* __restrict__ q,
+                                                                const R* __restrict__ partials,
+                                                                const int* __restrict__ bnd_rowptr, MassArgs ma,
+                                                                double mf, const uint8_t* __restrict__ fixed,
+                                                                CgScalars* cg, int N, SolveConsts sc)
+{
+    if (cg->done) return;
+    const R alpha = (R)cg->alpha;
+    const R nalpha = -alpha;
+    const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    double local = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const size_t i3 = 3 * (size_t)n;
+        const R pp[3] = {p[i3], p[i3 + 1], p[i3 + 2]};
+        R qq[3];
+        const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
+        if (b0 == b1) {
+            qq[0] = q[i3];
+            qq[1] = q[i3 + 1];
+            qq[2] = q[i3 + 2];
+        } else {
+            R a0 = R(0), a1 = R(0), a2 = R(0);
+            for (int b = b0; b < b1; ++b) {
+                a0 += partials[3 * (size_t)b];
+                a1 += partials[3 * (size_t)b + 1];
+                a2 += partials[3 * (size_t)b + 2];
+            }
+            const R mm = ma.node_mass ? (R)(ma.node_mass[n] * mf) : mmu;
+            qq[0] = mm * pp[0] - a0;
+            qq[1] = mm * pp[1] - a1;
+            qq[2] = mm * pp[2] - a2;
+            if (fixed[n]) qq[0] = qq[1] = qq[2] = R(0);
+        }
+        R rr[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            xs[i3 + k] = xs[i3 + k] + pp[k] * alpha;
+            rr[k] = r[i3 + k] + qq[k] * nalpha;
+            r[i3 + k] = rr[k];
+        }
+        // the node's three-term sum in R, the running sum over nodes in FP64
+        local += (double)(rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2]);
+    }
+    finish_dot<FIN_RHO>(local, cg, nullptr, N, sc);
+}
+
+// ------------------------------------------------------------------------
 // host launchers
 // ------------------------------------------------------------------------
 inline int node_grid(int N)
@@ -773,8 +985,8 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
 {
     if (m->n_tets == 0) return;
     k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
-        m->rest_pos, m->tets, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K, (R*)m->J,
-        (R*)m->rest, (R*)m->rot, (R*)m->R0, vol);
+        m->rest_pos, m->tets, m->elem_orig, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K,
+        (R*)m->J, (R*)m->rest, (R*)m->rot, (R*)m->R0, vol);
 }
 
 template <typename R>
@@ -803,6 +1015,54 @@ void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScala
         k_elem_dforce<R, VIN, METHOD_LARGE, DIR><<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce);
 }
 
+inline PatchView patch_view(TfemMesh* m)
+{
+    PatchView pv;
+    pv.elem_start = m->pl.elem_start;
+    pv.node_start = m->pl.node_start;
+    pv.lnode_gid = m->pl.lnode_gid;
+    pv.lnode_info = m->pl.lnode_info;
+    pv.lrow = m->pl.lrow;
+    pv.lslots = m->pl.lslots;
+    pv.lconn = m->pl.lconn;
+    pv.bnd_rowptr = m->pl.bnd_rowptr;
+    pv.n_patches = m->pl.n_patches;
+    pv.pe = m->pl.pe;
+    pv.max_lnodes = m->pl.max_lnodes;
+    return pv;
+}
+
+template <typename R>
+size_t patch_smem_bytes(const TfemMesh* m)
+{
+    return sizeof(R) * (12 * (size_t)m->pl.pe + 3 * (size_t)m->pl.max_lnodes);
+}
+
+// Sets the shared-memory attribute of the patch kernels and returns the grid
+// (CTAs resident at once, capped by the dot-product partial array).
+template <typename R>
+int prepare_patch(TfemMesh* m)
+{
+    const size_t smem = patch_smem_bytes<R>(m);
+    int dev = 0, sms = 0, nb0 = 0, nb1 = 0, nb2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(k_patch_matvec<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, k_patch_matvec<R, 0>, kPatchThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, kPatchThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, kPatchThreads, smem);
+    int nb = nb0 < nb1 ? nb0 : nb1;
+    nb = nb < nb2 ? nb : nb2;
+    if (nb < 1) nb = 1;
+    long long g = (long long)nb * sms;
+    if (g > kMaxNodeBlocks) g = kMaxNodeBlocks;
+    if (g > m->pl.n_patches) g = m->pl.n_patches;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
 // Public per-call operations (the drop-in for
 // TetrahedronFEMForceFieldCuda3{f,d}_addForce / _addDForce).
 template <typename R, typename VO>
@@ -817,6 +1077,16 @@ void api_add_force(TfemMesh* m, const double* x, VO* f, cudaStream_t s)
 template <typename R>
 void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
 {
+    if (m->pl.n_patches > 0 && m->method != METHOD_SMALL) {
+        PatchView pv = patch_view(m);
+        MassArgs ma{nullptr, 0.0, {0.0, 0.0, 0.0}};
+        SolveConsts sc{0.0, 0.0, 0};
+        k_patch_matvec<R, 0><<<m->patch_grid, kPatchThreads, patch_smem_bytes<R>(m), s>>>(
+            pv, view<R>(m), dx, nullptr, nullptr, nullptr, kfactor, ma, 1.0, nullptr, df, (R*)m->pl.partials, sc);
+        k_patch_fixup<R><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(m->pl.bnd_rowptr, (const R*)m->pl.partials, df,
+                                                                      m->n_nodes);
+        return;
+    }
     launch_elem_dforce<R, R, 0>(m, dx, nullptr, nullptr, kfactor, s);
     NodeCSR csr{m->rowptr, m->slots};
     k_gather_accumulate<R, R, true><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, df,
@@ -868,6 +1138,54 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
                                                             sc->fixed, q, sc->cg, dot_terms, N, cons);
         }
         k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons);
+    }
+    const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
+    k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);
+}
+
+// The same step with the fused patch matvec: two launches per CG iteration
+// (patch matvec + update), the CG direction p ping-pongs between two buffers.
+template <typename R>
+void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
+{
+    TfemMesh* m = sc->mesh;
+    const int N = sc->n;
+    const SceneParams& P = sc->prm;
+    const double h = P.dt;
+    NodeCSR csr{m->rowptr, m->slots};
+    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const int ng = node_grid(N);
+    R* f = (R*)sc->f;
+    R* b = (R*)sc->b;
+    R* r = (R*)sc->r;
+    R* pb[2] = {(R*)sc->p, (R*)sc->p2};
+    R* q = (R*)sc->q;
+    R* xs = (R*)sc->xs;
+    R* partials = (R*)m->pl.partials;
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1};
+    launch_elem_force<R>(m, sc->x, s);
+    k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
+    const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
+    launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)kf_rhs, s);
+    k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass, mass_first,
+                                              h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons);
+    const double mf = 1 + 1.0 * h * P.rayleigh_mass;
+    const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    PatchView pv = patch_view(m);
+    ElemView<R> ev = view<R>(m);
+    const size_t smem = patch_smem_bytes<R>(m);
+    for (int it = 1; it <= P.cg_iterations; ++it) {
+        cons.it = it;
+        R* pold = pb[it & 1];
+        R* pnew = pb[(it + 1) & 1];
+        if (it == 1)
+            k_patch_matvec<R, 1><<<m->patch_grid, kPatchThreads, smem, s>>>(pv, ev, r, pold, pnew, sc->cg, (R)kf, ma,
+                                                                             mf, sc->fixed, q, partials, cons);
+        else
+            k_patch_matvec<R, 2><<<m->patch_grid, kPatchThreads, smem, s>>>(pv, ev, r, pold, pnew, sc->cg, (R)kf, ma,
+                                                                             mf, sc->fixed, q, partials, cons);
+        k_cg_update_patch<R><<<ng, kNodeBlock, 0, s>>>(xs, r, pnew, q, partials, m->pl.bnd_rowptr, ma, mf, sc->fixed,
+                                                       sc->cg, N, cons);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);

@@ -3,4 +3,5 @@
 #define SGB_REAL float
 #define SGB_TABLE ops_mixed
 #define SGB_VARIANT_NAME "mixed"
+#define SGB_USES_PATCHES 1
 #include "variant_def.cuh"

@@ -19,11 +19,16 @@ static void v_add_dforce(TfemMesh* m, const void* dx, void* df, double k, cudaSt
 }
 static void v_scene_step(Scene* sc, double* terms, int mass_first, cudaStream_t s)
 {
-    scene_step<SGB_REAL>(sc, terms, mass_first, s);
+    if (SGB_USES_PATCHES && sc->mesh->pl.n_patches > 0 && sc->mesh->method != METHOD_SMALL)
+        scene_step_patch<SGB_REAL>(sc, mass_first, s);
+    else
+        scene_step<SGB_REAL>(sc, terms, mass_first, s);
 }
+static int v_prepare(TfemMesh* m) { return m->pl.n_patches > 0 ? prepare_patch<SGB_REAL>(m) : 0; }
 }  // namespace SGB_NS
 
 namespace sgb {
-const VariantOps SGB_TABLE = {SGB_VARIANT_NAME, sizeof(SGB_REAL), SGB_NS::v_init, SGB_NS::v_add_force,
-                              SGB_NS::v_add_dforce, SGB_NS::v_scene_step};
+const VariantOps SGB_TABLE = {SGB_VARIANT_NAME,     sizeof(SGB_REAL),     SGB_USES_PATCHES,
+                              SGB_NS::v_init,       SGB_NS::v_add_force,  SGB_NS::v_add_dforce,
+                              SGB_NS::v_scene_step, SGB_NS::v_prepare};
 }

@@ -9,11 +9,13 @@ namespace sgb {
 struct VariantOps {
     const char* name;
     size_t real_size;
+    int uses_patches;  // fused patch matvec (the reference-rounding variant keeps the element-order gather)
     void (*init)(TfemMesh*, const double* young, int ny, const double* poisson, int np, const double* lsf, int nl,
                  double* vol, cudaStream_t);
     void (*add_force)(TfemMesh*, const double* x, void* f, cudaStream_t);
     void (*add_dforce)(TfemMesh*, const void* dx, void* df, double kfactor, cudaStream_t);
     void (*scene_step)(Scene*, double* dot_terms, int mass_first, cudaStream_t);
+    int (*prepare)(TfemMesh*);  // kernel attributes; returns the patch-kernel grid
 };
 
 extern const VariantOps ops_fp64_exact;

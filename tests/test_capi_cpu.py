@@ -70,3 +70,40 @@ def test_scene_params_defaults_match_reference_data(capi):
     # EulerImplicitSolver.cpp:40-51 and CGLinearSolver.inl:34-46 defaults
     assert p.rayleigh_stiffness == 0.0 and p.rayleigh_mass == 0.0
     assert p.cg_iterations == 25 and p.cg_tolerance == 1e-5 and p.cg_threshold == 1e-5
+
+
+@pytest.mark.parametrize("n,pe,pn", [((5, 5, 21), 64, 64), ((9, 7, 13), 1024, 1024), ((12, 12, 40), 1024, 1024),
+                                      ((6, 6, 6), 7, 20)])
+def test_patch_layout_invariants(capi, n, pe, pn):
+    """The fused matvec's layout: every element corner is gathered exactly
+    once, every node has one owner, shared nodes get one partial slot per
+    patch (host logic, no GPU)."""
+    from sofa_gb300 import topology as topo
+
+    mesh = topo.beam(n, spacing=0.5, jitter=0.05, seed=1)
+    stats = (ctypes.c_int * 5)()
+    lib = capi.load()
+    lib.sgb_patch_layout_check.argtypes = [ctypes.c_int, capi._dp, ctypes.c_int, capi._ip, ctypes.c_int,
+                                           ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    pos = np.ascontiguousarray(mesh.positions)
+    tets = np.ascontiguousarray(mesh.tetrahedra, dtype=np.int32)
+    rc = lib.sgb_patch_layout_check(mesh.n_nodes, pos.ctypes.data_as(capi._dp), mesh.n_tets,
+                                    tets.ctypes.data_as(capi._ip), pe, pn, stats)
+    assert rc == 0, capi.last_error()
+    patches, max_ln, total_ln, boundary, partials = list(stats)
+    assert patches >= mesh.n_tets // pe
+    assert max_ln <= pn
+    assert total_ln >= mesh.n_nodes
+    assert partials >= 2 * boundary
+
+
+def test_patch_layout_random_soup(capi):
+    """Unstructured input: random tetrahedra over random points."""
+    rng = np.random.default_rng(3)
+    pos = rng.normal(size=(300, 3))
+    tets = np.stack([rng.choice(300, 4, replace=False) for _ in range(2000)]).astype(np.int32)
+    stats = (ctypes.c_int * 5)()
+    lib = capi.load()
+    rc = lib.sgb_patch_layout_check(300, pos.ctypes.data_as(capi._dp), 2000, tets.ctypes.data_as(capi._ip), 128, 100,
+                                    stats)
+    assert rc == 0, capi.last_error()
