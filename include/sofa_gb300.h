@@ -107,6 +107,36 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
 int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method, int* precision,
                   size_t* device_bytes);
 
+/* addDForce for callers that cannot allocate device memory: a framework
+ * that hands out device buffers from its own pool, a real-time loop that
+ * must avoid the device synchronisation cudaMalloc/cudaFree imply, or code
+ * running where new allocations are not allowed. It calls no cudaMalloc,
+ * cudaFree or allocating routine: the caller passes every input and output
+ * as device arrays, and the only scratch (12 floats per tetrahedron between
+ * the element pass and the node gather) lives in a fixed array of the
+ * library's device memory holding 262,144 tetrahedra (12 MiB, kept by every
+ * GPU that loads the library until the process exits). Larger meshes are
+ * rejected with SGB_ERR_INVALID_ARGUMENT. All calls share that array, so two
+ * calls that overlap on the GPU (unordered streams) race and give wrong
+ * results; order them on one stream. The first call on a device looks up
+ * the array's device address once for that device; make that first call
+ * before any stream capture. This entry point has no counterpart in the
+ * reference: it is a variant of sgb_tfem_add_dforce_f32 for such callers.
+ * Computes df -= kfactor R K R^T dx per tetrahedron, FP32, with arrays:
+ *   tetrahedra_dev        4 int32 per tetrahedron (node indices < n_nodes), 16-byte aligned
+ *   rotations_dev         9 x n_tets floats: entry k of tetrahedron e at [k*n_tets+e] is
+ *                         R(k/3, k%3), R's rows being the element frame (R = rotations[e]^T
+ *                         of TetrahedronFEMForceField)
+ *   stiffness_dev         3 x n_tets: K(0,0), K(0,1), K(3,3) of the 6x6 material stiffness / (36 V)
+ *   strain_displacement_dev 12 x n_tets: per node i, J(3i,0), J(3i,3), J(3i,5)
+ *   node_rowptr_dev, node_slots_dev  node -> (tetrahedron*4 + corner) table, n_nodes+1
+ *                         offsets and 4*n_tets entries, each row in increasing order
+ *   dx_dev, df_dev        n_nodes xyz triples; df accumulates. */
+int sgb_tfem_add_dforce_f32_noalloc(int n_nodes, int n_tets, const int32_t* tetrahedra_dev, const float* rotations_dev,
+                                    const float* stiffness_dev, const float* strain_displacement_dev,
+                                    const int32_t* node_rowptr_dev, const int32_t* node_slots_dev,
+                                    const float* dx_dev, float* df_dev, float kfactor, void* stream);
+
 /* Host-only check of the element ordering and patch layout the fused
  * kernels use (no GPU needed): every (element, corner) gathered exactly once
  * by one patch, one owner per node, partial-sum slots in patch order.

@@ -29,6 +29,7 @@ UNITS = {
     "tfem_mixed.cu": ["-fmad=true"],
     "capi.cu": [],
     "mesh_layout.cu": [],
+    "noalloc.cu": [],
 }
 
 

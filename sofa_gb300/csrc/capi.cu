@@ -77,6 +77,8 @@ struct sgb_scene {
 };
 
 namespace sgb {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 const VariantOps* variant_for(int precision)
 {
     switch (precision) {
