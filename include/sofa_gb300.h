@@ -213,6 +213,55 @@ int sgb_scene_state_device(sgb_scene_t* scene, double** x_dev, double** v_dev);
 /* The scene's stream (cudaStream_t as void*). */
 void* sgb_scene_stream(sgb_scene_t* scene);
 
+/* ------------------------------------------------------------------ */
+/* Batch: many meshes advanced together on one GPU                      */
+/* ------------------------------------------------------------------ */
+/* Every admitted mesh advances one implicit Euler step per sgb_batch_step,
+ * through one persistent kernel per phase for all meshes (no reference
+ * counterpart: the reference visits each mesh's components one after the
+ * other, Sofa/framework/Simulation/Core/src/sofa/simulation/
+ * MappingGraphMechanicalOperations.cpp:41-92). Meshes live in a fixed HBM
+ * arena whose size is the admission budget; they can be added and removed
+ * between steps. Methods large and polar; precision MIXED or FP64_FMA. */
+typedef struct sgb_batch sgb_batch_t;
+
+typedef struct sgb_mesh_desc {
+    int n_nodes;
+    const double* rest_positions_host;  /* 3 n_nodes */
+    int n_tets;
+    const int32_t* tetrahedra_host;     /* 4 n_tets */
+    const double* young;                /* 1 or n_tets values */
+    int n_young;
+    const double* poisson;              /* 1 or n_tets values */
+    int n_poisson;
+    int method;                         /* SGB_METHOD_LARGE or SGB_METHOD_POLAR */
+    sgb_scene_params params;            /* solver, mass, gravity, fixed nodes */
+    const double* external_force_host;  /* optional 3 n_nodes constant external force, or NULL */
+} sgb_mesh_desc;
+
+/* hbm_budget_bytes is reserved at once and is the admission budget;
+ * max_cg_iterations bounds every mesh's CGLinearSolver iterations. */
+int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, int max_meshes,
+                     int max_cg_iterations);
+int sgb_batch_destroy(sgb_batch_t* batch);
+/* Bytes a mesh would take in the budget (host-side planning only). */
+int sgb_batch_mesh_bytes(const sgb_batch_t* batch, const sgb_mesh_desc* mesh, size_t* bytes);
+/* Admission: SGB_ERR_BUDGET when the mesh does not fit or no slot is free.
+ * Synchronous; positions start at rest, velocities at zero. */
+int sgb_batch_add_mesh(sgb_batch_t* batch, const sgb_mesh_desc* mesh, int* slot);
+int sgb_batch_remove_mesh(sgb_batch_t* batch, int slot);
+/* Advances every admitted mesh by n_steps (stream-ordered, CUDA graph). */
+int sgb_batch_step(sgb_batch_t* batch, int n_steps);
+int sgb_batch_sync(sgb_batch_t* batch);
+int sgb_batch_mesh_stats(sgb_batch_t* batch, int slot, int* cg_iterations, double* cg_residual, long long* steps);
+int sgb_batch_get_state(sgb_batch_t* batch, int slot, double* x_host, double* v_host);
+/* Queues the copy of a mesh's positions on the batch stream (no wait). */
+int sgb_batch_get_positions_async(sgb_batch_t* batch, int slot, double* x_host);
+int sgb_batch_set_state(sgb_batch_t* batch, int slot, const double* x_host, const double* v_host);
+int sgb_batch_info(const sgb_batch_t* batch, int* active_meshes, long long* active_tets, size_t* budget_used,
+                   size_t* budget_total);
+void* sgb_batch_stream(sgb_batch_t* batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,7 @@ UNITS = {
     "capi.cu": [],
     "mesh_layout.cu": [],
     "noalloc.cu": [],
+    "batch.cu": [],
 }
 
 

@@ -54,6 +54,22 @@ class SceneParams(ctypes.Structure):
     ]
 
 
+class MeshDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_nodes", ctypes.c_int),
+        ("rest_positions_host", ctypes.POINTER(ctypes.c_double)),
+        ("n_tets", ctypes.c_int),
+        ("tetrahedra_host", ctypes.POINTER(ctypes.c_int32)),
+        ("young", ctypes.POINTER(ctypes.c_double)),
+        ("n_young", ctypes.c_int),
+        ("poisson", ctypes.POINTER(ctypes.c_double)),
+        ("n_poisson", ctypes.c_int),
+        ("method", ctypes.c_int),
+        ("params", SceneParams),
+        ("external_force_host", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
 _lib = None
 _dp = ctypes.POINTER(ctypes.c_double)
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -94,6 +110,20 @@ def load():
         "sgb_scene_set_external_force": (c_int, [_vp, _dp]),
         "sgb_scene_state_device": (c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
         "sgb_scene_stream": (_vp, [_vp]),
+        "sgb_batch_create": (c_int, [ctypes.POINTER(_vp), c_int, ctypes.c_size_t, c_int, c_int]),
+        "sgb_batch_destroy": (c_int, [_vp]),
+        "sgb_batch_mesh_bytes": (c_int, [_vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(ctypes.c_size_t)]),
+        "sgb_batch_add_mesh": (c_int, [_vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(c_int)]),
+        "sgb_batch_remove_mesh": (c_int, [_vp, c_int]),
+        "sgb_batch_step": (c_int, [_vp, c_int]),
+        "sgb_batch_sync": (c_int, [_vp]),
+        "sgb_batch_mesh_stats": (c_int, [_vp, c_int, ctypes.POINTER(c_int), _dp, ctypes.POINTER(ctypes.c_longlong)]),
+        "sgb_batch_get_state": (c_int, [_vp, c_int, _dp, _dp]),
+        "sgb_batch_get_positions_async": (c_int, [_vp, c_int, _dp]),
+        "sgb_batch_set_state": (c_int, [_vp, c_int, _dp, _dp]),
+        "sgb_batch_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong),
+                                   ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+        "sgb_batch_stream": (_vp, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -278,3 +308,137 @@ class Scene:
     @property
     def stream(self):
         return load().sgb_scene_stream(self._h)
+
+
+def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0, cg_iterations=25,
+                 cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0), vertex_mass=1.0,
+                 node_masses=None, fixed=(), fix_all=False, keep=None):
+    """A filled SceneParams; `keep` collects the numpy buffers it points to."""
+    lib = load()
+    p = SceneParams()
+    lib.sgb_scene_params_default(ctypes.byref(p))
+    p.dt = dt
+    p.rayleigh_stiffness = rayleigh_stiffness
+    p.rayleigh_mass = rayleigh_mass
+    p.vdamping = vdamping
+    p.cg_iterations = int(cg_iterations)
+    p.cg_tolerance = cg_tolerance
+    p.cg_threshold = cg_threshold
+    for k in range(3):
+        p.gravity[k] = float(gravity[k])
+    p.vertex_mass = float(vertex_mass)
+    keep = [] if keep is None else keep
+    if node_masses is not None:
+        nm, p.node_masses_host = _d(node_masses)
+        keep.append(nm)
+    fx, p.fixed_host = _i(np.asarray(fixed, dtype=np.int32).reshape(-1) if len(fixed) else np.zeros(1, np.int32))
+    keep.append(fx)
+    p.n_fixed = len(fixed)
+    p.fix_all = int(fix_all)
+    p.mass_first = 1
+    return p
+
+
+class Batch:
+    """Handle of sgb_batch_t: many meshes stepped together in one HBM arena."""
+
+    def __init__(self, precision="mixed", budget_bytes=1 << 30, max_meshes=64, max_cg_iterations=25):
+        lib = load()
+        h = _vp()
+        check(lib.sgb_batch_create(ctypes.byref(h), PRECISIONS[precision], int(budget_bytes), int(max_meshes),
+                                   int(max_cg_iterations)))
+        self._h = h
+        self.precision = precision
+        self.n_nodes = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().sgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def mesh_desc(positions, tetrahedra, young=5000.0, poisson=0.45, method="large", external_force=None, **params):
+        keep = []
+        d = MeshDesc()
+        pos, d.rest_positions_host = _d(np.asarray(positions).reshape(-1, 3))
+        tets, d.tetrahedra_host = _i(np.asarray(tetrahedra).reshape(-1, 4))
+        y, d.young = _d(np.atleast_1d(young))
+        nu, d.poisson = _d(np.atleast_1d(poisson))
+        keep += [pos, tets, y, nu]
+        d.n_nodes = pos.shape[0]
+        d.n_tets = tets.shape[0]
+        d.n_young = y.size
+        d.n_poisson = nu.size
+        d.method = METHODS[method]
+        if "vertex_mass" not in params:
+            params["vertex_mass"] = float(params.pop("total_mass", 1.0)) / d.n_nodes
+        d.params = scene_params(keep=keep, **params)
+        if external_force is not None:
+            ext, d.external_force_host = _d(np.asarray(external_force).reshape(-1, 3))
+            keep.append(ext)
+        return d, keep
+
+    def mesh_bytes(self, positions, tetrahedra, **kw):
+        d, keep = self.mesh_desc(positions, tetrahedra, **kw)
+        b = ctypes.c_size_t()
+        check(load().sgb_batch_mesh_bytes(self._h, ctypes.byref(d), ctypes.byref(b)))
+        return b.value
+
+    def add_mesh(self, positions, tetrahedra, **kw):
+        """Admits a mesh; returns its slot. Raises SgbError(-6) when it does not fit."""
+        d, keep = self.mesh_desc(positions, tetrahedra, **kw)
+        slot = ctypes.c_int()
+        check(load().sgb_batch_add_mesh(self._h, ctypes.byref(d), ctypes.byref(slot)))
+        self.n_nodes[slot.value] = d.n_nodes
+        return slot.value
+
+    def remove_mesh(self, slot):
+        check(load().sgb_batch_remove_mesh(self._h, int(slot)))
+        self.n_nodes.pop(slot, None)
+
+    def step(self, n=1):
+        check(load().sgb_batch_step(self._h, int(n)))
+
+    def sync(self):
+        check(load().sgb_batch_sync(self._h))
+
+    def stats(self, slot):
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        steps = ctypes.c_longlong()
+        check(load().sgb_batch_mesh_stats(self._h, int(slot), ctypes.byref(it), ctypes.byref(res),
+                                          ctypes.byref(steps)))
+        return it.value, res.value, steps.value
+
+    def state(self, slot):
+        n = self.n_nodes[slot]
+        x = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        check(load().sgb_batch_get_state(self._h, int(slot), x.ctypes.data_as(_dp), v.ctypes.data_as(_dp)))
+        return x, v
+
+    def positions_async(self, slot, out):
+        check(load().sgb_batch_get_positions_async(self._h, int(slot), out.ctypes.data_as(_dp)))
+
+    def set_state(self, slot, x=None, v=None):
+        xa, px = _d(np.asarray(x).reshape(-1, 3)) if x is not None else (None, _dp())
+        va, pv = _d(np.asarray(v).reshape(-1, 3)) if v is not None else (None, _dp())
+        check(load().sgb_batch_set_state(self._h, int(slot), px, pv))
+
+    def info(self):
+        n = ctypes.c_int()
+        t = ctypes.c_longlong()
+        u = ctypes.c_size_t()
+        tot = ctypes.c_size_t()
+        check(load().sgb_batch_info(self._h, ctypes.byref(n), ctypes.byref(t), ctypes.byref(u), ctypes.byref(tot)))
+        return {"meshes": n.value, "tets": t.value, "budget_used": u.value, "budget_total": tot.value}
+
+    @property
+    def stream(self):
+        return load().sgb_batch_stream(self._h)

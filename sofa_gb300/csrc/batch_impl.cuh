@@ -1,0 +1,406 @@
+// Batched multi-mesh kernels: every admitted mesh advances one implicit
+// Euler step through the same launches. Each launch is a persistent grid
+// that walks a device-resident work list (patches, element ranges or node
+// chunks of all active meshes); the mesh of an item is found through its
+// slot's BMeshDesc. Per-mesh dot products are reduced without float atomics:
+// every item writes its partial sum, an integer ticket per mesh elects the
+// last item, which adds the mesh's partials in index order and updates that
+// mesh's CG scalars (CGLinearSolver::solve, Sofa/Component/LinearSolver/
+// Iterative/src/sofa/component/linearsolver/iterative/CGLinearSolver.inl:
+// 102-272). Meshes whose CG has stopped skip their items.
+//
+// Included by the variant translation units after tfem_impl.cuh, inside
+// SGB_NS, for R = float (mixed) and R = double (FP64 with FMA).
+#pragma once
+
+namespace SGB_NS {
+
+constexpr int kBatchThreads = 256;
+
+template <typename R>
+__device__ __forceinline__ ElemView<R> bm_elem_view(const BMeshDesc& m)
+{
+    ElemView<R> ev;
+    ev.tets = m.tets;
+    ev.rot = (R*)m.rot;
+    ev.K = (const R*)m.K;
+    ev.J = (const R*)m.J;
+    ev.rest = (const R*)m.rest;
+    ev.n_tets = m.n_tets;
+    ev.method = m.method;
+    return ev;
+}
+
+__device__ __forceinline__ PatchView bm_patch_view(const BMeshDesc& m, int pe)
+{
+    PatchView pv;
+    pv.elem_start = m.elem_start;
+    pv.node_start = m.node_start;
+    pv.lnode_gid = m.lnode_gid;
+    pv.lnode_info = m.lnode_info;
+    pv.lrow = m.lrow;
+    pv.lslots = m.lslots;
+    pv.lconn = m.lconn;
+    pv.bnd_rowptr = m.bnd_rowptr;
+    pv.n_patches = m.n_patches;
+    pv.pe = pe;
+    pv.max_lnodes = kBatchMaxLocalNodes;
+    return pv;
+}
+
+__device__ __forceinline__ bool bm_cg_skip(const BMeshDesc& m, int it)
+{
+    return m.done || it > m.cg_iterations || !m.active;
+}
+
+// Block-wide: store this item's partial, take the mesh's ticket; when this
+// is the mesh's last item, returns true in every thread with the mesh total
+// in `total` (valid in thread 0).
+__device__ __forceinline__ bool bm_ticket_sum(double mine, double* partials, int idx, unsigned int* ticket,
+                                              int count, double* total)
+{
+    __shared__ int last;
+    const double bsum = block_sum(mine);
+    if (threadIdx.x == 0) {
+        partials[idx] = bsum;
+        __threadfence();
+        const unsigned int t = atomicAdd(ticket, 1u);
+        last = (t == (unsigned int)count - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double v = 0.0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) v += __ldcg(&partials[i]);
+    *total = block_sum(v);
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+// ---- force: f = ext + m g + internal forces --------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_force_elem(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                               const int* __restrict__ counts)
+{
+    const int L = counts[WL_ELEM];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        const BMeshDesc& m = M[it.slot];
+        const ElemView<R> ev = bm_elem_view<R>(m);
+        R* ef = (R*)m.eforce;
+        for (int e = it.a + threadIdx.x; e < it.b; e += blockDim.x) {
+            if (m.method == METHOD_LARGE)
+                elem_force_body<R, METHOD_LARGE>(ev, e, m.x, m.rest_pos, ef);
+            else
+                elem_force_body<R, METHOD_POLAR>(ev, e, m.x, m.rest_pos, ef);
+        }
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_force_gather(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                                 const int* __restrict__ counts)
+{
+    const int L = counts[WL_NODE];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        const BMeshDesc& m = M[it.slot];
+        const R* ef = (const R*)m.eforce;
+        const R* ext = (const R*)m.ext;
+        R* f = (R*)m.f;
+        const R mg0 = (R)(m.g[0] * m.vertex_mass), mg1 = (R)(m.g[1] * m.vertex_mass),
+                mg2 = (R)(m.g[2] * m.vertex_mass);
+        for (int n = it.a + threadIdx.x; n < it.b; n += blockDim.x) {
+            R a0 = R(0), a1 = R(0), a2 = R(0);
+            if (ext) {
+                a0 += ext[3 * (size_t)n];
+                a1 += ext[3 * (size_t)n + 1];
+                a2 += ext[3 * (size_t)n + 2];
+            }
+            if (m.node_mass) {
+                const double mm = m.node_mass[n];
+                a0 += (R)(m.g[0] * mm);
+                a1 += (R)(m.g[1] * mm);
+                a2 += (R)(m.g[2] * mm);
+            } else {
+                a0 += mg0;
+                a1 += mg1;
+                a2 += mg2;
+            }
+            for (int s = m.rowptr[n]; s < m.rowptr[n + 1]; ++s) {
+                const R* c = ef + 3 * (size_t)m.slots[s];
+                a0 += c[0];
+                a1 += c[1];
+                a2 += c[2];
+            }
+            f[3 * (size_t)n] = a0;
+            f[3 * (size_t)n + 1] = a1;
+            f[3 * (size_t)n + 2] = a2;
+        }
+    }
+}
+
+// ---- right-hand side b = h (f - (h+rs) K v - rm M v), CG start -------------
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_rhs_elem(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                             const int* __restrict__ counts)
+{
+    const int L = counts[WL_ELEM];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        const BMeshDesc& m = M[it.slot];
+        const ElemView<R> ev = bm_elem_view<R>(m);
+        for (int e = it.a + threadIdx.x; e < it.b; e += blockDim.x)
+            elem_dforce_body<R, double, METHOD_LARGE, 0>(ev, e, m.v, nullptr, R(0), (R)m.kf_rhs, (R*)m.eforce);
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                               const int* __restrict__ counts)
+{
+    const int L = counts[WL_NODE];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        BMeshDesc& m = M[it.slot];
+        const R* ef = (const R*)m.eforce;
+        const R* f = (const R*)m.f;
+        R* b = (R*)m.b;
+        R* r = (R*)m.r;
+        R* xs = (R*)m.xs;
+        const double rmf = m.rm_factor;  // -rm
+        const R mmu = (R)(rmf != 1.0 ? m.vertex_mass * rmf : m.vertex_mass);
+        const R hr = (R)m.h;
+        double dlocal = 0.0;
+        for (int n = it.a + threadIdx.x; n < it.b; n += blockDim.x) {
+            R a[3] = {f[3 * (size_t)n], f[3 * (size_t)n + 1], f[3 * (size_t)n + 2]};
+            const R vv[3] = {(R)m.v[3 * (size_t)n], (R)m.v[3 * (size_t)n + 1], (R)m.v[3 * (size_t)n + 2]};
+            if (rmf != 0.0) {
+                const R mm = m.node_mass ? (R)(m.node_mass[n] * rmf) : mmu;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) a[k] += vv[k] * mm;
+            }
+            for (int s = m.rowptr[n]; s < m.rowptr[n + 1]; ++s) {
+                const R* c = ef + 3 * (size_t)m.slots[s];
+                a[0] -= c[0];
+                a[1] -= c[1];
+                a[2] -= c[2];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] *= hr;
+            if (m.fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                b[3 * (size_t)n + k] = a[k];
+                r[3 * (size_t)n + k] = a[k];
+                xs[3 * (size_t)n + k] = R(0);
+            }
+            dlocal += (double)(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        }
+        double total;
+        if (bm_ticket_sum(dlocal, m.chunk_sum, it.c, &m.ticket_rhs, m.n_chunks, &total) && threadIdx.x == 0) {
+            m.rho = total;
+            m.normb = sqrt(total);
+            m.iters = 0;
+            m.last_err = 0.0;
+            m.den = 0.0;
+            if (!isfinite(total)) {
+                m.status |= 1;
+                m.done = 1;
+            } else if (m.normb == 0.0 || m.cg_iterations <= 0) {
+                m.done = 1;
+            } else {
+                const double err = sqrt(total) / m.normb;
+                m.last_err = err;
+                m.done = (err <= m.tol && m.tsc != 0) ? 1 : 0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- CG matvec over patches ------------------------------------------------
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kPatchThreads) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                           const int* __restrict__ counts, int it, int pe)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* ef = reinterpret_cast<R*>(smem_raw);  // [12][pe]
+    R* lp = ef + 12 * pe;                    // [kBatchMaxLocalNodes][3]
+    const int L = counts[WL_PATCH];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem wi = items[w];
+        BMeshDesc& m = M[wi.slot];
+        if (bm_cg_skip(m, it)) continue;  // uniform over the block: read before this mesh's last item ends
+        const PatchView pv = bm_patch_view(m, pe);
+        const ElemView<R> ev = bm_elem_view<R>(m);
+        const R beta = (MODE == 2) ? (R)m.beta : R(0);
+        const R* pold = (const R*)((it & 1) ? m.p1 : m.p0);
+        R* pnew = (R*)((it & 1) ? m.p0 : m.p1);
+        const double mf = m.mf;
+        const R mmu = (R)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
+        MassArgs ma{m.node_mass, m.vertex_mass, {m.g[0], m.g[1], m.g[2]}};
+        const R pen = patch_body<R, MODE>(pv, ev, wi.a, (const R*)m.r, pold, pnew, beta, (R)m.kf, ma, mf, mmu,
+                                          m.fixed, (R*)m.q, (R*)m.partials, ef, lp);
+        double total;
+        if (bm_ticket_sum((double)pen, m.patch_energy, wi.a, &m.ticket_den, m.n_patches, &total) &&
+            threadIdx.x == 0) {
+            m.den = total;
+            const bool first_of_first = (it == 1 && m.tsc == 0);
+            if (!isfinite(total)) {
+                m.status |= 1;
+                m.done = 1;
+            } else if (total != 0.0) {
+                if (fabs(total) <= m.thr && !first_of_first)
+                    m.done = 1;
+                else
+                    m.alpha = m.rho / total;
+            } else {
+                m.done = 1;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- CG update: shared-node q, x += alpha p, r -= alpha q, rho -------------
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                           const int* __restrict__ counts, int it)
+{
+    const int L = counts[WL_NODE];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem wi = items[w];
+        BMeshDesc& m = M[wi.slot];
+        if (bm_cg_skip(m, it)) continue;
+        const R alpha = (R)m.alpha;
+        const R nalpha = -alpha;
+        const R* p = (const R*)((it & 1) ? m.p0 : m.p1);
+        const R* q = (const R*)m.q;
+        const R* partials = (const R*)m.partials;
+        R* xs = (R*)m.xs;
+        R* r = (R*)m.r;
+        const double mf = m.mf;
+        const R mmu = (R)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
+        double local = 0.0;
+        for (int n = wi.a + threadIdx.x; n < wi.b; n += blockDim.x) {
+            const size_t i3 = 3 * (size_t)n;
+            const R pp[3] = {p[i3], p[i3 + 1], p[i3 + 2]};
+            R qq[3];
+            const int b0 = m.bnd_rowptr[n], b1 = m.bnd_rowptr[n + 1];
+            if (b0 == b1) {
+                qq[0] = q[i3];
+                qq[1] = q[i3 + 1];
+                qq[2] = q[i3 + 2];
+            } else {
+                R a0 = R(0), a1 = R(0), a2 = R(0);
+                for (int bb = b0; bb < b1; ++bb) {
+                    a0 += partials[3 * (size_t)bb];
+                    a1 += partials[3 * (size_t)bb + 1];
+                    a2 += partials[3 * (size_t)bb + 2];
+                }
+                const R mm = m.node_mass ? (R)(m.node_mass[n] * mf) : mmu;
+                qq[0] = mm * pp[0] - a0;
+                qq[1] = mm * pp[1] - a1;
+                qq[2] = mm * pp[2] - a2;
+                if (m.fixed[n]) qq[0] = qq[1] = qq[2] = R(0);
+            }
+            R rr[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                xs[i3 + k] = xs[i3 + k] + pp[k] * alpha;
+                rr[k] = r[i3 + k] + qq[k] * nalpha;
+                r[i3 + k] = rr[k];
+            }
+            local += (double)(rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2]);
+        }
+        double total;
+        if (bm_ticket_sum(local, m.chunk_sum, wi.c, &m.ticket_rho, m.n_chunks, &total) && threadIdx.x == 0) {
+            m.rho_prev = m.rho;
+            m.rho = total;
+            m.iters = it;
+            m.beta = total / m.rho_prev;
+            const double err = sqrt(total) / m.normb;
+            m.last_err = err;
+            if (!isfinite(total)) {
+                m.status |= 1;
+                m.done = 1;
+            } else if (err <= m.tol || it >= m.cg_iterations) {
+                m.done = 1;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- v += dv, x += h v -------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_euler(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                          const int* __restrict__ counts)
+{
+    const int L = counts[WL_NODE];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem wi = items[w];
+        BMeshDesc& m = M[wi.slot];
+        const R* xs = (const R*)m.xs;
+        const double h = m.h, vd = m.vdamp;
+        for (int n = wi.a + threadIdx.x; n < wi.b; n += blockDim.x) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const size_t i = 3 * (size_t)n + k;
+                double vv = m.v[i] + (double)xs[i];
+                m.x[i] = m.x[i] + vv * h;
+                if (vd != 1.0) vv *= vd;
+                m.v[i] = vv;
+            }
+        }
+        if (wi.c == 0 && threadIdx.x == 0) m.tsc += 1;
+    }
+}
+
+// ---- host side: record one step of the whole batch ---------------------------
+template <typename R>
+size_t batch_patch_smem(int pe)
+{
+    return sizeof(R) * (12 * (size_t)pe + 3 * (size_t)kBatchMaxLocalNodes);
+}
+
+template <typename R>
+int batch_prepare(int pe, int* grid_patch)
+{
+    const size_t smem = batch_patch_smem<R>(pe);
+    int dev = 0, sms = 0, nb1 = 0, nb2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaFuncSetAttribute(kb_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kb_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, kb_matvec<R, 1>, kPatchThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, kb_matvec<R, 2>, kPatchThreads, smem);
+    int nb = nb1 < nb2 ? nb1 : nb2;
+    *grid_patch = (nb < 1 ? 1 : nb) * sms;
+    return sms;
+}
+
+template <typename R>
+void batch_record_step(const BatchLaunch& B, cudaStream_t s)
+{
+    const WorkItem* pit = B.items[WL_PATCH];
+    const WorkItem* eit = B.items[WL_ELEM];
+    const WorkItem* nit = B.items[WL_NODE];
+    kb_force_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
+    kb_force_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+    kb_rhs_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
+    kb_rhs_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+    const size_t smem = batch_patch_smem<R>(B.pe);
+    for (int it = 1; it <= B.max_iterations; ++it) {
+        if (it == 1)
+            kb_matvec<R, 1><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe);
+        else
+            kb_matvec<R, 2><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe);
+        kb_update<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
+    }
+    kb_euler<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+}
+
+}  // namespace SGB_NS

@@ -151,4 +151,80 @@ struct Scene {
     size_t device_bytes = 0;
 };
 
+// ---------------------------------------------------------------------------
+// Batched multi-mesh engine
+// ---------------------------------------------------------------------------
+
+// Unit of work of the persistent batch kernels: a patch (a = patch index), a
+// range of elements [a, b) or a chunk of nodes [a, b) numbered c in its mesh.
+struct WorkItem {
+    int slot, a, b, c;
+};
+
+enum { WL_PATCH = 0, WL_ELEM = 1, WL_NODE = 2 };
+constexpr int kBatchElemChunk = 1024;
+constexpr int kBatchNodeChunk = 1024;
+constexpr int kBatchMaxLocalNodes = 1024;
+
+// Device-resident descriptor of one admitted mesh: its arrays (inside the
+// batch's HBM arena), its solver parameters and its CG scalars. Kernels read
+// it through the slot index of a work item; reductions update its scalars.
+struct BMeshDesc {
+    // element data, patch order
+    const int4* tets;
+    void* rot;
+    const void* K;
+    const void* J;
+    const void* rest;
+    void* eforce;
+    // node -> (element*4+corner) gather table
+    const int* rowptr;
+    const int* slots;
+    // patch layout
+    const int* elem_start;
+    const int* node_start;
+    const int* lnode_gid;
+    const int* lnode_info;
+    const int* lrow;
+    const uint16_t* lslots;
+    const ushort4* lconn;
+    const int* bnd_rowptr;
+    void* partials;
+    // node data
+    double* x;
+    double* v;
+    const double* rest_pos;
+    const uint8_t* fixed;
+    const double* node_mass;
+    const void* ext;
+    void* f;
+    void* b;
+    void* r;
+    void* p0;
+    void* p1;
+    void* q;
+    void* xs;
+    double* patch_energy;
+    double* chunk_sum;
+    // sizes and parameters
+    int n_nodes, n_tets, method, n_patches, n_chunks, cg_iterations;
+    double h, kf_rhs, rm_factor, mf, kf, vdamp, tol, thr, vertex_mass;
+    double g[3];
+    // CG state
+    double normb, rho, rho_prev, den, alpha, beta, last_err;
+    long long tsc;
+    int done, iters, status, active;
+    unsigned int ticket_rhs, ticket_den, ticket_rho, ticket_pad;
+};
+
+// Everything a precision variant needs to record one batch step.
+struct BatchLaunch {
+    BMeshDesc* meshes;
+    const WorkItem* items[3];
+    const int* counts;
+    int grid_patch, grid_elem, grid_node;
+    int pe;
+    int max_iterations;
+};
+
 }  // namespace sgb

@@ -169,12 +169,9 @@ __device__ __forceinline__ void store_eforce(R* eforce, int e, const R c[12])
 // (TFEM.inl:534-623, 870-986, 1025-1079). Writes rotations and the corner
 // forces R^T F (method=small: F).
 template <typename R, int METHOD>
-__global__ void __launch_bounds__(kElemBlock) k_elem_force(ElemView<R> ev, const double* __restrict__ x,
-                                                           const double* __restrict__ rest_pos,
-                                                           R* __restrict__ eforce)
+__device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, const double* __restrict__ x,
+                                                const double* __restrict__ rest_pos, R* __restrict__ eforce)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ev.n_tets) return;
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
     double p[4][3];
@@ -285,6 +282,16 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_force(ElemView<R> ev, const
     store_eforce(eforce, e, c);
 }
 
+template <typename R, int METHOD>
+__global__ void __launch_bounds__(kElemBlock) k_elem_force(ElemView<R> ev, const double* __restrict__ x,
+                                                           const double* __restrict__ rest_pos,
+                                                           R* __restrict__ eforce)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ev.n_tets) return;
+    elem_force_body<R, METHOD>(ev, e, x, rest_pos, eforce);
+}
+
 // Direction of the CG step for the matvec element pass. DIR 0: the input
 // vector itself; DIR 1: p = r (first iteration); DIR 2: p = p_old*beta + r
 // (vOp_avf, Sofa/Component/StateContainer/src/sofa/component/statecontainer/
@@ -300,19 +307,14 @@ __device__ __forceinline__ R cg_dir(R r, R pold, R beta)
 // (TFEM.inl:721-749, 1193-1237). Writes the corner terms R K (R^T dx) fact
 // that the gather subtracts.
 template <typename R, typename VIN, int METHOD, int DIR>
-__global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, const VIN* __restrict__ dx,
-                                                            const R* __restrict__ pold, const CgScalars* cg,
-                                                            R fact, R* __restrict__ eforce)
+__device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, const VIN* __restrict__ dx,
+                                                 const R* __restrict__ pold, R beta, R fact,
+                                                 R* __restrict__ eforce)
 {
-    if (DIR != 0 && cg->done) return;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ev.n_tets) return;
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
     const int node[4] = {t.x, t.y, t.z, t.w};
     R xin[4][3];
-    R beta = R(0);
-    if (DIR == 2) beta = (R)cg->beta;
     VIN v0[3];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -383,6 +385,18 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, cons
             c[3 * i + k] = acc;
         }
     store_eforce(eforce, e, c);
+}
+
+template <typename R, typename VIN, int METHOD, int DIR>
+__global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, const VIN* __restrict__ dx,
+                                                            const R* __restrict__ pold, const CgScalars* cg,
+                                                            R fact, R* __restrict__ eforce)
+{
+    if (DIR != 0 && cg->done) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ev.n_tets) return;
+    const R beta = (DIR == 2) ? (R)cg->beta : R(0);
+    elem_dforce_body<R, VIN, METHOD, DIR>(ev, e, dx, pold, beta, fact, eforce);
 }
 
 // ------------------------------------------------------------------------
@@ -758,6 +772,120 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict_
 // ------------------------------------------------------------------------
 constexpr int kPatchThreads = 128;
 
+// One patch of the fused matvec, executed by the whole block (it contains
+// block barriers). Returns this thread's share of the patch's p^T A p.
+template <typename R, int MODE>
+__device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& ev, int P, const R* __restrict__ rin,
+                                        const R* __restrict__ pold, R* __restrict__ pnew, R beta, R kf,
+                                        const MassArgs& ma, double mf, R mmu, const uint8_t* __restrict__ fixed,
+                                        R* __restrict__ qout, R* __restrict__ partials, R* ef, R* lp)
+{
+    const size_t En = (size_t)ev.n_tets;
+    R pen = R(0);
+    const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
+    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+    // phase 0: nodal values of the patch
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int g = pv.lnode_gid[n0 + l];
+        R v[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const R rv = rin[3 * (size_t)g + k];
+            v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
+            lp[3 * l + k] = v[k];
+        }
+        if (MODE != 0) {
+            const int info = pv.lnode_info[n0 + l];
+            if (info < 0 || (info & 1)) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
+            }
+        }
+    }
+    __syncthreads();
+    // phase 1: element terms
+    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+        const size_t e = (size_t)(e0 + le);
+        const ushort4 c = pv.lconn[e];
+        const int ln[4] = {c.x, c.y, c.z, c.w};
+        R xr[4][3];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
+        // relative to node a: J^T annihilates translations
+#pragma unroll
+        for (int i = 3; i >= 0; --i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
+        R Rm[9], K[3], J[12];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
+#pragma unroll
+        for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
+        R X[12], F[12];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
+        element_force(F, X, K, J, kf);
+        R en = R(0);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const R ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
+                ef[(3 * i + k) * pv.pe + le] = ck;
+                en += xr[i][k] * ck;
+            }
+        if (MODE != 0) pen -= en;
+    }
+    __syncthreads();
+    // phase 2: per local node, its slots in element order
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int s0 = pv.lrow[n0 + l], s1 = pv.lrow[n0 + l + 1];
+        R a0 = R(0), a1 = R(0), a2 = R(0);
+        for (int s = s0; s < s1; ++s) {
+            const int slot = pv.lslots[s];
+            const int le = slot >> 2, cc = slot & 3;
+            a0 += ef[(3 * cc + 0) * pv.pe + le];
+            a1 += ef[(3 * cc + 1) * pv.pe + le];
+            a2 += ef[(3 * cc + 2) * pv.pe + le];
+        }
+        const int g = pv.lnode_gid[n0 + l];
+        const int info = pv.lnode_info[n0 + l];
+        if (info >= 0) {
+            R* o = partials + 3 * (size_t)(info >> 1);
+            o[0] = a0;
+            o[1] = a1;
+            o[2] = a2;
+        }
+        if (MODE == 0) {
+            if (info < 0) {
+                qout[3 * (size_t)g] -= a0;
+                qout[3 * (size_t)g + 1] -= a1;
+                qout[3 * (size_t)g + 2] -= a2;
+            }
+        } else if (info < 0 || (info & 1)) {
+            const R p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
+            const R mm = ma.node_mass ? (R)(ma.node_mass[g] * mf) : mmu;
+            pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
+            if (info < 0) {
+                R q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
+                if (fixed[g]) q0 = q1 = q2 = R(0);
+                qout[3 * (size_t)g] = q0;
+                qout[3 * (size_t)g + 1] = q1;
+                qout[3 * (size_t)g + 2] = q2;
+            }
+        }
+    }
+    __syncthreads();
+    return pen;
+}
+
 template <typename R, int MODE>
 __global__ void __launch_bounds__(kPatchThreads) k_patch_matvec(PatchView pv, ElemView<R> ev,
                                                                 const R* __restrict__ rin, const R* __restrict__ pold,
@@ -772,113 +900,10 @@ __global__ void __launch_bounds__(kPatchThreads) k_patch_matvec(PatchView pv, El
     if (MODE != 0 && cg->done) return;
     const R beta = (MODE == 2) ? (R)cg->beta : R(0);
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
-    const size_t En = (size_t)ev.n_tets;
     double energy = 0.0;  // FP64 across patches; FP32 within one patch
-    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
-        R pen = R(0);
-        const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
-        const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
-        // phase 0: nodal values of the patch
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const int g = pv.lnode_gid[n0 + l];
-            R v[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const R rv = rin[3 * (size_t)g + k];
-                v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
-                lp[3 * l + k] = v[k];
-            }
-            if (MODE != 0) {
-                const int info = pv.lnode_info[n0 + l];
-                if (info < 0 || (info & 1)) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
-                }
-            }
-        }
-        __syncthreads();
-        // phase 1: element terms
-        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
-            const size_t e = (size_t)(e0 + le);
-            const ushort4 c = pv.lconn[e];
-            const int ln[4] = {c.x, c.y, c.z, c.w};
-            R xr[4][3];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
-            // relative to node a: J^T annihilates translations
-#pragma unroll
-            for (int i = 3; i >= 0; --i)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
-            R Rm[9], K[3], J[12];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
-#pragma unroll
-            for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
-            R X[12], F[12];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-                    X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
-            element_force(F, X, K, J, kf);
-            R en = R(0);
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const R ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
-                    ef[(3 * i + k) * pv.pe + le] = ck;
-                    en += xr[i][k] * ck;
-                }
-            if (MODE != 0) pen -= en;
-        }
-        __syncthreads();
-        // phase 2: per local node, its slots in element order
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const int s0 = pv.lrow[n0 + l], s1 = pv.lrow[n0 + l + 1];
-            R a0 = R(0), a1 = R(0), a2 = R(0);
-            for (int s = s0; s < s1; ++s) {
-                const int slot = pv.lslots[s];
-                const int le = slot >> 2, cc = slot & 3;
-                a0 += ef[(3 * cc + 0) * pv.pe + le];
-                a1 += ef[(3 * cc + 1) * pv.pe + le];
-                a2 += ef[(3 * cc + 2) * pv.pe + le];
-            }
-            const int g = pv.lnode_gid[n0 + l];
-            const int info = pv.lnode_info[n0 + l];
-            if (info >= 0) {
-                R* o = partials + 3 * (size_t)(info >> 1);
-                o[0] = a0;
-                o[1] = a1;
-                o[2] = a2;
-            }
-            if (MODE == 0) {
-                if (info < 0) {
-                    qout[3 * (size_t)g] -= a0;
-                    qout[3 * (size_t)g + 1] -= a1;
-                    qout[3 * (size_t)g + 2] -= a2;
-                }
-            } else if (info < 0 || (info & 1)) {
-                const R p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
-                const R mm = ma.node_mass ? (R)(ma.node_mass[g] * mf) : mmu;
-                pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
-                if (info < 0) {
-                    R q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
-                    if (fixed[g]) q0 = q1 = q2 = R(0);
-                    qout[3 * (size_t)g] = q0;
-                    qout[3 * (size_t)g + 1] = q1;
-                    qout[3 * (size_t)g + 2] = q2;
-                }
-            }
-        }
-        energy += (double)pen;
-        __syncthreads();
-    }
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
+        energy += (double)patch_body<R, MODE>(pv, ev, P, rin, pold, pnew, beta, kf, ma, mf, mmu, fixed, qout,
+                                              partials, ef, lp);
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
 

@@ -1,6 +1,9 @@
 // Instantiates tfem_impl.cuh for one real type and exports its table.
 // Expects SGB_NS, SGB_REAL and SGB_TABLE to be defined.
 #include "tfem_impl.cuh"
+#if SGB_USES_PATCHES
+#include "batch_impl.cuh"
+#endif
 #include "variants.h"
 
 namespace SGB_NS {
@@ -25,10 +28,18 @@ static void v_scene_step(Scene* sc, double* terms, int mass_first, cudaStream_t 
         scene_step<SGB_REAL>(sc, terms, mass_first, s);
 }
 static int v_prepare(TfemMesh* m) { return m->pl.n_patches > 0 ? prepare_patch<SGB_REAL>(m) : 0; }
+#if SGB_USES_PATCHES
+static int v_batch_prepare(int pe, int* grid_patch) { return batch_prepare<SGB_REAL>(pe, grid_patch); }
+static void v_batch_record(const BatchLaunch& b, cudaStream_t s) { batch_record_step<SGB_REAL>(b, s); }
+#else
+static int (*const v_batch_prepare)(int, int*) = nullptr;
+static void (*const v_batch_record)(const BatchLaunch&, cudaStream_t) = nullptr;
+#endif
 }  // namespace SGB_NS
 
 namespace sgb {
 const VariantOps SGB_TABLE = {SGB_VARIANT_NAME,     sizeof(SGB_REAL),     SGB_USES_PATCHES,
                               SGB_NS::v_init,       SGB_NS::v_add_force,  SGB_NS::v_add_dforce,
-                              SGB_NS::v_scene_step, SGB_NS::v_prepare};
+                              SGB_NS::v_scene_step, SGB_NS::v_prepare,   SGB_NS::v_batch_prepare,
+                              SGB_NS::v_batch_record};
 }

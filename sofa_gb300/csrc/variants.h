@@ -16,6 +16,9 @@ struct VariantOps {
     void (*add_dforce)(TfemMesh*, const void* dx, void* df, double kfactor, cudaStream_t);
     void (*scene_step)(Scene*, double* dot_terms, int mass_first, cudaStream_t);
     int (*prepare)(TfemMesh*);  // kernel attributes; returns the patch-kernel grid
+    // batch engine (null for the reference-rounding variant)
+    int (*batch_prepare)(int pe, int* grid_patch);  // returns the SM count, -1 on failure
+    void (*batch_record)(const BatchLaunch&, cudaStream_t);
 };
 
 extern const VariantOps ops_fp64_exact;
