@@ -262,6 +262,54 @@ int sgb_batch_info(const sgb_batch_t* batch, int* active_meshes, long long* acti
                    size_t* budget_total);
 void* sgb_batch_stream(sgb_batch_t* batch);
 
+/* ------------------------------------------------------------------ */
+/* Serving: continuous batching of simulate-K-steps requests            */
+/* ------------------------------------------------------------------ */
+/* Requests are prepared on host worker threads, admitted in arrival order
+ * when the HBM budget and a mesh slot allow, and stepped together with the
+ * other admitted meshes; each launch advances every mesh by up to
+ * max_steps_per_launch steps, never past the nearest finishing request.
+ * Latency is measured from submission to the copy of the final positions.
+ * Modelled on the SofaPhysicsAPI load/step/get-positions cycle
+ * (applications/projects/SofaPhysicsAPI/src/SofaPhysicsAPI/SofaPhysicsAPI.h:73-152);
+ * the continuous batching itself has no reference counterpart. */
+typedef struct sgb_server sgb_server_t;
+
+typedef struct sgb_request {
+    sgb_mesh_desc mesh;          /* host arrays must stay valid until the request completes */
+    int n_steps;                 /* K implicit Euler steps */
+    double* positions_out_host;  /* 3 n_nodes doubles, written before completion is reported */
+    uint64_t id;
+} sgb_request;
+
+typedef struct sgb_completion {
+    uint64_t id;
+    int status;               /* SGB_OK or the SGB_ERR_* that failed the request */
+    double latency_ms;        /* submission -> positions copied */
+    double queue_ms;          /* submission -> admission */
+    int cg_iterations_last;   /* CG iterations of its last step */
+    long long n_tets;
+    int n_steps;
+} sgb_completion;
+
+typedef struct sgb_server_stats {
+    long long submitted, completed, failed;
+    long long tet_steps;      /* completed requests: tets x steps */
+    double p50_ms, p99_ms, max_ms;
+    double busy_s;            /* time spent in batch launches */
+    double wall_s;            /* since the first submission */
+} sgb_server_stats;
+
+int sgb_server_create(sgb_server_t** out, int precision, size_t hbm_budget_bytes, int max_meshes,
+                      int max_cg_iterations, int prep_threads, int max_steps_per_launch);
+int sgb_server_submit(sgb_server_t* server, const sgb_request* request);
+/* Non-blocking: moves up to max_out completions into out. */
+int sgb_server_poll(sgb_server_t* server, sgb_completion* out, int max_out, int* n_out);
+/* Blocks until every submitted request has completed (or timeout_s passes). */
+int sgb_server_wait_idle(sgb_server_t* server, double timeout_s);
+int sgb_server_get_stats(sgb_server_t* server, sgb_server_stats* stats);
+int sgb_server_destroy(sgb_server_t* server);
+
 #ifdef __cplusplus
 }
 #endif

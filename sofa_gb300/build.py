@@ -31,6 +31,7 @@ UNITS = {
     "mesh_layout.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],
+    "server.cu": [],
 }
 
 

@@ -70,6 +70,41 @@ class MeshDesc(ctypes.Structure):
     ]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("mesh", MeshDesc),
+        ("n_steps", ctypes.c_int),
+        ("positions_out_host", ctypes.POINTER(ctypes.c_double)),
+        ("id", ctypes.c_uint64),
+    ]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [
+        ("id", ctypes.c_uint64),
+        ("status", ctypes.c_int),
+        ("latency_ms", ctypes.c_double),
+        ("queue_ms", ctypes.c_double),
+        ("cg_iterations_last", ctypes.c_int),
+        ("n_tets", ctypes.c_longlong),
+        ("n_steps", ctypes.c_int),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_longlong),
+        ("completed", ctypes.c_longlong),
+        ("failed", ctypes.c_longlong),
+        ("tet_steps", ctypes.c_longlong),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("busy_s", ctypes.c_double),
+        ("wall_s", ctypes.c_double),
+    ]
+
+
 _lib = None
 _dp = ctypes.POINTER(ctypes.c_double)
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -124,6 +159,12 @@ def load():
         "sgb_batch_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong),
                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
         "sgb_batch_stream": (_vp, [_vp]),
+        "sgb_server_create": (c_int, [ctypes.POINTER(_vp), c_int, ctypes.c_size_t, c_int, c_int, c_int, c_int]),
+        "sgb_server_submit": (c_int, [_vp, ctypes.POINTER(Request)]),
+        "sgb_server_poll": (c_int, [_vp, ctypes.POINTER(Completion), c_int, ctypes.POINTER(c_int)]),
+        "sgb_server_wait_idle": (c_int, [_vp, c_double]),
+        "sgb_server_get_stats": (c_int, [_vp, ctypes.POINTER(ServerStats)]),
+        "sgb_server_destroy": (c_int, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -442,3 +483,64 @@ class Batch:
     @property
     def stream(self):
         return load().sgb_batch_stream(self._h)
+
+
+class Server:
+    """Handle of sgb_server_t: continuous batching of simulate-K-steps requests."""
+
+    def __init__(self, precision="mixed", budget_bytes=1 << 30, max_meshes=256, max_cg_iterations=25,
+                 prep_threads=4, max_steps_per_launch=8):
+        lib = load()
+        h = _vp()
+        check(lib.sgb_server_create(ctypes.byref(h), PRECISIONS[precision], int(budget_bytes), int(max_meshes),
+                                    int(max_cg_iterations), int(prep_threads), int(max_steps_per_launch)))
+        self._h = h
+        self._keep = {}
+        self._next = 1
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().sgb_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, positions, tetrahedra, n_steps, out=None, **kw):
+        """Queues a request; returns (id, output array filled at completion)."""
+        d, keep = Batch.mesh_desc(positions, tetrahedra, **kw)
+        n = d.n_nodes
+        out = np.zeros((n, 3)) if out is None else out
+        r = Request()
+        r.mesh = d
+        r.n_steps = int(n_steps)
+        r.positions_out_host = out.ctypes.data_as(_dp)
+        rid = self._next
+        self._next += 1
+        r.id = rid
+        self._keep[rid] = (keep, out, r)
+        check(load().sgb_server_submit(self._h, ctypes.byref(r)))
+        return rid, out
+
+    def poll(self, max_out=1024):
+        buf = (Completion * max_out)()
+        n = ctypes.c_int()
+        check(load().sgb_server_poll(self._h, buf, max_out, ctypes.byref(n)))
+        res = []
+        for i in range(n.value):
+            c = buf[i]
+            res.append({"id": c.id, "status": c.status, "latency_ms": c.latency_ms, "queue_ms": c.queue_ms,
+                        "cg_iterations_last": c.cg_iterations_last, "n_tets": c.n_tets, "n_steps": c.n_steps})
+            self._keep.pop(c.id, None)
+        return res
+
+    def wait_idle(self, timeout_s=600.0):
+        check(load().sgb_server_wait_idle(self._h, float(timeout_s)))
+
+    def stats(self):
+        st = ServerStats()
+        check(load().sgb_server_get_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}

@@ -12,10 +12,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/sofa_gb300.h"
-#include "mesh_layout.h"
-#include "sgb_internal.h"
-#include "variants.h"
+#include "batch_internal.h"
 
 namespace sgb {
 void set_last_error(const std::string& msg);
@@ -47,63 +44,6 @@ constexpr size_t kAlign = 256;
 
 inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
-// First-fit allocator over one device buffer.
-struct Arena {
-    char* base = nullptr;
-    size_t size = 0;
-    std::map<size_t, size_t> free_;  // offset -> length
-    size_t used = 0;
-
-    void reset(char* b, size_t n)
-    {
-        base = b;
-        size = n;
-        free_.clear();
-        free_[0] = n;
-        used = 0;
-    }
-    bool alloc(size_t n, size_t* off)
-    {
-        n = align_up(n);
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second >= n) {
-                *off = it->first;
-                const size_t rest = it->second - n;
-                const size_t o = it->first + n;
-                free_.erase(it);
-                if (rest) free_[o] = rest;
-                used += n;
-                return true;
-            }
-        }
-        return false;
-    }
-    void release(size_t off, size_t n)
-    {
-        n = align_up(n);
-        used -= n;
-        auto it = free_.emplace(off, n).first;
-        auto nx = std::next(it);
-        if (nx != free_.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free_.erase(nx);
-        }
-        if (it != free_.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-    size_t largest_free() const
-    {
-        size_t m = 0;
-        for (auto& kv : free_) m = std::max(m, kv.second);
-        return m;
-    }
-};
-
 // Sub-allocations of one mesh inside its arena block.
 struct Carve {
     size_t total = 0;
@@ -126,36 +66,57 @@ struct Carve {
 
 }  // namespace
 
-struct BatchMeshHost {
-    bool active = false;
-    size_t off = 0, bytes = 0;
-    int n_nodes = 0, n_tets = 0, n_patches = 0, n_chunks = 0;
-    long long steps = 0;
-    std::vector<int> perm;
-    BMeshDesc d{};  // host copy of the device descriptor's pointers/params
-};
 
-struct sgb_batch {
-    const VariantOps* ops = nullptr;
-    int precision = 0;
-    size_t rs = 4;
-    int pe = 512;
-    int max_slots = 0;
-    int max_iterations = 0;
-    Arena arena;
-    char* arena_mem = nullptr;
-    BMeshDesc* d_meshes = nullptr;
-    std::vector<BatchMeshHost> slots;
-    WorkItem* d_items[3] = {nullptr, nullptr, nullptr};
-    int cap[3] = {0, 0, 0};
-    int* d_counts = nullptr;
-    int counts_h[3] = {0, 0, 0};
-    cudaStream_t stream = nullptr;
-    cudaGraphExec_t graph = nullptr;
-    bool graph_valid = false;
-    int sms = 152, grid_patch = 152;
-    size_t device_bytes = 0;
-};
+namespace sgb {
+void Arena::reset(char* b, size_t n)
+{
+    base = b;
+    size = n;
+    free_.clear();
+    free_[0] = n;
+    used = 0;
+}
+bool Arena::alloc(size_t n, size_t* off)
+{
+    n = (n + 255) / 256 * 256;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= n) {
+            *off = it->first;
+            const size_t rest = it->second - n;
+            const size_t o = it->first + n;
+            free_.erase(it);
+            if (rest) free_[o] = rest;
+            used += n;
+            return true;
+        }
+    }
+    return false;
+}
+void Arena::release(size_t off, size_t n)
+{
+    n = (n + 255) / 256 * 256;
+    used -= n;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            free_.erase(it);
+        }
+    }
+}
+size_t Arena::largest_free() const
+{
+    size_t m = 0;
+    for (auto& kv : free_) m = std::max(m, kv.second);
+    return m;
+}
+}  // namespace sgb
 
 static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool node_mass, bool ext, Carve& c,
                         BMeshDesc& d, double** young, double** poisson, int** elem_orig, size_t ny, size_t np)
@@ -325,18 +286,10 @@ static int validate_mesh(const sgb_mesh_desc* m)
 int sgb_batch_mesh_bytes(const sgb_batch_t* B, const sgb_mesh_desc* m, size_t* bytes)
 {
     if (!B || !bytes) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_mesh_bytes: NULL argument");
-    int rc = validate_mesh(m);
+    PreparedMesh pm;
+    int rc = prepare_mesh(m, B->pe, B->rs, pm);
     if (rc) return rc;
-    HostLayout L;
-    build_patch_layout(m->n_nodes, m->n_tets, m->tetrahedra_host, m->rest_positions_host, B->pe,
-                       kBatchMaxLocalNodes, L);
-    Carve c;
-    BMeshDesc d{};
-    double *y, *p;
-    int* eo;
-    *bytes = align_up(mesh_plan((sgb_batch*)B, m->n_nodes, m->n_tets, L, m->params.node_masses_host != nullptr,
-                                m->external_force_host != nullptr, c, d, &y, &p, &eo,
-                                std::max(m->n_young, 1), std::max(m->n_poisson, 1)));
+    *bytes = pm.bytes;
     return SGB_OK;
 }
 
@@ -344,8 +297,70 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
 {
     if (!B || !slot_out) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_add_mesh: NULL argument");
     *slot_out = -1;
+    PreparedMesh pm;
+    int rc = prepare_mesh(m, B->pe, B->rs, pm);
+    if (rc) return rc;
+    return admit_prepared(B, pm, slot_out);
+}
+
+}  // extern "C"
+
+namespace sgb {
+
+// Host-only part of admission: validation, material checks like the
+// reference (BaseLinearElasticityFEMForceField.inl:53-85), element order,
+// patch layout, gather tables and the byte count. Safe on any thread.
+int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm)
+{
     int rc = validate_mesh(m);
     if (rc) return rc;
+    const int N = m->n_nodes, E = m->n_tets;
+    pm.N = N;
+    pm.E = E;
+    pm.method = m->method;
+    pm.P = m->params;
+    pm.rest.assign(m->rest_positions_host, m->rest_positions_host + 3 * (size_t)N);
+    if (m->young && m->n_young > 0) pm.Eh.assign(m->young, m->young + m->n_young);
+    if (m->poisson && m->n_poisson > 0) pm.nuh.assign(m->poisson, m->poisson + m->n_poisson);
+    if (pm.Eh.empty()) pm.Eh.push_back(5000.0);
+    if (pm.nuh.empty()) pm.nuh.push_back(0.45);
+    for (double& y : pm.Eh)
+        if (!(y >= 0)) y = 5000.0;
+    for (double& v : pm.nuh)
+        if (!(v >= 0 && v < 0.5)) v = 0.45;
+    build_patch_layout(N, E, m->tetrahedra_host, m->rest_positions_host, pe, kBatchMaxLocalNodes, pm.L);
+    int maxval = 0;
+    build_node_csr(N, E, m->tetrahedra_host, pm.L.inv, pm.rowptr, pm.slots, maxval);
+    pm.tets_store.resize((size_t)E * 4);
+    for (size_t s = 0; s < (size_t)E; ++s)
+        for (int c = 0; c < 4; ++c) pm.tets_store[4 * s + c] = m->tetrahedra_host[4 * (size_t)pm.L.perm[s] + c];
+    pm.fixed.assign((size_t)N, 0);
+    const sgb_scene_params& P = m->params;
+    if (P.fix_all)
+        std::fill(pm.fixed.begin(), pm.fixed.end(), 1);
+    else
+        for (int i = 0; i < P.n_fixed; ++i)
+            if (P.fixed_host[i] >= 0 && P.fixed_host[i] < N) pm.fixed[(size_t)P.fixed_host[i]] = 1;
+    if (P.node_masses_host) pm.node_mass.assign(P.node_masses_host, P.node_masses_host + N);
+    if (m->external_force_host) pm.ext.assign(m->external_force_host, m->external_force_host + 3 * (size_t)N);
+    pm.P.fixed_host = nullptr;
+    pm.P.node_masses_host = nullptr;
+    Carve c;
+    BMeshDesc d{};
+    double *y, *p;
+    int* eo;
+    sgb_batch tmp;
+    tmp.rs = rs;
+    pm.bytes = align_up(mesh_plan(&tmp, N, E, pm.L, !pm.node_mass.empty(), !pm.ext.empty(), c, d, &y, &p, &eo,
+                                  pm.Eh.size(), pm.nuh.size()));
+    return SGB_OK;
+}
+
+// Device part of admission: arena block, uploads, per-element init,
+// descriptor and work lists. Synchronous on the batch stream.
+int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot_out)
+{
+    *slot_out = -1;
     int slot = -1;
     for (int s = 0; s < B->max_slots; ++s)
         if (!B->slots[(size_t)s].active) {
@@ -353,41 +368,15 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
             break;
         }
     if (slot < 0) return bfail(SGB_ERR_BUDGET, "sgb_batch_add_mesh: every mesh slot is taken");
-    const int N = m->n_nodes, E = m->n_tets;
-    const sgb_scene_params& P = m->params;
-    // Young's modulus / Poisson ratio, checked like the reference
-    // (BaseLinearElasticityFEMForceField.inl:53-85)
-    std::vector<double> Eh, nuh;
-    if (m->young && m->n_young > 0) Eh.assign(m->young, m->young + m->n_young);
-    if (m->poisson && m->n_poisson > 0) nuh.assign(m->poisson, m->poisson + m->n_poisson);
-    if (Eh.empty()) Eh.push_back(5000.0);
-    if (nuh.empty()) nuh.push_back(0.45);
-    for (double& y : Eh)
-        if (!(y >= 0)) y = 5000.0;
-    for (double& v : nuh)
-        if (!(v >= 0 && v < 0.5)) v = 0.45;
-
-    HostLayout L;
-    build_patch_layout(N, E, m->tetrahedra_host, m->rest_positions_host, B->pe, kBatchMaxLocalNodes, L);
-    std::vector<int> rowptr, slots;
-    int maxval = 0;
-    build_node_csr(N, E, m->tetrahedra_host, L.inv, rowptr, slots, maxval);
-    std::vector<int32_t> tets_store((size_t)E * 4);
-    for (size_t s = 0; s < (size_t)E; ++s)
-        for (int c = 0; c < 4; ++c) tets_store[4 * s + c] = m->tetrahedra_host[4 * (size_t)L.perm[s] + c];
-    std::vector<uint8_t> fixed((size_t)N, 0);
-    if (P.fix_all)
-        std::fill(fixed.begin(), fixed.end(), 1);
-    else
-        for (int i = 0; i < P.n_fixed; ++i)
-            if (P.fixed_host[i] >= 0 && P.fixed_host[i] < N) fixed[(size_t)P.fixed_host[i]] = 1;
-
+    const int N = pm.N, E = pm.E;
+    const sgb_scene_params& P = pm.P;
+    const HostLayout& L = pm.L;
     Carve c;
     BMeshDesc d{};
     double *d_young = nullptr, *d_poisson = nullptr;
     int* d_elem_orig = nullptr;
-    const size_t bytes = mesh_plan(B, N, E, L, P.node_masses_host != nullptr, m->external_force_host != nullptr, c,
-                                   d, &d_young, &d_poisson, &d_elem_orig, Eh.size(), nuh.size());
+    const size_t bytes = mesh_plan(B, N, E, L, !pm.node_mass.empty(), !pm.ext.empty(), c, d, &d_young, &d_poisson,
+                                   &d_elem_orig, pm.Eh.size(), pm.nuh.size());
     size_t off = 0;
     if (!B->arena.alloc(bytes, &off))
         return bfail(SGB_ERR_BUDGET, "sgb_batch_add_mesh: the mesh needs " + std::to_string(bytes) +
@@ -400,20 +389,21 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     cudaStream_t s = B->stream;
     std::vector<float> ext32;
     auto fail_free = [&](int code) {
+        cudaStreamSynchronize(s);
         B->arena.release(off, bytes);
         return code;
     };
-#define BUP(dst, src, n)                                                                              \
-    do {                                                                                              \
-        if ((n) > 0) {                                                                                \
+#define BUP(dst, src, n)                                                                                      \
+    do {                                                                                                      \
+        if ((n) > 0) {                                                                                        \
             cudaError_t _e = cudaMemcpyAsync((void*)(dst), (const void*)(src), (n), cudaMemcpyHostToDevice, s); \
-            if (_e != cudaSuccess) return fail_free(bcuda(_e, "upload"));                             \
-        }                                                                                             \
+            if (_e != cudaSuccess) return fail_free(bcuda(_e, "upload"));                                     \
+        }                                                                                                     \
     } while (0)
-    BUP(d.tets, tets_store.data(), sizeof(int4) * E);
+    BUP(d.tets, pm.tets_store.data(), sizeof(int4) * E);
     BUP(d_elem_orig, L.perm.data(), sizeof(int) * E);
-    BUP(d.rowptr, rowptr.data(), sizeof(int) * rowptr.size());
-    BUP(d.slots, slots.data(), sizeof(int) * slots.size());
+    BUP(d.rowptr, pm.rowptr.data(), sizeof(int) * pm.rowptr.size());
+    BUP(d.slots, pm.slots.data(), sizeof(int) * pm.slots.size());
     BUP(d.elem_start, L.elem_start.data(), sizeof(int) * L.elem_start.size());
     BUP(d.node_start, L.node_start.data(), sizeof(int) * L.node_start.size());
     BUP(d.lnode_gid, L.lnode_gid.data(), sizeof(int) * L.lnode_gid.size());
@@ -422,18 +412,18 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     BUP(d.lslots, L.lslots.data(), sizeof(uint16_t) * L.lslots.size());
     BUP(d.lconn, L.lconn.data(), sizeof(ushort4) * L.lconn.size());
     BUP(d.bnd_rowptr, L.bnd_rowptr.data(), sizeof(int) * L.bnd_rowptr.size());
-    BUP(d.rest_pos, m->rest_positions_host, sizeof(double) * 3 * N);
-    BUP(d.x, m->rest_positions_host, sizeof(double) * 3 * N);
-    BUP(d.fixed, fixed.data(), (size_t)N);
-    BUP(d_young, Eh.data(), sizeof(double) * Eh.size());
-    BUP(d_poisson, nuh.data(), sizeof(double) * nuh.size());
-    if (P.node_masses_host) BUP(d.node_mass, P.node_masses_host, sizeof(double) * N);
-    if (m->external_force_host) {
+    BUP(d.rest_pos, pm.rest.data(), sizeof(double) * 3 * N);
+    BUP(d.x, pm.rest.data(), sizeof(double) * 3 * N);
+    BUP(d.fixed, pm.fixed.data(), (size_t)N);
+    BUP(d_young, pm.Eh.data(), sizeof(double) * pm.Eh.size());
+    BUP(d_poisson, pm.nuh.data(), sizeof(double) * pm.nuh.size());
+    if (!pm.node_mass.empty()) BUP(d.node_mass, pm.node_mass.data(), sizeof(double) * N);
+    if (!pm.ext.empty()) {
         if (rs == sizeof(double)) {
-            BUP(d.ext, m->external_force_host, sizeof(double) * 3 * N);
+            BUP(d.ext, pm.ext.data(), sizeof(double) * 3 * N);
         } else {
             ext32.resize((size_t)3 * N);
-            for (size_t i = 0; i < ext32.size(); ++i) ext32[i] = (float)m->external_force_host[i];
+            for (size_t i = 0; i < ext32.size(); ++i) ext32[i] = (float)pm.ext[i];
             BUP(d.ext, ext32.data(), sizeof(float) * ext32.size());
         }
     }
@@ -446,7 +436,7 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     TfemMesh tmp;
     tmp.n_nodes = N;
     tmp.n_tets = E;
-    tmp.method = m->method;
+    tmp.method = pm.method;
     tmp.precision = B->precision;
     tmp.real_size = rs;
     tmp.tets = (int4*)d.tets;
@@ -459,13 +449,12 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     tmp.elem_orig = d_elem_orig;
     // element volumes land in the scratch too, after the initial rotations
     double* vol = (double*)((char*)d.eforce + ((rs * 9 * (size_t)E + 7) & ~(size_t)7));
-    B->ops->init(&tmp, d_young, (int)Eh.size(), d_poisson, (int)nuh.size(), nullptr, 0, vol, s);
+    B->ops->init(&tmp, d_young, (int)pm.Eh.size(), d_poisson, (int)pm.nuh.size(), nullptr, 0, vol, s);
     tmp = TfemMesh();  // the arena owns these buffers
     if ((ce = cudaGetLastError()) != cudaSuccess) return fail_free(bcuda(ce, "init kernel"));
-    // descriptor
     d.n_nodes = N;
     d.n_tets = E;
-    d.method = m->method;
+    d.method = pm.method;
     d.n_patches = Pn;
     d.n_chunks = chunks;
     d.cg_iterations = std::min(P.cg_iterations, B->max_iterations);
@@ -483,7 +472,6 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     d.active = 1;
     if ((ce = cudaMemcpyAsync(&B->d_meshes[slot], &d, sizeof(BMeshDesc), cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return fail_free(bcuda(ce, "descriptor upload"));
-    // wait for the uploads of host vectors before they go out of scope
     if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return fail_free(bcuda(ce, "admission"));
     BatchMeshHost& hm = B->slots[(size_t)slot];
     hm.active = true;
@@ -496,11 +484,15 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     hm.steps = 0;
     hm.perm = L.perm;
     hm.d = d;
-    rc = upload_work_lists(B);
+    int rc = upload_work_lists(B);
     if (rc) return rc;
     *slot_out = slot;
     return SGB_OK;
 }
+
+}  // namespace sgb
+
+extern "C" {
 
 int sgb_batch_remove_mesh(sgb_batch_t* B, int slot)
 {
