@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: build the mixed scene, run warm-up + steps, print a short line")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-beam batched workload")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    ap.add_argument("--beams", type=int, default=256)
+    ap.add_argument("--requests", type=int, default=150, help="requests per arrival rate in the serving sample")
     return ap.parse_args()
 
 
@@ -201,6 +205,132 @@ def e2e_steps(torch, capi, scene, mesh, steps):
         xr, _ = scene.state()
     t1 = time.perf_counter()
     return t1 - t0, 2 * xh.nbytes, 2 * xh.nbytes  # set_state copies x and v; get_state reads x and v
+
+
+def beam_population(n, seed):
+    """Beams of the batched/serving workloads: node counts log-uniform in
+    [1e3, 2e5], aspect z:x uniform in [2, 8], youngModulus log-uniform in
+    [1e3, 1e5], poissonRatio uniform in [0.3, 0.49], method large or polar at
+    50/50; dt 0.01, Rayleigh 0.1/0.1, CG 25 iterations with the reference's
+    default tolerance and threshold (1e-5), total mass 1, z = 0 fixed."""
+    from sofa_gb300 import topology as topo
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nn = 10 ** rng.uniform(3.0, np.log10(2e5))
+        dims = topo.beam_dims(nn, rng.uniform(2.0, 8.0))
+        kw = dict(young=float(10 ** rng.uniform(3, 5)), poisson=float(rng.uniform(0.3, 0.49)),
+                  method="large" if rng.random() < 0.5 else "polar")
+        mesh = topo.beam(dims, 0.5, 0.05, seed * 100003 + i)
+        kw.update(dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=25, cg_tolerance=1e-5,
+                  cg_threshold=1e-5, total_mass=1.0, fixed=mesh.fixed)
+        out.append((mesh, kw))
+    return out
+
+
+def run_batched(torch, capi, args, plain_best):
+    beams = beam_population(args.beams, seed=3)
+    tets = sum(m.n_tets for m, _ in beams)
+    nodes = sum(m.n_nodes for m, _ in beams)
+    b = capi.Batch("mixed", budget_bytes=int(60e9), max_meshes=args.beams + 8, max_cg_iterations=25)
+    t0 = time.perf_counter()
+    b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=min(16, host_threads()))
+    admit_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(b.stream)
+    b.step(args.warmup)
+    b.sync()
+    k = max(2, min(args.steps, 10))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(k)
+    e1.record(stream)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    info = b.info()
+    b.close()
+    value = tets * k / t
+    # position error of mixed vs FP64 (FMA) after 50 steps on a subset
+    sub = beams[:: max(1, len(beams) // 8)][:8]
+    errs, derrs = [], []
+    for prec in ("mixed", "fp64_fma"):
+        bb = capi.Batch(prec, budget_bytes=int(20e9), max_meshes=len(sub) + 1, max_cg_iterations=25)
+        slots = bb.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in sub], threads=min(16, host_threads()))
+        bb.step(50)
+        res = [bb.state(s_)[0] for s_ in slots]
+        bb.close()
+        if prec == "mixed":
+            xm = res
+        else:
+            for (m, _), a, r in zip(sub, xm, res):
+                errs.append(float(np.linalg.norm(a - r) / np.linalg.norm(r)))
+                d = np.linalg.norm(r - m.positions)
+                derrs.append(float(np.linalg.norm(a - r) / d) if d > 0 else 0.0)
+    return {"workload": f"{len(beams)} beams, {nodes} nodes, {tets} tets, mixed precision, one launch per phase, "
+                        "CUDA-graph steps", "tet_steps_per_s": value, "ms_per_step": t / k * 1e3, "steps": k,
+            "admission_s": admit_s, "budget_used_bytes": info["budget_used"],
+            "speedup_vs_plain_fp64_single_mesh": value / plain_best,
+            "position_error_50_steps": {"beams_checked": len(sub), "rel_l2_position_max": max(errs),
+                                        "rel_l2_displacement_max": max(derrs),
+                                        "reference": "the same beams batched in FP64 (FMA)"}}
+
+
+def run_serving(torch, capi, args, plain_best):
+    """Poisson arrivals of simulate-K-steps requests (K uniform in [1, 200])
+    on beams drawn from the batched workload's distribution, a bounded sample
+    of requests per arrival rate, HBM budget 150 GB."""
+    pool = beam_population(32, seed=5)
+    rng = np.random.default_rng(11)
+    results = {}
+    for lam in (50, 200, 1000):
+        srv = capi.Server("mixed", budget_bytes=int(150e9), max_meshes=512, max_cg_iterations=25,
+                          prep_threads=min(8, host_threads()), max_steps_per_launch=8)
+        picks = rng.integers(0, len(pool), args.requests)
+        ks = rng.integers(1, 201, args.requests)
+        gaps = rng.exponential(1.0 / lam, args.requests)
+        t_start = time.perf_counter()
+        t_next = t_start
+        for i in range(args.requests):
+            t_next += gaps[i]
+            dt = t_next - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            mesh, kw = pool[picks[i]]
+            srv.submit(mesh.positions, mesh.tetrahedra, int(ks[i]), **kw)
+        srv.wait_idle(900)
+        st = srv.stats()
+        done = srv.poll(args.requests + 16)
+        srv.close()
+        ok = [c for c in done if c["status"] == 0]
+        offered = float(np.mean([pool[p][0].n_tets * k for p, k in zip(picks, ks)])) * lam
+        results[str(lam)] = {"requests": args.requests, "completed": st["completed"], "failed": st["failed"],
+                             "tet_steps_per_s": st["tet_steps"] / st["wall_s"], "p50_ms": st["p50_ms"],
+                             "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                             "mean_queue_ms": float(np.mean([c["queue_ms"] for c in ok])) if ok else None,
+                             "offered_tet_steps_per_s": offered, "gpu_busy_fraction": st["busy_s"] / st["wall_s"]}
+    # plain path: one request at a time through the FP64 single-mesh scene
+    m_fp = 6
+    t0 = time.perf_counter()
+    ts = 0
+    for i in range(m_fp):
+        mesh, kw = pool[int(rng.integers(0, len(pool)))]
+        k = int(rng.integers(1, 201))
+        fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, kw["young"], kw["poisson"], kw["method"],
+                                  "fp64_fma")
+        sc = capi.Scene(fem, dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=25,
+                        cg_tolerance=1e-5, cg_threshold=1e-5, total_mass=1.0, fixed=mesh.fixed)
+        sc.step(k)
+        sc.state()
+        sc.close()
+        ts += mesh.n_tets * k
+    plain_serial = ts / (time.perf_counter() - t0)
+    best = max(v["tet_steps_per_s"] for v in results.values())
+    return {"arrival_rates": results, "sample": f"{args.requests} requests per rate (bounded sample of the "
+                                                 "10,000-request stream), 32 distinct beams",
+            "plain_fp64_one_at_a_time_tet_steps_per_s": plain_serial,
+            "speedup_vs_plain_fp64_one_at_a_time": best / plain_serial,
+            "speedup_vs_plain_fp64_single_mesh": best / plain_best}
 
 
 def cpu_baseline(mesh, cfg, threads, steps=1):
@@ -357,13 +487,29 @@ def main():
                "sample": f"1 full step of the workload ({E} tets, CG {cfg['cg_iterations']}), FP64 CPU oracle "
                          f"with {threads} threads, {dt:.1f} s"}
 
+    plain_best = max(p["tet_steps_per_s"] for p in plain.values())
+    batched = None
+    if not args.no_batched and rank == 0:
+        batched = run_batched(torch, capi, args, plain_best)
+    serving = None
+    if not args.no_serving and rank == 0:
+        serving = run_serving(torch, capi, args, plain_best)
+
     traffic = None
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
             traffic = json.load(open(prof)).get("adddforce_mixed_bytes_per_call")
         except Exception:
-            traffic = None
+            plain_best = max(p["tet_steps_per_s"] for p in plain.values())
+    batched = None
+    if not args.no_batched and rank == 0:
+        batched = run_batched(torch, capi, args, plain_best)
+    serving = None
+    if not args.no_serving and rank == 0:
+        serving = run_serving(torch, capi, args, plain_best)
+
+    traffic = None
 
     launches_per_step = 5 + 3 * cfg["cg_iterations"]
     line = {
@@ -373,7 +519,9 @@ def main():
         "config": workload_config(cfg, mesh),
         "cg_iterations_last_step": iters_mixed, "cg_residual_last_step": res_mixed,
         "plain_fp64": plain,
-        "speedup_vs_plain_fp64": value / max(p["tet_steps_per_s"] for p in plain.values()),
+        "speedup_vs_plain_fp64": value / plain_best,
+        "batched": batched,
+        "serving": serving,
         "position_error": err,
         "roofline": {"kernel": "addDForce (element + gather kernels, mixed)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,

@@ -249,6 +249,10 @@ int sgb_batch_mesh_bytes(const sgb_batch_t* batch, const sgb_mesh_desc* mesh, si
 /* Admission: SGB_ERR_BUDGET when the mesh does not fit or no slot is free.
  * Synchronous; positions start at rest, velocities at zero. */
 int sgb_batch_add_mesh(sgb_batch_t* batch, const sgb_mesh_desc* mesh, int* slot);
+/* Admits n meshes, preparing them on `threads` host threads; slots[i]
+ * receives mesh i's slot. Stops at the first mesh that cannot be admitted
+ * (the ones before it stay admitted; the others get slot -1). */
+int sgb_batch_add_meshes(sgb_batch_t* batch, const sgb_mesh_desc* meshes, int n, int* slots, int threads);
 int sgb_batch_remove_mesh(sgb_batch_t* batch, int slot);
 /* Advances every admitted mesh by n_steps (stream-ordered, CUDA graph). */
 int sgb_batch_step(sgb_batch_t* batch, int n_steps);

@@ -150,6 +150,7 @@ def load():
         "sgb_batch_mesh_bytes": (c_int, [_vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(ctypes.c_size_t)]),
         "sgb_batch_add_mesh": (c_int, [_vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(c_int)]),
         "sgb_batch_remove_mesh": (c_int, [_vp, c_int]),
+        "sgb_batch_add_meshes": (c_int, [_vp, ctypes.POINTER(MeshDesc), c_int, ctypes.POINTER(c_int), c_int]),
         "sgb_batch_step": (c_int, [_vp, c_int]),
         "sgb_batch_sync": (c_int, [_vp]),
         "sgb_batch_mesh_stats": (c_int, [_vp, c_int, ctypes.POINTER(c_int), _dp, ctypes.POINTER(ctypes.c_longlong)]),
@@ -438,6 +439,21 @@ class Batch:
         check(load().sgb_batch_add_mesh(self._h, ctypes.byref(d), ctypes.byref(slot)))
         self.n_nodes[slot.value] = d.n_nodes
         return slot.value
+
+    def add_meshes(self, meshes, threads=8):
+        """Admits [(positions, tetrahedra, kwargs), ...], preparing them in
+        parallel host threads; returns their slots."""
+        descs = (MeshDesc * len(meshes))()
+        keep = []
+        for i, (pos, tets, kw) in enumerate(meshes):
+            d, k = self.mesh_desc(pos, tets, **kw)
+            descs[i] = d
+            keep.append(k)
+        slots = (ctypes.c_int * len(meshes))()
+        check(load().sgb_batch_add_meshes(self._h, descs, len(meshes), slots, int(threads)))
+        for i in range(len(meshes)):
+            self.n_nodes[slots[i]] = descs[i].n_nodes
+        return list(slots)
 
     def remove_mesh(self, slot):
         check(load().sgb_batch_remove_mesh(self._h, int(slot)))

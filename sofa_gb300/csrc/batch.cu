@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -493,6 +494,33 @@ int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot_out)
 }  // namespace sgb
 
 extern "C" {
+
+int sgb_batch_add_meshes(sgb_batch_t* B, const sgb_mesh_desc* meshes, int n, int* slots, int threads)
+{
+    if (!B || n < 0 || (n > 0 && (!meshes || !slots)))
+        return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_add_meshes: invalid argument");
+    if (threads < 1) threads = 1;
+    std::vector<PreparedMesh> pms((size_t)n);
+    std::vector<int> rcs((size_t)n, SGB_OK);
+    std::vector<std::string> errs((size_t)n);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&, t] {
+            for (int i = t; i < n; i += threads) {
+                rcs[(size_t)i] = prepare_mesh(&meshes[i], B->pe, B->rs, pms[(size_t)i]);
+                if (rcs[(size_t)i]) errs[(size_t)i] = sgb_last_error();
+            }
+        });
+    for (auto& th : pool) th.join();
+    for (int i = 0; i < n; ++i) slots[i] = -1;
+    for (int i = 0; i < n; ++i) {
+        if (rcs[(size_t)i]) return bfail(rcs[(size_t)i], "mesh " + std::to_string(i) + ": " + errs[(size_t)i]);
+        int rc = admit_prepared(B, pms[(size_t)i], &slots[i]);
+        pms[(size_t)i] = PreparedMesh();
+        if (rc) return rc;
+    }
+    return SGB_OK;
+}
 
 int sgb_batch_remove_mesh(sgb_batch_t* B, int slot)
 {

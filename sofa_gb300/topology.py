@@ -41,9 +41,11 @@ _TET6_PLAIN = ((0, 5, 1, 6), (0, 1, 3, 6), (1, 3, 6, 2), (6, 3, 0, 7), (6, 7, 0,
 _TET6_SWAPPED = ((0, 5, 6, 1), (0, 1, 6, 3), (1, 3, 2, 6), (6, 3, 7, 0), (6, 7, 5, 0), (7, 5, 0, 4))
 
 # 5-tet split: four corner tetrahedra cut off alternate corners plus the
-# central one. Even cells cut corners 1,3,4,6; odd cells cut 0,2,5,7.
-_TET5_EVEN = ((1, 0, 2, 5), (3, 0, 7, 2), (4, 0, 5, 7), (6, 2, 7, 5), (0, 2, 5, 7))
-_TET5_ODD = ((0, 1, 4, 3), (2, 1, 3, 6), (5, 1, 6, 4), (7, 3, 4, 6), (1, 3, 6, 4))
+# central one. Even cells cut corners 1,3,4,6; odd cells cut 0,2,5,7. The
+# vertex order gives every tetrahedron of an undistorted cell a positive
+# volume (a jitter below a quarter of the spacing cannot flip one).
+_TET5_EVEN = ((1, 0, 5, 2), (3, 0, 2, 7), (4, 0, 7, 5), (6, 2, 5, 7), (0, 2, 7, 5))
+_TET5_ODD = ((0, 1, 3, 4), (2, 1, 6, 3), (5, 1, 4, 6), (7, 3, 6, 4), (1, 3, 4, 6))
 
 
 def grid_index(n, i, j, k):
@@ -123,8 +125,9 @@ def hexa_to_tetra6(hexa, n_cells=None, swapping=False):
 def hexa_to_tetra5(hexa, n_nodes_per_axis, positions=None):
     """5 tetrahedra per grid cell, diagonals alternating with (i+j+k) parity.
 
-    Every tetrahedron is returned with positive signed volume (vertices 2 and
-    3 swapped where needed) when ``positions`` is given.
+    The patterns are positively oriented on undistorted cells; with
+    ``positions`` given, any tetrahedron that still has a negative volume
+    (a strongly distorted grid) gets vertices 2 and 3 swapped.
     """
     nx, ny, nz = (int(v) for v in n_nodes_per_axis)
     hexa = np.asarray(hexa, dtype=np.int64)
@@ -139,6 +142,14 @@ def hexa_to_tetra5(hexa, n_nodes_per_axis, positions=None):
     if positions is not None:
         tets = orient_positive(tets, positions)
     return tets.astype(np.int32)
+
+
+def beam_dims(n_nodes, aspect):
+    """Grid of a square-section beam with about ``n_nodes`` nodes and
+    length/width ratio ``aspect`` (z : x)."""
+    nx = max(2, int(round((n_nodes / aspect) ** (1.0 / 3.0))))
+    nz = max(2, int(round(n_nodes / (nx * nx))))
+    return (nx, nx, nz)
 
 
 def signed_volumes(tets, positions):
@@ -203,7 +214,7 @@ def beam(n, spacing=0.5, jitter=0.05, seed=0, split=5):
         delta = rng.uniform(-jitter * spacing, jitter * spacing, size=pos.shape)
         pos = pos + np.where(interior[:, None], delta, 0.0)
     if split == 5:
-        tets = hexa_to_tetra5(hexa, (nx, ny, nz), pos)
+        tets = hexa_to_tetra5(hexa, (nx, ny, nz), pos if jitter > 0.2 else None)
     elif split == 6:
         tets = hexa_to_tetra6(hexa, (nx - 1, ny - 1))
     else:
