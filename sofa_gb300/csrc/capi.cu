@@ -388,6 +388,26 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
     SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
     for (int w = 0; w < 2; ++w) {
         if (!dst[w] || E == 0) continue;
+        if (w == 0 && rs == sizeof(float)) {
+            // FP32 keeps the current rotation as a unit quaternion (x, y, z, w;
+            // w <= -2 flags a reflection)
+            std::vector<float> q(4 * E);
+            SGB_CUDA_TRY(cudaMemcpy(q.data(), src[w], sizeof(float) * 4 * E, cudaMemcpyDeviceToHost));
+            for (size_t e = 0; e < E; ++e) {
+                double x = q[4 * e], y = q[4 * e + 1], z = q[4 * e + 2], ww = q[4 * e + 3], sg = 1.0;
+                if (ww <= -1.5) {
+                    sg = -1.0;
+                    ww = -ww - 2.0;
+                }
+                const double Rm[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - ww * z), 2 * (x * z + ww * y),
+                                      2 * (x * y + ww * z), 1 - 2 * (x * x + z * z), 2 * (y * z - ww * x),
+                                      2 * (x * z - ww * y), 2 * (y * z + ww * x), 1 - 2 * (x * x + y * y)};
+                const size_t o = (size_t)fem->m.perm_h[e];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) dst[w][9 * o + 3 * i + j] = sg * Rm[3 * j + i];
+            }
+            continue;
+        }
         SGB_CUDA_TRY(cudaMemcpy(buf.data(), src[w], rs * 9 * E, cudaMemcpyDeviceToHost));
         for (size_t e = 0; e < E; ++e) {
             const size_t o = (size_t)fem->m.perm_h[e];  // caller's element index

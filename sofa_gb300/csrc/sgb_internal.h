@@ -164,7 +164,7 @@ struct WorkItem {
 enum { WL_PATCH = 0, WL_ELEM = 1, WL_NODE = 2 };
 constexpr int kBatchElemChunk = 1024;
 constexpr int kBatchNodeChunk = 1024;
-constexpr int kBatchMaxLocalNodes = 1024;
+constexpr int kBatchMaxLocalNodes = 512;
 
 // Device-resident descriptor of one admitted mesh: its arrays (inside the
 // batch's HBM arena), its solver parameters and its CG scalars. Kernels read

@@ -53,6 +53,144 @@ __device__ __forceinline__ void ld3(const float* p, long long i, float o[3])
 }
 
 // ------------------------------------------------------------------------
+// Element-data access. FP64 keeps the reference's quantities as rows of
+// n_tets entries: R (9), K(0,0), K(0,1), K(3,3) (3), J (12). FP32 packs
+// what every CG matvec reads into 64 bytes: the rotation as a unit
+// quaternion (one float4 in `rot`; a reflection, which the polar factor of an
+// inverted element can be, is flagged by w <= -2), and in `J` three float4
+// planes holding J scaled by sqrt(K(0,0)) for nodes b, c, d and the ratios
+// K(0,1)/K(0,0), K(3,3)/K(0,0). Node a's J is minus the sum of the other
+// three (the columns of J sum to zero over the nodes), so a translation
+// gives exactly zero strain.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ float4 rot_to_quat(const float Rm[9])
+{
+    // Shepperd's method on the largest of the trace and the diagonal
+    float det = Rm[0] * (Rm[4] * Rm[8] - Rm[5] * Rm[7]) - Rm[1] * (Rm[3] * Rm[8] - Rm[5] * Rm[6]) +
+                Rm[2] * (Rm[3] * Rm[7] - Rm[4] * Rm[6]);
+    const float sg = det < 0.f ? -1.f : 1.f;
+    float M[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) M[i] = sg * Rm[i];
+    const float tr = M[0] + M[4] + M[8];
+    float x, y, z, w;
+    if (tr > 0.f) {
+        const float t = sqrtf(tr + 1.f) * 2.f;
+        w = 0.25f * t;
+        x = (M[7] - M[5]) / t;
+        y = (M[2] - M[6]) / t;
+        z = (M[3] - M[1]) / t;
+    } else if (M[0] > M[4] && M[0] > M[8]) {
+        const float t = sqrtf(1.f + M[0] - M[4] - M[8]) * 2.f;
+        w = (M[7] - M[5]) / t;
+        x = 0.25f * t;
+        y = (M[1] + M[3]) / t;
+        z = (M[2] + M[6]) / t;
+    } else if (M[4] > M[8]) {
+        const float t = sqrtf(1.f + M[4] - M[0] - M[8]) * 2.f;
+        w = (M[2] - M[6]) / t;
+        x = (M[1] + M[3]) / t;
+        y = 0.25f * t;
+        z = (M[5] + M[7]) / t;
+    } else {
+        const float t = sqrtf(1.f + M[8] - M[0] - M[4]) * 2.f;
+        w = (M[3] - M[1]) / t;
+        x = (M[2] + M[6]) / t;
+        y = (M[5] + M[7]) / t;
+        z = 0.25f * t;
+    }
+    const float n = rsqrtf(x * x + y * y + z * z + w * w);
+    x *= n;
+    y *= n;
+    z *= n;
+    w *= n;
+    if (w < 0.f) {  // q and -q are the same rotation: keep w >= 0
+        x = -x;
+        y = -y;
+        z = -z;
+        w = -w;
+    }
+    if (sg < 0.f) w = -w - 2.f;  // reflection flag
+    return make_float4(x, y, z, w);
+}
+
+__device__ __forceinline__ void quat_to_rot(float4 q, float Rm[9])
+{
+    float sg = 1.f;
+    float w = q.w;
+    if (w <= -1.5f) {
+        sg = -1.f;
+        w = -w - 2.f;
+    }
+    const float x = q.x, y = q.y, z = q.z;
+    const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y,
+                wz = w * z;
+    Rm[0] = sg * (1.f - 2.f * (yy + zz));
+    Rm[1] = sg * (2.f * (xy - wz));
+    Rm[2] = sg * (2.f * (xz + wy));
+    Rm[3] = sg * (2.f * (xy + wz));
+    Rm[4] = sg * (1.f - 2.f * (xx + zz));
+    Rm[5] = sg * (2.f * (yz - wx));
+    Rm[6] = sg * (2.f * (xz - wy));
+    Rm[7] = sg * (2.f * (yz + wx));
+    Rm[8] = sg * (1.f - 2.f * (xx + yy));
+}
+
+template <typename R>
+__device__ __forceinline__ void load_rot(const ElemView<R>& ev, size_t e, R Rm[9])
+{
+    if constexpr (is_mixed<R>::value) {
+        quat_to_rot(reinterpret_cast<const float4*>(ev.rot)[e], Rm);
+    } else {
+        const size_t En = (size_t)ev.n_tets;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void store_rot(const ElemView<R>& ev, size_t e, const R Rm[9])
+{
+    if constexpr (is_mixed<R>::value) {
+        reinterpret_cast<float4*>(ev.rot)[e] = rot_to_quat(Rm);
+    } else {
+        const size_t En = (size_t)ev.n_tets;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) ev.rot[i * En + e] = Rm[i];
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void load_KJ(const ElemView<R>& ev, size_t e, R K[3], R J[12])
+{
+    const size_t En = (size_t)ev.n_tets;
+    if constexpr (is_mixed<R>::value) {
+        const float4* P = reinterpret_cast<const float4*>(ev.J);
+        const float4 a = P[e], b = P[En + e], c = P[2 * En + e];
+        J[3] = a.x;
+        J[4] = a.y;
+        J[5] = a.z;
+        J[6] = a.w;
+        J[7] = b.x;
+        J[8] = b.y;
+        J[9] = b.z;
+        J[10] = b.w;
+        J[11] = c.x;
+        J[0] = -(J[3] + J[6] + J[9]);
+        J[1] = -(J[4] + J[7] + J[10]);
+        J[2] = -(J[5] + J[8] + J[11]);
+        K[0] = 1.f;
+        K[1] = c.y;
+        K[2] = c.z;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
+#pragma unroll
+        for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
+    }
+}
+
+// ------------------------------------------------------------------------
 // initialisation: per-element K, J, initial rotation and rotated rest
 // coordinates, computed in FP64 (computeMaterialStiffness TFEM.inl:256-291,
 // initSmall/initLarge/initPolar TFEM.inl:526-532, 835-868, 993-1023) and
@@ -136,26 +274,26 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
             rr[0] = rr[1] = rr[2] = 0.0;
         }
     }
-    for (int i = 0; i < 12; ++i) J[(size_t)i * En + s] = (R)Jd[i];
-    for (int i = 0; i < 12; ++i) rest[(size_t)i * En + s] = (R)rr[i];
-    for (int i = 0; i < 9; ++i) {
-        rot[(size_t)i * En + s] = (R)Rm[i];
-        R0[(size_t)i * En + s] = (R)Rm[i];
+    if constexpr (is_mixed<R>::value) {
+        const double sk = sqrt(k0);
+        float4* P = reinterpret_cast<float4*>(J);
+        P[s] = make_float4((float)(sk * Jd[3]), (float)(sk * Jd[4]), (float)(sk * Jd[5]), (float)(sk * Jd[6]));
+        P[En + s] = make_float4((float)(sk * Jd[7]), (float)(sk * Jd[8]), (float)(sk * Jd[9]), (float)(sk * Jd[10]));
+        P[2 * En + s] = make_float4((float)(sk * Jd[11]), (float)(k1 / k0), (float)(k2 / k0), 0.f);
+        float Rf[9];
+        for (int i = 0; i < 9; ++i) Rf[i] = (float)Rm[i];
+        reinterpret_cast<float4*>(rot)[s] = rot_to_quat(Rf);
+    } else {
+        for (int i = 0; i < 12; ++i) J[(size_t)i * En + s] = (R)Jd[i];
+        for (int i = 0; i < 9; ++i) rot[(size_t)i * En + s] = (R)Rm[i];
     }
+    for (int i = 0; i < 12; ++i) rest[(size_t)i * En + s] = (R)rr[i];
+    for (int i = 0; i < 9; ++i) R0[(size_t)i * En + s] = (R)Rm[i];
 }
 
 // ------------------------------------------------------------------------
 // element kernels
 // ------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ void load_elem_KJ(const ElemView<R>& ev, int e, R K[3], R J[12])
-{
-    const size_t En = (size_t)ev.n_tets;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
-#pragma unroll
-    for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
-}
 
 template <typename R>
 __device__ __forceinline__ void store_eforce(R* eforce, int e, const R c[12])
@@ -180,7 +318,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
     ld3(x, t.z, p[2]);
     ld3(x, t.w, p[3]);
     R K[3], J[12];
-    load_elem_KJ(ev, e, K, J);
+    load_KJ(ev, (size_t)e, K, J);
     R D[12], F[12], c[12];
     if (METHOD == METHOD_SMALL) {
         double q[4][3];
@@ -266,8 +404,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
             }
         if (METHOD == METHOD_LARGE) D[4] = D[5] = D[8] = R(0);
     }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) ev.rot[i * En + e] = Rm[i];
+    store_rot(ev, (size_t)e, Rm);
     element_force_nofact(F, D, K, J);
     // f[node] += rotations[e] * F_node, rotations[e] = R^T
 #pragma unroll
@@ -349,7 +486,7 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
             for (int k = 0; k < 3; ++k) xin[i][k] -= xin[0][k];
     }
     R K[3], J[12];
-    load_elem_KJ(ev, e, K, J);
+    load_KJ(ev, (size_t)e, K, J);
     R X[12], F[12], c[12];
     if (METHOD == METHOD_SMALL) {
 #pragma unroll
@@ -363,8 +500,7 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
         return;
     }
     R Rm[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
+    load_rot(ev, (size_t)e, Rm);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -819,12 +955,8 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
 #pragma unroll
             for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
         R Rm[9], K[3], J[12];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Rm[i] = ev.rot[i * En + e];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) K[i] = ev.K[i * En + e];
-#pragma unroll
-        for (int i = 0; i < 12; ++i) J[i] = ev.J[i * En + e];
+        load_rot(ev, e, Rm);
+        load_KJ(ev, e, K, J);
         R X[12], F[12];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
