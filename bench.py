@@ -428,7 +428,10 @@ def main():
     mixed.sync()
     if args.profile:
         t = time_steps(torch, mixed, args.steps, args.warmup)
-        print(json.dumps({"profile_run": True, "n_tets": E, "ms_per_step": t / max(args.steps, 1) * 1e3}))
+        # then three addDForce calls through the C ABI (the roofline unit)
+        t_df = time_add_dforce(torch, capi, mixed, mesh, reps=3)
+        print(json.dumps({"profile_run": True, "n_tets": E, "ms_per_step": t / max(args.steps, 1) * 1e3,
+                          "adddforce_ms": t_df * 1e3}))
         return 0
     if world > 1:
         torch.distributed.barrier()

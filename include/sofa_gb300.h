@@ -39,6 +39,7 @@ extern "C" {
 #define SGB_ERR_NUMERICAL -5   /* a non-finite value was met in the CG solve */
 #define SGB_ERR_BUDGET -6      /* admission refused: HBM budget exceeded */
 #define SGB_ERR_NOT_FOUND -7
+#define SGB_ERR_DEVICE_TIMEOUT -8 /* a bounded device-side wait (bulk copy completion) ran out */
 
 /* TetrahedronFEMForceField Data "method"
  * (TetrahedronFEMForceField.inl:45): small, large (QR frame), polar. */
@@ -102,6 +103,12 @@ int sgb_tfem_add_dforce_f32(sgb_tfem_t* fem, const float* dx_dev, float* df_dev,
  * 9 doubles row-major per element (TetrahedronFEMForceField.h
  * getActualTetraRotation / getInitialTetraRotation). Synchronous. */
 int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* initial_rotations_host);
+
+/* Reads and clears the force field's sticky device error flag (synchronises
+ * the device). SGB_OK, or SGB_ERR_DEVICE_TIMEOUT when a bounded device-side
+ * wait of an earlier add_dforce (the completion of the bulk copies that
+ * stage element data) ran out; that call's df is then incomplete. */
+int sgb_tfem_check_device(sgb_tfem_t* fem);
 
 /* Sizes and device footprint of the force field. */
 int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method, int* precision,

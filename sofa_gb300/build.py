@@ -32,6 +32,10 @@ UNITS = {
     "noalloc.cu": [],
     "batch.cu": [],
     "server.cu": [],
+    "scene_graph.cpp": [],
+    "scene_components.cpp": [],
+    "scene_xml.cpp": [],
+    "plugin.cpp": [],
 }
 
 

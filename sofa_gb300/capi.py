@@ -23,6 +23,7 @@ ERRORS = {
     -5: "non-finite value in the CG solve",
     -6: "HBM budget exceeded",
     -7: "not found",
+    -8: "a bounded device-side wait ran out",
 }
 METHODS = {"small": 0, "large": 1, "polar": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1, "fp64_fma": 2}
@@ -166,6 +167,29 @@ def load():
         "sgb_server_wait_idle": (c_int, [_vp, c_double]),
         "sgb_server_get_stats": (c_int, [_vp, ctypes.POINTER(ServerStats)]),
         "sgb_server_destroy": (c_int, [_vp]),
+        "sgb_sofa_scene_load": (c_int, [ctypes.POINTER(_vp), ctypes.c_char_p, c_int]),
+        "sgb_sofa_scene_destroy": (c_int, [_vp]),
+        "sgb_sofa_scene_describe": (c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "sgb_sofa_scene_bodies": (c_int, [_vp, ctypes.POINTER(c_int)]),
+        "sgb_sofa_scene_body_info": (c_int, [_vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                             ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+        "sgb_sofa_scene_body_arrays": (c_int, [_vp, c_int, _ip, _dp, _ip]),
+        "sgb_sofa_scene_init_device": (c_int, [_vp]),
+        "sgb_sofa_scene_animate": (c_int, [_vp, c_int]),
+        "sgb_sofa_scene_get_positions": (c_int, [_vp, c_int, _dp]),
+        "sgb_sofa_scene_time": (c_int, [_vp, _dp]),
+        "sgb_object_factory_new": (_vp, []),
+        "sgb_object_factory_delete": (None, [_vp]),
+        "sgb_object_factory_has": (c_int, [_vp, ctypes.c_char_p]),
+        "sgb_object_factory_count": (c_int, [_vp]),
+        "initExternalModule": (None, []),
+        "getModuleName": (ctypes.c_char_p, []),
+        "getModuleVersion": (ctypes.c_char_p, []),
+        "getModuleLicense": (ctypes.c_char_p, []),
+        "getModuleDescription": (ctypes.c_char_p, []),
+        "getModuleComponentList": (ctypes.c_char_p, []),
+        "moduleIsInitialized": (ctypes.c_bool, []),
+        "registerObjects": (None, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -560,3 +584,73 @@ class Server:
         st = ServerStats()
         check(load().sgb_server_get_stats(self._h, ctypes.byref(st)))
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+
+class SofaScene:
+    """Handle of sgb_sofa_scene_t: a SOFA scene file (.scn XML) parsed into
+    the component graph and run on the GPU, one library scene per node that
+    holds an EulerImplicitSolver."""
+
+    def __init__(self, xml_text: str, precision: int = -1):
+        lib = load()
+        h = _vp()
+        check(lib.sgb_sofa_scene_load(ctypes.byref(h), xml_text.encode(), int(precision)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().sgb_sofa_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def describe(self) -> dict:
+        import json
+
+        lib = load()
+        need = ctypes.c_size_t()
+        check(lib.sgb_sofa_scene_describe(self._h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        check(lib.sgb_sofa_scene_describe(self._h, buf, need.value, None))
+        return json.loads(buf.value.decode())
+
+    @property
+    def n_bodies(self) -> int:
+        n = ctypes.c_int()
+        check(load().sgb_sofa_scene_bodies(self._h, ctypes.byref(n)))
+        return n.value
+
+    def body_info(self, body=0) -> dict:
+        v = [ctypes.c_int() for _ in range(5)]
+        check(load().sgb_sofa_scene_body_info(self._h, int(body), *[ctypes.byref(x) for x in v]))
+        return dict(zip(("n_nodes", "n_tets", "method", "precision", "n_fixed"), (x.value for x in v)))
+
+    def body_arrays(self, body=0):
+        info = self.body_info(body)
+        tets = np.zeros((info["n_tets"], 4), np.int32)
+        masses = np.zeros(info["n_nodes"], np.float64)
+        fixed = np.zeros(max(info["n_fixed"], 1), np.int32)
+        check(load().sgb_sofa_scene_body_arrays(self._h, int(body), tets.ctypes.data_as(_ip),
+                                                 masses.ctypes.data_as(_dp), fixed.ctypes.data_as(_ip)))
+        return tets, masses, fixed[: info["n_fixed"]]
+
+    def init_device(self):
+        check(load().sgb_sofa_scene_init_device(self._h))
+
+    def animate(self, n_steps=1):
+        check(load().sgb_sofa_scene_animate(self._h, int(n_steps)))
+
+    def positions(self, body=0):
+        x = np.zeros((self.body_info(body)["n_nodes"], 3), np.float64)
+        check(load().sgb_sofa_scene_get_positions(self._h, int(body), x.ctypes.data_as(_dp)))
+        return x
+
+    @property
+    def time(self) -> float:
+        t = ctypes.c_double()
+        check(load().sgb_sofa_scene_time(self._h, ctypes.byref(t)))
+        return t.value

@@ -139,7 +139,7 @@ static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool no
     c.add((int**)&d.lnode_info, sizeof(int) * L.lnode_info.size());
     c.add((int**)&d.lrow, sizeof(int) * L.lrow.size());
     c.add((uint16_t**)&d.lslots, sizeof(uint16_t) * L.lslots.size());
-    c.add((ushort4**)&d.lconn, sizeof(ushort4) * L.lconn.size());
+    c.add((ushort4**)&d.lconn, sizeof(ushort4) * (L.lconn.size() + 2));
     c.add((int**)&d.bnd_rowptr, sizeof(int) * (N + 1));
     c.add(&d.partials, rs * 3 * (size_t)std::max(L.n_partials, 1));
     c.add(&d.x, sizeof(double) * 3 * N);
@@ -227,15 +227,17 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
         (e = cudaMalloc((void**)&B->arena_mem, hbm_budget_bytes)) != cudaSuccess ||
         (e = cudaMalloc((void**)&B->d_meshes, sizeof(BMeshDesc) * max_meshes)) != cudaSuccess ||
         (e = cudaMalloc((void**)&B->d_counts, sizeof(int) * 4)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&B->d_err, sizeof(int))) != cudaSuccess ||
         (e = cudaMemset(B->d_meshes, 0, sizeof(BMeshDesc) * max_meshes)) != cudaSuccess ||
-        (e = cudaMemset(B->d_counts, 0, sizeof(int) * 4)) != cudaSuccess) {
+        (e = cudaMemset(B->d_counts, 0, sizeof(int) * 4)) != cudaSuccess ||
+        (e = cudaMemset(B->d_err, 0, sizeof(int))) != cudaSuccess) {
         int rc = bcuda(e, "sgb_batch_create");
         sgb_batch_destroy(B);
         return rc;
     }
     B->arena.reset(B->arena_mem, hbm_budget_bytes);
     B->device_bytes = hbm_budget_bytes + sizeof(BMeshDesc) * max_meshes;
-    B->sms = ops->batch_prepare(B->pe, &B->grid_patch);
+    B->sms = ops->batch_prepare(B->pe, &B->grid_patch, &B->staged);
     if (B->sms <= 0) {
         sgb_batch_destroy(B);
         return bfail(SGB_ERR_CUDA, "sgb_batch_create: kernel attributes");
@@ -256,6 +258,7 @@ int sgb_batch_destroy(sgb_batch_t* B)
     if (B->graph) cudaGraphExecDestroy(B->graph);
     for (int k = 0; k < 3; ++k) cudaFree(B->d_items[k]);
     cudaFree(B->d_counts);
+    cudaFree(B->d_err);
     cudaFree(B->d_meshes);
     cudaFree(B->arena_mem);
     if (B->stream) cudaStreamDestroy(B->stream);
@@ -552,6 +555,8 @@ int sgb_batch_step(sgb_batch_t* B, int n_steps)
         L.grid_node = B->sms * 4;
         L.pe = B->pe;
         L.max_iterations = B->max_iterations;
+        L.staged = B->staged;
+        L.err = B->d_err;
         cudaGraph_t g;
         BTRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
         B->ops->batch_record(L, B->stream);
@@ -573,7 +578,10 @@ int sgb_batch_step(sgb_batch_t* B, int n_steps)
 int sgb_batch_sync(sgb_batch_t* B)
 {
     if (!B) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_sync: NULL batch");
+    int err = 0;
+    BTRY(cudaMemcpyAsync(&err, B->d_err, sizeof(int), cudaMemcpyDeviceToHost, B->stream));
     BTRY(cudaStreamSynchronize(B->stream));
+    if (err) return bfail(SGB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait ran out in the batch step");
     return SGB_OK;
 }
 
@@ -588,6 +596,7 @@ int sgb_batch_mesh_stats(sgb_batch_t* B, int slot, int* cg_iterations, double* c
     if (cg_residual) *cg_residual = d.last_err;
     if (steps) *steps = B->slots[(size_t)slot].steps;
     if (d.status & 1) return bfail(SGB_ERR_NUMERICAL, "non-finite value in this mesh's CG solve");
+    if (d.status & 2) return bfail(SGB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait ran out in this mesh's solve");
     return SGB_OK;
 }
 

@@ -65,11 +65,12 @@ struct sgb_batch {
     sgb::WorkItem* d_items[3] = {nullptr, nullptr, nullptr};
     int cap[3] = {0, 0, 0};
     int* d_counts = nullptr;
+    int* d_err = nullptr;  // sticky device error flag: 1 = a bounded device wait ran out
     int counts_h[3] = {0, 0, 0};
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
-    int sms = 152, grid_patch = 152;
+    int sms = 152, grid_patch = 152, staged = 0;
     size_t device_bytes = 0;
 };
 

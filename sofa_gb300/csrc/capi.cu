@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <cstdlib>
 #include <vector>
 
 #include "../../include/sofa_gb300.h"
@@ -112,6 +113,7 @@ static void free_mesh(TfemMesh& m)
     cudaFree(m.pl.lconn);
     cudaFree(m.pl.bnd_rowptr);
     cudaFree(m.pl.partials);
+    cudaFree(m.dev_flags);
     m = TfemMesh();
 }
 
@@ -185,7 +187,14 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     // the fused variants; the reference-rounding variant keeps the caller's
     // element order
     HostLayout L;
-    const int pe = ops->real_size == 4 ? 512 : 256;
+    // elements per patch: 512 (FP32) / 256 (FP64); SGB_PATCH_PE overrides the
+    // FP32 value (an even count in [32, 1024])
+    int pe = ops->real_size == 4 ? 512 : 256;
+    if (ops->real_size == 4)
+        if (const char* e = getenv("SGB_PATCH_PE")) {
+            const int v = atoi(e);
+            if (v >= 32 && v <= 1024 && v % 2 == 0) pe = v;
+        }
     if (ops->uses_patches && method != SGB_METHOD_SMALL && n_tets > 0) {
         build_patch_layout(n_nodes, n_tets, tetrahedra_host, rest_positions_host, pe, 1024, L);
     } else {
@@ -213,8 +222,12 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
         (rc = dev_alloc_bytes(&m.J, rs * 12 * E, acc)) || (rc = dev_alloc_bytes(&m.rest, rs * 12 * E, acc)) ||
         (rc = dev_alloc_bytes(&m.eforce, rs * 12 * E, acc)) || (rc = dev_alloc(&m.rest_pos, 3 * (size_t)n_nodes, acc)) ||
         (rc = dev_alloc(&m.rowptr, (size_t)n_nodes + 1, acc)) || (rc = dev_alloc(&m.slots, 4 * E, acc)) ||
-        (rc = dev_alloc(&m.elem_orig, E, acc)))
+        (rc = dev_alloc(&m.elem_orig, E, acc)) || (rc = dev_alloc(&m.dev_flags, 1, acc)))
         goto fail_out;
+    if ((ce = cudaMemsetAsync(m.dev_flags, 0, sizeof(int), h->stream)) != cudaSuccess) {
+        rc = cuda_fail(ce, "cudaMemsetAsync");
+        goto fail_out;
+    }
     if (!L.elem_start.empty()) {
         PatchLayout& pl = m.pl;
         pl.n_patches = (int)L.elem_start.size() - 1;
@@ -228,7 +241,7 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
             (rc = dev_alloc(&pl.lnode_gid, L.lnode_gid.size(), acc)) ||
             (rc = dev_alloc(&pl.lnode_info, L.lnode_info.size(), acc)) ||
             (rc = dev_alloc(&pl.lrow, L.lrow.size(), acc)) || (rc = dev_alloc(&pl.lslots, L.lslots.size(), acc)) ||
-            (rc = dev_alloc(&pl.lconn, L.lconn.size(), acc)) ||
+            (rc = dev_alloc(&pl.lconn, L.lconn.size() + 2, acc)) ||
             (rc = dev_alloc(&pl.bnd_rowptr, L.bnd_rowptr.size(), acc)) ||
             (rc = dev_alloc_bytes(&pl.partials, rs * 3 * (size_t)std::max(L.n_partials, 1), acc)))
             goto fail_out;
@@ -423,6 +436,20 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
     return SGB_OK;
 }
 
+int sgb_tfem_check_device(sgb_tfem_t* fem)
+{
+    if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_check_device: NULL handle");
+    int flag = 0;
+    const int zero = 0;
+    SGB_CUDA_TRY(cudaDeviceSynchronize());
+    SGB_CUDA_TRY(cudaMemcpy(&flag, fem->m.dev_flags, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        SGB_CUDA_TRY(cudaMemcpy(fem->m.dev_flags, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        return fail(SGB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait ran out in an earlier add_dforce");
+    }
+    return SGB_OK;
+}
+
 int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method, int* precision, size_t* device_bytes)
 {
     if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_info: NULL handle");
@@ -442,7 +469,7 @@ int sgb_patch_layout_check(int n_nodes, const double* rest_positions_host, int n
                            int elements_per_patch, int max_nodes_per_patch, int* stats)
 {
     if (n_nodes <= 0 || n_tets < 0 || !rest_positions_host || (n_tets > 0 && !tetrahedra_host) ||
-        elements_per_patch < 1 || elements_per_patch > 16384 || max_nodes_per_patch < 4 ||
+        elements_per_patch < 2 || elements_per_patch > 16384 || max_nodes_per_patch < 8 ||
         max_nodes_per_patch > 65535)
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_patch_layout_check: invalid argument");
     for (size_t i = 0; i < (size_t)n_tets * 4; ++i)
@@ -459,6 +486,7 @@ int sgb_patch_layout_check(int n_nodes, const double* rest_positions_host, int n
     for (int p = 0; p < P; ++p) {
         const int e0 = L.elem_start[p], e1 = L.elem_start[p + 1];
         if (e1 - e0 > elements_per_patch || e1 <= e0) return fail(SGB_ERR_NUMERICAL, "patch element range");
+        if (p + 1 < P && ((e1 - e0) & 1)) return fail(SGB_ERR_NUMERICAL, "odd element count before the last patch");
         const int n0 = L.node_start[p], n1 = L.node_start[p + 1];
         if (n1 - n0 > max_nodes_per_patch) return fail(SGB_ERR_NUMERICAL, "patch node count");
         for (int l = n0; l < n1; ++l) {
@@ -659,6 +687,7 @@ int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual)
     if (cg_iterations) *cg_iterations = s.cg_h->iters;
     if (cg_residual) *cg_residual = s.cg_h->last_err;
     if (s.cg_h->status & 1) return fail(SGB_ERR_NUMERICAL, "non-finite value in the CG solve");
+    if (s.cg_h->status & 2) return fail(SGB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait ran out in the CG solve");
     return SGB_OK;
 }
 

@@ -54,10 +54,16 @@ void build_patch_layout(int N, int E, const int32_t* tets, const double* pos, in
     keys.clear();
     keys.shrink_to_fit();
 
-    // 2. greedy patches of at most `pe` elements and `pn_max` distinct nodes
+    // 2. greedy patches of at most `pe` elements and `pn_max` distinct nodes.
+    //    Every patch but the last has an even element count (pe is even), so
+    //    each patch's per-element arrays start on a 16-byte boundary for the
+    //    kernels' bulk copies; a patch closes only at an even count, keeping
+    //    room for the four nodes of one more element under pn_max.
     std::vector<int> stamp((size_t)N, -1);
     L.elem_start.clear();
     L.elem_start.push_back(0);
+    pe = pe & ~1;
+    if (pe < 2) pe = 2;
     {
         int patch = 0, count = 0, nodes = 0;
         for (int s = 0; s < E; ++s) {
@@ -65,7 +71,7 @@ void build_patch_layout(int N, int E, const int32_t* tets, const double* pos, in
             int fresh = 0;
             for (int i = 0; i < 4; ++i)
                 if (stamp[(size_t)t[i]] != patch) fresh++;
-            if (count > 0 && (count + 1 > pe || nodes + fresh > pn_max)) {
+            if (count > 0 && (count % 2) == 0 && (count + 1 > pe || nodes + fresh > pn_max - 4)) {
                 L.elem_start.push_back(s);
                 patch++;
                 count = 0;

@@ -18,6 +18,9 @@ enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
 // finish reduces them in index order, so a dot product is bit-reproducible.
 constexpr int kNodeBlock = 256;
 constexpr int kMaxNodeBlocks = 152 * 8;
+// Largest grid of a kernel that finishes a dot product (size of the per-block
+// partial array): the persistent patch kernels run up to 32 small CTAs per SM.
+constexpr int kMaxDotBlocks = 152 * 32;
 constexpr int kElemBlock = 128;
 
 // Structure-of-arrays view of the per-element data. Arrays of width W are
@@ -93,6 +96,12 @@ struct TfemMesh {
     int max_valence = 0;
     void* eforce = nullptr;   // scratch: 12 reals per element (corner forces)
     int patch_grid = 0;       // CTAs of the persistent patch kernels
+    int patch_threads = 128;  // threads per CTA of the patch kernels
+    int patch_prefetch = 0;   // 1: each CTA prefetches its next patch into L2
+    int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads
+    bool staged = false;      // FP32: the patch kernels stage element data with bulk copies
+    int staged_grid = 0;      // CTAs of the staged patch kernels
+    int* dev_flags = nullptr; // sticky device error flag: 1 = a bounded device wait ran out
     double rest_volume = 0.0;
     std::vector<double> young_h, poisson_h;  // as given (for inspection)
     size_t device_bytes = 0;
@@ -106,11 +115,11 @@ struct CgScalars {
     long long time_step_count;
     int done;
     int iters;
-    int status;  // bit 0: non-finite value seen
+    int status;  // bit 0: non-finite value seen; bit 1: a bounded device wait ran out
     int pad;
     unsigned int ticket;
     unsigned int pad2;
-    double partials[kMaxNodeBlocks];
+    double partials[kMaxDotBlocks];
 };
 
 struct SceneParams {
@@ -225,6 +234,8 @@ struct BatchLaunch {
     int grid_patch, grid_elem, grid_node;
     int pe;
     int max_iterations;
+    int staged;  // FP32: use the bulk-copy staged matvec
+    int* err;    // sticky device error flag of the batch
 };
 
 }  // namespace sgb

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstdlib>
 #include <type_traits>
 
 #include "sgb_internal.h"
@@ -906,7 +907,39 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict_
 // (first iteration) or p = p_old*beta + r, q = mF M p - sum, projected, and
 // p^T A p from element energies plus the mass term.
 // ------------------------------------------------------------------------
-constexpr int kPatchThreads = 128;
+constexpr int kPatchThreads = 128;     // batch patch kernels
+constexpr int kPatchMaxThreads = 256;  // single-mesh patch kernels: 64, 128 or 256 threads
+
+// L2 prefetch of [lo, hi) by the bulk-copy unit (cp.async.bulk.prefetch.L2),
+// trimmed to whole 16-byte chunks inside the range's allocation: the start
+// is rounded down (allocations are 256-byte aligned), the end rounded down.
+__device__ __forceinline__ void l2_prefetch(const void* lo, const void* hi)
+{
+    const unsigned long long a = (unsigned long long)lo & ~15ull;
+    const unsigned long long b = (unsigned long long)hi & ~15ull;
+    if (b > a) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(b - a)) : "memory");
+}
+
+// Issued by one thread: the element data (FP32 compressed form) and the
+// local tables of patch P into L2, so that the block's next patch starts on
+// L2 hits instead of DRAM latency.
+template <typename R>
+__device__ __forceinline__ void prefetch_patch(const PatchView& pv, const ElemView<R>& ev, int P)
+{
+    const int e0 = pv.elem_start[P], e1 = pv.elem_start[P + 1];
+    const int n0 = pv.node_start[P], n1 = pv.node_start[P + 1];
+    const size_t En = (size_t)ev.n_tets;
+    const float4* q = reinterpret_cast<const float4*>(ev.rot);
+    const float4* J = reinterpret_cast<const float4*>(ev.J);
+    l2_prefetch(q + e0, q + e1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) l2_prefetch(J + k * En + e0, J + k * En + e1);
+    l2_prefetch(pv.lconn + e0, pv.lconn + e1);
+    l2_prefetch(pv.lslots + 4 * (size_t)e0, pv.lslots + 4 * (size_t)e1);
+    l2_prefetch(pv.lnode_gid + n0, pv.lnode_gid + n1);
+    l2_prefetch(pv.lnode_info + n0, pv.lnode_info + n1);
+    l2_prefetch(pv.lrow + n0, pv.lrow + n1 + 1);
+}
 
 // One patch of the fused matvec, executed by the whole block (it contains
 // block barriers). Returns this thread's share of the patch's p^T A p.
@@ -1019,12 +1052,13 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
 }
 
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kPatchThreads) k_patch_matvec(PatchView pv, ElemView<R> ev,
-                                                                const R* __restrict__ rin, const R* __restrict__ pold,
-                                                                R* __restrict__ pnew, CgScalars* cg, R kf, MassArgs ma,
-                                                                double mf, const uint8_t* __restrict__ fixed,
-                                                                R* __restrict__ qout, R* __restrict__ partials,
-                                                                SolveConsts sc)
+__global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv, ElemView<R> ev,
+                                                                   const R* __restrict__ rin,
+                                                                   const R* __restrict__ pold, R* __restrict__ pnew,
+                                                                   CgScalars* cg, R kf, MassArgs ma, double mf,
+                                                                   const uint8_t* __restrict__ fixed,
+                                                                   R* __restrict__ qout, R* __restrict__ partials,
+                                                                   SolveConsts sc, int prefetch)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* ef = reinterpret_cast<R*>(smem_raw);  // [12][pe]
@@ -1033,9 +1067,335 @@ __global__ void __launch_bounds__(kPatchThreads) k_patch_matvec(PatchView pv, El
     const R beta = (MODE == 2) ? (R)cg->beta : R(0);
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
     double energy = 0.0;  // FP64 across patches; FP32 within one patch
-    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
+        if constexpr (is_mixed<R>::value)
+            if (prefetch && threadIdx.x == 0 && P + (int)gridDim.x < pv.n_patches)
+                prefetch_patch(pv, ev, P + gridDim.x);
         energy += (double)patch_body<R, MODE>(pv, ev, P, rin, pold, pnew, beta, kf, ma, mf, mmu, fixed, qout,
                                               partials, ef, lp);
+    }
+    if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
+}
+
+// ------------------------------------------------------------------------
+// FP32 fused matvec with TMA staging. Each patch's element data -- quaternion,
+// three J/K planes and the local connectivity, 72 bytes per element, laid out
+// contiguously per patch by the element order -- is brought into shared
+// memory by bulk copies (cp.async.bulk, completion counted on an mbarrier)
+// issued by one thread. Two stage buffers alternate: while a CTA gathers and
+// computes patch i, the copy engine fetches patch i+1, so the DRAM stream does
+// not stop at the block barriers between the phases. Every wait on an
+// mbarrier is bounded; a wait that runs out sets an error flag, waits (also
+// bounded) for the copies it issued and leaves the loop.
+// ------------------------------------------------------------------------
+constexpr int kStagedThreads = 256;
+constexpr long long kStageWaitTries = 1LL << 22;
+
+// Shared-memory stages: stage s holds, at base + s*stride, pe quaternions
+// (16 B each), three planes of pe float4 J/K values and pe local
+// connectivities (8 B each).
+struct StageSmem {
+    unsigned char* base;
+    unsigned stride;
+    int pe;
+    uint64_t* bar;  // 2 mbarriers
+    __device__ __forceinline__ float4* q(int s) const { return reinterpret_cast<float4*>(base + s * stride); }
+    __device__ __forceinline__ float4* jk(int s) const
+    {
+        return reinterpret_cast<float4*>(base + s * stride + 16u * (unsigned)pe);
+    }
+    __device__ __forceinline__ ushort4* lc(int s) const
+    {
+        return reinterpret_cast<ushort4*>(base + s * stride + 64u * (unsigned)pe);
+    }
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Bounded wait for the mbarrier phase with the given parity.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
+{
+    for (long long i = 0; i < kStageWaitTries; ++i) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Shared-memory bytes of a staged patch kernel: two mbarriers, two stages of
+// 72 bytes per element, the corner terms (48 bytes per element) and the
+// patch's nodal values (12 bytes per local node). Every region starts on a
+// 16-byte boundary (pe is even).
+inline size_t staged_smem_bytes(int pe, int max_lnodes)
+{
+    return 16 + 2 * 72 * (size_t)pe + 12 * sizeof(float) * (size_t)pe + 12 * (size_t)max_lnodes;
+}
+
+__device__ __forceinline__ StageSmem stage_layout(unsigned char* base, int pe, float** ef, float** lp, int max_lnodes)
+{
+    StageSmem st;
+    st.bar = reinterpret_cast<uint64_t*>(base);
+    st.base = base + 16;
+    st.stride = 72u * (unsigned)pe;
+    st.pe = pe;
+    *ef = reinterpret_cast<float*>(st.base + 2 * st.stride);
+    *lp = *ef + 12 * pe;
+    (void)max_lnodes;
+    return st;
+}
+
+// Issued by one thread: the element data of elements [e0, e0+ne) into stage
+// s. The global addresses are 16-byte aligned (patches start at even element
+// positions; the arrays are 256-byte aligned); the connectivity copy is
+// rounded up to 16 bytes, which the arrays' two padding entries cover.
+__device__ __forceinline__ void stage_issue(const StageSmem& st, int s, const ElemView<float>& ev,
+                                            const ushort4* lconn, int e0, int ne, int pe)
+{
+    const size_t En = (size_t)ev.n_tets;
+    const float4* q = reinterpret_cast<const float4*>(ev.rot) + e0;
+    const float4* J = reinterpret_cast<const float4*>(ev.J);
+    const unsigned qb = 16u * (unsigned)ne;
+    const unsigned lb = (8u * (unsigned)ne + 15u) & ~15u;
+    fence_async_shared();
+    mbar_expect_tx(&st.bar[s], 4 * qb + lb);
+    bulk_load(st.q(s), q, qb, &st.bar[s]);
+    for (int k = 0; k < 3; ++k) bulk_load(st.jk(s) + (size_t)k * pe, J + k * En + e0, qb, &st.bar[s]);
+    bulk_load(st.lc(s), lconn + e0, lb, &st.bar[s]);
+}
+
+// Phase 0 of a patch: nodal values (and the CG direction) into lp.
+template <int MODE>
+__device__ __forceinline__ void staged_phase0(const PatchView& pv, int P, const float* __restrict__ rin,
+                                              const float* __restrict__ pold, float* __restrict__ pnew, float beta,
+                                              float* lp)
+{
+    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int g = pv.lnode_gid[n0 + l];
+        float v[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float rv = rin[3 * (size_t)g + k];
+            v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
+            lp[3 * l + k] = v[k];
+        }
+        if (MODE != 0) {
+            const int info = pv.lnode_info[n0 + l];
+            if (info < 0 || (info & 1)) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
+            }
+        }
+    }
+}
+
+// Phase 1 from stage s: element corner terms into ef; returns -p^T K p share.
+template <int MODE>
+__device__ __forceinline__ float staged_phase1(const StageSmem& st, int s, int ne, int pe, float kf, const float* lp,
+                                               float* ef)
+{
+    float pen = 0.f;
+    const float4* jk = st.jk(s);
+    const float4* qs = st.q(s);
+    const ushort4* lcs = st.lc(s);
+    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+        const ushort4 c = lcs[le];
+        const int ln[4] = {c.x, c.y, c.z, c.w};
+        float xr[4][3];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
+#pragma unroll
+        for (int i = 3; i >= 0; --i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
+        float Rm[9], K[3], J[12];
+        quat_to_rot(qs[le], Rm);
+        const float4 a = jk[le], b = jk[pe + le], cc = jk[2 * pe + le];
+        J[3] = a.x;
+        J[4] = a.y;
+        J[5] = a.z;
+        J[6] = a.w;
+        J[7] = b.x;
+        J[8] = b.y;
+        J[9] = b.z;
+        J[10] = b.w;
+        J[11] = cc.x;
+        J[0] = -(J[3] + J[6] + J[9]);
+        J[1] = -(J[4] + J[7] + J[10]);
+        J[2] = -(J[5] + J[8] + J[11]);
+        K[0] = 1.f;
+        K[1] = cc.y;
+        K[2] = cc.z;
+        float X[12], F[12];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
+        element_force(F, X, K, J, kf);
+        float en = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
+                ef[(3 * i + k) * pe + le] = ck;
+                en += xr[i][k] * ck;
+            }
+        if (MODE != 0) pen -= en;
+    }
+    return pen;
+}
+
+// Phase 2: per local node, its slots in element order; interior nodes
+// finished, shared nodes leave partial sums. Returns the mass term of
+// p^T A p for the nodes this patch owns.
+template <int MODE>
+__device__ __forceinline__ float staged_phase2(const PatchView& pv, int P, int pe, const float* lp, const float* ef,
+                                               const MassArgs& ma, double mf, float mmu,
+                                               const uint8_t* __restrict__ fixed, float* __restrict__ qout,
+                                               float* __restrict__ partials)
+{
+    float pen = 0.f;
+    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int s0 = pv.lrow[n0 + l], s1 = pv.lrow[n0 + l + 1];
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int s = s0; s < s1; ++s) {
+            const int slot = pv.lslots[s];
+            const int le = slot >> 2, cc = slot & 3;
+            a0 += ef[(3 * cc + 0) * pe + le];
+            a1 += ef[(3 * cc + 1) * pe + le];
+            a2 += ef[(3 * cc + 2) * pe + le];
+        }
+        const int g = pv.lnode_gid[n0 + l];
+        const int info = pv.lnode_info[n0 + l];
+        if (info >= 0) {
+            float* o = partials + 3 * (size_t)(info >> 1);
+            o[0] = a0;
+            o[1] = a1;
+            o[2] = a2;
+        }
+        if (MODE == 0) {
+            if (info < 0) {
+                qout[3 * (size_t)g] -= a0;
+                qout[3 * (size_t)g + 1] -= a1;
+                qout[3 * (size_t)g + 2] -= a2;
+            }
+        } else if (info < 0 || (info & 1)) {
+            const float p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
+            const float mm = ma.node_mass ? (float)(ma.node_mass[g] * mf) : mmu;
+            pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
+            if (info < 0) {
+                float q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
+                if (fixed[g]) q0 = q1 = q2 = 0.f;
+                qout[3 * (size_t)g] = q0;
+                qout[3 * (size_t)g + 1] = q1;
+                qout[3 * (size_t)g + 2] = q2;
+            }
+        }
+    }
+    return pen;
+}
+
+// Single-mesh staged matvec (FP32). `err` (device int) is set to 1 when a
+// stage wait runs out; the CG modes also stop the solve with status bit 2.
+template <int MODE>
+__global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
+    PatchView pv, ElemView<float> ev, const float* __restrict__ rin, const float* __restrict__ pold,
+    float* __restrict__ pnew, CgScalars* cg, float kf, MassArgs ma, double mf, const uint8_t* __restrict__ fixed,
+    float* __restrict__ qout, float* __restrict__ partials, SolveConsts sc, int* err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *ef, *lp;
+    const int pe = pv.pe;
+    const StageSmem st = stage_layout(smem_raw, pe, &ef, &lp, pv.max_lnodes);
+    if (MODE != 0 && cg->done) return;
+    const float beta = (MODE == 2) ? (float)cg->beta : 0.f;
+    const float mmu = (float)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    if (threadIdx.x == 0) {
+        mbar_init(&st.bar[0], 1);
+        mbar_init(&st.bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int G = gridDim.x, NP = pv.n_patches;
+    int P = blockIdx.x;
+    if (threadIdx.x == 0 && P < NP)
+        stage_issue(st, 0, ev, pv.lconn, pv.elem_start[P], pv.elem_start[P + 1] - pv.elem_start[P], pe);
+    double energy = 0.0;
+    bool failed = false;
+    int issued_next = 0;
+    for (int i = 0; P < NP; P += G, ++i) {
+        const int s = i & 1;
+        const int Pn = P + G;
+        issued_next = 0;
+        if (Pn < NP) {
+            issued_next = 1;
+            if (threadIdx.x == 0)
+                stage_issue(st, s ^ 1, ev, pv.lconn, pv.elem_start[Pn], pv.elem_start[Pn + 1] - pv.elem_start[Pn],
+                            pe);
+        }
+        staged_phase0<MODE>(pv, P, rin, pold, pnew, beta, lp);
+        const bool ok = mbar_wait(&st.bar[s], (unsigned)((i >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        const int ne = pv.elem_start[P + 1] - pv.elem_start[P];
+        float pen = staged_phase1<MODE>(st, s, ne, pe, kf, lp, ef);
+        __syncthreads();
+        pen += staged_phase2<MODE>(pv, P, pe, lp, ef, ma, mf, mmu, fixed, qout, partials);
+        energy += (double)pen;
+        __syncthreads();
+    }
+    if (failed) {
+        if (threadIdx.x == 0) {
+            *err = 1;
+            if (MODE != 0) {
+                cg->status |= 2;
+                cg->done = 1;
+            }
+        }
+        // the copies this block issued must land before it exits
+        const int i = (P - (int)blockIdx.x) / G;
+        mbar_wait(&st.bar[i & 1], (unsigned)((i >> 1) & 1));
+        if (issued_next) mbar_wait(&st.bar[(i + 1) & 1], (unsigned)(((i + 1) >> 1) & 1));
+        return;
+    }
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
 
@@ -1060,53 +1420,156 @@ __global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restric
     }
 }
 
-// CG update after a patch matvec: completes q on shared nodes (mass term
-// minus the patches' partial sums, projected), then x += alpha p,
-// r += -alpha q and rho = r.r.
+// CG update of one node after a patch matvec: completes q on a shared node
+// (mass term minus the patches' partial sums, projected), then x += alpha p,
+// r += -alpha q. Returns the node's r.r (three-term sum in R).
+template <typename R>
+__device__ __forceinline__ R cg_update1(size_t n, R* __restrict__ xs, R* __restrict__ r, const R* __restrict__ p,
+                                        const R* __restrict__ q, const R* __restrict__ partials,
+                                        const int* __restrict__ bnd_rowptr, const double* __restrict__ node_mass,
+                                        R mmu, double mf, const uint8_t* __restrict__ fixed, R alpha)
+{
+    const size_t i3 = 3 * n;
+    const R pp[3] = {p[i3], p[i3 + 1], p[i3 + 2]};
+    R qq[3];
+    const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
+    if (b0 == b1) {
+        qq[0] = q[i3];
+        qq[1] = q[i3 + 1];
+        qq[2] = q[i3 + 2];
+    } else {
+        R a0 = R(0), a1 = R(0), a2 = R(0);
+        for (int b = b0; b < b1; ++b) {
+            a0 += partials[3 * (size_t)b];
+            a1 += partials[3 * (size_t)b + 1];
+            a2 += partials[3 * (size_t)b + 2];
+        }
+        const R mm = node_mass ? (R)(node_mass[n] * mf) : mmu;
+        qq[0] = mm * pp[0] - a0;
+        qq[1] = mm * pp[1] - a1;
+        qq[2] = mm * pp[2] - a2;
+        if (fixed[n]) qq[0] = qq[1] = qq[2] = R(0);
+    }
+    const R nalpha = -alpha;
+    R rr[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        xs[i3 + k] = xs[i3 + k] + pp[k] * alpha;
+        rr[k] = r[i3 + k] + qq[k] * nalpha;
+        r[i3 + k] = rr[k];
+    }
+    return rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
+}
+
+__device__ __forceinline__ void ld12(const float* __restrict__ a, size_t n0, float v[12])
+{
+    const float4* s = reinterpret_cast<const float4*>(a + 3 * n0);
+    const float4 x = s[0], y = s[1], z = s[2];
+    v[0] = x.x, v[1] = x.y, v[2] = x.z, v[3] = x.w;
+    v[4] = y.x, v[5] = y.y, v[6] = y.z, v[7] = y.w;
+    v[8] = z.x, v[9] = z.y, v[10] = z.z, v[11] = z.w;
+}
+
+__device__ __forceinline__ void st12(float* __restrict__ a, size_t n0, const float v[12])
+{
+    float4* d = reinterpret_cast<float4*>(a + 3 * n0);
+    d[0] = make_float4(v[0], v[1], v[2], v[3]);
+    d[1] = make_float4(v[4], v[5], v[6], v[7]);
+    d[2] = make_float4(v[8], v[9], v[10], v[11]);
+}
+
+// The same update for four consecutive nodes n0..n0+3 (n0 a multiple of 4)
+// with 16-byte loads, every load of the group issued before the first use.
+// Returns the group's r.r: per node the three-term FP32 sum, summed in FP64
+// in node order.
+__device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, float* __restrict__ r,
+                                             const float* __restrict__ p, const float* __restrict__ q,
+                                             const float* __restrict__ partials, const int* __restrict__ bnd_rowptr,
+                                             const double* __restrict__ node_mass, float mmu, double mf,
+                                             const uint8_t* __restrict__ fixed, float alpha)
+{
+    float pp[12], qq[12], xx[12], rr[12];
+    ld12(p, n0, pp);
+    ld12(q, n0, qq);
+    ld12(xs, n0, xx);
+    ld12(r, n0, rr);
+    const int4 br = *reinterpret_cast<const int4*>(bnd_rowptr + n0);
+    const int bb[5] = {br.x, br.y, br.z, br.w, bnd_rowptr[n0 + 4]};
+    const uchar4 fx = *reinterpret_cast<const uchar4*>(fixed + n0);
+    const uint8_t ff[4] = {fx.x, fx.y, fx.z, fx.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (bb[j + 1] > bb[j]) {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+            for (int b = bb[j]; b < bb[j + 1]; ++b) {
+                a0 += partials[3 * (size_t)b];
+                a1 += partials[3 * (size_t)b + 1];
+                a2 += partials[3 * (size_t)b + 2];
+            }
+            const float mm = node_mass ? (float)(node_mass[n0 + j] * mf) : mmu;
+            qq[3 * j] = mm * pp[3 * j] - a0;
+            qq[3 * j + 1] = mm * pp[3 * j + 1] - a1;
+            qq[3 * j + 2] = mm * pp[3 * j + 2] - a2;
+            if (ff[j]) qq[3 * j] = qq[3 * j + 1] = qq[3 * j + 2] = 0.f;
+        }
+    }
+    const float nalpha = -alpha;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+        xx[k] = xx[k] + pp[k] * alpha;
+        rr[k] = rr[k] + qq[k] * nalpha;
+    }
+    st12(xs, n0, xx);
+    st12(r, n0, rr);
+    double local = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        local += (double)(rr[3 * j] * rr[3 * j] + rr[3 * j + 1] * rr[3 * j + 1] + rr[3 * j + 2] * rr[3 * j + 2]);
+    return local;
+}
+
+template <typename R>
+__device__ __forceinline__ double cg_update4g(size_t n0, R* xs, R* r, const R* p, const R* q, const R* partials,
+                                              const int* bnd_rowptr, const double* node_mass, R mmu, double mf,
+                                              const uint8_t* fixed, R alpha)
+{
+    if constexpr (is_mixed<R>::value) {
+        return cg_update4(n0, xs, r, p, q, partials, bnd_rowptr, node_mass, mmu, mf, fixed, alpha);
+    } else {
+        double local = 0.0;
+        for (int j = 0; j < 4; ++j)
+            local += (double)cg_update1<R>(n0 + j, xs, r, p, q, partials, bnd_rowptr, node_mass, mmu, mf, fixed, alpha);
+        return local;
+    }
+}
+
+// CG update after a patch matvec over all nodes, then rho = r.r. FP32: one
+// thread per group of four nodes (16-byte loads), the N % 4 last nodes one
+// per thread.
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_cg_update_patch(R* __restrict__ xs, R* __restrict__ r,
                                                                 const R* __restrict__ p, const R* __restrict__ q,
                                                                 const R* __restrict__ partials,
                                                                 const int* __restrict__ bnd_rowptr, MassArgs ma,
                                                                 double mf, const uint8_t* __restrict__ fixed,
-                                                                CgScalars* cg, int N, SolveConsts sc)
+                                                                CgScalars* cg, int N, SolveConsts sc, int vec4)
 {
     if (cg->done) return;
     const R alpha = (R)cg->alpha;
-    const R nalpha = -alpha;
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
     double local = 0.0;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-        const size_t i3 = 3 * (size_t)n;
-        const R pp[3] = {p[i3], p[i3 + 1], p[i3 + 2]};
-        R qq[3];
-        const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
-        if (b0 == b1) {
-            qq[0] = q[i3];
-            qq[1] = q[i3 + 1];
-            qq[2] = q[i3 + 2];
-        } else {
-            R a0 = R(0), a1 = R(0), a2 = R(0);
-            for (int b = b0; b < b1; ++b) {
-                a0 += partials[3 * (size_t)b];
-                a1 += partials[3 * (size_t)b + 1];
-                a2 += partials[3 * (size_t)b + 2];
-            }
-            const R mm = ma.node_mass ? (R)(ma.node_mass[n] * mf) : mmu;
-            qq[0] = mm * pp[0] - a0;
-            qq[1] = mm * pp[1] - a1;
-            qq[2] = mm * pp[2] - a2;
-            if (fixed[n]) qq[0] = qq[1] = qq[2] = R(0);
-        }
-        R rr[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            xs[i3 + k] = xs[i3 + k] + pp[k] * alpha;
-            rr[k] = r[i3 + k] + qq[k] * nalpha;
-            r[i3 + k] = rr[k];
-        }
-        // the node's three-term sum in R, the running sum over nodes in FP64
-        local += (double)(rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2]);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    if (is_mixed<R>::value && vec4) {
+        const int G4 = N >> 2;
+        for (int g = tid; g < G4; g += stride)
+            local += cg_update4g(4 * (size_t)g, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf, fixed, alpha);
+        for (int n = 4 * G4 + tid; n < N; n += stride)
+            local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf, fixed,
+                                           alpha);
+    } else {
+        for (int n = tid; n < N; n += stride)
+            local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf, fixed,
+                                           alpha);
     }
     finish_dot<FIN_RHO>(local, cg, nullptr, N, sc);
 }
@@ -1204,19 +1667,60 @@ int prepare_patch(TfemMesh* m)
     int dev = 0, sms = 0, nb0 = 0, nb1 = 0, nb2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // launch-shape knobs: threads per CTA (64/128/256), L2 prefetch of the
+    // next patch, vectorised FP32 update
+    int threads = 128;
+    if (const char* e = getenv("SGB_PATCH_THREADS")) {
+        const int t = atoi(e);
+        if (t == 64 || t == 128 || t == 256) threads = t;
+    }
+    m->patch_threads = threads;
+    if (const char* e = getenv("SGB_PATCH_PREFETCH")) m->patch_prefetch = (e[0] == '1');
+    if (const char* e = getenv("SGB_UPDATE_VEC4")) m->update_vec4 = (e[0] != '0');
     cudaFuncSetAttribute(k_patch_matvec<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_patch_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_patch_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, k_patch_matvec<R, 0>, kPatchThreads, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, kPatchThreads, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, kPatchThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, k_patch_matvec<R, 0>, threads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, threads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, threads, smem);
     int nb = nb0 < nb1 ? nb0 : nb1;
     nb = nb < nb2 ? nb : nb2;
     if (nb < 1) nb = 1;
     long long g = (long long)nb * sms;
-    if (g > kMaxNodeBlocks) g = kMaxNodeBlocks;
+    if (g > kMaxDotBlocks) g = kMaxDotBlocks;
     if (g > m->pl.n_patches) g = m->pl.n_patches;
     if (g < 1) g = 1;
+    m->staged = false;
+    if constexpr (is_mixed<R>::value) {
+        // FP32: the bulk-copy staged kernels when their shared memory fits
+        // (even pe: every patch but the last starts on a 16-byte element
+        // boundary; the device error flag exists)
+        const char* env = getenv("SGB_PATCH_STAGING");
+        if (env && env[0] == '1' && (m->pl.pe % 2) == 0 && m->dev_flags) {
+            const size_t ss = staged_smem_bytes(m->pl.pe, m->pl.max_lnodes);
+            int s0 = 0, s1 = 0, s2 = 0;
+            if (cudaFuncSetAttribute(k_patch_matvec_staged<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
+                    cudaSuccess &&
+                cudaFuncSetAttribute(k_patch_matvec_staged<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
+                    cudaSuccess &&
+                cudaFuncSetAttribute(k_patch_matvec_staged<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
+                    cudaSuccess) {
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s0, k_patch_matvec_staged<0>, kStagedThreads, ss);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s1, k_patch_matvec_staged<1>, kStagedThreads, ss);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s2, k_patch_matvec_staged<2>, kStagedThreads, ss);
+                int sb = s0 < s1 ? s0 : s1;
+                sb = sb < s2 ? sb : s2;
+                if (sb >= 1) {
+                    long long sg = (long long)sb * sms;
+                    if (sg > kMaxDotBlocks) sg = kMaxDotBlocks;
+                    if (sg > m->pl.n_patches) sg = m->pl.n_patches;
+                    m->staged = true;
+                    m->staged_grid = (int)sg;
+                }
+            }
+            cudaGetLastError();
+        }
+    }
     return (int)g;
 }
 
@@ -1238,8 +1742,20 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
         PatchView pv = patch_view(m);
         MassArgs ma{nullptr, 0.0, {0.0, 0.0, 0.0}};
         SolveConsts sc{0.0, 0.0, 0};
-        k_patch_matvec<R, 0><<<m->patch_grid, kPatchThreads, patch_smem_bytes<R>(m), s>>>(
-            pv, view<R>(m), dx, nullptr, nullptr, nullptr, kfactor, ma, 1.0, nullptr, df, (R*)m->pl.partials, sc);
+        bool done = false;
+        if constexpr (is_mixed<R>::value) {
+            if (m->staged) {
+                k_patch_matvec_staged<0>
+                    <<<m->staged_grid, kStagedThreads, staged_smem_bytes(m->pl.pe, m->pl.max_lnodes), s>>>(
+                        pv, view<R>(m), dx, nullptr, nullptr, nullptr, kfactor, ma, 1.0, nullptr, df,
+                        (R*)m->pl.partials, sc, m->dev_flags);
+                done = true;
+            }
+        }
+        if (!done)
+            k_patch_matvec<R, 0><<<m->patch_grid, m->patch_threads, patch_smem_bytes<R>(m), s>>>(
+                pv, view<R>(m), dx, nullptr, nullptr, nullptr, kfactor, ma, 1.0, nullptr, df, (R*)m->pl.partials, sc,
+                m->patch_prefetch);
         k_patch_fixup<R><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(m->pl.bnd_rowptr, (const R*)m->pl.partials, df,
                                                                       m->n_nodes);
         return;
@@ -1331,18 +1847,34 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     PatchView pv = patch_view(m);
     ElemView<R> ev = view<R>(m);
     const size_t smem = patch_smem_bytes<R>(m);
+    const int ng_update = is_mixed<R>::value ? node_grid((N + 3) / 4) : ng;
     for (int it = 1; it <= P.cg_iterations; ++it) {
         cons.it = it;
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
-        if (it == 1)
-            k_patch_matvec<R, 1><<<m->patch_grid, kPatchThreads, smem, s>>>(pv, ev, r, pold, pnew, sc->cg, (R)kf, ma,
-                                                                             mf, sc->fixed, q, partials, cons);
+        bool done = false;
+        if constexpr (is_mixed<R>::value) {
+            if (m->staged) {
+                const size_t ss = staged_smem_bytes(m->pl.pe, m->pl.max_lnodes);
+                if (it == 1)
+                    k_patch_matvec_staged<1><<<m->staged_grid, kStagedThreads, ss, s>>>(
+                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->dev_flags);
+                else
+                    k_patch_matvec_staged<2><<<m->staged_grid, kStagedThreads, ss, s>>>(
+                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->dev_flags);
+                done = true;
+            }
+        }
+        if (done)
+            ;
+        else if (it == 1)
+            k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
+                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
         else
-            k_patch_matvec<R, 2><<<m->patch_grid, kPatchThreads, smem, s>>>(pv, ev, r, pold, pnew, sc->cg, (R)kf, ma,
-                                                                             mf, sc->fixed, q, partials, cons);
-        k_cg_update_patch<R><<<ng, kNodeBlock, 0, s>>>(xs, r, pnew, q, partials, m->pl.bnd_rowptr, ma, mf, sc->fixed,
-                                                       sc->cg, N, cons);
+            k_patch_matvec<R, 2><<<m->patch_grid, m->patch_threads, smem, s>>>(
+                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+        k_cg_update_patch<R><<<m->update_vec4 ? ng_update : ng, kNodeBlock, 0, s>>>(
+            xs, r, pnew, q, partials, m->pl.bnd_rowptr, ma, mf, sc->fixed, sc->cg, N, cons, m->update_vec4);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);

@@ -1,0 +1,62 @@
+"""Scene files on the GPU: the known-answer grid scene run through the
+component layer reproduces the reference's checkFEMValues position and the
+oracle's trajectory; a mixed-precision scene file runs and stays within the
+position tolerance of its FP64 run."""
+import os
+
+import numpy as np
+import pytest
+
+from sofa_gb300 import topology as topo
+
+pytestmark = pytest.mark.gpu
+
+SCENES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "scenes")
+
+
+def _read(name):
+    with open(os.path.join(SCENES, name)) as f:
+        return f.read()
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from sofa_gb300 import build, capi
+
+    build.build()
+    return capi
+
+
+def test_grid_scene_file_known_answer(capi, oracle):
+    """checkFEMValues (BaseTetrahedronFEMForceField_test.h:379-431) through
+    the scene file: x[159] after 100 steps, and the whole trajectory against
+    the oracle run of the same scene."""
+    s = capi.SofaScene(_read("grid_fem_4x10x4.scn"))
+    s.animate(100)
+    x = s.positions(0)
+    assert s.time == pytest.approx(1.0)
+    np.testing.assert_allclose(x[159], [9.99985, 45.0487, 30.0011], atol=1e-4)
+
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+    osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01, cg_iterations=20,
+                             cg_tolerance=1e-5, cg_threshold=1e-6)
+    osc.step(100)
+    xo, _ = osc.state()
+    # parallel (non-serial) dot products: not bit-identical, within 1e-10 of the positions
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+
+
+def test_mixed_scene_file_against_its_fp64_run(capi):
+    mixed = capi.SofaScene(_read("beam_polar_gpu.scn"))
+    fp64 = capi.SofaScene(_read("beam_polar_gpu.scn"), precision=2)
+    assert mixed.body_info(0)["precision"] == 1
+    mixed.animate(50)
+    fp64.animate(50)
+    xm, xd = mixed.positions(0), fp64.positions(0)
+    assert np.all(np.isfinite(xm))
+    rest = topo.regular_grid((12, 4, 4), (0, 0, 0), (6, 1.5, 1.5))[0]
+    assert np.linalg.norm(xd - rest) > 1e-3  # it moved
+    assert np.linalg.norm(xm - xd) / np.linalg.norm(xd) <= 1e-4

@@ -1,0 +1,163 @@
+"""Component layer on the CPU: SOFA scene files parsed into the component
+graph, their host initialisation (topology, masses, fixed sets, solver Data)
+checked against the oracle-side helpers, the plugin entry points and the
+factory, and the errors the reference's factory and components raise.
+Nothing here touches a GPU."""
+import os
+
+import numpy as np
+import pytest
+
+from sofa_gb300 import topology as topo
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SCENES = os.path.join(HERE, "scenes")
+REF_BENCH = "/root/reference/applications/plugins/SofaCUDA/scenes/benchmarks"
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from sofa_gb300 import build, capi
+
+    build.build()
+    return capi
+
+
+def _read(name):
+    with open(os.path.join(SCENES, name)) as f:
+        return f.read()
+
+
+def test_plugin_entry_points_and_factory(capi):
+    lib = capi.load()
+    lib.initExternalModule()
+    assert lib.moduleIsInitialized()
+    assert lib.getModuleName() == b"SofaGB300"
+    comps = lib.getModuleComponentList().decode().split()
+    for c in ("TetrahedronFEMForceField", "EulerImplicitSolver", "CGLinearSolver", "UniformMass", "DiagonalMass",
+              "FixedProjectiveConstraint", "MechanicalObject", "RegularGridTopology",
+              "Hexa2TetraTopologicalMapping", "BoxROI", "TetrahedronSetTopologyContainer"):
+        assert c in comps
+    f = lib.sgb_object_factory_new()
+    try:
+        assert lib.sgb_object_factory_count(f) == 0
+        lib.registerObjects(f)
+        assert lib.sgb_object_factory_count(f) == len(comps)
+        assert lib.sgb_object_factory_has(f, b"TetrahedronFEMForceField") == 1
+        assert lib.sgb_object_factory_has(f, b"HexahedronFEMForceField") == 0
+    finally:
+        lib.sgb_object_factory_delete(f)
+
+
+def test_grid_scene_host_init_matches_oracle_inputs(capi):
+    """The known-answer grid scene: topology, lumped masses and the fixed
+    set as the oracle test builds them."""
+    s = capi.SofaScene(_read("grid_fem_4x10x4.scn"))
+    assert s.n_bodies == 1
+    info = s.body_info(0)
+    assert info == {"n_nodes": 160, "n_tets": 486, "method": 1, "precision": 0, "n_fixed": info["n_fixed"]}
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets_ref = topo.hexa_to_tetra6(hexa, (3, 9))
+    tets, masses, fixed = s.body_arrays(0)
+    np.testing.assert_array_equal(tets, tets_ref)
+    np.testing.assert_array_equal(s.positions(0), pos)
+    vol = np.abs(topo.signed_volumes(tets_ref, pos))
+    m_ref = np.zeros(len(pos))
+    for t, v in zip(tets_ref, vol):
+        m_ref[t] += v / 4.0
+    np.testing.assert_allclose(masses, m_ref, rtol=1e-13)
+    np.testing.assert_array_equal(fixed, topo.box_roi(pos, (-1, -1, 0, 10, 1, 50)))
+    d = s.describe()
+    b = d["bodies"][0]
+    assert d["gravity"] == [0, 10, 0] and d["dt"] == 0.01
+    assert (b["cg_iterations"], b["cg_tolerance"], b["cg_threshold"]) == (20, 1e-5, 1e-6)
+    assert (b["rayleigh_stiffness"], b["rayleigh_mass"], b["mass_first"]) == (0.0, 0.0, 1)
+    assert any("BlockGaussSeidelConstraintSolver" in x for x in d["ignored"])
+
+
+def test_benchmark_style_scene(capi):
+    s = capi.SofaScene(_read("beam_polar_gpu.scn"))
+    assert s.n_bodies == 1
+    info = s.body_info(0)
+    assert info["n_nodes"] == 12 * 4 * 4 and info["n_tets"] == 11 * 3 * 3 * 6
+    assert info["method"] == 2 and info["precision"] == 1  # polar, CudaVec3f -> mixed
+    pos, _ = topo.regular_grid((12, 4, 4), (0, 0, 0), (6, 1.5, 1.5))
+    tets, masses, fixed = s.body_arrays(0)
+    np.testing.assert_array_equal(fixed, topo.box_roi(pos, (-0.1, -0.1, -0.1, 0.1, 2, 2)))
+    np.testing.assert_allclose(masses, 3.0 / len(pos), rtol=0, atol=0)
+    d = s.describe()
+    ign = " ".join(d["ignored"])
+    for c in ("RequiredPlugin", "VisualStyle", "CollisionPipeline", "OglModel", "IdentityMapping",
+              "Tetra2TriangleTopologicalMapping", "TriangleSetTopologyContainer"):
+        assert c in ign
+    b = d["bodies"][0]
+    assert (b["rayleigh_stiffness"], b["rayleigh_mass"], b["cg_iterations"]) == (0.1, 0.1, 25)
+    assert d["gravity"] == [0, -9, 0]
+    # a precision override
+    s64 = capi.SofaScene(_read("beam_polar_gpu.scn"), precision=2)
+    assert s64.body_info(0)["precision"] == 2
+
+
+def test_reference_scene_with_an_out_of_scope_force_field(capi):
+    """The 16x16x76 benchmark adds a PlaneForceField (penalty contact with a
+    plane), which is not part of this component set: the load fails with
+    SGB_ERR_NOT_SUPPORTED naming it, as the reference's factory does for a
+    class it does not know."""
+    path = os.path.join(REF_BENCH, "TetrahedronFEMForceField_beam16x16x76_gpu.scn")
+    if not os.path.exists(path):
+        pytest.skip("reference tree not present")
+    with open(path) as f, pytest.raises(capi.SgbError) as e:
+        capi.SofaScene(f.read())
+    assert e.value.code == -4 and "PlaneForceField" in str(e.value)
+
+
+@pytest.mark.parametrize("name,precision", [("TetrahedronFEMForceField_beam10x10x40_gpu.scn", 1),
+                                            ("TetrahedronFEMForceField_beam10x10x40_cpu.scn", 0)])
+def test_reference_benchmark_scene_files(capi, name, precision):
+    """The reference's own SofaCUDA benchmark scenes, read where the reference
+    tree is present, load unchanged."""
+    path = os.path.join(REF_BENCH, name)
+    if not os.path.exists(path):
+        pytest.skip("reference tree not present")
+    with open(path) as f:
+        s = capi.SofaScene(f.read())
+    assert s.n_bodies == 1
+    info = s.body_info(0)
+    d = s.describe()
+    grid = [o for n in d["root"]["children"] for o in n["objects"] if o["class"] == "RegularGridTopology"][0]
+    nx, ny, nz = (int(v) for v in grid["data"]["n"].split())
+    assert info["n_nodes"] == nx * ny * nz
+    assert info["n_tets"] == (nx - 1) * (ny - 1) * (nz - 1) * 6
+    assert info["precision"] == precision and info["method"] == 1
+    tets, masses, fixed = s.body_arrays(0)
+    assert info["n_fixed"] == ny * nz  # the x = 0 face
+    assert masses.sum() == pytest.approx(50.0, rel=1e-12)  # DiagonalMass totalMass="50.0"
+
+
+BAD = {
+    "unknown component": ("<Node name='r'><HexahedronFEMForceField/></Node>", -4),
+    "unterminated": ("<Node name='r'><EulerImplicitSolver></Node>", -1),
+    "not a node root": ("<EulerImplicitSolver/>", -1),
+}
+
+
+@pytest.mark.parametrize("case", sorted(BAD))
+def test_scene_errors(capi, case):
+    xml, rc = BAD[case]
+    with pytest.raises(capi.SgbError) as e:
+        capi.SofaScene(xml)
+    assert e.value.code == rc
+
+
+@pytest.mark.parametrize("edit,msg", [
+    (('method="large"', 'method="svd"'), "svd"),
+    (('<DiagonalMass name="mass" massDensity="1.0" />', ''), "mass"),
+    (('<EulerImplicitSolver />', '<EulerImplicitSolver firstOrder="1" />'), "firstOrder"),
+    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField plasticMaxThreshold="0.1" name="FEM"'),
+     "plastic"),
+])
+def test_unsupported_component_settings(capi, edit, msg):
+    xml = _read("grid_fem_4x10x4.scn").replace(*edit)
+    with pytest.raises(capi.SgbError) as e:
+        capi.SofaScene(xml)
+    assert e.value.code == -4 and msg in str(e.value)
