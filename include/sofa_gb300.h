@@ -189,6 +189,12 @@ typedef struct sgb_scene_params {
      * MechanicalObject::vDot does (bit-identical to the reference with
      * SGB_PRECISION_FP64; slow on large meshes) */
     int serial_dots;
+    /* SGB_PRECISION_MIXED scenes: every residual_replacement CG iterations the
+     * FP32 solution increment is accumulated in FP64 and the residual is
+     * recomputed as b - A x in FP64 with an FP64 copy of the operator
+     * (reliable-update CG: the FP32 recurrence cannot drift from the true
+     * residual). 0: off. The FP64 copy doubles the force field's memory. */
+    int residual_replacement;
 } sgb_scene_params;
 
 /* Fills params with the reference Data defaults: dt 0.01, Rayleigh 0, CG

@@ -52,6 +52,7 @@ class SceneParams(ctypes.Structure):
         ("fix_all", ctypes.c_int),
         ("mass_first", ctypes.c_int),
         ("serial_dots", ctypes.c_int),
+        ("residual_replacement", ctypes.c_int),
     ]
 
 

@@ -138,7 +138,7 @@ static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool no
     c.add((int**)&d.lnode_gid, sizeof(int) * L.lnode_gid.size());
     c.add((int**)&d.lnode_info, sizeof(int) * L.lnode_info.size());
     c.add((int**)&d.lrow, sizeof(int) * L.lrow.size());
-    c.add((uint16_t**)&d.lslots, sizeof(uint16_t) * L.lslots.size());
+    c.add((uint16_t**)&d.lslots, sizeof(uint16_t) * (L.lslots.size() + 8));
     c.add((ushort4**)&d.lconn, sizeof(ushort4) * (L.lconn.size() + 2));
     c.add((int**)&d.bnd_rowptr, sizeof(int) * (N + 1));
     c.add(&d.partials, rs * 3 * (size_t)std::max(L.n_partials, 1));
@@ -218,7 +218,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
     B->ops = ops;
     B->precision = precision;
     B->rs = ops->real_size;
-    B->pe = B->rs == 4 ? 512 : 256;
+    B->pe = 256;
     B->max_slots = max_meshes;
     B->max_iterations = max_cg_iterations;
     B->slots.resize((size_t)max_meshes);

@@ -225,8 +225,11 @@ __global__ void __launch_bounds__(kPatchThreads, 7) kb_matvec(BMeshDesc* M, cons
                                                            const int* __restrict__ counts, int it, int pe)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* ef = reinterpret_cast<R*>(smem_raw);  // [12][pe]
-    R* lp = ef + 12 * pe;                    // [kBatchMaxLocalNodes][3]
+    R* ef;
+    R* lp;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve<R>(smem_raw, pe, kBatchMaxLocalNodes, &ef, &sl, &lr, &lp);
     const int L = counts[WL_PATCH];
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem wi = items[w];
@@ -250,7 +253,7 @@ __global__ void __launch_bounds__(kPatchThreads, 7) kb_matvec(BMeshDesc* M, cons
         const R mmu = (R)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
         MassArgs ma{m.node_mass, m.vertex_mass, {m.g[0], m.g[1], m.g[2]}};
         const R pen = patch_body<R, MODE>(pv, ev, wi.a, (const R*)m.r, pold, pnew, beta, (R)m.kf, ma, mf, mmu,
-                                          m.fixed, (R*)m.q, (R*)m.partials, ef, lp);
+                                          m.fixed, (R*)m.q, (R*)m.partials, ef, lp, sl, lr);
         double total;
         if (bm_ticket_sum((double)pen, m.patch_energy, wi.a, &m.ticket_den, m.n_patches, &total) &&
             threadIdx.x == 0) {
@@ -269,116 +272,6 @@ __global__ void __launch_bounds__(kPatchThreads, 7) kb_matvec(BMeshDesc* M, cons
             }
         }
         __syncthreads();
-    }
-}
-
-// ---- FP32 CG matvec with TMA-staged element data ---------------------------
-// The staged form of kb_matvec (see k_patch_matvec_staged): one thread copies
-// the next live work item's element data into the other stage while the
-// block computes the current one. Items of meshes that skip this iteration
-// are never fetched: whether a mesh skips is fixed for the whole launch
-// before any of its items runs (its den ticket closes after its last item).
-__device__ __forceinline__ int kb_next_live(const BMeshDesc* M, const WorkItem* __restrict__ items, int w, int L,
-                                            int G, int it)
-{
-    for (; w < L; w += G)
-        if (!bm_cg_skip(M[items[w].slot], it)) break;
-    return w;
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(kStagedThreads) kb_matvec_staged(BMeshDesc* M, const WorkItem* __restrict__ items,
-                                                                   const int* __restrict__ counts, int it, int pe,
-                                                                   int* err)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int next_w;
-    float *ef, *lp;
-    const StageSmem st = stage_layout(smem_raw, pe, &ef, &lp, kBatchMaxLocalNodes);
-    const int L = counts[WL_PATCH];
-    const int G = gridDim.x;
-    if (threadIdx.x == 0) {
-        mbar_init(&st.bar[0], 1);
-        mbar_init(&st.bar[1], 1);
-        mbar_fence_init();
-        const int w0 = kb_next_live(M, items, blockIdx.x, L, G, it);
-        next_w = w0;
-        if (w0 < L) {
-            const WorkItem wi = items[w0];
-            const BMeshDesc& m = M[wi.slot];
-            stage_issue(st, 0, bm_elem_view<float>(m), m.lconn, m.elem_start[wi.a],
-                        m.elem_start[wi.a + 1] - m.elem_start[wi.a], pe);
-        }
-    }
-    __syncthreads();
-    int w = next_w;
-    int i = 0;
-    bool failed = false, issued_next = false;
-    for (; w < L; ++i) {
-        const int s = i & 1;
-        const WorkItem wi = items[w];
-        BMeshDesc& m = M[wi.slot];
-        if (threadIdx.x == 0) {
-            const int wn = kb_next_live(M, items, w + G, L, G, it);
-            next_w = wn;
-            if (wn < L) {
-                const WorkItem ni = items[wn];
-                const BMeshDesc& nm = M[ni.slot];
-                stage_issue(st, s ^ 1, bm_elem_view<float>(nm), nm.lconn, nm.elem_start[ni.a],
-                            nm.elem_start[ni.a + 1] - nm.elem_start[ni.a], pe);
-            }
-        }
-        const PatchView pv = bm_patch_view(m, pe);
-        const float beta = (MODE == 2) ? (float)m.beta : 0.f;
-        const float* pold = (const float*)((it & 1) ? m.p1 : m.p0);
-        float* pnew = (float*)((it & 1) ? m.p0 : m.p1);
-        const double mf = m.mf;
-        const float mmu = (float)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
-        MassArgs ma{m.node_mass, m.vertex_mass, {m.g[0], m.g[1], m.g[2]}};
-        staged_phase0<MODE>(pv, wi.a, (const float*)m.r, pold, pnew, beta, lp);
-        const bool ok = mbar_wait(&st.bar[s], (unsigned)((i >> 1) & 1));
-        const int fail_any = __syncthreads_or(!ok);
-        // written by thread 0 before the barrier above; rewritten only after
-        // the barrier that ends this iteration
-        const int wn = next_w;
-        issued_next = wn < L;
-        if (fail_any) {
-            failed = true;
-            if (threadIdx.x == 0) {
-                m.status |= 2;
-                m.done = 1;
-            }
-            break;
-        }
-        const int ne = pv.elem_start[wi.a + 1] - pv.elem_start[wi.a];
-        float pen = staged_phase1<MODE>(st, s, ne, pe, (float)m.kf, lp, ef);
-        __syncthreads();
-        pen += staged_phase2<MODE>(pv, wi.a, pe, lp, ef, ma, mf, mmu, m.fixed, (float*)m.q, (float*)m.partials);
-        double total;
-        if (bm_ticket_sum((double)pen, m.patch_energy, wi.a, &m.ticket_den, m.n_patches, &total) &&
-            threadIdx.x == 0) {
-            m.den = total;
-            const bool first_of_first = (it == 1 && m.tsc == 0);
-            if (!isfinite(total)) {
-                m.status |= 1;
-                m.done = 1;
-            } else if (total != 0.0) {
-                if (fabs(total) <= m.thr && !first_of_first)
-                    m.done = 1;
-                else
-                    m.alpha = m.rho / total;
-            } else {
-                m.done = 1;
-            }
-        }
-        __syncthreads();
-        w = wn;
-    }
-    if (failed) {
-        if (threadIdx.x == 0) *err = 1;
-        // the copies this block issued must land before it exits
-        mbar_wait(&st.bar[i & 1], (unsigned)((i >> 1) & 1));
-        if (issued_next) mbar_wait(&st.bar[(i + 1) & 1], (unsigned)(((i + 1) >> 1) & 1));
     }
 }
 
@@ -464,7 +357,7 @@ __global__ void __launch_bounds__(kBatchThreads) kb_euler(BMeshDesc* M, const Wo
 template <typename R>
 size_t batch_patch_smem(int pe)
 {
-    return sizeof(R) * (12 * (size_t)pe + 3 * (size_t)kBatchMaxLocalNodes);
+    return patch_smem_size<R>(pe, kBatchMaxLocalNodes);
 }
 
 template <typename R>
@@ -482,28 +375,6 @@ int batch_prepare(int pe, int* grid_patch, int* staged)
     int nb = nb1 < nb2 ? nb1 : nb2;
     *grid_patch = (nb < 1 ? 1 : nb) * sms;
     *staged = 0;
-    if constexpr (is_mixed<R>::value) {
-        // the bulk-copy staged matvec when its shared memory fits (even pe:
-        // every patch but the last starts on a 16-byte element boundary)
-        const char* env = getenv("SGB_PATCH_STAGING");
-        if (env && env[0] == '1' && (pe % 2) == 0) {
-            const size_t ss = staged_smem_bytes(pe, kBatchMaxLocalNodes);
-            int s1 = 0, s2 = 0;
-            if (cudaFuncSetAttribute(kb_matvec_staged<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
-                    cudaSuccess &&
-                cudaFuncSetAttribute(kb_matvec_staged<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
-                    cudaSuccess) {
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s1, kb_matvec_staged<1>, kStagedThreads, ss);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s2, kb_matvec_staged<2>, kStagedThreads, ss);
-                const int sb = s1 < s2 ? s1 : s2;
-                if (sb >= 1) {
-                    *staged = 1;
-                    *grid_patch = sb * sms;
-                }
-            }
-            cudaGetLastError();
-        }
-    }
     return sms;
 }
 
@@ -519,19 +390,6 @@ void batch_record_step(const BatchLaunch& B, cudaStream_t s)
     kb_rhs_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
     const size_t smem = batch_patch_smem<R>(B.pe);
     for (int it = 1; it <= B.max_iterations; ++it) {
-        if constexpr (is_mixed<R>::value) {
-            if (B.staged) {
-                const size_t ss = staged_smem_bytes(B.pe, kBatchMaxLocalNodes);
-                if (it == 1)
-                    kb_matvec_staged<1><<<B.grid_patch, kStagedThreads, ss, s>>>(B.meshes, pit, B.counts, it, B.pe,
-                                                                                 B.err);
-                else
-                    kb_matvec_staged<2><<<B.grid_patch, kStagedThreads, ss, s>>>(B.meshes, pit, B.counts, it, B.pe,
-                                                                                 B.err);
-                kb_update<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
-                continue;
-            }
-        }
         if (it == 1)
             kb_matvec<R, 1><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe);
         else

@@ -187,9 +187,10 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     // the fused variants; the reference-rounding variant keeps the caller's
     // element order
     HostLayout L;
-    // elements per patch: 512 (FP32) / 256 (FP64); SGB_PATCH_PE overrides the
-    // FP32 value (an even count in [32, 1024])
-    int pe = ops->real_size == 4 ? 512 : 256;
+    // elements per patch: 256 (measured best for FP32 on GB300 among 128..512
+    // with 64..256 threads) and 256 for FP64; SGB_PATCH_PE overrides the FP32
+    // value (an even count in [32, 1024])
+    int pe = 256;
     if (ops->real_size == 4)
         if (const char* e = getenv("SGB_PATCH_PE")) {
             const int v = atoi(e);
@@ -240,7 +241,7 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
             (rc = dev_alloc(&pl.node_start, L.node_start.size(), acc)) ||
             (rc = dev_alloc(&pl.lnode_gid, L.lnode_gid.size(), acc)) ||
             (rc = dev_alloc(&pl.lnode_info, L.lnode_info.size(), acc)) ||
-            (rc = dev_alloc(&pl.lrow, L.lrow.size(), acc)) || (rc = dev_alloc(&pl.lslots, L.lslots.size(), acc)) ||
+            (rc = dev_alloc(&pl.lrow, L.lrow.size(), acc)) || (rc = dev_alloc(&pl.lslots, L.lslots.size() + 8, acc)) ||
             (rc = dev_alloc(&pl.lconn, L.lconn.size() + 2, acc)) ||
             (rc = dev_alloc(&pl.bnd_rowptr, L.bnd_rowptr.size(), acc)) ||
             (rc = dev_alloc_bytes(&pl.partials, rs * 3 * (size_t)std::max(L.n_partials, 1), acc)))

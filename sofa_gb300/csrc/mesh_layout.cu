@@ -165,6 +165,7 @@ void build_patch_layout(int N, int E, const int32_t* tets, const double* pos, in
                 L.lslots[(size_t)fill[(size_t)n0 + ln[i]]++] = (uint16_t)((s - s0) * 4 + i);
         }
     }
+
 }
 
 // Node -> (storage position*4 + corner) table with each row sorted by the

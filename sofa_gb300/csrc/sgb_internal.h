@@ -158,6 +158,15 @@ struct Scene {
     bool graph_valid = false;
     int graph_steps = 0;
     size_t device_bytes = 0;
+    // residual replacement (FP32 scenes): every `replace_every` CG iterations
+    // the FP32 increment is accumulated into x64 and the residual recomputed
+    // as b64 - A x64 with an FP64 copy of the operator (`shadow`)
+    int replace_every = 0;
+    TfemMesh* shadow = nullptr;
+    double* b64 = nullptr;
+    double* x64 = nullptr;
+    double* w64 = nullptr;    // scratch: FP64 forces, then -kf K x64
+    double* ext64 = nullptr;  // external force in FP64
 };
 
 // ---------------------------------------------------------------------------

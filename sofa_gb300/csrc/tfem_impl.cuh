@@ -941,18 +941,92 @@ __device__ __forceinline__ void prefetch_patch(const PatchView& pv, const ElemVi
     l2_prefetch(pv.lrow + n0, pv.lrow + n1 + 1);
 }
 
+// Shared memory of the patch kernels: ef[12][pe] corner terms, sl[4*pe]
+// slot lists, lr[max_lnodes+1] row starts (padded to 16 bytes), then
+// lp[max_lnodes][3] nodal values. pe is even, so every region starts on a
+// 16-byte boundary.
+template <typename R>
+__host__ __device__ __forceinline__ size_t patch_smem_size(int pe, int max_lnodes)
+{
+    return sizeof(R) * 12 * (size_t)pe + 8 * (size_t)pe + ((4 * ((size_t)max_lnodes + 1) + 15) & ~(size_t)15) +
+           sizeof(R) * 3 * (size_t)max_lnodes;
+}
+
+template <typename R>
+__device__ __forceinline__ void patch_smem_carve(unsigned char* base, int pe, int max_lnodes, R** ef, uint16_t** sl,
+                                                 int** lr, R** lp)
+{
+    unsigned char* p = base;
+    *ef = reinterpret_cast<R*>(p);
+    p += sizeof(R) * 12 * (size_t)pe;
+    *sl = reinterpret_cast<uint16_t*>(p);
+    p += 8 * (size_t)pe;
+    *lr = reinterpret_cast<int*>(p);
+    p += (4 * ((size_t)max_lnodes + 1) + 15) & ~(size_t)15;
+    *lp = reinterpret_cast<R*>(p);
+}
+
+// One element of a patch: nodal values relative to node a (J^T annihilates
+// translations), rotated into the element frame, F = J K J^T X (computeForce,
+// TFEM.inl:417-521), and the four corner terms R^T F_i into ef[12][pe];
+// `pen` collects -p_rel^T (R^T F) for the CG modes.
+template <typename R, int MODE>
+__device__ __forceinline__ void patch_element(int le, ushort4 c, const R Rm[9], const R K[3], const R J[12], R kf,
+                                              int pe, const R* lp, R* ef, R& pen)
+{
+    const int ln[4] = {c.x, c.y, c.z, c.w};
+    R xr[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
+#pragma unroll
+    for (int i = 3; i >= 0; --i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
+    R X[12], F[12];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
+    element_force(F, X, K, J, kf);
+    R en = R(0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const R ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
+            ef[(3 * i + k) * pe + le] = ck;
+            en += xr[i][k] * ck;
+        }
+    if (MODE != 0) pen -= en;
+}
+
 // One patch of the fused matvec, executed by the whole block (it contains
 // block barriers). Returns this thread's share of the patch's p^T A p.
 template <typename R, int MODE>
 __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& ev, int P, const R* __restrict__ rin,
                                         const R* __restrict__ pold, R* __restrict__ pnew, R beta, R kf,
                                         const MassArgs& ma, double mf, R mmu, const uint8_t* __restrict__ fixed,
-                                        R* __restrict__ qout, R* __restrict__ partials, R* ef, R* lp)
+                                        R* __restrict__ qout, R* __restrict__ partials, R* ef, R* lp,
+                                        uint16_t* sl, int* lr)
 {
     const size_t En = (size_t)ev.n_tets;
     R pen = R(0);
     const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
     const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+    // phase 0: the patch's slot lists (4 per element, from slot 4*e0; e0 is
+    // even, so the copy starts on a 16-byte boundary and may read 8 bytes of
+    // padding past the end) and row starts into shared memory, so that the
+    // gather of phase 2 runs on shared memory only
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
+        uint4* dst = reinterpret_cast<uint4*>(sl);
+        const int n16 = (8 * ne + 15) >> 4;
+        for (int k = threadIdx.x; k < n16; k += blockDim.x) dst[k] = src[k];
+        for (int l = threadIdx.x; l <= nn; l += blockDim.x) lr[l] = pv.lrow[n0 + l] - 4 * e0;
+    }
     // phase 0: nodal values of the patch
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const int g = pv.lnode_gid[n0 + l];
@@ -975,46 +1049,18 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
     // phase 1: element terms
     for (int le = threadIdx.x; le < ne; le += blockDim.x) {
         const size_t e = (size_t)(e0 + le);
-        const ushort4 c = pv.lconn[e];
-        const int ln[4] = {c.x, c.y, c.z, c.w};
-        R xr[4][3];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
-        // relative to node a: J^T annihilates translations
-#pragma unroll
-        for (int i = 3; i >= 0; --i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
         R Rm[9], K[3], J[12];
         load_rot(ev, e, Rm);
         load_KJ(ev, e, K, J);
-        R X[12], F[12];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
-        element_force(F, X, K, J, kf);
-        R en = R(0);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const R ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
-                ef[(3 * i + k) * pv.pe + le] = ck;
-                en += xr[i][k] * ck;
-            }
-        if (MODE != 0) pen -= en;
+        patch_element<R, MODE>(le, pv.lconn[e], Rm, K, J, kf, pv.pe, lp, ef, pen);
     }
     __syncthreads();
     // phase 2: per local node, its slots in element order
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int s0 = pv.lrow[n0 + l], s1 = pv.lrow[n0 + l + 1];
+        const int s0 = lr[l], s1 = lr[l + 1];
         R a0 = R(0), a1 = R(0), a2 = R(0);
         for (int s = s0; s < s1; ++s) {
-            const int slot = pv.lslots[s];
+            const int slot = sl[s];
             const int le = slot >> 2, cc = slot & 3;
             a0 += ef[(3 * cc + 0) * pv.pe + le];
             a1 += ef[(3 * cc + 1) * pv.pe + le];
@@ -1061,8 +1107,11 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
                                                                    SolveConsts sc, int prefetch)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* ef = reinterpret_cast<R*>(smem_raw);  // [12][pe]
-    R* lp = ef + 12 * pv.pe;                 // [max_lnodes][3]
+    R* ef;
+    R* lp;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
     if (MODE != 0 && cg->done) return;
     const R beta = (MODE == 2) ? (R)cg->beta : R(0);
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
@@ -1072,43 +1121,25 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
             if (prefetch && threadIdx.x == 0 && P + (int)gridDim.x < pv.n_patches)
                 prefetch_patch(pv, ev, P + gridDim.x);
         energy += (double)patch_body<R, MODE>(pv, ev, P, rin, pold, pnew, beta, kf, ma, mf, mmu, fixed, qout,
-                                              partials, ef, lp);
+                                              partials, ef, lp, sl, lr);
     }
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
 
 // ------------------------------------------------------------------------
-// FP32 fused matvec with TMA staging. Each patch's element data -- quaternion,
-// three J/K planes and the local connectivity, 72 bytes per element, laid out
-// contiguously per patch by the element order -- is brought into shared
-// memory by bulk copies (cp.async.bulk, completion counted on an mbarrier)
-// issued by one thread. Two stage buffers alternate: while a CTA gathers and
-// computes patch i, the copy engine fetches patch i+1, so the DRAM stream does
-// not stop at the block barriers between the phases. Every wait on an
-// mbarrier is bounded; a wait that runs out sets an error flag, waits (also
-// bounded) for the copies it issued and leaves the loop.
+// FP32 fused matvec with the element data staged by bulk copies. Phase 1 is
+// the only reader of a patch's element data (quaternion and three J/K
+// planes, 64 B per element, and the local connectivity, 8 B), which is
+// contiguous per patch. Right after phase 1 of patch i, one thread issues
+// the bulk copies (cp.async.bulk, completion counted on an mbarrier) of the
+// block's next patch into the same stage buffer; they land while the block
+// runs phase 2 of patch i and phase 0 of patch i+1, so the element stream
+// keeps DRAM busy across the block barriers. Every wait on the mbarrier is
+// bounded; a wait that runs out sets an error flag, waits (also bounded)
+// once more for the copies in flight and leaves the loop.
 // ------------------------------------------------------------------------
-constexpr int kStagedThreads = 256;
+constexpr int kStagedThreads = 128;
 constexpr long long kStageWaitTries = 1LL << 22;
-
-// Shared-memory stages: stage s holds, at base + s*stride, pe quaternions
-// (16 B each), three planes of pe float4 J/K values and pe local
-// connectivities (8 B each).
-struct StageSmem {
-    unsigned char* base;
-    unsigned stride;
-    int pe;
-    uint64_t* bar;  // 2 mbarriers
-    __device__ __forceinline__ float4* q(int s) const { return reinterpret_cast<float4*>(base + s * stride); }
-    __device__ __forceinline__ float4* jk(int s) const
-    {
-        return reinterpret_cast<float4*>(base + s * stride + 16u * (unsigned)pe);
-    }
-    __device__ __forceinline__ ushort4* lc(int s) const
-    {
-        return reinterpret_cast<ushort4*>(base + s * stride + 64u * (unsigned)pe);
-    }
-};
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -1153,186 +1184,33 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
     return false;
 }
 
-// Shared-memory bytes of a staged patch kernel: two mbarriers, two stages of
-// 72 bytes per element, the corner terms (48 bytes per element) and the
-// patch's nodal values (12 bytes per local node). Every region starts on a
-// 16-byte boundary (pe is even).
+// Shared memory of the staged kernel: an mbarrier (16 B), the stage
+// (q[pe] float4, jk[3][pe] float4, lc[pe] ushort4: 72 B per element), then
+// the regions of the plain patch kernel.
 inline size_t staged_smem_bytes(int pe, int max_lnodes)
 {
-    return 16 + 2 * 72 * (size_t)pe + 12 * sizeof(float) * (size_t)pe + 12 * (size_t)max_lnodes;
+    return 16 + 72 * (size_t)pe + patch_smem_size<float>(pe, max_lnodes);
 }
 
-__device__ __forceinline__ StageSmem stage_layout(unsigned char* base, int pe, float** ef, float** lp, int max_lnodes)
+// Issued by one thread: the element data of patch P into the stage. Global
+// addresses are 16-byte aligned (patches start at even element positions,
+// the arrays are 256-byte aligned); the connectivity copy is rounded up to
+// 16 bytes, which the array's two padding entries cover.
+__device__ __forceinline__ void stage_elements(unsigned char* stage, uint64_t* bar, const ElemView<float>& ev,
+                                               const ushort4* lconn, int e0, int ne, int pe)
 {
-    StageSmem st;
-    st.bar = reinterpret_cast<uint64_t*>(base);
-    st.base = base + 16;
-    st.stride = 72u * (unsigned)pe;
-    st.pe = pe;
-    *ef = reinterpret_cast<float*>(st.base + 2 * st.stride);
-    *lp = *ef + 12 * pe;
-    (void)max_lnodes;
-    return st;
-}
-
-// Issued by one thread: the element data of elements [e0, e0+ne) into stage
-// s. The global addresses are 16-byte aligned (patches start at even element
-// positions; the arrays are 256-byte aligned); the connectivity copy is
-// rounded up to 16 bytes, which the arrays' two padding entries cover.
-__device__ __forceinline__ void stage_issue(const StageSmem& st, int s, const ElemView<float>& ev,
-                                            const ushort4* lconn, int e0, int ne, int pe)
-{
-    const size_t En = (size_t)ev.n_tets;
-    const float4* q = reinterpret_cast<const float4*>(ev.rot) + e0;
+    const float4* q = reinterpret_cast<const float4*>(ev.rot);
     const float4* J = reinterpret_cast<const float4*>(ev.J);
+    const size_t En = (size_t)ev.n_tets;
     const unsigned qb = 16u * (unsigned)ne;
     const unsigned lb = (8u * (unsigned)ne + 15u) & ~15u;
     fence_async_shared();
-    mbar_expect_tx(&st.bar[s], 4 * qb + lb);
-    bulk_load(st.q(s), q, qb, &st.bar[s]);
-    for (int k = 0; k < 3; ++k) bulk_load(st.jk(s) + (size_t)k * pe, J + k * En + e0, qb, &st.bar[s]);
-    bulk_load(st.lc(s), lconn + e0, lb, &st.bar[s]);
+    mbar_expect_tx(bar, 4 * qb + lb);
+    bulk_load(stage, q + e0, qb, bar);
+    for (int k = 0; k < 3; ++k) bulk_load(stage + 16u * pe * (1 + k), J + k * En + e0, qb, bar);
+    bulk_load(stage + 64u * pe, lconn + e0, lb, bar);
 }
 
-// Phase 0 of a patch: nodal values (and the CG direction) into lp.
-template <int MODE>
-__device__ __forceinline__ void staged_phase0(const PatchView& pv, int P, const float* __restrict__ rin,
-                                              const float* __restrict__ pold, float* __restrict__ pnew, float beta,
-                                              float* lp)
-{
-    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
-    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int g = pv.lnode_gid[n0 + l];
-        float v[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float rv = rin[3 * (size_t)g + k];
-            v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
-            lp[3 * l + k] = v[k];
-        }
-        if (MODE != 0) {
-            const int info = pv.lnode_info[n0 + l];
-            if (info < 0 || (info & 1)) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
-            }
-        }
-    }
-}
-
-// Phase 1 from stage s: element corner terms into ef; returns -p^T K p share.
-template <int MODE>
-__device__ __forceinline__ float staged_phase1(const StageSmem& st, int s, int ne, int pe, float kf, const float* lp,
-                                               float* ef)
-{
-    float pen = 0.f;
-    const float4* jk = st.jk(s);
-    const float4* qs = st.q(s);
-    const ushort4* lcs = st.lc(s);
-    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
-        const ushort4 c = lcs[le];
-        const int ln[4] = {c.x, c.y, c.z, c.w};
-        float xr[4][3];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) xr[i][k] = lp[3 * ln[i] + k];
-#pragma unroll
-        for (int i = 3; i >= 0; --i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) xr[i][k] -= xr[0][k];
-        float Rm[9], K[3], J[12];
-        quat_to_rot(qs[le], Rm);
-        const float4 a = jk[le], b = jk[pe + le], cc = jk[2 * pe + le];
-        J[3] = a.x;
-        J[4] = a.y;
-        J[5] = a.z;
-        J[6] = a.w;
-        J[7] = b.x;
-        J[8] = b.y;
-        J[9] = b.z;
-        J[10] = b.w;
-        J[11] = cc.x;
-        J[0] = -(J[3] + J[6] + J[9]);
-        J[1] = -(J[4] + J[7] + J[10]);
-        J[2] = -(J[5] + J[8] + J[11]);
-        K[0] = 1.f;
-        K[1] = cc.y;
-        K[2] = cc.z;
-        float X[12], F[12];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                X[3 * i + k] = Rm[3 * k] * xr[i][0] + Rm[3 * k + 1] * xr[i][1] + Rm[3 * k + 2] * xr[i][2];
-        element_force(F, X, K, J, kf);
-        float en = 0.f;
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float ck = Rm[k] * F[3 * i] + Rm[3 + k] * F[3 * i + 1] + Rm[6 + k] * F[3 * i + 2];
-                ef[(3 * i + k) * pe + le] = ck;
-                en += xr[i][k] * ck;
-            }
-        if (MODE != 0) pen -= en;
-    }
-    return pen;
-}
-
-// Phase 2: per local node, its slots in element order; interior nodes
-// finished, shared nodes leave partial sums. Returns the mass term of
-// p^T A p for the nodes this patch owns.
-template <int MODE>
-__device__ __forceinline__ float staged_phase2(const PatchView& pv, int P, int pe, const float* lp, const float* ef,
-                                               const MassArgs& ma, double mf, float mmu,
-                                               const uint8_t* __restrict__ fixed, float* __restrict__ qout,
-                                               float* __restrict__ partials)
-{
-    float pen = 0.f;
-    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
-    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int s0 = pv.lrow[n0 + l], s1 = pv.lrow[n0 + l + 1];
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        for (int s = s0; s < s1; ++s) {
-            const int slot = pv.lslots[s];
-            const int le = slot >> 2, cc = slot & 3;
-            a0 += ef[(3 * cc + 0) * pe + le];
-            a1 += ef[(3 * cc + 1) * pe + le];
-            a2 += ef[(3 * cc + 2) * pe + le];
-        }
-        const int g = pv.lnode_gid[n0 + l];
-        const int info = pv.lnode_info[n0 + l];
-        if (info >= 0) {
-            float* o = partials + 3 * (size_t)(info >> 1);
-            o[0] = a0;
-            o[1] = a1;
-            o[2] = a2;
-        }
-        if (MODE == 0) {
-            if (info < 0) {
-                qout[3 * (size_t)g] -= a0;
-                qout[3 * (size_t)g + 1] -= a1;
-                qout[3 * (size_t)g + 2] -= a2;
-            }
-        } else if (info < 0 || (info & 1)) {
-            const float p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
-            const float mm = ma.node_mass ? (float)(ma.node_mass[g] * mf) : mmu;
-            pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
-            if (info < 0) {
-                float q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
-                if (fixed[g]) q0 = q1 = q2 = 0.f;
-                qout[3 * (size_t)g] = q0;
-                qout[3 * (size_t)g + 1] = q1;
-                qout[3 * (size_t)g + 2] = q2;
-            }
-        }
-    }
-    return pen;
-}
-
-// Single-mesh staged matvec (FP32). `err` (device int) is set to 1 when a
-// stage wait runs out; the CG modes also stop the solve with status bit 2.
 template <int MODE>
 __global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
     PatchView pv, ElemView<float> ev, const float* __restrict__ rin, const float* __restrict__ pold,
@@ -1340,45 +1218,132 @@ __global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
     float* __restrict__ qout, float* __restrict__ partials, SolveConsts sc, int* err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *ef, *lp;
     const int pe = pv.pe;
-    const StageSmem st = stage_layout(smem_raw, pe, &ef, &lp, pv.max_lnodes);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* stage = smem_raw + 16;
+    const float4* sq = reinterpret_cast<const float4*>(stage);
+    const float4* sj = reinterpret_cast<const float4*>(stage + 16u * pe);
+    const ushort4* slc = reinterpret_cast<const ushort4*>(stage + 64u * pe);
+    float *ef, *lp;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve<float>(stage + 72u * pe, pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
     if (MODE != 0 && cg->done) return;
     const float beta = (MODE == 2) ? (float)cg->beta : 0.f;
     const float mmu = (float)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
     if (threadIdx.x == 0) {
-        mbar_init(&st.bar[0], 1);
-        mbar_init(&st.bar[1], 1);
+        mbar_init(bar, 1);
         mbar_fence_init();
     }
     __syncthreads();
     const int G = gridDim.x, NP = pv.n_patches;
     int P = blockIdx.x;
     if (threadIdx.x == 0 && P < NP)
-        stage_issue(st, 0, ev, pv.lconn, pv.elem_start[P], pv.elem_start[P + 1] - pv.elem_start[P], pe);
+        stage_elements(stage, bar, ev, pv.lconn, pv.elem_start[P], pv.elem_start[P + 1] - pv.elem_start[P], pe);
     double energy = 0.0;
     bool failed = false;
-    int issued_next = 0;
-    for (int i = 0; P < NP; P += G, ++i) {
-        const int s = i & 1;
-        const int Pn = P + G;
-        issued_next = 0;
-        if (Pn < NP) {
-            issued_next = 1;
-            if (threadIdx.x == 0)
-                stage_issue(st, s ^ 1, ev, pv.lconn, pv.elem_start[Pn], pv.elem_start[Pn + 1] - pv.elem_start[Pn],
-                            pe);
+    unsigned parity = 0;
+    for (; P < NP; P += G, parity ^= 1u) {
+        const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
+        const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+        float pen = 0.f;
+        // phase 0: slot lists and row starts, then the nodal values
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
+            uint4* dst = reinterpret_cast<uint4*>(sl);
+            const int n16 = (8 * ne + 15) >> 4;
+            for (int k = threadIdx.x; k < n16; k += blockDim.x) dst[k] = src[k];
+            for (int l = threadIdx.x; l <= nn; l += blockDim.x) lr[l] = pv.lrow[n0 + l] - 4 * e0;
         }
-        staged_phase0<MODE>(pv, P, rin, pold, pnew, beta, lp);
-        const bool ok = mbar_wait(&st.bar[s], (unsigned)((i >> 1) & 1));
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int g = pv.lnode_gid[n0 + l];
+            float v[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float rv = rin[3 * (size_t)g + k];
+                v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
+                lp[3 * l + k] = v[k];
+            }
+            if (MODE != 0) {
+                const int info = pv.lnode_info[n0 + l];
+                if (info < 0 || (info & 1)) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
+                }
+            }
+        }
+        const bool ok = mbar_wait(bar, parity);
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
         }
-        const int ne = pv.elem_start[P + 1] - pv.elem_start[P];
-        float pen = staged_phase1<MODE>(st, s, ne, pe, kf, lp, ef);
+        // phase 1 from the stage
+        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+            float Rm[9], K[3], J[12];
+            quat_to_rot(sq[le], Rm);
+            const float4 a = sj[le], b = sj[pe + le], d = sj[2 * pe + le];
+            J[3] = a.x;
+            J[4] = a.y;
+            J[5] = a.z;
+            J[6] = a.w;
+            J[7] = b.x;
+            J[8] = b.y;
+            J[9] = b.z;
+            J[10] = b.w;
+            J[11] = d.x;
+            J[0] = -(J[3] + J[6] + J[9]);
+            J[1] = -(J[4] + J[7] + J[10]);
+            J[2] = -(J[5] + J[8] + J[11]);
+            K[0] = 1.f;
+            K[1] = d.y;
+            K[2] = d.z;
+            patch_element<float, MODE>(le, slc[le], Rm, K, J, kf, pe, lp, ef, pen);
+        }
         __syncthreads();
-        pen += staged_phase2<MODE>(pv, P, pe, lp, ef, ma, mf, mmu, fixed, qout, partials);
+        // the stage is free: the next patch's element data streams in now
+        const int Pn = P + G;
+        if (threadIdx.x == 0 && Pn < NP)
+            stage_elements(stage, bar, ev, pv.lconn, pv.elem_start[Pn], pv.elem_start[Pn + 1] - pv.elem_start[Pn],
+                           pe);
+        // phase 2: per local node, its slots in element order
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int s0 = lr[l], s1 = lr[l + 1];
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+            for (int k = s0; k < s1; ++k) {
+                const int slot = sl[k];
+                const int le = slot >> 2, cc = slot & 3;
+                a0 += ef[(3 * cc + 0) * pe + le];
+                a1 += ef[(3 * cc + 1) * pe + le];
+                a2 += ef[(3 * cc + 2) * pe + le];
+            }
+            const int g = pv.lnode_gid[n0 + l];
+            const int info = pv.lnode_info[n0 + l];
+            if (info >= 0) {
+                float* o = partials + 3 * (size_t)(info >> 1);
+                o[0] = a0;
+                o[1] = a1;
+                o[2] = a2;
+            }
+            const size_t g3 = 3 * (size_t)g;
+            if (MODE == 0) {
+                if (info < 0) {
+                    qout[g3] -= a0;
+                    qout[g3 + 1] -= a1;
+                    qout[g3 + 2] -= a2;
+                }
+            } else if (info < 0 || (info & 1)) {
+                const float p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
+                const float mm = ma.node_mass ? (float)(ma.node_mass[g] * mf) : mmu;
+                pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
+                if (info < 0) {
+                    float q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
+                    if (fixed[g]) q0 = q1 = q2 = 0.f;
+                    qout[g3] = q0;
+                    qout[g3 + 1] = q1;
+                    qout[g3 + 2] = q2;
+                }
+            }
+        }
         energy += (double)pen;
         __syncthreads();
     }
@@ -1390,10 +1355,8 @@ __global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
                 cg->done = 1;
             }
         }
-        // the copies this block issued must land before it exits
-        const int i = (P - (int)blockIdx.x) / G;
-        mbar_wait(&st.bar[i & 1], (unsigned)((i >> 1) & 1));
-        if (issued_next) mbar_wait(&st.bar[(i + 1) & 1], (unsigned)(((i + 1) >> 1) & 1));
+        // the copies of the current patch must land before the block exits
+        mbar_wait(bar, parity);
         return;
     }
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
@@ -1655,7 +1618,7 @@ inline PatchView patch_view(TfemMesh* m)
 template <typename R>
 size_t patch_smem_bytes(const TfemMesh* m)
 {
-    return sizeof(R) * (12 * (size_t)m->pl.pe + 3 * (size_t)m->pl.max_lnodes);
+    return patch_smem_size<R>(m->pl.pe, m->pl.max_lnodes);
 }
 
 // Sets the shared-memory attribute of the patch kernels and returns the grid
@@ -1858,10 +1821,12 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
                 const size_t ss = staged_smem_bytes(m->pl.pe, m->pl.max_lnodes);
                 if (it == 1)
                     k_patch_matvec_staged<1><<<m->staged_grid, kStagedThreads, ss, s>>>(
-                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->dev_flags);
+                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons,
+                        m->dev_flags);
                 else
                     k_patch_matvec_staged<2><<<m->staged_grid, kStagedThreads, ss, s>>>(
-                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->dev_flags);
+                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons,
+                        m->dev_flags);
                 done = true;
             }
         }
