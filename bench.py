@@ -55,6 +55,8 @@ def parse():
                     help="profiling run: build the mixed scene, run warm-up + steps, print a short line")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-beam batched workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    ap.add_argument("--no-ill-conditioned", action="store_true", help="skip the stiff-inclusion workload")
+    ap.add_argument("--ill-steps", type=int, default=50)
     ap.add_argument("--beams", type=int, default=256)
     ap.add_argument("--requests", type=int, default=150, help="requests per arrival rate in the serving sample")
     return ap.parse_args()
@@ -333,6 +335,65 @@ def run_serving(torch, capi, args, plain_best):
             "speedup_vs_plain_fp64_single_mesh": best / plain_best}
 
 
+ILL = dict(n=(48, 48, 193), young_out=1e3, young_in=1e6, poisson=0.49, method="polar", cg_iterations=200,
+           cg_tolerance=1e-10, replace_every=20, seed=0)
+
+
+def run_ill_conditioned(torch, capi, args):
+    """Stiff spherical inclusion (E 1e6 in a 1e3 beam, nu 0.49), gravity and a
+    seeded tip traction, CG 200 / 1e-10: the FP32 solve with an FP64 residual
+    every 20 iterations and the plain FP32 solve against a pure FP64 run."""
+    from sofa_gb300 import topology as topo
+
+    ib = topo.inclusion_beam(ILL["n"], seed=ILL["seed"], young_out=ILL["young_out"], young_in=ILL["young_in"])
+    m = ib.mesh
+    steps = max(1, args.ill_steps)
+
+    def run(precision, replace):
+        fem = capi.TetrahedronFEM(m.positions, m.tetrahedra, ib.young, ILL["poisson"], ILL["method"], precision)
+        sc = capi.Scene(fem, dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=ILL["cg_iterations"],
+                        cg_tolerance=ILL["cg_tolerance"], cg_threshold=1e-20, gravity=(0.0, -9.81, 0.0),
+                        vertex_mass=1.0 / m.n_nodes, fixed=m.fixed, residual_replacement=replace)
+        sc.set_external_force(ib.tip_force)
+        stream = torch.cuda.ExternalStream(sc.stream)
+        sc.step(1)
+        sc.sync()
+        sc.set_state(m.positions, np.zeros_like(m.positions))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sc.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        its, res = sc.sync()
+        x, _ = sc.state()
+        sc.close()
+        return x, t, its, res
+
+    x64, t64, i64, r64 = run("fp64_fma", 0)
+    xr, tr, ir, rr = run("mixed", ILL["replace_every"])
+    xm, tm, im, rm = run("mixed", 0)
+    d = float(np.linalg.norm(x64 - m.positions))
+    nx = float(np.linalg.norm(x64))
+
+    def arm(x, t, its, res):
+        return {"tet_steps_per_s": m.n_tets * steps / t, "ms_per_step": t / steps * 1e3,
+                "cg_iterations_last_step": its, "cg_residual_last_step": res,
+                "rel_l2_position": float(np.linalg.norm(x - x64) / nx),
+                "rel_l2_displacement": float(np.linalg.norm(x - x64) / d) if d > 0 else None}
+
+    return {"workload": f"{ILL['n'][0]}x{ILL['n'][1]}x{ILL['n'][2]} beam, {m.n_tets} tets, spherical inclusion "
+                        f"radius 0.25 width, E {ILL['young_in']:g} in {ILL['young_out']:g}, nu {ILL['poisson']}, "
+                        f"tip traction {ib.traction:.3f} along -y, CG {ILL['cg_iterations']}/{ILL['cg_tolerance']:g}",
+            "steps": steps, "reference": "pure FP64 (FMA) run of the same scene",
+            "fp64": {"tet_steps_per_s": m.n_tets * steps / t64, "ms_per_step": t64 / steps * 1e3,
+                     "cg_iterations_last_step": i64, "cg_residual_last_step": r64},
+            "mixed_residual_replacement": dict(arm(xr, tr, ir, rr), every=ILL["replace_every"]),
+            "mixed_plain": arm(xm, tm, im, rm)}
+
+
 def cpu_baseline(mesh, cfg, threads, steps=1):
     from oracle import pyoracle
 
@@ -498,23 +559,24 @@ def main():
     if not args.no_serving and rank == 0:
         serving = run_serving(torch, capi, args, plain_best)
 
+    ill = None
+    if not args.no_ill_conditioned and rank == 0:
+        ill = run_ill_conditioned(torch, capi, args)
+
+    # DRAM bytes of one addDForce launch from an ncu capture of the same
+    # kernel (profiles/), scaled to this workload's element count
     traffic = None
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get("adddforce_mixed_bytes_per_call")
-        except Exception:
-            plain_best = max(p["tet_steps_per_s"] for p in plain.values())
-    batched = None
-    if not args.no_batched and rank == 0:
-        batched = run_batched(torch, capi, args, plain_best)
-    serving = None
-    if not args.no_serving and rank == 0:
-        serving = run_serving(torch, capi, args, plain_best)
+            t = json.load(open(prof))
+            traffic = t["dram_bytes_per_launch"] * E / t["n_tets"]
+        except (OSError, ValueError, KeyError, ZeroDivisionError):
+            traffic = None
 
-    traffic = None
-
-    launches_per_step = 5 + 3 * cfg["cg_iterations"]
+    # per step: element force, force gather, RHS element pass, RHS gather,
+    # CG iterations x (matvec + update), Euler update
+    launches_per_step = 5 + 2 * cfg["cg_iterations"]
     line = {
         "metric": "tet-steps/s", "value": value, "unit": "tet-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
@@ -526,6 +588,7 @@ def main():
         "batched": batched,
         "serving": serving,
         "position_error": err,
+        "ill_conditioned": ill,
         "roofline": {"kernel": "addDForce (element + gather kernels, mixed)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg,

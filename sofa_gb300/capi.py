@@ -297,7 +297,7 @@ class Scene:
     def __init__(self, fem: TetrahedronFEM, dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0,
                  cg_iterations=25, cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0),
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
-                 serial_dots=False):
+                 serial_dots=False, residual_replacement=0):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -323,6 +323,7 @@ class Scene:
         p.fix_all = int(fix_all)
         p.mass_first = int(mass_first)
         p.serial_dots = int(serial_dots)
+        p.residual_replacement = int(residual_replacement)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now

@@ -218,7 +218,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
     B->ops = ops;
     B->precision = precision;
     B->rs = ops->real_size;
-    B->pe = 256;
+    B->pe = B->rs == 4 ? 512 : 256;
     B->max_slots = max_meshes;
     B->max_iterations = max_cg_iterations;
     B->slots.resize((size_t)max_meshes);

@@ -55,7 +55,7 @@ struct sgb_batch {
     const sgb::VariantOps* ops = nullptr;
     int precision = 0;
     size_t rs = 4;
-    int pe = 256;  // elements per patch (shared-memory stride of the batch matvec)
+    int pe = 512;  // elements per patch (shared-memory stride of the batch matvec)
     int max_slots = 0;
     int max_iterations = 0;
     sgb::Arena arena;

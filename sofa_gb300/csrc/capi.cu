@@ -71,6 +71,7 @@ struct sgb_tfem {
 struct sgb_scene {
     Scene s;
     sgb_tfem* fem = nullptr;
+    sgb_tfem* shadow = nullptr;  // FP64 copy of the force field (residual replacement)
     const VariantOps* ops = nullptr;
     double* dot_terms = nullptr;
     int serial_dots = 0;
@@ -181,6 +182,7 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     m.precision = precision;
     m.real_size = ops->real_size;
     m.young_h = E_h;
+    if (n_lsf > 0) m.lsf_h.assign(local_stiffness_factor, local_stiffness_factor + n_lsf);
     m.poisson_h = nu_h;
     int rc = SGB_OK;
     // element storage order and patch layout (Morton-ordered patches) for
@@ -568,7 +570,15 @@ static void free_scene(sgb_scene* sc)
     cudaFree(s.r);
     cudaFree(s.cg);
     cudaFree(sc->dot_terms);
+    cudaFree(s.b64);
+    cudaFree(s.x64);
+    cudaFree(s.w64);
+    cudaFree(s.r64);
+    cudaFree(s.ext64);
     if (s.cg_h) cudaFreeHost(s.cg_h);
+    if (sc->shadow) sgb_tfem_destroy(sc->shadow);
+    sc->shadow = nullptr;
+    s.shadow = nullptr;
 }
 
 int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params* params)
@@ -580,6 +590,12 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: invalid solver parameters");
     if (P.n_fixed < 0 || (P.n_fixed > 0 && !P.fixed_host))
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: invalid fixed indices");
+    if (P.residual_replacement < 0)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: residual_replacement must be >= 0");
+    if (P.residual_replacement > 0 &&
+        (fem->m.precision != SGB_PRECISION_MIXED || fem->m.pl.n_patches == 0 || fem->m.method == SGB_METHOD_SMALL))
+        return fail(SGB_ERR_NOT_SUPPORTED,
+                    "sgb_scene_create: residual replacement needs a mixed-precision large/polar force field");
     sgb_scene* sc = new sgb_scene();
     Scene& s = sc->s;
     const int N = fem->m.n_nodes;
@@ -618,6 +634,31 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
         goto fail_out;
     if (P.node_masses_host && (rc = dev_alloc(&s.node_mass, (size_t)N, acc))) goto fail_out;
     if (P.serial_dots && (rc = dev_alloc(&sc->dot_terms, (size_t)N, acc))) goto fail_out;
+    if (P.residual_replacement > 0) {
+        // the FP64 copy of the operator, created from the force field's
+        // inputs (rest positions and tetrahedra read back, caller order)
+        const TfemMesh& fm = fem->m;
+        std::vector<double> rest((size_t)N * 3);
+        std::vector<int32_t> store((size_t)fm.n_tets * 4), tets((size_t)fm.n_tets * 4);
+        if ((ce = cudaMemcpy(rest.data(), fm.rest_pos, sizeof(double) * rest.size(), cudaMemcpyDeviceToHost)) ||
+            (ce = cudaMemcpy(store.data(), fm.tets, sizeof(int32_t) * store.size(), cudaMemcpyDeviceToHost))) {
+            rc = cuda_fail(ce, "residual replacement set-up");
+            goto fail_out;
+        }
+        for (size_t st = 0; st < (size_t)fm.n_tets; ++st)
+            for (int c = 0; c < 4; ++c) tets[4 * (size_t)fm.perm_h[st] + c] = store[4 * st + c];
+        if ((rc = sgb_tfem_create(&sc->shadow, N, rest.data(), fm.n_tets, tets.data(), fm.young_h.data(),
+                                  (int)fm.young_h.size(), fm.poisson_h.data(), (int)fm.poisson_h.size(),
+                                  fm.lsf_h.empty() ? nullptr : fm.lsf_h.data(), (int)fm.lsf_h.size(), fm.method,
+                                  SGB_PRECISION_FP64_FMA)))
+            goto fail_out;
+        s.shadow = &sc->shadow->m;
+        s.replace_every = P.residual_replacement;
+        *acc += sc->shadow->m.device_bytes;
+        if ((rc = dev_alloc(&s.b64, 3 * (size_t)N, acc)) || (rc = dev_alloc(&s.x64, 3 * (size_t)N, acc)) ||
+            (rc = dev_alloc(&s.w64, 3 * (size_t)N, acc)) || (rc = dev_alloc(&s.r64, 3 * (size_t)N, acc)))
+            goto fail_out;
+    }
     if ((ce = cudaMallocHost((void**)&s.cg_h, sizeof(CgScalars))) != cudaSuccess) {
         rc = cuda_fail(ce, "cudaMallocHost");
         goto fail_out;
@@ -727,6 +768,18 @@ int sgb_scene_set_external_force(sgb_scene_t* scene, const double* fext_host)
             cudaGraphExecDestroy(s.graph);
             s.graph = nullptr;
         }
+    }
+    if (s.shadow) {
+        if (!s.ext64) {
+            int rc = dev_alloc(&s.ext64, n3, &s.device_bytes);
+            if (rc) return rc;
+            s.graph_valid = false;
+            if (s.graph) {
+                cudaGraphExecDestroy(s.graph);
+                s.graph = nullptr;
+            }
+        }
+        SGB_CUDA_TRY(cudaMemcpyAsync(s.ext64, fext_host, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));
     }
     if (rs == sizeof(double)) {
         SGB_CUDA_TRY(cudaMemcpyAsync(s.ext, fext_host, sizeof(double) * n3, cudaMemcpyHostToDevice, s.stream));

@@ -104,6 +104,7 @@ struct TfemMesh {
     int* dev_flags = nullptr; // sticky device error flag: 1 = a bounded device wait ran out
     double rest_volume = 0.0;
     std::vector<double> young_h, poisson_h;  // as given (for inspection)
+    std::vector<double> lsf_h;               // localStiffnessFactor as given
     size_t device_bytes = 0;
 };
 
@@ -166,6 +167,7 @@ struct Scene {
     double* b64 = nullptr;
     double* x64 = nullptr;
     double* w64 = nullptr;    // scratch: FP64 forces, then -kf K x64
+    double* r64 = nullptr;    // FP64 residual written by the right-hand side gather
     double* ext64 = nullptr;  // external force in FP64
 };
 

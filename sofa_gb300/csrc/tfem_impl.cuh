@@ -603,7 +603,7 @@ __device__ __forceinline__ double dot3(const A a[3], const B b[3])
     return r;
 }
 
-enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2 };
+enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2, FIN_REPLACE = 3 };
 
 struct SolveConsts {
     double tol, threshold;
@@ -673,7 +673,7 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         } else {
             cg->done = 1;
         }
-    } else {
+    } else if (FIN == FIN_RHO) {
         cg->rho_prev = cg->rho;
         cg->rho = total;
         cg->iters = sc.it;
@@ -681,6 +681,15 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         double err = sqrt(total) / cg->normb;
         cg->last_err = err;
         if (err <= sc.tol) cg->done = 1;
+    } else {
+        // residual replacement after the update of iteration sc.it: the true
+        // residual's r.r replaces the recurrence's, for beta and for the
+        // stopping test (which may now continue a solve the recurrence ended)
+        cg->rho = total;
+        cg->beta = total / cg->rho_prev;
+        double err = sqrt(total) / cg->normb;
+        cg->last_err = err;
+        cg->done = (err <= sc.tol) ? 1 : 0;
     }
 }
 
@@ -1113,6 +1122,9 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
     int* lr;
     patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
     if (MODE != 0 && cg->done) return;
+    // MODE 0 with a CG state: run only if iteration sc.it of the solve ran
+    // (residual replacement inside a captured step)
+    if (MODE == 0 && cg && cg->iters != sc.it) return;
     const R beta = (MODE == 2) ? (R)cg->beta : R(0);
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
     double energy = 0.0;  // FP64 across patches; FP32 within one patch
@@ -1366,8 +1378,10 @@ __global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
 // their partial sums in patch order.
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restrict__ bnd_rowptr,
-                                                            const R* __restrict__ partials, R* __restrict__ df, int N)
+                                                            const R* __restrict__ partials, R* __restrict__ df, int N,
+                                                            const CgScalars* gate = nullptr, int gate_it = 0)
 {
+    if (gate && gate->iters != gate_it) return;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
         if (b0 == b1) continue;
@@ -1535,6 +1549,90 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_update_patch(R* __restrict__ 
                                            alpha);
     }
     finish_dot<FIN_RHO>(local, cg, nullptr, N, sc);
+}
+
+// ------------------------------------------------------------------------
+// Residual replacement for FP32 scenes (reliable-update CG, after van der
+// Vorst and Ye, "Residual replacement strategies for Krylov subspace
+// iterative methods for the convergence of true residuals", SIAM J. Sci.
+// Comput. 22(3), 2000): the FP32 recurrence r -= alpha q drifts from
+// b - A x; every few iterations the FP32 increment is folded into an FP64
+// solution x64 and the residual recomputed from b64 in FP64 with an FP64
+// copy of the operator.
+// ------------------------------------------------------------------------
+
+// r32 = b64 (rounded), xs32 = 0: the FP32 solve starts from the FP64 RHS.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_refine_start(const double* __restrict__ b64, R* __restrict__ r,
+                                                             R* __restrict__ xs, int N)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 3 * (size_t)N;
+         i += (size_t)gridDim.x * blockDim.x) {
+        r[i] = (R)b64[i];
+        xs[i] = R(0);
+    }
+}
+
+// x64 += xs32, xs32 = 0, if iteration `it` of the solve ran.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_refine_accumulate(double* __restrict__ x64, R* __restrict__ xs,
+                                                                  const CgScalars* cg, int it, int N)
+{
+    if (cg->iters != it) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 3 * (size_t)N;
+         i += (size_t)gridDim.x * blockDim.x) {
+        x64[i] += (double)xs[i];
+        xs[i] = R(0);
+    }
+}
+
+// r = b64 - (mF M x64 - kF K x64), with w64 = -kF K x64 from the FP64
+// operator; projected; r32 = r (rounded); r.r in FP64 replaces rho.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_refine_residual(const double* __restrict__ b64,
+                                                                const double* __restrict__ x64,
+                                                                const double* __restrict__ w64, MassArgs ma,
+                                                                double mf, const uint8_t* __restrict__ fixed,
+                                                                R* __restrict__ r, CgScalars* cg, int N,
+                                                                SolveConsts sc)
+{
+    if (cg->iters != sc.it) return;
+    const double mmu = ma.vertex_mass * mf;
+    double local = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const double mm = ma.node_mass ? ma.node_mass[n] * mf : mmu;
+        double rr[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const size_t i = 3 * (size_t)n + k;
+            rr[k] = fixed[n] ? 0.0 : b64[i] - (mm * x64[i] + w64[i]);
+            r[i] = (R)rr[k];
+        }
+        local += dot3(rr, rr);
+    }
+    finish_dot<FIN_REPLACE>(local, cg, nullptr, N, sc);
+}
+
+// v += x64 + xs32, x += h v (EulerImplicitSolver.cpp:256-295 with the
+// solution split in two parts).
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_euler_refined(double* __restrict__ x, double* __restrict__ v,
+                                                              const double* __restrict__ x64,
+                                                              const R* __restrict__ xs, double h, double vdamp,
+                                                              CgScalars* cg, int N)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const size_t i = 3 * (size_t)n + k;
+            double vv = v[i] + (x64[i] + (double)xs[i]);
+            double t = vv * h;
+            x[i] = x[i] + t;
+            if (vdamp != 1.0) vv *= vdamp;
+            v[i] = vv;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cg->time_step_count += 1;
 }
 
 // ------------------------------------------------------------------------
@@ -1843,6 +1941,75 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);
+}
+
+// The FP32 patch step with residual replacement every sc->replace_every CG
+// iterations: forces, right-hand side and the replaced residuals in FP64 on
+// the FP64 copy of the operator (sc->shadow), the CG iterations in FP32.
+template <typename R>
+void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
+{
+    TfemMesh* m = sc->mesh;
+    TfemMesh* sh = sc->shadow;
+    const int N = sc->n;
+    const SceneParams& P = sc->prm;
+    const double h = P.dt;
+    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const int ng = node_grid(N);
+    const int ng3 = node_grid(3 * N);
+    R* r = (R*)sc->r;
+    R* pb[2] = {(R*)sc->p, (R*)sc->p2};
+    R* q = (R*)sc->q;
+    R* xs = (R*)sc->xs;
+    R* partials = (R*)m->pl.partials;
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1};
+    // FP64: f = F(x) and b = h (f - (h+rs) K v - rm M v) on the FP64 operator
+    NodeCSR csr64{sh->rowptr, sh->slots};
+    launch_elem_force<double>(sh, sc->x, s);
+    k_gather_force<double><<<ng, kNodeBlock, 0, s>>>(csr64, (const double*)sh->eforce, sc->ext64, ma, mass_first,
+                                                     sc->w64, N);
+    const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
+    launch_elem_dforce<double, double, 0>(sh, sc->v, nullptr, sc->cg, kf_rhs, s);
+    k_gather_rhs<double><<<ng, kNodeBlock, 0, s>>>(csr64, (const double*)sh->eforce, sc->w64, sc->v, ma,
+                                                   -P.rayleigh_mass, mass_first, h, sc->fixed, sc->b64, sc->r64,
+                                                   sc->x64, sc->cg, nullptr, N, cons);
+    // FP32: the element rotations at x, r = b, xs = 0
+    launch_elem_force<R>(m, sc->x, s);
+    k_refine_start<R><<<ng3, kNodeBlock, 0, s>>>(sc->b64, r, xs, N);
+    const double mf = 1 + 1.0 * h * P.rayleigh_mass;
+    const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    PatchView pv = patch_view(m);
+    ElemView<R> ev = view<R>(m);
+    const size_t smem = patch_smem_bytes<R>(m);
+    const int ng_update = m->update_vec4 ? node_grid((N + 3) / 4) : ng;
+    const int k = sc->replace_every;
+    for (int it = 1; it <= P.cg_iterations; ++it) {
+        cons.it = it;
+        R* pold = pb[it & 1];
+        R* pnew = pb[(it + 1) & 1];
+        if (it == 1)
+            k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
+                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+        else
+            k_patch_matvec<R, 2><<<m->patch_grid, m->patch_threads, smem, s>>>(
+                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+        k_cg_update_patch<R><<<ng_update, kNodeBlock, 0, s>>>(xs, r, pnew, q, partials, m->pl.bnd_rowptr, ma, mf,
+                                                              sc->fixed, sc->cg, N, cons, m->update_vec4);
+        if (k > 0 && it % k == 0 && it < P.cg_iterations) {
+            k_refine_accumulate<R><<<ng3, kNodeBlock, 0, s>>>(sc->x64, xs, sc->cg, it, N);
+            cudaMemsetAsync(sc->w64, 0, sizeof(double) * 3 * (size_t)N, s);
+            MassArgs none{nullptr, 0.0, {0.0, 0.0, 0.0}};
+            k_patch_matvec<double, 0><<<sh->patch_grid, sh->patch_threads, patch_smem_bytes<double>(sh), s>>>(
+                patch_view(sh), view<double>(sh), sc->x64, nullptr, nullptr, sc->cg, kf, none, 1.0, nullptr, sc->w64,
+                (double*)sh->pl.partials, cons, 0);
+            k_patch_fixup<double><<<ng, kNodeBlock, 0, s>>>(sh->pl.bnd_rowptr, (const double*)sh->pl.partials,
+                                                            sc->w64, N, sc->cg, it);
+            k_refine_residual<R><<<ng, kNodeBlock, 0, s>>>(sc->b64, sc->x64, sc->w64, ma, mf, sc->fixed, r, sc->cg,
+                                                           N, cons);
+        }
+    }
+    const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
+    k_euler_refined<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, sc->x64, xs, h, vd, sc->cg, N);
 }
 
 }  // namespace SGB_NS

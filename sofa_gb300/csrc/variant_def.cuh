@@ -25,8 +25,12 @@ static void v_scene_step(Scene* sc, double* terms, int mass_first, cudaStream_t 
     // FP32 runs the fused patch matvec; FP64 (FMA) is bound by the FP64 issue
     // rate, where the element-order path with its plain gather is faster
     if (SGB_USES_PATCHES && sizeof(SGB_REAL) == 4 && sc->mesh->pl.n_patches > 0 &&
-        sc->mesh->method != METHOD_SMALL)
-        scene_step_patch<SGB_REAL>(sc, mass_first, s);
+        sc->mesh->method != METHOD_SMALL) {
+        if (sc->replace_every > 0 && sc->shadow && sc->shadow->pl.n_patches > 0)
+            scene_step_refined<SGB_REAL>(sc, mass_first, s);
+        else
+            scene_step_patch<SGB_REAL>(sc, mass_first, s);
+    }
     else
         scene_step<SGB_REAL>(sc, terms, mass_first, s);
 }

@@ -221,3 +221,36 @@ def beam(n, spacing=0.5, jitter=0.05, seed=0, split=5):
         raise ValueError("split must be 5 or 6")
     fixed = np.nonzero(np.abs(pos[:, 2]) <= 1e-12)[0].astype(np.int32)
     return BeamMesh(pos, tets, fixed, (nx, ny, nz))
+
+
+@dataclass
+class InclusionBeam:
+    """A beam with a stiff spherical inclusion and a tip load."""
+
+    mesh: BeamMesh
+    young: np.ndarray  # (E,) per-element Young's modulus
+    tip_force: np.ndarray  # (N,3) constant external force on the tip nodes
+    traction: float
+
+
+def inclusion_beam(n, spacing=0.5, jitter=0.05, seed=0, young_out=1e3, young_in=1e6, radius_frac=0.25,
+                   traction_max=10.0):
+    """Cantilever beam with a sphere of radius radius_frac * width at
+    mid-length whose elements (by centroid) have young_in, the others
+    young_out; a tip traction of magnitude U[0, traction_max] (seeded) along
+    -y over the free end face, applied as equal forces on its nodes."""
+    m = beam(n, spacing, jitter, seed, split=5)
+    nx, ny, nz = m.n
+    width = (nx - 1) * spacing
+    centre = np.array([width / 2, (ny - 1) * spacing / 2, (nz - 1) * spacing / 2])
+    cen = m.positions[m.tetrahedra].mean(axis=1)
+    inside = np.linalg.norm(cen - centre, axis=1) <= radius_frac * width
+    young = np.where(inside, young_in, young_out).astype(np.float64)
+    rng = np.random.default_rng(seed + 7)
+    t = float(rng.uniform(0.0, traction_max))
+    zmax = m.positions[:, 2].max()
+    tip = np.nonzero(np.abs(m.positions[:, 2] - zmax) <= 1e-12)[0]
+    area = width * (ny - 1) * spacing
+    f = np.zeros_like(m.positions)
+    f[tip, 1] = -t * area / len(tip)
+    return InclusionBeam(m, young, f, t)
