@@ -18,10 +18,11 @@ def capi():
     return capi
 
 
-def _run(capi, mesh, young, poisson, precision, replace, steps, iters, fext=None):
+def _run(capi, mesh, young, poisson, precision, replace, steps, iters, fext=None, vertex_mass=None):
     fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, young, poisson, "polar", precision)
     sc = capi.Scene(fem, dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=iters, cg_tolerance=1e-10,
-                    cg_threshold=1e-30, gravity=(0.0, -9.81, 0.0), vertex_mass=1.0 / mesh.n_nodes, fixed=mesh.fixed,
+                    cg_threshold=1e-30, gravity=(0.0, -9.81, 0.0),
+                    vertex_mass=(1.0 / mesh.n_nodes) if vertex_mass is None else vertex_mass, fixed=mesh.fixed,
                     residual_replacement=replace)
     if fext is not None:
         sc.set_external_force(fext)
@@ -36,12 +37,14 @@ def test_residual_replacement_reaches_fp64_accuracy(capi):
     residual recomputed in FP64 every 20 iterations the mixed-precision run
     converges on the true residual and lands on the FP64 trajectory, far
     closer than the plain FP32 recurrence can."""
+    # unit mass per node and E = 5000: A = M + h(h+rs) K has a condition
+    # number of a few tens, so FP64 CG reaches 1e-10 in well under 400 steps
     m = topo.beam((6, 6, 17), seed=5)
     steps = 10
-    x64, i64, r64 = _run(capi, m, 1e5, 0.45, "fp64_fma", 0, steps, 400)
+    x64, i64, r64 = _run(capi, m, 5000.0, 0.45, "fp64_fma", 0, steps, 400, vertex_mass=1.0)
     assert r64 <= 1e-10 and i64 < 400, (r64, i64)
-    xr, ir, rr = _run(capi, m, 1e5, 0.45, "mixed", 20, steps, 400)
-    xm, im, rm = _run(capi, m, 1e5, 0.45, "mixed", 0, steps, 400)
+    xr, ir, rr = _run(capi, m, 5000.0, 0.45, "mixed", 20, steps, 400, vertex_mass=1.0)
+    xm, im, rm = _run(capi, m, 5000.0, 0.45, "mixed", 0, steps, 400, vertex_mass=1.0)
     disp = np.linalg.norm(x64 - m.positions)
     assert disp > 1e-8
     err_r = np.linalg.norm(xr - x64) / disp
