@@ -145,17 +145,42 @@ def make_scene(capi, mesh, cfg, precision):
                       vertex_mass=cfg["total_mass"] / mesh.n_nodes, fixed=mesh.fixed)
 
 
-def time_steps(torch, scene, steps, warmup):
+def replica_barrier(torch, world):
+    """Barrier across replicas (no-op for one process)."""
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def replica_max(torch, t_local, world, device):
+    """Max over ranks of a per-rank duration: replicas exchange no data, the
+    job's time is the slowest rank's."""
+    t = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, n_tets, steps, t_max):
+    """Whole-job tet-steps/s: every rank advances its own copy of the workload."""
+    return world * n_tets * steps / t_max
+
+
+def time_steps(torch, scene, steps, warmup, world=1):
+    """CUDA-event time of `steps` steps on the scene's stream after `warmup`
+    untimed steps, with a barrier and a device synchronisation on both sides."""
     stream = torch.cuda.ExternalStream(scene.stream)
     scene.step(warmup)
     scene.sync()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    replica_barrier(torch, world)
     e0.record(stream)
     scene.step(steps)
     e1.record(stream)
     e1.synchronize()
+    torch.cuda.synchronize()
+    replica_barrier(torch, world)
     return e0.elapsed_time(e1) / 1e3
 
 
@@ -494,17 +519,12 @@ def main():
         print(json.dumps({"profile_run": True, "n_tets": E, "ms_per_step": t / max(args.steps, 1) * 1e3,
                           "adddforce_ms": t_df * 1e3}))
         return 0
-    if world > 1:
-        torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        t_mixed = time_steps(torch, mixed, args.steps, args.warmup)
+        t_mixed = time_steps(torch, mixed, args.steps, args.warmup, world)
     iters_mixed, res_mixed = mixed.sync()
-    t_all = torch.tensor([t_mixed], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_all, op=torch.distributed.ReduceOp.MAX)
-    t_max = float(t_all.item())
-    value = world * E * args.steps / t_max
+    t_max = replica_max(torch, t_mixed, world, "cuda")
+    value = replica_value(world, E, args.steps, t_max)
 
     # addDForce roofline on the mixed path
     t_df = time_add_dforce(torch, capi, mixed, mesh)

@@ -1457,8 +1457,8 @@ __device__ __forceinline__ void st12(float* __restrict__ a, size_t n0, const flo
 
 // The same update for four consecutive nodes n0..n0+3 (n0 a multiple of 4)
 // with 16-byte loads, every load of the group issued before the first use.
-// Returns the group's r.r: per node the three-term FP32 sum, summed in FP64
-// in node order.
+// Returns the group's r.r: the twelve squares summed in FP32 in node order
+// (the caller's running sum is FP64).
 __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, float* __restrict__ r,
                                              const float* __restrict__ p, const float* __restrict__ q,
                                              const float* __restrict__ partials, const int* __restrict__ bnd_rowptr,
@@ -1498,11 +1498,11 @@ __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, 
     }
     st12(xs, n0, xx);
     st12(r, n0, rr);
-    double local = 0.0;
+    float local = 0.f;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-        local += (double)(rr[3 * j] * rr[3 * j] + rr[3 * j + 1] * rr[3 * j + 1] + rr[3 * j + 2] * rr[3 * j + 2]);
-    return local;
+        local += rr[3 * j] * rr[3 * j] + rr[3 * j + 1] * rr[3 * j + 1] + rr[3 * j + 2] * rr[3 * j + 2];
+    return (double)local;
 }
 
 template <typename R>
@@ -1524,7 +1524,7 @@ __device__ __forceinline__ double cg_update4g(size_t n0, R* xs, R* r, const R* p
 // thread per group of four nodes (16-byte loads), the N % 4 last nodes one
 // per thread.
 template <typename R>
-__global__ void __launch_bounds__(kNodeBlock) k_cg_update_patch(R* __restrict__ xs, R* __restrict__ r,
+__global__ void __launch_bounds__(kNodeBlock, 4) k_cg_update_patch(R* __restrict__ xs, R* __restrict__ r,
                                                                 const R* __restrict__ p, const R* __restrict__ q,
                                                                 const R* __restrict__ partials,
                                                                 const int* __restrict__ bnd_rowptr, MassArgs ma,
