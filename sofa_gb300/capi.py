@@ -135,6 +135,7 @@ def load():
         "sgb_tfem_add_dforce": (c_int, [_vp, _vp, _vp, c_double, _vp]),
         "sgb_tfem_add_dforce_f32": (c_int, [_vp, _vp, _vp, c_float, _vp]),
         "sgb_tfem_get_rotations": (c_int, [_vp, _dp, _dp]),
+        "sgb_tfem_check_device": (c_int, [_vp]),
         "sgb_tfem_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                   ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_size_t)]),
         "sgb_scene_params_default": (None, [ctypes.POINTER(SceneParams)]),
@@ -261,6 +262,11 @@ class TetrahedronFEM:
             self.close()
         except Exception:
             pass
+
+    def check_device(self):
+        """SGB_OK, or raises for SGB_ERR_DEVICE_TIMEOUT (a bounded device wait of
+        an earlier call ran out); synchronises."""
+        return check(load().sgb_tfem_check_device(self._h))
 
     def add_force(self, x_dev, f_dev, stream=None):
         """f += F(x); device pointers (ints). f is FP64 (fp64 handles) or FP32 (mixed)."""
