@@ -214,24 +214,24 @@ def adddforce_bytes(n_tets, n_nodes, p_e, p_v):
 
 
 def e2e_steps(torch, capi, scene, mesh, steps):
-    """Through the C ABI with host buffers: each step uploads the state from
-    pinned host memory, steps once and reads the positions back."""
+    """Through the C ABI with host buffers: each step uploads the state
+    (positions and velocities) from pinned host memory, steps once and reads
+    the resulting positions back into pinned host memory."""
     n3 = (mesh.n_nodes, 3)
     xh = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
     vh = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
-    x0, v0 = scene.state()
-    xh[:] = x0
-    vh[:] = v0
+    xo = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
+    scene.state_into(xh, vh)
     scene.set_state(xh, vh)
     scene.step(1)
-    scene.state()
+    scene.state_into(xo)
     t0 = time.perf_counter()
     for _ in range(steps):
         scene.set_state(xh, vh)
         scene.step(1)
-        xr, _ = scene.state()
+        scene.state_into(xo)
     t1 = time.perf_counter()
-    return t1 - t0, 2 * xh.nbytes, 2 * xh.nbytes  # set_state copies x and v; get_state reads x and v
+    return t1 - t0, xh.nbytes + vh.nbytes, xo.nbytes
 
 
 def beam_population(n, seed):

@@ -216,7 +216,11 @@ int sgb_scene_step(sgb_scene_t* scene, int n_steps);
  * non-finite value was met. */
 int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual);
 
-/* State access (FP64). get_* synchronise; set_* are stream-ordered. */
+/* State access (FP64). get_* synchronise; set_* are stream-ordered: from
+ * pinned host memory the copies run asynchronously, and the caller keeps the
+ * buffers unchanged until a later synchronising call (get_state,
+ * sgb_scene_sync); pageable buffers are consumed before the call returns.
+ * Either pointer may be NULL. */
 int sgb_scene_get_state(sgb_scene_t* scene, double* x_host, double* v_host);
 int sgb_scene_set_state(sgb_scene_t* scene, const double* x_host, const double* v_host);
 /* MechanicalObject externalForce (accumulateForce, MechanicalObject.inl:1357-1376). */

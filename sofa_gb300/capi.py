@@ -364,9 +364,17 @@ class Scene:
         check(load().sgb_scene_get_state(self._h, x.ctypes.data_as(_dp), v.ctypes.data_as(_dp)))
         return x, v
 
+    def state_into(self, x_out=None, v_out=None):
+        """Read x and/or v into caller buffers (C-contiguous float64, n x 3;
+        pinned buffers give full-speed copies); synchronises."""
+        px = x_out.ctypes.data_as(_dp) if x_out is not None else _dp()
+        pv = v_out.ctypes.data_as(_dp) if v_out is not None else _dp()
+        check(load().sgb_scene_get_state(self._h, px, pv))
+
     def set_state(self, x=None, v=None):
         xa, px = _d(np.asarray(x).reshape(-1, 3)) if x is not None else (None, _dp())
         va, pv = _d(np.asarray(v).reshape(-1, 3)) if v is not None else (None, _dp())
+        self._pending_state = (xa, va)  # kept alive until the stream-ordered copies have run
         check(load().sgb_scene_set_state(self._h, px, pv))
 
     def set_external_force(self, fext):

@@ -749,9 +749,11 @@ int sgb_scene_set_state(sgb_scene_t* scene, const double* x_host, const double* 
     if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_set_state: NULL scene");
     Scene& s = scene->s;
     const size_t bytes = sizeof(double) * 3 * (size_t)s.n;
+    // stream-ordered: with pinned host buffers the copies run asynchronously
+    // (the caller keeps the buffers unchanged until a later synchronising
+    // call); pageable buffers are copied before the call returns
     if (x_host) SGB_CUDA_TRY(cudaMemcpyAsync(s.x, x_host, bytes, cudaMemcpyHostToDevice, s.stream));
     if (v_host) SGB_CUDA_TRY(cudaMemcpyAsync(s.v, v_host, bytes, cudaMemcpyHostToDevice, s.stream));
-    SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
     return SGB_OK;
 }
 

@@ -1138,6 +1138,28 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
 
+// addDForce (MODE 0) as its own kernel so that it can carry its own register
+// cap: 128-thread CTAs, at least 10 per SM in FP32 (51 registers), measured
+// faster than the 64 the CG modes need. `gate`: run only if iteration
+// gate_it of that solve ran (residual replacement inside a captured step).
+template <typename R>
+__global__ void __launch_bounds__(kPatchThreads, sizeof(R) == 4 ? 10 : 1)
+    k_patch_adddforce(PatchView pv, ElemView<R> ev, const R* __restrict__ dx, R kf, R* __restrict__ df,
+                      R* __restrict__ partials, const CgScalars* gate, int gate_it)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* ef;
+    R* lp;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
+    if (gate && gate->iters != gate_it) return;
+    const MassArgs none{nullptr, 0.0, {0.0, 0.0, 0.0}};
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
+        (void)patch_body<R, 0>(pv, ev, P, dx, nullptr, nullptr, R(0), kf, none, 1.0, R(0), nullptr, df, partials, ef,
+                               lp, sl, lr);
+}
+
 // ------------------------------------------------------------------------
 // FP32 fused matvec with the element data staged by bulk copies. Phase 1 is
 // the only reader of a patch's element data (quaternion and three J/K
@@ -1725,7 +1747,7 @@ template <typename R>
 int prepare_patch(TfemMesh* m)
 {
     const size_t smem = patch_smem_bytes<R>(m);
-    int dev = 0, sms = 0, nb0 = 0, nb1 = 0, nb2 = 0;
+    int dev = 0, sms = 0, nb1 = 0, nb2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     // launch-shape knobs: threads per CTA (64/128/256), L2 prefetch of the
@@ -1738,19 +1760,25 @@ int prepare_patch(TfemMesh* m)
     m->patch_threads = threads;
     if (const char* e = getenv("SGB_PATCH_PREFETCH")) m->patch_prefetch = (e[0] == '1');
     if (const char* e = getenv("SGB_UPDATE_VEC4")) m->update_vec4 = (e[0] != '0');
-    cudaFuncSetAttribute(k_patch_matvec<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_patch_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_patch_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, k_patch_matvec<R, 0>, threads, smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, threads, smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, threads, smem);
-    int nb = nb0 < nb1 ? nb0 : nb1;
+    int nb = nb1;
     nb = nb < nb2 ? nb : nb2;
     if (nb < 1) nb = 1;
     long long g = (long long)nb * sms;
     if (g > kMaxDotBlocks) g = kMaxDotBlocks;
     if (g > m->pl.n_patches) g = m->pl.n_patches;
     if (g < 1) g = 1;
+    {
+        int na = 0;
+        cudaFuncSetAttribute(k_patch_adddforce<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&na, k_patch_adddforce<R>, kPatchThreads, smem);
+        long long ga = (long long)(na < 1 ? 1 : na) * sms;
+        if (ga > m->pl.n_patches) ga = m->pl.n_patches;
+        m->adddforce_grid = (int)(ga < 1 ? 1 : ga);
+    }
     m->staged = false;
     if constexpr (is_mixed<R>::value) {
         // FP32: the bulk-copy staged kernels when their shared memory fits
@@ -1814,9 +1842,8 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
             }
         }
         if (!done)
-            k_patch_matvec<R, 0><<<m->patch_grid, m->patch_threads, patch_smem_bytes<R>(m), s>>>(
-                pv, view<R>(m), dx, nullptr, nullptr, nullptr, kfactor, ma, 1.0, nullptr, df, (R*)m->pl.partials, sc,
-                m->patch_prefetch);
+            k_patch_adddforce<R><<<m->adddforce_grid, kPatchThreads, patch_smem_bytes<R>(m), s>>>(
+                pv, view<R>(m), dx, kfactor, df, (R*)m->pl.partials, nullptr, 0);
         k_patch_fixup<R><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(m->pl.bnd_rowptr, (const R*)m->pl.partials, df,
                                                                       m->n_nodes);
         return;
@@ -1998,10 +2025,8 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
         if (k > 0 && it % k == 0 && it < P.cg_iterations) {
             k_refine_accumulate<R><<<ng3, kNodeBlock, 0, s>>>(sc->x64, xs, sc->cg, it, N);
             cudaMemsetAsync(sc->w64, 0, sizeof(double) * 3 * (size_t)N, s);
-            MassArgs none{nullptr, 0.0, {0.0, 0.0, 0.0}};
-            k_patch_matvec<double, 0><<<sh->patch_grid, sh->patch_threads, patch_smem_bytes<double>(sh), s>>>(
-                patch_view(sh), view<double>(sh), sc->x64, nullptr, nullptr, sc->cg, kf, none, 1.0, nullptr, sc->w64,
-                (double*)sh->pl.partials, cons, 0);
+            k_patch_adddforce<double><<<sh->patch_grid, kPatchThreads, patch_smem_bytes<double>(sh), s>>>(
+                patch_view(sh), view<double>(sh), sc->x64, kf, sc->w64, (double*)sh->pl.partials, sc->cg, it);
             k_patch_fixup<double><<<ng, kNodeBlock, 0, s>>>(sh->pl.bnd_rowptr, (const double*)sh->pl.partials,
                                                             sc->w64, N, sc->cg, it);
             k_refine_residual<R><<<ng, kNodeBlock, 0, s>>>(sc->b64, sc->x64, sc->w64, ma, mf, sc->fixed, r, sc->cg,
