@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, con
 
 // ---- CG matvec over patches ------------------------------------------------
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kPatchThreads, 7) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(kPatchThreads, 6) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
                                                            const int* __restrict__ counts, int it, int pe)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
