@@ -137,6 +137,20 @@ __device__ __forceinline__ void quat_to_rot(float4 q, float Rm[9])
     Rm[8] = sg * (1.f - 2.f * (xx + yy));
 }
 
+// One Newton step of the polar iteration X <- (X + X^-T) / 2 in FP64 (X^-T
+// is the cofactor matrix over the determinant): from a rotation accurate to
+// FP32 it gives a matrix orthonormal to FP64 precision.
+__device__ __forceinline__ void orthonormalize_newton(double X[9])
+{
+    const double c[9] = {X[4] * X[8] - X[5] * X[7], X[5] * X[6] - X[3] * X[8], X[3] * X[7] - X[4] * X[6],
+                         X[7] * X[2] - X[8] * X[1], X[8] * X[0] - X[6] * X[2], X[6] * X[1] - X[7] * X[0],
+                         X[1] * X[5] - X[2] * X[4], X[2] * X[3] - X[0] * X[5], X[0] * X[4] - X[1] * X[3]};
+    const double det = X[0] * c[0] + X[1] * c[1] + X[2] * c[2];
+    const double h = 0.5 / det;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) X[i] = 0.5 * X[i] + h * c[i];
+}
+
 template <typename R>
 __device__ __forceinline__ void load_rot(const ElemView<R>& ev, size_t e, R Rm[9])
 {
@@ -201,7 +215,8 @@ template <typename R>
 __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4* __restrict__ tets,
                                 const int* __restrict__ elem_orig, int E, int method,
                                 const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
-                                int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest, R* rot,
+                                int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest,
+                                double* rest64, R* rot,
                                 R* R0, double* vol)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -289,6 +304,8 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
         for (int i = 0; i < 9; ++i) rot[(size_t)i * En + s] = (R)Rm[i];
     }
     for (int i = 0; i < 12; ++i) rest[(size_t)i * En + s] = (R)rr[i];
+    if (rest64)
+        for (int i = 0; i < 12; ++i) rest64[(size_t)i * En + s] = rr[i];
     for (int i = 0; i < 9; ++i) R0[(size_t)i * En + s] = (R)Rm[i];
 }
 
@@ -342,7 +359,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
     R rr[12];
 #pragma unroll
     for (int i = 0; i < 12; ++i) rr[i] = ev.rest[i * En + e];
-    if (!is_mixed<R>::value) {
+    if constexpr (!is_mixed<R>::value) {
         // FP64: the reference's formulation on absolute positions
         R eab[3] = {R(p[1][0] - p[0][0]), R(p[1][1] - p[0][1]), R(p[1][2] - p[0][2])};
         R eac[3] = {R(p[2][0] - p[0][0]), R(p[2][1] - p[0][1]), R(p[2][2] - p[0][2])};
@@ -389,20 +406,58 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int k = 0; k < 3; ++k) ed[i][k] = (R)(p[i + 1][k] - p[0][k]);
-        if (METHOD == METHOD_LARGE) {
-            rotation_large(ed[0], ed[1], Rm);
-        } else {
-            R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
-            polar3(A, Rm);
-        }
-        D[0] = D[1] = D[2] = R(0);
+        if (ev.rest64) {
+            // The strain D = rest - R e is a small difference of edge-sized
+            // terms: it is formed in FP64 from FP64 rest coordinates and
+            // edges with a rotation orthonormal to FP64 precision (large:
+            // the QR frame built in FP64, whose zero components D[4], D[5],
+            // D[8] are then exact; polar: the FP32 polar factor plus one
+            // Newton step X <- (X + X^-T)/2 in FP64). A residual error of R
+            // that is a rotation adds no first-order strain; a
+            // non-orthonormal R (FP32 rounding) would add strain noise of the
+            // size of the edges' FP32 rounding, which on stiff, lightly
+            // loaded meshes is as large as the load itself.
+            double ee[3][3], Rd[9];
 #pragma unroll
-        for (int i = 1; i < 4; ++i)
+            for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                R d = Rm[3 * k] * ed[i - 1][0] + Rm[3 * k + 1] * ed[i - 1][1] + Rm[3 * k + 2] * ed[i - 1][2];
-                D[3 * i + k] = rr[3 * i + k] - d;
+                for (int k = 0; k < 3; ++k) ee[i][k] = p[i + 1][k] - p[0][k];
+            if (METHOD == METHOD_LARGE) {
+                rotation_large(ee[0], ee[1], Rd);
+            } else {
+                R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
+                polar3(A, Rm);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Rd[i] = (double)Rm[i];
+                orthonormalize_newton(Rd);
             }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Rm[i] = (R)Rd[i];
+            D[0] = D[1] = D[2] = R(0);
+#pragma unroll
+            for (int i = 1; i < 4; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double d =
+                        Rd[3 * k] * ee[i - 1][0] + Rd[3 * k + 1] * ee[i - 1][1] + Rd[3 * k + 2] * ee[i - 1][2];
+                    D[3 * i + k] = (R)(ev.rest64[(size_t)(3 * i + k) * En + e] - d);
+                }
+        } else {
+            if (METHOD == METHOD_LARGE) {
+                rotation_large(ed[0], ed[1], Rm);
+            } else {
+                R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
+                polar3(A, Rm);
+            }
+            D[0] = D[1] = D[2] = R(0);
+#pragma unroll
+            for (int i = 1; i < 4; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    R d = Rm[3 * k] * ed[i - 1][0] + Rm[3 * k + 1] * ed[i - 1][1] + Rm[3 * k + 2] * ed[i - 1][2];
+                    D[3 * i + k] = rr[3 * i + k] - d;
+                }
+        }
         if (METHOD == METHOD_LARGE) D[4] = D[5] = D[8] = R(0);
     }
     store_rot(ev, (size_t)e, Rm);
@@ -1677,6 +1732,7 @@ ElemView<R> view(TfemMesh* m)
     ev.K = (const R*)m->K;
     ev.J = (const R*)m->J;
     ev.rest = (const R*)m->rest;
+    ev.rest64 = m->rest64;
     ev.n_tets = m->n_tets;
     ev.method = m->method;
     return ev;
@@ -1689,7 +1745,7 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
     if (m->n_tets == 0) return;
     k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
         m->rest_pos, m->tets, m->elem_orig, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K,
-        (R*)m->J, (R*)m->rest, (R*)m->rot, (R*)m->R0, vol);
+        (R*)m->J, (R*)m->rest, m->rest64, (R*)m->rot, (R*)m->R0, vol);
 }
 
 template <typename R>
