@@ -140,15 +140,71 @@ __device__ __forceinline__ void quat_to_rot(float4 q, float Rm[9])
 // One Newton step of the polar iteration X <- (X + X^-T) / 2 in FP64 (X^-T
 // is the cofactor matrix over the determinant): from a rotation accurate to
 // FP32 it gives a matrix orthonormal to FP64 precision.
+//
+// FP64 reciprocal and reciprocal square root by Newton-Raphson iteration from
+// the FP32 hardware estimate (y <- y (2 - a y) and y <- y (3 - a y^2) / 2;
+// each step doubles the number of correct digits, two steps take the ~1e-7
+// estimate to FP64 precision): a few FP64 fused multiply-adds instead of the
+// long FP64 division and square-root sequences, which the FP64 pipe of this
+// GPU runs at a small fraction of the FP32 rate.
+__device__ __forceinline__ double rcp_nr(double a)
+{
+    double y = (double)(1.0f / (float)a);
+    y = y * (2.0 - a * y);
+    y = y * (2.0 - a * y);
+    return y;
+}
+
+__device__ __forceinline__ double rsqrt_nr(double a)
+{
+    double y = (double)rsqrtf((float)a);
+    y = y * (1.5 - 0.5 * a * y * y);
+    y = y * (1.5 - 0.5 * a * y * y);
+    return y;
+}
+
 __device__ __forceinline__ void orthonormalize_newton(double X[9])
 {
     const double c[9] = {X[4] * X[8] - X[5] * X[7], X[5] * X[6] - X[3] * X[8], X[3] * X[7] - X[4] * X[6],
                          X[7] * X[2] - X[8] * X[1], X[8] * X[0] - X[6] * X[2], X[6] * X[1] - X[7] * X[0],
                          X[1] * X[5] - X[2] * X[4], X[2] * X[3] - X[0] * X[5], X[0] * X[4] - X[1] * X[3]};
     const double det = X[0] * c[0] + X[1] * c[1] + X[2] * c[2];
-    const double h = 0.5 / det;
+    const double h = 0.5 * rcp_nr(det);
 #pragma unroll
     for (int i = 0; i < 9; ++i) X[i] = 0.5 * X[i] + h * c[i];
+}
+
+// The QR frame of computeRotationLarge (TFEM.inl:755-778) in FP64, with the
+// normalisations by rsqrt_nr: rows = unit edge ab, in-plane unit vector,
+// unit normal. Degenerate edges (squared length below the FP64 epsilon) are
+// left unscaled, as Vec::normalize does.
+__device__ __forceinline__ void rotation_large_f64(const double eab[3], const double eac[3], double R[9])
+{
+    double ex[3] = {eab[0], eab[1], eab[2]};
+    const double nx = ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2];
+    if (nx > 4.930380657631324e-32) {
+        const double s = rsqrt_nr(nx);
+        ex[0] *= s;
+        ex[1] *= s;
+        ex[2] *= s;
+    }
+    double ez[3];
+    cross3(ex, eac, ez);
+    const double nz = ez[0] * ez[0] + ez[1] * ez[1] + ez[2] * ez[2];
+    if (nz > 4.930380657631324e-32) {
+        const double s = rsqrt_nr(nz);
+        ez[0] *= s;
+        ez[1] *= s;
+        ez[2] *= s;
+    }
+    double ey[3];
+    cross3(ez, ex, ey);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        R[k] = ex[k];
+        R[3 + k] = ey[k];
+        R[6 + k] = ez[k];
+    }
 }
 
 template <typename R>
@@ -423,7 +479,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
 #pragma unroll
                 for (int k = 0; k < 3; ++k) ee[i][k] = p[i + 1][k] - p[0][k];
             if (METHOD == METHOD_LARGE) {
-                rotation_large(ee[0], ee[1], Rd);
+                rotation_large_f64(ee[0], ee[1], Rd);
             } else {
                 R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
                 polar3(A, Rm);
