@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <thread>
@@ -165,6 +166,8 @@ static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool no
     return c.total;
 }
 
+// Each mesh's items are contiguous and in mesh-local index order in every
+// list: the kernels' per-mesh reductions index their block partials by it.
 static void rebuild_work_lists(sgb_batch* B, std::vector<WorkItem> wl[3])
 {
     for (int k = 0; k < 3; ++k) wl[k].clear();
@@ -220,7 +223,16 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
     B->ops = ops;
     B->precision = precision;
     B->rs = ops->real_size;
+    // elements per patch (512 FP32, 256 FP64); SGB_BATCH_PE overrides the FP32
+    // value (even, in [64, 512]); SGB_BATCH_PREFETCH=1 turns on the L2
+    // prefetch of a block's next patch
     B->pe = B->rs == 4 ? 512 : 256;
+    if (B->rs == 4)
+        if (const char* e = getenv("SGB_BATCH_PE")) {
+            const int v = atoi(e);
+            if (v >= 64 && v <= 512 && v % 2 == 0) B->pe = v;
+        }
+    if (const char* e = getenv("SGB_BATCH_PREFETCH")) B->prefetch = (e[0] == '1');
     B->max_slots = max_meshes;
     B->max_iterations = max_cg_iterations;
     B->slots.resize((size_t)max_meshes);
@@ -239,7 +251,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
     }
     B->arena.reset(B->arena_mem, hbm_budget_bytes);
     B->device_bytes = hbm_budget_bytes + sizeof(BMeshDesc) * max_meshes;
-    B->sms = ops->batch_prepare(B->pe, &B->grid_patch, &B->staged);
+    B->sms = ops->batch_prepare(B->pe, &B->grid_patch);
     if (B->sms <= 0) {
         sgb_batch_destroy(B);
         return bfail(SGB_ERR_CUDA, "sgb_batch_create: kernel attributes");
@@ -556,9 +568,11 @@ int sgb_batch_step(sgb_batch_t* B, int n_steps)
         L.grid_patch = B->grid_patch;
         L.grid_elem = B->sms * 4;
         L.grid_node = B->sms * 4;
+        L.n_slots = B->max_slots;
+        L.grid_slots = std::min(B->max_slots, B->sms * 8);
         L.pe = B->pe;
         L.max_iterations = B->max_iterations;
-        L.staged = B->staged;
+        L.prefetch = B->prefetch;
         L.err = B->d_err;
         cudaGraph_t g;
         BTRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));

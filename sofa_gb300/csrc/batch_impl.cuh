@@ -3,11 +3,12 @@
 // that walks a device-resident work list (patches, element ranges or node
 // chunks of all active meshes); the mesh of an item is found through its
 // slot's BMeshDesc. Per-mesh dot products are reduced without float atomics:
-// every item writes its partial sum, an integer ticket per mesh elects the
-// last item, which adds the mesh's partials in index order and updates that
+// inside the CG loop every item writes its partial sum and a small kernel
+// with one block per mesh slot adds them in index order and updates that
 // mesh's CG scalars (CGLinearSolver::solve, Sofa/Component/LinearSolver/
 // Iterative/src/sofa/component/linearsolver/iterative/CGLinearSolver.inl:
-// 102-272). Meshes whose CG has stopped skip their items.
+// 102-272); the once-per-step start of CG reduces with a per-mesh ticket.
+// Meshes whose CG has stopped skip their items.
 //
 // Included by the variant translation units after tfem_impl.cuh, inside
 // SGB_NS, for R = float (mixed) and R = double (FP64 with FMA).
@@ -16,6 +17,9 @@
 namespace SGB_NS {
 
 constexpr int kBatchThreads = 256;
+#ifndef KB_MATVEC_MIN_BLOCKS
+#define KB_MATVEC_MIN_BLOCKS 6
+#endif
 
 template <typename R>
 __device__ __forceinline__ ElemView<R> bm_elem_view(const BMeshDesc& m)
@@ -76,6 +80,65 @@ __device__ __forceinline__ bool bm_ticket_sum(double mine, double* partials, int
     *total = block_sum(v);
     if (threadIdx.x == 0) *ticket = 0u;
     return true;
+}
+
+// A block's share of one mesh's dot product. Each mesh's items are
+// contiguous in every work list and blocks stride through a list by the grid
+// size, so the items a block takes of one mesh are consecutive in its loop:
+// the block reduces once per mesh, into partial slot `first` (the mesh-local
+// index of its first item of that mesh, which is below min(grid, items of
+// the mesh)). The mesh's ticket counts min(grid, items) arrivals, and the
+// last arrival adds the partials in index order.
+struct BlockRun {
+    int slot;
+    int first;
+    double acc;  // this thread's share
+    __device__ BlockRun() : slot(-1), first(0), acc(0.0) {}
+    __device__ void open(int s, int f)
+    {
+        slot = s;
+        first = f;
+        acc = 0.0;
+    }
+};
+
+__device__ __forceinline__ bool bm_run_sum(const BlockRun& run, double* partials, unsigned int* ticket, int count,
+                                           double* total)
+{
+    const int arrivals = count < (int)gridDim.x ? count : (int)gridDim.x;
+    return bm_ticket_sum(run.acc, partials, run.first, ticket, arrivals, total);
+}
+
+// Stores the block's share of a run at partial slot `first` (no ticket: a
+// later kernel adds the mesh's min(grid, items) partials).
+__device__ __forceinline__ void bm_run_store(const BlockRun& run, double* partials)
+{
+    const double tot = block_sum(run.acc);
+    if (threadIdx.x == 0) partials[run.first] = tot;
+}
+
+// CG start: rho = r.r, |b| (every block that took items of the mesh calls it)
+__device__ __forceinline__ void rhs_done(BMeshDesc& m, const BlockRun& run)
+{
+    double total;
+    if (bm_run_sum(run, m.chunk_sum, &m.ticket_rhs, m.n_chunks, &total) && threadIdx.x == 0) {
+        m.rho = total;
+        m.normb = sqrt(total);
+        m.iters = 0;
+        m.last_err = 0.0;
+        m.den = 0.0;
+        if (!isfinite(total)) {
+            m.status |= 1;
+            m.done = 1;
+        } else if (m.normb == 0.0 || m.cg_iterations <= 0) {
+            m.done = 1;
+        } else {
+            const double err = sqrt(total) / m.normb;
+            m.last_err = err;
+            m.done = (err <= m.tol && m.tsc != 0) ? 1 : 0;
+        }
+    }
+    __syncthreads();
 }
 
 // ---- force: f = ext + m g + internal forces --------------------------------
@@ -161,8 +224,14 @@ __global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, con
                                                                const int* __restrict__ counts)
 {
     const int L = counts[WL_NODE];
+    BlockRun run;
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem it = items[w];
+        if (run.slot >= 0 && it.slot != run.slot) {
+            rhs_done(M[run.slot], run);
+            run.slot = -1;
+        }
+        if (run.slot < 0) run.open(it.slot, it.c);
         BMeshDesc& m = M[it.slot];
         const R* ef = (const R*)m.eforce;
         const R* f = (const R*)m.f;
@@ -198,32 +267,16 @@ __global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, con
             }
             dlocal += (double)(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
         }
-        double total;
-        if (bm_ticket_sum(dlocal, m.chunk_sum, it.c, &m.ticket_rhs, m.n_chunks, &total) && threadIdx.x == 0) {
-            m.rho = total;
-            m.normb = sqrt(total);
-            m.iters = 0;
-            m.last_err = 0.0;
-            m.den = 0.0;
-            if (!isfinite(total)) {
-                m.status |= 1;
-                m.done = 1;
-            } else if (m.normb == 0.0 || m.cg_iterations <= 0) {
-                m.done = 1;
-            } else {
-                const double err = sqrt(total) / m.normb;
-                m.last_err = err;
-                m.done = (err <= m.tol && m.tsc != 0) ? 1 : 0;
-            }
-        }
-        __syncthreads();
+        run.acc += dlocal;
     }
+    if (run.slot >= 0) rhs_done(M[run.slot], run);
 }
 
 // ---- CG matvec over patches ------------------------------------------------
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kPatchThreads, 6) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
-                                                           const int* __restrict__ counts, int it, int pe)
+__global__ void __launch_bounds__(kPatchThreads, KB_MATVEC_MIN_BLOCKS) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                           const int* __restrict__ counts, int it, int pe,
+                                                           int prefetch)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* ef;
@@ -231,49 +284,54 @@ __global__ void __launch_bounds__(kPatchThreads, 6) kb_matvec(BMeshDesc* M, cons
     uint16_t* sl;
     int* lr;
     patch_smem_carve<R>(smem_raw, pe, kBatchMaxLocalNodes, &ef, &sl, &lr, &lp);
+    // the open mesh's views and operands, read where they are used
+    __shared__ PatchView spv;
+    __shared__ ElemView<R> sev;
+    __shared__ PatchArgs<R> sa;
     const int L = counts[WL_PATCH];
+    BlockRun run;
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem wi = items[w];
+        if (run.slot >= 0 && wi.slot != run.slot) {
+            bm_run_store(run, M[run.slot].patch_energy);
+            run.slot = -1;
+        }
         BMeshDesc& m = M[wi.slot];
-        if (bm_cg_skip(m, it)) continue;  // uniform over the block: read before this mesh's last item ends
-        const PatchView pv = bm_patch_view(m, pe);
-        const ElemView<R> ev = bm_elem_view<R>(m);
+        if (bm_cg_skip(m, it)) continue;  // uniform over the block
+        if (run.slot < 0) {
+            run.open(wi.slot, wi.a);
+            // the previous patch ended with a block barrier: no thread still
+            // reads the shared copies
+            if (threadIdx.x == 0) {
+                spv = bm_patch_view(m, pe);
+                sev = bm_elem_view<R>(m);
+                const double mf = m.mf;
+                sa.rin = (const R*)m.r;
+                sa.pold = (const R*)((it & 1) ? m.p1 : m.p0);
+                sa.pnew = (R*)((it & 1) ? m.p0 : m.p1);
+                sa.beta = (MODE == 2) ? (R)m.beta : R(0);
+                sa.kf = (R)m.kf;
+                sa.mmu = (R)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
+                sa.ma = MassArgs{m.node_mass, m.vertex_mass, {m.g[0], m.g[1], m.g[2]}};
+                sa.mf = mf;
+                sa.fixed = m.fixed;
+                sa.qout = (R*)m.q;
+                sa.partials = (R*)m.partials;
+            }
+            __syncthreads();
+        }
         if constexpr (is_mixed<R>::value) {
             // the block's next item into L2 while this one computes
             const int wn = w + (int)gridDim.x;
-            if (threadIdx.x == 0 && wn < L) {
+            if (prefetch && threadIdx.x == 0 && wn < L) {
                 const WorkItem ni = items[wn];
                 const BMeshDesc& nm = M[ni.slot];
                 prefetch_patch(bm_patch_view(nm, pe), bm_elem_view<R>(nm), ni.a);
             }
         }
-        const R beta = (MODE == 2) ? (R)m.beta : R(0);
-        const R* pold = (const R*)((it & 1) ? m.p1 : m.p0);
-        R* pnew = (R*)((it & 1) ? m.p0 : m.p1);
-        const double mf = m.mf;
-        const R mmu = (R)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
-        MassArgs ma{m.node_mass, m.vertex_mass, {m.g[0], m.g[1], m.g[2]}};
-        const R pen = patch_body<R, MODE>(pv, ev, wi.a, (const R*)m.r, pold, pnew, beta, (R)m.kf, ma, mf, mmu,
-                                          m.fixed, (R*)m.q, (R*)m.partials, ef, lp, sl, lr);
-        double total;
-        if (bm_ticket_sum((double)pen, m.patch_energy, wi.a, &m.ticket_den, m.n_patches, &total) &&
-            threadIdx.x == 0) {
-            m.den = total;
-            const bool first_of_first = (it == 1 && m.tsc == 0);
-            if (!isfinite(total)) {
-                m.status |= 1;
-                m.done = 1;
-            } else if (total != 0.0) {
-                if (fabs(total) <= m.thr && !first_of_first)
-                    m.done = 1;
-                else
-                    m.alpha = m.rho / total;
-            } else {
-                m.done = 1;
-            }
-        }
-        __syncthreads();
+        run.acc += (double)patch_body<R, MODE>(spv, sev, wi.a, sa, ef, lp, sl, lr);
     }
+    if (run.slot >= 0) bm_run_store(run, M[run.slot].patch_energy);
 }
 
 // ---- CG update: shared-node q, x += alpha p, r -= alpha q, rho -------------
@@ -282,10 +340,16 @@ __global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const W
                                                            const int* __restrict__ counts, int it)
 {
     const int L = counts[WL_NODE];
+    BlockRun run;
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem wi = items[w];
+        if (run.slot >= 0 && wi.slot != run.slot) {
+            bm_run_store(run, M[run.slot].chunk_sum);
+            run.slot = -1;
+        }
         BMeshDesc& m = M[wi.slot];
         if (bm_cg_skip(m, it)) continue;
+        if (run.slot < 0) run.open(wi.slot, wi.c);
         const R alpha = (R)m.alpha;
         const R* p = (const R*)((it & 1) ? m.p0 : m.p1);
         const R* q = (const R*)m.q;
@@ -310,19 +374,70 @@ __global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const W
                 local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, m.bnd_rowptr, m.node_mass, mmu, mf,
                                                m.fixed, alpha);
         }
-        double total;
-        if (bm_ticket_sum(local, m.chunk_sum, wi.c, &m.ticket_rho, m.n_chunks, &total) && threadIdx.x == 0) {
-            m.rho_prev = m.rho;
-            m.rho = total;
-            m.iters = it;
-            m.beta = total / m.rho_prev;
-            const double err = sqrt(total) / m.normb;
-            m.last_err = err;
-            if (!isfinite(total)) {
-                m.status |= 1;
-                m.done = 1;
-            } else if (err <= m.tol || it >= m.cg_iterations) {
-                m.done = 1;
+        run.acc += local;
+    }
+    if (run.slot >= 0) bm_run_store(run, M[run.slot].chunk_sum);
+}
+
+// ---- per-mesh CG scalars of one iteration ----------------------------------
+// One block per mesh slot adds the mesh's partials (one per block run, at
+// the run's first item index: min(grid, items) of them) in a fixed order
+// (thread-strided, then the block tree). Which items share a partial depends
+// only on the item index modulo the grid, so the sum does not depend on the
+// other meshes of the batch.
+// WHAT 0, after the matvec: den = p.Ap, the threshold test, alpha.
+// WHAT 1, after the update: rho = r.r, beta, the tolerance and iteration tests.
+template <int WHAT>
+__global__ void __launch_bounds__(kBatchThreads) kb_cg_scalars(BMeshDesc* M, int n_slots, int it, int grid_items)
+{
+    for (int s = blockIdx.x; s < n_slots; s += gridDim.x) {
+        BMeshDesc& m = M[s];
+        if (bm_cg_skip(m, it)) continue;  // uniform over the block
+        const double* part = (WHAT == 0) ? m.patch_energy : m.chunk_sum;
+        const int items_m = (WHAT == 0) ? m.n_patches : m.n_chunks;
+        const int n = items_m < grid_items ? items_m : grid_items;  // one partial per block run
+        // thread t adds entries t, t + blockDim, ... in that order; eight
+        // loads are issued before their additions
+        double v = 0.0;
+        for (int i0 = threadIdx.x; i0 < n; i0 += 8 * blockDim.x) {
+            double a[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int i = i0 + j * (int)blockDim.x;
+                a[j] = i < n ? __ldcg(&part[i]) : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v += a[j];
+        }
+        const double total = block_sum(v);
+        if (threadIdx.x == 0) {
+            if (WHAT == 0) {
+                m.den = total;
+                const bool first_of_first = (it == 1 && m.tsc == 0);
+                if (!isfinite(total)) {
+                    m.status |= 1;
+                    m.done = 1;
+                } else if (total != 0.0) {
+                    if (fabs(total) <= m.thr && !first_of_first)
+                        m.done = 1;
+                    else
+                        m.alpha = m.rho / total;
+                } else {
+                    m.done = 1;
+                }
+            } else {
+                m.rho_prev = m.rho;
+                m.rho = total;
+                m.iters = it;
+                m.beta = total / m.rho_prev;
+                const double err = sqrt(total) / m.normb;
+                m.last_err = err;
+                if (!isfinite(total)) {
+                    m.status |= 1;
+                    m.done = 1;
+                } else if (err <= m.tol || it >= m.cg_iterations) {
+                    m.done = 1;
+                }
             }
         }
         __syncthreads();
@@ -362,7 +477,7 @@ size_t batch_patch_smem(int pe)
 }
 
 template <typename R>
-int batch_prepare(int pe, int* grid_patch, int* staged)
+int batch_prepare(int pe, int* grid_patch)
 {
     const size_t smem = batch_patch_smem<R>(pe);
     int dev = 0, sms = 0, nb1 = 0, nb2 = 0;
@@ -375,7 +490,6 @@ int batch_prepare(int pe, int* grid_patch, int* staged)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, kb_matvec<R, 2>, kPatchThreads, smem);
     int nb = nb1 < nb2 ? nb1 : nb2;
     *grid_patch = (nb < 1 ? 1 : nb) * sms;
-    *staged = 0;
     return sms;
 }
 
@@ -392,10 +506,14 @@ void batch_record_step(const BatchLaunch& B, cudaStream_t s)
     const size_t smem = batch_patch_smem<R>(B.pe);
     for (int it = 1; it <= B.max_iterations; ++it) {
         if (it == 1)
-            kb_matvec<R, 1><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe);
+            kb_matvec<R, 1><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe,
+                                                                      B.prefetch);
         else
-            kb_matvec<R, 2><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe);
+            kb_matvec<R, 2><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe,
+                                                                      B.prefetch);
+        kb_cg_scalars<0><<<B.grid_slots, kBatchThreads, 0, s>>>(B.meshes, B.n_slots, it, B.grid_patch);
         kb_update<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
+        kb_cg_scalars<1><<<B.grid_slots, kBatchThreads, 0, s>>>(B.meshes, B.n_slots, it, B.grid_node);
     }
     kb_euler<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
 }

@@ -70,7 +70,8 @@ struct sgb_batch {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
-    int sms = 152, grid_patch = 152, staged = 0;
+    int sms = 152, grid_patch = 152;
+    int prefetch = 0;  // FP32 matvec: the block's next patch into L2 while this one computes (measured slower)
     size_t device_bytes = 0;
 };
 

@@ -246,10 +246,11 @@ struct BatchLaunch {
     BMeshDesc* meshes;
     const WorkItem* items[3];
     const int* counts;
-    int grid_patch, grid_elem, grid_node;
+    int grid_patch, grid_elem, grid_node, grid_slots;
+    int n_slots;  // mesh slots of the batch (the CG scalar kernels take one block per slot)
     int pe;
     int max_iterations;
-    int staged;  // FP32: use the bulk-copy staged matvec
+    int prefetch;  // FP32 matvec: prefetch the block's next patch into L2
     int* err;    // sticky device error flag of the batch
 };
 

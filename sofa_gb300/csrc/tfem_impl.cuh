@@ -1123,14 +1123,28 @@ __device__ __forceinline__ void patch_element(int le, ushort4 c, const R Rm[9], 
     if (MODE != 0) pen -= en;
 }
 
+// Per-call operands of the fused matvec. The single-mesh kernels build it
+// from their parameters; the batch kernel keeps one per mesh in shared
+// memory, so that its pointers are read where they are used instead of
+// being held in registers across the patch.
+template <typename R>
+struct PatchArgs {
+    const R* __restrict__ rin;   // input vector (r for the CG modes)
+    const R* __restrict__ pold;  // previous direction (MODE 2)
+    R* __restrict__ pnew;        // new direction (CG modes)
+    R beta, kf, mmu;
+    MassArgs ma;
+    double mf;
+    const uint8_t* __restrict__ fixed;
+    R* __restrict__ qout;
+    R* __restrict__ partials;
+};
+
 // One patch of the fused matvec, executed by the whole block (it contains
 // block barriers). Returns this thread's share of the patch's p^T A p.
 template <typename R, int MODE>
-__device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& ev, int P, const R* __restrict__ rin,
-                                        const R* __restrict__ pold, R* __restrict__ pnew, R beta, R kf,
-                                        const MassArgs& ma, double mf, R mmu, const uint8_t* __restrict__ fixed,
-                                        R* __restrict__ qout, R* __restrict__ partials, R* ef, R* lp,
-                                        uint16_t* sl, int* lr)
+__device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& ev, int P, const PatchArgs<R>& a, R* ef,
+                                        R* lp, uint16_t* sl, int* lr)
 {
     const size_t En = (size_t)ev.n_tets;
     R pen = R(0);
@@ -1153,15 +1167,15 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         R v[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const R rv = rin[3 * (size_t)g + k];
-            v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
+            const R rv = a.rin[3 * (size_t)g + k];
+            v[k] = (MODE == 2) ? cg_dir(rv, a.pold[3 * (size_t)g + k], a.beta) : rv;
             lp[3 * l + k] = v[k];
         }
         if (MODE != 0) {
             const int info = pv.lnode_info[n0 + l];
             if (info < 0 || (info & 1)) {
 #pragma unroll
-                for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
+                for (int k = 0; k < 3; ++k) a.pnew[3 * (size_t)g + k] = v[k];
             }
         }
     }
@@ -1172,7 +1186,7 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         R Rm[9], K[3], J[12];
         load_rot(ev, e, Rm);
         load_KJ(ev, e, K, J);
-        patch_element<R, MODE>(le, pv.lconn[e], Rm, K, J, kf, pv.pe, lp, ef, pen);
+        patch_element<R, MODE>(le, pv.lconn[e], Rm, K, J, a.kf, pv.pe, lp, ef, pen);
     }
     __syncthreads();
     // phase 2: per local node, its slots in element order
@@ -1189,27 +1203,27 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         const int g = pv.lnode_gid[n0 + l];
         const int info = pv.lnode_info[n0 + l];
         if (info >= 0) {
-            R* o = partials + 3 * (size_t)(info >> 1);
+            R* o = a.partials + 3 * (size_t)(info >> 1);
             o[0] = a0;
             o[1] = a1;
             o[2] = a2;
         }
         if (MODE == 0) {
             if (info < 0) {
-                qout[3 * (size_t)g] -= a0;
-                qout[3 * (size_t)g + 1] -= a1;
-                qout[3 * (size_t)g + 2] -= a2;
+                a.qout[3 * (size_t)g] -= a0;
+                a.qout[3 * (size_t)g + 1] -= a1;
+                a.qout[3 * (size_t)g + 2] -= a2;
             }
         } else if (info < 0 || (info & 1)) {
             const R p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
-            const R mm = ma.node_mass ? (R)(ma.node_mass[g] * mf) : mmu;
+            const R mm = a.ma.node_mass ? (R)(a.ma.node_mass[g] * a.mf) : a.mmu;
             pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
             if (info < 0) {
                 R q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
-                if (fixed[g]) q0 = q1 = q2 = R(0);
-                qout[3 * (size_t)g] = q0;
-                qout[3 * (size_t)g + 1] = q1;
-                qout[3 * (size_t)g + 2] = q2;
+                if (a.fixed[g]) q0 = q1 = q2 = R(0);
+                a.qout[3 * (size_t)g] = q0;
+                a.qout[3 * (size_t)g + 1] = q1;
+                a.qout[3 * (size_t)g + 2] = q2;
             }
         }
     }
@@ -1238,13 +1252,13 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
     if (MODE == 0 && cg && cg->iters != sc.it) return;
     const R beta = (MODE == 2) ? (R)cg->beta : R(0);
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    const PatchArgs<R> args{rin, pold, pnew, beta, kf, mmu, ma, mf, fixed, qout, partials};
     double energy = 0.0;  // FP64 across patches; FP32 within one patch
     for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
         if constexpr (is_mixed<R>::value)
             if (prefetch && threadIdx.x == 0 && P + (int)gridDim.x < pv.n_patches)
                 prefetch_patch(pv, ev, P + gridDim.x);
-        energy += (double)patch_body<R, MODE>(pv, ev, P, rin, pold, pnew, beta, kf, ma, mf, mmu, fixed, qout,
-                                              partials, ef, lp, sl, lr);
+        energy += (double)patch_body<R, MODE>(pv, ev, P, args, ef, lp, sl, lr);
     }
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
@@ -1265,10 +1279,9 @@ __global__ void __launch_bounds__(kPatchThreads, sizeof(R) == 4 ? 10 : 1)
     int* lr;
     patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
     if (gate && gate->iters != gate_it) return;
-    const MassArgs none{nullptr, 0.0, {0.0, 0.0, 0.0}};
-    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
-        (void)patch_body<R, 0>(pv, ev, P, dx, nullptr, nullptr, R(0), kf, none, 1.0, R(0), nullptr, df, partials, ef,
-                               lp, sl, lr);
+    const PatchArgs<R> args{dx, nullptr, nullptr, R(0), kf, R(0), {nullptr, 0.0, {0.0, 0.0, 0.0}}, 1.0, nullptr, df,
+                            partials};
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) (void)patch_body<R, 0>(pv, ev, P, args, ef, lp, sl, lr);
 }
 
 // ------------------------------------------------------------------------

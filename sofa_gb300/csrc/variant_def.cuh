@@ -36,13 +36,13 @@ static void v_scene_step(Scene* sc, double* terms, int mass_first, cudaStream_t 
 }
 static int v_prepare(TfemMesh* m) { return m->pl.n_patches > 0 ? prepare_patch<SGB_REAL>(m) : 0; }
 #if SGB_USES_PATCHES
-static int v_batch_prepare(int pe, int* grid_patch, int* staged)
+static int v_batch_prepare(int pe, int* grid_patch)
 {
-    return batch_prepare<SGB_REAL>(pe, grid_patch, staged);
+    return batch_prepare<SGB_REAL>(pe, grid_patch);
 }
 static void v_batch_record(const BatchLaunch& b, cudaStream_t s) { batch_record_step<SGB_REAL>(b, s); }
 #else
-static int (*const v_batch_prepare)(int, int*, int*) = nullptr;
+static int (*const v_batch_prepare)(int, int*) = nullptr;
 static void (*const v_batch_record)(const BatchLaunch&, cudaStream_t) = nullptr;
 #endif
 }  // namespace SGB_NS

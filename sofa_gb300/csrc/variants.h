@@ -17,7 +17,7 @@ struct VariantOps {
     void (*scene_step)(Scene*, double* dot_terms, int mass_first, cudaStream_t);
     int (*prepare)(TfemMesh*);  // kernel attributes; returns the patch-kernel grid
     // batch engine (null for the reference-rounding variant)
-    int (*batch_prepare)(int pe, int* grid_patch, int* staged);  // returns the SM count, -1 on failure
+    int (*batch_prepare)(int pe, int* grid_patch);  // returns the SM count, -1 on failure
     void (*batch_record)(const BatchLaunch&, cudaStream_t);
 };
 
