@@ -131,8 +131,8 @@ static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool no
     c.add((void**)&d.K, rs * 3 * E);
     c.add((void**)&d.J, rs * 12 * E);
     c.add((void**)&d.rest, rs * 12 * E);
-    d.rest64 = nullptr;
-    if (rs == sizeof(float)) c.add((double**)&d.rest64, sizeof(double) * 12 * E);
+    d.rest_ff = nullptr;
+    if (rs == sizeof(float)) c.add((float2**)&d.rest_ff, sizeof(float2) * 9 * E);
     c.add(&d.eforce, rs * 12 * E);
     c.add((int**)&d.rowptr, sizeof(int) * (N + 1));
     c.add((int**)&d.slots, sizeof(int) * 4 * (size_t)E);
@@ -462,7 +462,7 @@ int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot_out)
     tmp.K = (void*)d.K;
     tmp.J = (void*)d.J;
     tmp.rest = (void*)d.rest;
-    tmp.rest64 = const_cast<double*>(d.rest64);
+    tmp.rest_ff = const_cast<float2*>(d.rest_ff);
     tmp.R0 = d.eforce;  // the initial rotation is not kept: the scratch takes it
     tmp.rest_pos = (double*)d.rest_pos;
     tmp.elem_orig = d_elem_orig;

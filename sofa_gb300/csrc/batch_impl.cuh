@@ -30,7 +30,7 @@ __device__ __forceinline__ ElemView<R> bm_elem_view(const BMeshDesc& m)
     ev.K = (const R*)m.K;
     ev.J = (const R*)m.J;
     ev.rest = (const R*)m.rest;
-    ev.rest64 = m.rest64;
+    ev.rest_ff = m.rest_ff;
     ev.n_tets = m.n_tets;
     ev.method = m.method;
     return ev;

@@ -99,7 +99,7 @@ static void free_mesh(TfemMesh& m)
     cudaFree(m.K);
     cudaFree(m.J);
     cudaFree(m.rest);
-    cudaFree(m.rest64);
+    cudaFree(m.rest_ff);
     cudaFree(m.R0);
     cudaFree(m.rest_pos);
     cudaFree(m.rowptr);
@@ -227,7 +227,7 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
         (rc = dev_alloc_bytes(&m.eforce, rs * 12 * E, acc)) || (rc = dev_alloc(&m.rest_pos, 3 * (size_t)n_nodes, acc)) ||
         (rc = dev_alloc(&m.rowptr, (size_t)n_nodes + 1, acc)) || (rc = dev_alloc(&m.slots, 4 * E, acc)) ||
         (rc = dev_alloc(&m.elem_orig, E, acc)) || (rc = dev_alloc(&m.dev_flags, 1, acc)) ||
-        (precision == SGB_PRECISION_MIXED && method != SGB_METHOD_SMALL && (rc = dev_alloc(&m.rest64, 12 * E, acc))))
+        (precision == SGB_PRECISION_MIXED && method != SGB_METHOD_SMALL && (rc = dev_alloc(&m.rest_ff, 9 * E, acc))))
         goto fail_out;
     if ((ce = cudaMemsetAsync(m.dev_flags, 0, sizeof(int), h->stream)) != cudaSuccess) {
         rc = cuda_fail(ce, "cudaMemsetAsync");

@@ -33,7 +33,7 @@ struct ElemView {
     const R* K;        // 3 rows: K(0,0), K(0,1), K(3,3) of the 6x6 material stiffness / (36 V)
     const R* J;        // 12 rows: the distinct values of the 12x6 strain-displacement matrix
     const R* rest;     // 12 rows: rotated rest coordinates (method dependent, see tfem.cu)
-    const double* rest64;  // mixed: the same 12 rows in FP64 for the force kernel (or null)
+    const float2* rest_ff;  // mixed: rows 3..11 (b-a, c-a, d-a) as float-float pairs for the force kernel (or null)
     int n_tets;
     int method;
 };
@@ -87,7 +87,7 @@ struct TfemMesh {
     void* K = nullptr;
     void* J = nullptr;
     void* rest = nullptr;
-    double* rest64 = nullptr; // mixed: rest coordinates in FP64 (12 rows), read by the force kernel
+    float2* rest_ff = nullptr;  // mixed: rest coordinates b-a, c-a, d-a (9 rows) as float-float pairs
     void* R0 = nullptr;       // initial rotation rows (for the rotation getter)
     double* rest_pos = nullptr;  // rest positions (FP64, n_nodes*3), used by method=small
     int* rowptr = nullptr;
@@ -199,7 +199,7 @@ struct BMeshDesc {
     const void* K;
     const void* J;
     const void* rest;
-    const double* rest64;
+    const float2* rest_ff;
     void* eforce;
     // node -> (element*4+corner) gather table
     const int* rowptr;

@@ -137,74 +137,83 @@ __device__ __forceinline__ void quat_to_rot(float4 q, float Rm[9])
     Rm[8] = sg * (1.f - 2.f * (xx + yy));
 }
 
-// One Newton step of the polar iteration X <- (X + X^-T) / 2 in FP64 (X^-T
-// is the cofactor matrix over the determinant): from a rotation accurate to
-// FP32 it gives a matrix orthonormal to FP64 precision.
-//
-// FP64 reciprocal and reciprocal square root by Newton-Raphson iteration from
-// the FP32 hardware estimate (y <- y (2 - a y) and y <- y (3 - a y^2) / 2;
-// each step doubles the number of correct digits, two steps take the ~1e-7
-// estimate to FP64 precision): a few FP64 fused multiply-adds instead of the
-// long FP64 division and square-root sequences, which the FP64 pipe of this
-// GPU runs at a small fraction of the FP32 rate.
-__device__ __forceinline__ double rcp_nr(double a)
+// ---- float-float arithmetic for the mixed-precision strain ----------------
+// The strain D = rest - R e is a small difference of edge-sized terms, so the
+// mixed variant forms it with about 47 significant bits: values are carried
+// as unevaluated sums hi + lo of two floats, built from the error-free
+// transformations TwoSum (Knuth) and TwoProduct (one FMA). GB300 runs FP64
+// arithmetic and FP64<->FP32 conversions at about 2 per clock per SM against
+// 128 FP32 FMAs, so none of this touches the FP64 pipe.
+struct ff {
+    float h, l;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b)
 {
-    double y = (double)(1.0f / (float)a);
-    y = y * (2.0 - a * y);
-    y = y * (2.0 - a * y);
-    return y;
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
 }
 
-__device__ __forceinline__ double rsqrt_nr(double a)
+__device__ __forceinline__ ff two_prod(float a, float b)
 {
-    double y = (double)rsqrtf((float)a);
-    y = y * (1.5 - 0.5 * a * y * y);
-    y = y * (1.5 - 0.5 * a * y * y);
-    return y;
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
 }
 
-__device__ __forceinline__ void orthonormalize_newton(double X[9])
+// FP64 -> hi + lo floats by bit manipulation (integer pipe only): hi keeps
+// the leading 24 significant bits, lo the next 23 (both truncated), so
+// hi + lo equals v to 2^-47 relative. Below 2^-80 in magnitude lo is zero
+// and below 2^-126 the value is flushed to zero; from 2^128 on (and for
+// infinities and NaNs) the value goes through the FP64 conversion, which
+// keeps non-finite states visible.
+__device__ __forceinline__ ff split_f64(double v)
 {
-    const double c[9] = {X[4] * X[8] - X[5] * X[7], X[5] * X[6] - X[3] * X[8], X[3] * X[7] - X[4] * X[6],
-                         X[7] * X[2] - X[8] * X[1], X[8] * X[0] - X[6] * X[2], X[6] * X[1] - X[7] * X[0],
-                         X[1] * X[5] - X[2] * X[4], X[2] * X[3] - X[0] * X[5], X[0] * X[4] - X[1] * X[3]};
-    const double det = X[0] * c[0] + X[1] * c[1] + X[2] * c[2];
-    const double h = 0.5 * rcp_nr(det);
+    const unsigned hw = (unsigned)__double2hiint(v);
+    const unsigned lw = (unsigned)__double2loint(v);
+    const int E = (int)((hw >> 20) & 0x7FFu);
+    const unsigned sgn = hw & 0x80000000u;
+    if ((unsigned)(E - 897) > 253u) {
+        if (E < 897) return {__uint_as_float(sgn), 0.f};
+        return {__double2float_rn(v), 0.f};
+    }
+    const unsigned mant = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
+    const float h = __uint_as_float(sgn | ((unsigned)(E - 896) << 23) | mant);
+    // the next 23 mantissa bits as an integer r < 2^23, worth r * 2^(E - 1069)
+    const unsigned r = (lw & 0x1FFFFFFFu) >> 6;
+    const float rf = __uint_as_float(0x4B000000u | r) - 8388608.0f;
+    const int k = E - 1069;
+    const float scale = k >= -126 ? __uint_as_float((unsigned)(k + 127) << 23) : 0.f;
+    const float l = rf * scale;
+    return {h, sgn ? -l : l};
+}
+
+// One Newton step of the polar iteration X <- (X + X^-T) / 2 = X/2 + cof(X)
+// / (2 det X) on an FP32 matrix X that is a rotation to FP32 precision; the
+// result X + dX is orthonormal to about 1e-14. The cofactors and the
+// determinant are formed in float-float; dX (of the size of X's rounding)
+// then needs only FP32: with det = 1 + d,
+// dX = (cof - X)/2 + (d^2 - d) cof / 2.
+__device__ __forceinline__ void orthonormalize_ff(const float X[9], float dX[9])
+{
+    const int cidx[9][4] = {{4, 8, 5, 7}, {5, 6, 3, 8}, {3, 7, 4, 6}, {7, 2, 8, 1}, {8, 0, 6, 2},
+                            {6, 1, 7, 0}, {1, 5, 2, 4}, {2, 3, 0, 5}, {0, 4, 1, 3}};
+    ff c[9];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) X[i] = 0.5 * X[i] + h * c[i];
-}
-
-// The QR frame of computeRotationLarge (TFEM.inl:755-778) in FP64, with the
-// normalisations by rsqrt_nr: rows = unit edge ab, in-plane unit vector,
-// unit normal. Degenerate edges (squared length below the FP64 epsilon) are
-// left unscaled, as Vec::normalize does.
-__device__ __forceinline__ void rotation_large_f64(const double eab[3], const double eac[3], double R[9])
-{
-    double ex[3] = {eab[0], eab[1], eab[2]};
-    const double nx = ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2];
-    if (nx > 4.930380657631324e-32) {
-        const double s = rsqrt_nr(nx);
-        ex[0] *= s;
-        ex[1] *= s;
-        ex[2] *= s;
+    for (int i = 0; i < 9; ++i) {
+        const ff p = two_prod(X[cidx[i][0]], X[cidx[i][1]]);
+        const ff q = two_prod(X[cidx[i][2]], X[cidx[i][3]]);
+        const ff s = two_sum(p.h, -q.h);
+        c[i] = {s.h, s.l + (p.l - q.l)};
     }
-    double ez[3];
-    cross3(ex, eac, ez);
-    const double nz = ez[0] * ez[0] + ez[1] * ez[1] + ez[2] * ez[2];
-    if (nz > 4.930380657631324e-32) {
-        const double s = rsqrt_nr(nz);
-        ez[0] *= s;
-        ez[1] *= s;
-        ez[2] *= s;
-    }
-    double ey[3];
-    cross3(ez, ex, ey);
+    const ff t0 = two_prod(X[0], c[0].h), t1 = two_prod(X[1], c[1].h), t2 = two_prod(X[2], c[2].h);
+    const ff s01 = two_sum(t0.h, t1.h);
+    const ff s = two_sum(s01.h, t2.h);
+    const float lo = s01.l + s.l + t0.l + t1.l + t2.l + X[0] * c[0].l + X[1] * c[1].l + X[2] * c[2].l;
+    const float d = (s.h - 1.0f) + lo;  // s.h is within 2^-20 of 1: exact subtraction
+    const float g = 0.5f * (d * d - d);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        R[k] = ex[k];
-        R[3 + k] = ey[k];
-        R[6 + k] = ez[k];
-    }
+    for (int i = 0; i < 9; ++i) dX[i] = 0.5f * ((c[i].h - X[i]) + c[i].l) + g * c[i].h;
 }
 
 template <typename R>
@@ -272,7 +281,7 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
                                 const int* __restrict__ elem_orig, int E, int method,
                                 const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
                                 int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest,
-                                double* rest64, R* rot,
+                                float2* rest_ff, R* rot,
                                 R* R0, double* vol)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -360,8 +369,11 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
         for (int i = 0; i < 9; ++i) rot[(size_t)i * En + s] = (R)Rm[i];
     }
     for (int i = 0; i < 12; ++i) rest[(size_t)i * En + s] = (R)rr[i];
-    if (rest64)
-        for (int i = 0; i < 12; ++i) rest64[(size_t)i * En + s] = rr[i];
+    if (rest_ff)  // rows b-a, c-a, d-a (rr[0..2] are zero) as float-float pairs
+        for (int i = 3; i < 12; ++i) {
+            const float hi = (float)rr[i];
+            rest_ff[(size_t)(i - 3) * En + s] = make_float2(hi, (float)(rr[i] - (double)hi));
+        }
     for (int i = 0; i < 9; ++i) R0[(size_t)i * En + s] = (R)Rm[i];
 }
 
@@ -455,50 +467,65 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
             for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
         }
     } else {
-        // mixed: edges are formed in FP64 and rounded once, the element math
-        // runs in FP32 on positions relative to node a
-        R ed[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) ed[i][k] = (R)(p[i + 1][k] - p[0][k]);
-        if (ev.rest64) {
-            // The strain D = rest - R e is a small difference of edge-sized
-            // terms: it is formed in FP64 from FP64 rest coordinates and
-            // edges with a rotation orthonormal to FP64 precision (large:
-            // the QR frame built in FP64, whose zero components D[4], D[5],
-            // D[8] are then exact; polar: the FP32 polar factor plus one
-            // Newton step X <- (X + X^-T)/2 in FP64). A residual error of R
-            // that is a rotation adds no first-order strain; a
-            // non-orthonormal R (FP32 rounding) would add strain noise of the
-            // size of the edges' FP32 rounding, which on stiff, lightly
-            // loaded meshes is as large as the load itself.
-            double ee[3][3], Rd[9];
+        if (ev.rest_ff) {
+            // mixed: D = rest - R e is a small difference of edge-sized terms,
+            // formed in float-float (about 47 bits) from the FP64 edges and
+            // float-float rest coordinates. R is the FP32 frame (large: the QR
+            // frame, polar: the polar factor) made orthonormal to ~1e-14 by one
+            // float-float Newton step. A residual error of R that is a rotation
+            // adds no first-order strain, so all nine components of D are
+            // computed (for large the reference's zero components D[4], D[5],
+            // D[8] come out at that rotation's size instead of being forced to
+            // zero, which would leave them inconsistent with R); a
+            // non-orthonormal R would add strain noise of the size of the
+            // edges' FP32 rounding, on stiff, lightly loaded meshes as large as
+            // the load itself.
+            // edges: one FP64 subtraction each (exact to the edge's own
+            // rounding, however far the mesh is from the origin), then split
+            ff eg[3][3];
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int k = 0; k < 3; ++k) ee[i][k] = p[i + 1][k] - p[0][k];
+                for (int k = 0; k < 3; ++k) eg[i][k] = split_f64(p[i + 1][k] - p[0][k]);
+            float X[9], dX[9];
             if (METHOD == METHOD_LARGE) {
-                rotation_large_f64(ee[0], ee[1], Rd);
+                const float eab[3] = {eg[0][0].h, eg[0][1].h, eg[0][2].h};
+                const float eac[3] = {eg[1][0].h, eg[1][1].h, eg[1][2].h};
+                rotation_large(eab, eac, X);
             } else {
-                R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
-                polar3(A, Rm);
-#pragma unroll
-                for (int i = 0; i < 9; ++i) Rd[i] = (double)Rm[i];
-                orthonormalize_newton(Rd);
+                float A[9] = {eg[0][0].h, eg[0][1].h, eg[0][2].h, eg[1][0].h, eg[1][1].h,
+                              eg[1][2].h, eg[2][0].h, eg[2][1].h, eg[2][2].h};
+                polar3(A, X);
             }
+            orthonormalize_ff(X, dX);
 #pragma unroll
-            for (int i = 0; i < 9; ++i) Rm[i] = (R)Rd[i];
+            for (int i = 0; i < 9; ++i) Rm[i] = X[i] + dX[i];
             D[0] = D[1] = D[2] = R(0);
 #pragma unroll
             for (int i = 1; i < 4; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const double d =
-                        Rd[3 * k] * ee[i - 1][0] + Rd[3 * k + 1] * ee[i - 1][1] + Rd[3 * k + 2] * ee[i - 1][2];
-                    D[3 * i + k] = (R)(ev.rest64[(size_t)(3 * i + k) * En + e] - d);
+                    const float* xr = &X[3 * k];
+                    const float* dr = &dX[3 * k];
+                    const ff* ei = eg[i - 1];
+                    const ff t0 = two_prod(xr[0], ei[0].h), t1 = two_prod(xr[1], ei[1].h);
+                    const ff t2 = two_prod(xr[2], ei[2].h);
+                    const ff s01 = two_sum(t0.h, t1.h);
+                    const ff s = two_sum(s01.h, t2.h);
+                    float lo = s01.l + s.l + t0.l + t1.l + t2.l;
+                    lo += xr[0] * ei[0].l + xr[1] * ei[1].l + xr[2] * ei[2].l;
+                    lo += dr[0] * ei[0].h + dr[1] * ei[1].h + dr[2] * ei[2].h;
+                    const float2 rv = ev.rest_ff[(size_t)(3 * (i - 1) + k) * En + e];
+                    D[3 * i + k] = (rv.x - s.h) + (rv.y - lo);
                 }
         } else {
+            // mixed without float-float rest coordinates: edges formed in FP64
+            // and rounded once, the strain in FP32 on positions relative to node a
+            R ed[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) ed[i][k] = (R)(p[i + 1][k] - p[0][k]);
             if (METHOD == METHOD_LARGE) {
                 rotation_large(ed[0], ed[1], Rm);
             } else {
@@ -513,8 +540,8 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
                     R d = Rm[3 * k] * ed[i - 1][0] + Rm[3 * k + 1] * ed[i - 1][1] + Rm[3 * k + 2] * ed[i - 1][2];
                     D[3 * i + k] = rr[3 * i + k] - d;
                 }
+            if (METHOD == METHOD_LARGE) D[4] = D[5] = D[8] = R(0);
         }
-        if (METHOD == METHOD_LARGE) D[4] = D[5] = D[8] = R(0);
     }
     store_rot(ev, (size_t)e, Rm);
     element_force_nofact(F, D, K, J);
@@ -1801,7 +1828,7 @@ ElemView<R> view(TfemMesh* m)
     ev.K = (const R*)m->K;
     ev.J = (const R*)m->J;
     ev.rest = (const R*)m->rest;
-    ev.rest64 = m->rest64;
+    ev.rest_ff = m->rest_ff;
     ev.n_tets = m->n_tets;
     ev.method = m->method;
     return ev;
@@ -1814,7 +1841,7 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
     if (m->n_tets == 0) return;
     k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
         m->rest_pos, m->tets, m->elem_orig, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K,
-        (R*)m->J, (R*)m->rest, m->rest64, (R*)m->rot, (R*)m->R0, vol);
+        (R*)m->J, (R*)m->rest, m->rest_ff, (R*)m->rot, (R*)m->R0, vol);
 }
 
 template <typename R>

@@ -94,6 +94,26 @@ def test_add_force_add_dforce_per_call(torch_cuda, capi, oracle, method, precisi
         np.testing.assert_allclose(rot[::97], ref_rot, rtol=0, atol=tol)
 
 
+@pytest.mark.parametrize("method", ["large", "polar"])
+def test_mixed_add_force_small_strain(torch_cuda, capi, oracle, method):
+    """Mixed addForce at strains of 1e-5..5e-5 on a rotated, translated beam.
+    The strain is formed in float-float, so the force matches the FP64
+    oracle to the FP32 element arithmetic; FP32 edges and an FP32 rotation
+    alone would leave strain noise of ~1e-7 absolute, ~1e-2 of this load."""
+    mesh = cases.beam_mesh()
+    p = mesh.positions
+    u = 1e-5 * np.stack([np.sin(1.3 * p[:, 2]), np.cos(0.7 * p[:, 0]) * p[:, 2], 0.5 * p[:, 1] * p[:, 2]], 1)
+    ax = np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
+    kx = np.array([[0.0, -ax[2], ax[1]], [ax[2], 0.0, -ax[0]], [-ax[1], ax[0], 0.0]])
+    rot = np.eye(3) + np.sin(0.3) * kx + (1.0 - np.cos(0.3)) * kx @ kx
+    x = (p + u) @ rot.T + np.array([7.0, -3.0, 11.0])
+    f0, f_gpu, _, _, _ = run_calls(torch_cuda, capi, mesh, method, "mixed", x, np.zeros_like(x), -0.001)
+    ofem = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, method)
+    f_ref = ofem.add_force(x, f0)
+    err = cases.rel_err(f_gpu - f0, f_ref - f0)
+    assert err <= 1e-4, err
+
+
 def test_scene_100_steps_bit_identical_with_serial_dots(torch_cuda, capi, oracle):
     """FP64 with serial dot products reproduces the reference's rounding
     sequence: positions after 100 steps are bit-identical to the oracle."""
