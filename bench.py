@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: build the mixed scene, run warm-up + steps, print a short line")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="profiling run of the batched workload alone: admission, warm-up + steps, a short line")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-beam batched workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--no-ill-conditioned", action="store_true", help="skip the stiff-inclusion workload")
@@ -505,6 +507,14 @@ def main():
 
     build.build()
     capi.load()
+    if args.profile_batched:
+        beams = beam_population(args.beams, seed=3)
+        b = capi.Batch("mixed", budget_bytes=int(60e9), max_meshes=args.beams + 8, max_cg_iterations=25)
+        b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=min(16, host_threads()))
+        b.step(args.warmup + args.steps)
+        b.sync()
+        print(json.dumps({"profile_run": True, "batched": b.info()}))
+        return 0
     mesh = make_mesh(cfg)
     E, N = mesh.n_tets, mesh.n_nodes
     hbm_peak, peak_kind = peaks()
