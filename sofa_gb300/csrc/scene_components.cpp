@@ -3,6 +3,7 @@
 // that turns a node holding an EulerImplicitSolver into a library scene.
 #include <algorithm>
 #include <cmath>
+#include <fstream>
 #include <set>
 #include <sstream>
 
@@ -417,6 +418,129 @@ int unsupported(std::string* err, const std::string& m)
     return SGB_ERR_NOT_SUPPORTED;
 }
 
+// WriteState (Sofa/Component/Playback/src/sofa/component/playback/
+// WriteState.inl: Data 36-46, init 73-220, handleEvent 240-380): at the
+// beginning of every step whose time reaches the next export time (or, once
+// the first export is done, the previous one plus the period) it appends
+// "T= t" and the selected vectors of its node's MechanicalObject, each as
+// "  X= x0 y0 z0 x1 y1 z1 ..." in default stream formatting (Vec and vector
+// stream operators, Vec.h:765-771, vector_T.h:121-130). Without `time` and
+// `period` it writes every step from t = 0. The kinetic-energy stop
+// (stopAt) and the force vector (writeF) are not available.
+class WriteState : public PermissiveObject {
+public:
+    WriteState() : PermissiveObject("WriteState")
+    {
+        declare("filename", "", "output file name");
+        declare("writeX", "1", "flag enabling output of X vector");
+        declare("writeX0", "0", "flag enabling output of X0 vector");
+        declare("writeV", "0", "flag enabling output of V vector");
+        declare("writeF", "0", "flag enabling output of F vector (not available)");
+        declare("time", "", "set time to write outputs (by default export at t=0)");
+        declare("period", "0", "period between outputs");
+        declare("DOFsX", "", "set the position DOFs to write");
+        declare("DOFsV", "", "set the velocity DOFs to write");
+        declare("stopAt", "0", "stop the simulation when the given threshold is reached (not available)");
+        declare("keperiod", "0", "set the period to measure the kinetic energy increase");
+    }
+
+    void init(Scene& s) override
+    {
+        valid = true;
+        periodic = false;
+        next = 0;
+        last_time = 0.0;
+        first_export = false;
+        times = is_set("time") ? get_reals(s, "time") : std::vector<double>();
+        period = get_real(s, "period");
+        if (is_set("period")) {
+            periodic = true;
+            if (times.empty()) times.assign(1, 0.0);
+            if (times.size() > 1) times.resize(1);
+        } else if (!is_set("time")) {
+            period = s.dt;
+            periodic = true;
+        }
+        if (!is_set("time")) {
+            times.assign(1, 0.0);
+        } else {
+            for (size_t i = 0; i < times.size(); ++i)
+                if (times[i] < 0.0 || (times[i] == 0.0 && i > 0)) {
+                    s.warnings.push_back("WriteState '" + name + "': export times must be positive; no export");
+                    valid = false;
+                }
+        }
+        path = get_string("filename");
+        if (path.empty()) path = "defaultExportFile";
+    }
+
+    // AnimateBeginEvent at simulation time t: writes the state if due.
+    int begin_step(Scene& s, double t, std::string* err)
+    {
+        if (!valid) return SGB_OK;
+        if (get_bool(s, "writeF")) return unsupported(err, "WriteState '" + name + "': writeF is not available");
+        if (get_real(s, "stopAt") > 0.0)
+            return unsupported(err, "WriteState '" + name + "': stopAt (kinetic-energy stop) is not available");
+        bool write_now = false;
+        const double eps = 0.1 * s.dt;
+        if (next < times.size()) {
+            last_time = times[next];
+            if (t > last_time || std::fabs(t - last_time) < eps) {
+                write_now = true;
+                first_export = true;
+                ++next;
+            }
+        } else if (first_export && periodic) {
+            const double nt = last_time + period;
+            if (t > nt || std::fabs(t - nt) < eps) {
+                write_now = true;
+                last_time += period;
+            }
+        }
+        if (!write_now) return SGB_OK;
+        Body* body = nullptr;
+        for (auto& b : s.bodies)
+            if (b.node == context) body = &b;
+        if (!body) return unsupported(err, "WriteState '" + name + "': no simulated MechanicalObject in its node");
+        if (!out.is_open()) {
+            out.open(path, std::ios::out | std::ios::trunc);
+            if (!out.is_open()) return unsupported(err, "WriteState '" + name + "': cannot create " + path);
+        }
+        const size_t n = body->rest.size() / 3;
+        std::vector<double> x(3 * n), v(3 * n);
+        int rc = sgb_scene_get_state(body->scene, x.data(), v.data());
+        if (rc) {
+            *err = sgb_last_error();
+            return rc;
+        }
+        out << "T= " << t << "\n";
+        if (get_bool(s, "writeX")) write_vec("  X= ", x);
+        if (get_bool(s, "writeX0")) write_vec("  X0= ", body->rest);
+        if (get_bool(s, "writeV")) write_vec("  V= ", v);
+        out.flush();
+        return SGB_OK;
+    }
+
+private:
+    void write_vec(const char* tag, const std::vector<double>& a)
+    {
+        out << tag;
+        for (size_t i = 0; i < a.size(); ++i) {
+            if (i) out << " ";
+            out << a[i];
+        }
+        out << "\n";
+    }
+
+    bool valid = false, periodic = false, first_export = false;
+    std::vector<double> times;
+    double period = 0.0, last_time = 0.0;
+    size_t next = 0;
+    std::string path;
+    std::ofstream out;
+};
+
+
 // Lumped tetrahedral masses (DiagonalMass.inl:332-376 for massDensity,
 // :1221-1257 for totalMass: masses at density 1, then scaled by
 // totalMass / their sum).
@@ -631,20 +755,38 @@ int Scene::init_device(std::string* err)
     return SGB_OK;
 }
 
+static void collect_writers(Node* n, std::vector<WriteState*>& out)
+{
+    for (auto& o : n->objects)
+        if (auto* w = dynamic_cast<WriteState*>(o.get())) out.push_back(w);
+    for (auto& c : n->children) collect_writers(c.get(), out);
+}
+
 int Scene::animate(int n_steps, std::string* err)
 {
     if (!device_ready) {
         int rc = init_device(err);
         if (rc) return rc;
     }
-    for (auto& b : bodies) {
-        int rc = sgb_scene_step(b.scene, n_steps);
-        if (rc) {
-            *err = sgb_last_error();
-            return rc;
+    std::vector<WriteState*> writers;
+    if (root) collect_writers(root.get(), writers);
+    // with state writers the steps go one at a time, each preceded by the
+    // writers' animate-begin check; otherwise in one call per body
+    const int chunk = writers.empty() ? n_steps : 1;
+    for (int done = 0; done < n_steps; done += chunk) {
+        for (auto* w : writers) {
+            int rc = w->begin_step(*this, time, err);
+            if (rc) return rc;
         }
+        for (auto& b : bodies) {
+            int rc = sgb_scene_step(b.scene, chunk);
+            if (rc) {
+                *err = sgb_last_error();
+                return rc;
+            }
+        }
+        time += dt * chunk;
     }
-    time += dt * n_steps;
     return SGB_OK;
 }
 
@@ -675,6 +817,7 @@ void register_components(ObjectFactory& f)
     f.register_object("EulerImplicitSolver", "implicit Euler integration", mod, make<EulerImplicitSolver>());
     f.register_object("CGLinearSolver", "matrix-free conjugate gradient", mod, make<CGLinearSolver>());
     f.register_object("DefaultAnimationLoop", "animation loop", mod, make<DefaultAnimationLoop>());
+    f.register_object("WriteState", "state export (T= / X= / V= lines)", mod, make<WriteState>());
 }
 
 }  // namespace scn

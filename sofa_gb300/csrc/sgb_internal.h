@@ -102,6 +102,8 @@ struct TfemMesh {
     int adddforce_grid = 0;   // CTAs of the addDForce patch kernel (128 threads)
     int patch_prefetch = 0;   // 1: each CTA prefetches its next patch into L2
     int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads
+    int update_minb = 4;      // CG update: resident CTAs per SM the register cap is set for
+    int update_grid = 0;      // CG update grid; 0: one thread per group of four nodes
     bool staged = false;      // FP32: the patch kernels stage element data with bulk copies
     int staged_grid = 0;      // CTAs of the staged patch kernels
     int* dev_flags = nullptr; // sticky device error flag: 1 = a bounded device wait ran out

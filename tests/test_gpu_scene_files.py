@@ -63,3 +63,44 @@ def test_mixed_scene_file_against_its_fp64_run(capi):
     # unconverged CG iterations: the FP32 and FP64 Krylov sequences part by
     # 1.6e-4 of the positions after 50 steps (measured on a GB300)
     assert np.linalg.norm(xm - xd) / np.linalg.norm(xd) <= 5e-4
+
+
+def _records(path):
+    """WriteState file -> [(t, {tag: values})]."""
+    recs = []
+    with open(path) as f:
+        for line in f:
+            line = line.strip()
+            if line.startswith("T="):
+                recs.append((float(line.split()[1]), {}))
+            elif line:
+                tag, _, vals = line.partition("=")
+                recs[-1][1][tag] = np.array([float(v) for v in vals.split()]).reshape(-1, 3)
+    return recs
+
+
+def test_write_state_records(capi, tmp_path):
+    """WriteState (WriteState.inl:240-380): without time/period it writes at
+    the beginning of every step from t = 0; with time="0.02" period="0.03"
+    it writes at 0.02, 0.05, 0.08. X0 is the rest position, X the state at
+    the record's time, in default stream formatting (6 significant digits)."""
+    text = _read("grid_fem_4x10x4.scn")
+    every = str(tmp_path / "every.txt")
+    timed = str(tmp_path / "timed.txt")
+    ws = (f'<WriteState filename="{every}" writeX0="1" writeV="1" />\n'
+          f'        <WriteState name="w2" filename="{timed}" time="0.02" period="0.03" />\n'
+          '        <TetrahedronFEMForceField')
+    s = capi.SofaScene(text.replace("<TetrahedronFEMForceField", ws, 1))
+    s.animate(10)
+    ref = capi.SofaScene(text)
+    ref.animate(9)
+    rec = _records(every)
+    assert [t for t, _ in rec] == pytest.approx([0.01 * k for k in range(10)])
+    rest = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))[0]
+    np.testing.assert_allclose(rec[0][1]["X0"], rest, rtol=1e-5)
+    np.testing.assert_allclose(rec[0][1]["X"], rest, rtol=1e-5)
+    assert np.abs(rec[0][1]["V"]).max() == 0.0
+    np.testing.assert_allclose(rec[-1][1]["X"], ref.positions(0), rtol=1e-5, atol=1e-6)
+    rec2 = _records(timed)
+    assert [t for t, _ in rec2] == pytest.approx([0.02, 0.05, 0.08])
+    assert set(rec2[0][1]) == {"X"}

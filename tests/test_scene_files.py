@@ -36,7 +36,7 @@ def test_plugin_entry_points_and_factory(capi):
     comps = lib.getModuleComponentList().decode().split()
     for c in ("TetrahedronFEMForceField", "EulerImplicitSolver", "CGLinearSolver", "UniformMass", "DiagonalMass",
               "FixedProjectiveConstraint", "MechanicalObject", "RegularGridTopology",
-              "Hexa2TetraTopologicalMapping", "BoxROI", "TetrahedronSetTopologyContainer"):
+              "Hexa2TetraTopologicalMapping", "BoxROI", "TetrahedronSetTopologyContainer", "WriteState"):
         assert c in comps
     f = lib.sgb_object_factory_new()
     try:
