@@ -42,10 +42,15 @@ extern "C" {
 #define SGB_ERR_DEVICE_TIMEOUT -8 /* a bounded device-side wait (bulk copy completion) ran out */
 
 /* TetrahedronFEMForceField Data "method"
- * (TetrahedronFEMForceField.inl:45): small, large (QR frame), polar. */
+ * (TetrahedronFEMForceField.inl:45): small, large (QR frame), polar, svd
+ * (initSVD / accumulateForceSVD, TetrahedronFEMForceField.inl:1090-1184:
+ * the polar frame, or for an element whose deformation gradient has
+ * determinant below 1e-6 the stable SVD polar factor of that gradient times
+ * the initial rotation; the batch engine takes large and polar only). */
 #define SGB_METHOD_SMALL 0
 #define SGB_METHOD_LARGE 1
 #define SGB_METHOD_POLAR 2
+#define SGB_METHOD_SVD 3   /* polar, with a stable SVD frame for inverted or flat elements */
 
 /* Precision of the element math and solver vectors.
  *  FP64       FP64 everywhere, rounding like the reference CPU code (no FMA,

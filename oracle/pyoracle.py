@@ -15,7 +15,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "libtfem_oracle.so")
 _REF_LIB = os.path.join(_HERE, "_ref", "libsofa_ref_math.so")
 
-METHODS = {"small": 0, "large": 1, "polar": 2}
+METHODS = {"small": 0, "large": 1, "polar": 2, "svd": 3}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -46,6 +46,8 @@ def _load():
     lib.orc_fem_rest_volume.argtypes = [vp]
     lib.orc_polar.restype = ctypes.c_double
     lib.orc_polar.argtypes = [_dp, _dp]
+    lib.orc_polar_stable.restype = ctypes.c_int
+    lib.orc_polar_stable.argtypes = [_dp, _dp]
     lib.orc_set_threads.argtypes = [ctypes.c_int]
     lib.orc_get_threads.restype = ctypes.c_int
     lib.orc_scene_create.restype = vp
@@ -88,6 +90,15 @@ def polar(M):
     _, pq = _d(Q)
     det = lib.orc_polar(pm, Q.ctypes.data_as(_dp))
     return Q, det
+
+
+def polar_stable(M):
+    """Decompose<double>::polarDecomposition_stable restated: (Q, degenerate or inverted)."""
+    lib = _load()
+    M, pm = _d(np.asarray(M, dtype=np.float64).reshape(3, 3))
+    Q = np.zeros((3, 3))
+    deg = lib.orc_polar_stable(pm, Q.ctypes.data_as(_dp))
+    return Q, bool(deg)
 
 
 class OracleFEM:
@@ -245,4 +256,6 @@ def ref_math_lib():
     lib.ref_polar_decomposition_f.restype = ctypes.c_float
     fp = ctypes.POINTER(ctypes.c_float)
     lib.ref_polar_decomposition_f.argtypes = [fp, fp]
+    lib.ref_polar_decomposition_stable_d.restype = ctypes.c_int
+    lib.ref_polar_decomposition_stable_d.argtypes = [_dp, _dp]
     return lib

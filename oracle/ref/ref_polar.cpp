@@ -31,6 +31,20 @@ float ref_polar_decomposition_f(const float* M, float* Q)
     return det;
 }
 
+// Stable polar factor through the 3x3 SVD (decompose.inl:756-765, SVD_stable
+// 1664-1825), used by the svd method for inverted or flat elements. Returns
+// whether the reference flagged the matrix degenerate or inverted.
+int ref_polar_decomposition_stable_d(const double* M, double* Q)
+{
+    sofa::type::Mat<3, 3, double> m, q;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) m(i, j) = M[3 * i + j];
+    const bool deg = sofa::helper::Decompose<double>::polarDecomposition_stable(m, q);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Q[3 * i + j] = q(i, j);
+    return deg ? 1 : 0;
+}
+
 // Reference 3x3 norms (Sofa/framework/Type/src/sofa/type/Mat.h:1056-1080).
 double ref_one_norm_d(const double* A)
 {

@@ -44,6 +44,7 @@
 #define ORC_SMALL 0
 #define ORC_LARGE 1
 #define ORC_POLAR 2
+#define ORC_SVD 3
 
 /* ------------------------------------------------------------------------- */
 /* small fixed-size helpers                                                   */
@@ -153,6 +154,239 @@ double orc_polar(const double M[9], double Q[9])
     } while (E_one > M_one * tol);
     mat_transpose(Mk, Q);
     return det;
+}
+
+/* ------------------------------------------------------------------------- */
+/* svd method: stable polar decomposition through a 3x3 SVD                   */
+/* (Decompose<double>::polarDecomposition_stable, SVD_stable,                 */
+/* eigenDecomposition_iterative and QLAlgorithm, decompose.inl:756-765,       */
+/* 1664-1825, 1563-1608, 1488-1558). Matrices are row-major m[3*i+j].         */
+/* ------------------------------------------------------------------------- */
+
+/* determinant(Mat<3,3>) (Mat.h:987-996), terms in the reference's order */
+static double mat_det(const double m[9])
+{
+    return m[0] * m[4] * m[8] + m[3] * m[7] * m[2] + m[6] * m[1] * m[5] - m[0] * m[7] * m[5] -
+           m[3] * m[1] * m[8] - m[6] * m[4] * m[2];
+}
+
+/* operator*(Mat<3,3>, Mat<3,3>) (Mat.h:1443-1481) */
+static void mat_mul(const double a[9], const double b[9], double r[9])
+{
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+}
+
+/* a * b^T (Mat::multTransposed, Mat.h:623-635) */
+static void mat_mul_bt(const double a[9], const double b[9], double r[9])
+{
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = a[3 * i] * b[3 * j];
+            s += a[3 * i + 1] * b[3 * j + 1];
+            s += a[3 * i + 2] * b[3 * j + 2];
+            r[3 * i + j] = s;
+        }
+}
+
+/* invertMatrix(Mat<3,3>) (Mat.h:1170-1192), each entry divided by det */
+int orc_invert3(const double f[9], double d[9])
+{
+    const double det = mat_det(f);
+    if (fabs(det) <= 2.220446049250313e-16) return 0; /* equalsZero (Mat.h:44-48) */
+    d[0] = (f[4] * f[8] - f[7] * f[5]) / det;
+    d[3] = (f[5] * f[6] - f[8] * f[3]) / det;
+    d[6] = (f[3] * f[7] - f[6] * f[4]) / det;
+    d[1] = (f[7] * f[2] - f[1] * f[8]) / det;
+    d[4] = (f[8] * f[0] - f[2] * f[6]) / det;
+    d[7] = (f[6] * f[1] - f[0] * f[7]) / det;
+    d[2] = (f[1] * f[5] - f[4] * f[2]) / det;
+    d[5] = (f[2] * f[3] - f[5] * f[0]) / det;
+    d[8] = (f[0] * f[4] - f[3] * f[1]) / det;
+    return 1;
+}
+
+/* QLAlgorithm for a symmetric tridiagonal matrix (decompose.inl:1488-1558):
+ * implicit shifts, at most 32 sweeps per eigenvalue, rotations applied to V */
+static void ql_algorithm(double diag[3], double sub[3], double V[9])
+{
+    for (int i0 = 0; i0 < 3; ++i0) {
+        int i1;
+        for (i1 = 0; i1 < 32; ++i1) {
+            int i2;
+            for (i2 = i0; i2 <= 1; ++i2) {
+                const double tmp = fabs(diag[i2]) + fabs(diag[i2 + 1]);
+                if (fabs(sub[i2]) + tmp == tmp) break;
+            }
+            if (i2 == i0) break;
+            double g = (diag[i0 + 1] - diag[i0]) / (2.0 * sub[i0]);
+            double r = sqrt(g * g + 1.0);
+            if (g < 0.0)
+                g = diag[i2] - diag[i0] + sub[i0] / (g - r);
+            else
+                g = diag[i2] - diag[i0] + sub[i0] / (g + r);
+            double sn = 1.0, cs = 1.0, p = 0.0;
+            for (int i3 = i2 - 1; i3 >= i0; --i3) {
+                double f = sn * sub[i3];
+                const double b = cs * sub[i3];
+                if (fabs(f) >= fabs(g)) {
+                    cs = g / f;
+                    r = sqrt(cs * cs + 1.0);
+                    sub[i3 + 1] = f * r;
+                    sn = 1.0 / r;
+                    cs *= sn;
+                } else {
+                    sn = f / g;
+                    r = sqrt(sn * sn + 1.0);
+                    sub[i3 + 1] = g * r;
+                    cs = 1.0 / r;
+                    sn *= cs;
+                }
+                g = diag[i3 + 1] - p;
+                r = (diag[i3] - g) * sn + 2.0 * b * cs;
+                p = sn * r;
+                diag[i3 + 1] = g + p;
+                g = cs * r - b;
+                for (int i4 = 0; i4 < 3; ++i4) {
+                    f = V[3 * i4 + i3 + 1];
+                    V[3 * i4 + i3 + 1] = sn * V[3 * i4 + i3] + cs * f;
+                    V[3 * i4 + i3] = cs * V[3 * i4 + i3] - sn * f;
+                }
+            }
+            diag[i0] -= p;
+            sub[i0] = g;
+            sub[i2] = 0.0;
+        }
+        if (i1 == 32) return;
+    }
+}
+
+/* eigenDecomposition_iterative (decompose.inl:1563-1608): Householder
+ * tridiagonalisation of the symmetric M, then QL */
+static void eigen_iterative(const double M[9], double V[9], double diag[3])
+{
+    double sub[3];
+    double m01 = M[1], m02 = M[2];
+    const double m00 = M[0], m11 = M[4], m12 = M[5], m22 = M[8];
+    diag[0] = m00;
+    sub[2] = 0.0;
+    if (m02 != 0.0) {
+        const double len = sqrt(m01 * m01 + m02 * m02);
+        const double inv = 1.0 / len;
+        m01 *= inv;
+        m02 *= inv;
+        const double q = 2.0 * m01 * m12 + m02 * (m22 - m11);
+        diag[1] = m11 + m02 * q;
+        diag[2] = m22 - m02 * q;
+        sub[0] = len;
+        sub[1] = m12 - m01 * q;
+        V[0] = 1.0, V[1] = 0.0, V[2] = 0.0;
+        V[3] = 0.0, V[4] = m01, V[5] = m02;
+        V[6] = 0.0, V[7] = m02, V[8] = -m01;
+    } else {
+        diag[1] = m11;
+        diag[2] = m22;
+        sub[0] = m01;
+        sub[1] = m12;
+        for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    }
+    ql_algorithm(diag, sub, V);
+}
+
+/* SVD_stable (decompose.inl:1664-1825): F = U diag(S) V^T with U and V
+ * rotations; a null singular value (S^2 below 1e-8) is rebuilt (one: from
+ * the cross product of the two valid columns; two: an arbitrary orthogonal
+ * frame around the valid column; three: identity) and an inversion is moved
+ * into the smallest singular value. Returns 1 when degenerate or inverted. */
+static int svd_stable(const double F[9], double U[9], double S[3], double V[9])
+{
+    double FtF[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) FtF[3 * i + j] = F[i] * F[j] + F[3 + i] * F[3 + j] + F[6 + i] * F[6 + j];
+    eigen_iterative(FtF, V, S);
+    if (mat_det(V) < 0.0)
+        for (int i = 0; i < 3; ++i) V[3 * i] = -V[3 * i];
+    int degenerated = 0;
+    double S_1[3];
+    for (int i = 0; i < 3; ++i) {
+        if (S[i] < 1e-8) {
+            degenerated++;
+            S[i] = 0.0;
+            S_1[i] = 1.0;
+        } else {
+            S[i] = sqrt(S[i]);
+            S_1[i] = 1.0 / S[i];
+        }
+    }
+    int o[3];
+    if (S[0] < S[1]) {
+        if (S[0] < S[2]) {
+            o[0] = 0;
+            if (S[1] < S[2]) o[1] = 1, o[2] = 2;
+            else o[1] = 2, o[2] = 1;
+        } else {
+            o[0] = 2, o[1] = 0, o[2] = 1;
+        }
+    } else {
+        if (S[1] < S[2]) {
+            o[0] = 1;
+            if (S[0] < S[2]) o[1] = 0, o[2] = 2;
+            else o[1] = 2, o[2] = 0;
+        } else {
+            o[0] = 2, o[1] = 1, o[2] = 0;
+        }
+    }
+    if (degenerated == 3) {
+        for (int i = 0; i < 9; ++i) U[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    } else {
+        double VS[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) VS[3 * i + j] = V[3 * i + j] * S_1[j];
+        mat_mul(F, VS, U);
+        if (degenerated == 1) {
+            const double a[3] = {U[o[1]], U[3 + o[1]], U[6 + o[1]]};
+            const double b[3] = {U[o[2]], U[3 + o[2]], U[6 + o[2]]};
+            double c[3];
+            vec_cross(a, b, c);
+            U[o[0]] = c[0];
+            U[3 + o[0]] = c[1];
+            U[6 + o[0]] = c[2];
+        } else if (degenerated == 2) {
+            /* the reference takes edge2 = (U(0,o2), U(1,o0), U(2,o0)) */
+            const double e2[3] = {U[o[2]], U[3 + o[0]], U[6 + o[0]]};
+            double e0[3], e1[3];
+            const double a0 = fabs(e2[0]), a1 = fabs(e2[1]), a2 = fabs(e2[2]);
+            if (a0 > a1) {
+                if (a0 > a2) e0[0] = 0, e0[1] = 1, e0[2] = 0;
+                else e0[0] = 1, e0[1] = 0, e0[2] = 0;
+            } else {
+                if (a1 > a2) e0[0] = 0, e0[1] = 0, e0[2] = 1;
+                else e0[0] = 1, e0[1] = 0, e0[2] = 0;
+            }
+            vec_cross(e2, e0, e1);
+            vec_normalize(e1);
+            vec_cross(e1, e2, e0);
+            U[o[0]] = e0[0], U[3 + o[0]] = e0[1], U[6 + o[0]] = e0[2];
+            U[o[1]] = e1[0], U[3 + o[1]] = e1[1], U[6 + o[1]] = e1[2];
+        }
+    }
+    const int inverted = mat_det(U) < 0.0;
+    if (inverted) {
+        U[o[0]] *= -1.0;
+        U[3 + o[0]] *= -1.0;
+        U[6 + o[0]] *= -1.0;
+        S[o[0]] *= -1.0;
+    }
+    return degenerated || inverted;
+}
+
+/* polarDecomposition_stable (decompose.inl:756-765): Q = U V^T */
+int orc_polar_stable(const double M[9], double Q[9])
+{
+    double U[9], S[3], V[9];
+    const int deg = svd_stable(M, U, S, V);
+    mat_mul_bt(U, V, Q);
+    return deg;
 }
 
 /* computeRotationLarge (TFEM.inl:755-778): rows of R are the unit edge
@@ -309,6 +543,7 @@ typedef struct orc_fem {
     double* R0t;       /* _initialRotations, 9 per element */
     double* rot;       /* rotations (= R^T), 9 per element */
     double* rest_rot;  /* _rotatedInitialElements, 12 per element */
+    double* A0inv;     /* svd: _initialTransformation (inverse rest edge matrix), 9 per element */
     double rest_volume;
     double* tl_buf;    /* thread-local force buffers for the threaded mode */
     int tl_threads;
@@ -340,6 +575,7 @@ orc_fem* orc_fem_create(int n_nodes, const double* rest, int n_tets, const int32
     m->R0t = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
     m->rot = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
     m->rest_rot = (double*)calloc(12 * (size_t)n_tets, sizeof(double));
+    if (method == ORC_SVD) m->A0inv = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
 
     for (int e = 0; e < n_tets; ++e) {
         const int32_t* t = &tets[4 * e];
@@ -381,8 +617,10 @@ orc_fem* orc_fem_create(int n_nodes, const double* rest, int n_tets, const int32
                 /* initLarge (TFEM.inl:835-868) */
                 rotation_large(pa, pb, pc, R);
             } else {
-                /* initPolar (TFEM.inl:993-1023) */
+                /* initPolar (TFEM.inl:993-1023); initSVD (:1090-1119) also
+                 * keeps the inverse of the rest edge matrix */
                 double A[9] = {ea[0], ea[1], ea[2], eb[0], eb[1], eb[2], ec[0], ec[1], ec[2]};
+                if (method == ORC_SVD) (void)orc_invert3(A, &m->A0inv[9 * e]);
                 orc_polar(A, R);
             }
             mat_transpose(R, &m->R0t[9 * e]);
@@ -412,6 +650,7 @@ void orc_fem_destroy(orc_fem* m)
     free(m->R0t);
     free(m->rot);
     free(m->rest_rot);
+    free(m->A0inv);
     free(m->tl_buf);
     free(m);
 }
@@ -444,7 +683,21 @@ static void element_force(orc_fem* m, int e, const double* p, double* f)
         const double *p0 = &p[3 * t[0]], *p1 = &p[3 * t[1]], *p2 = &p[3 * t[2]], *p3 = &p[3 * t[3]];
         double A[9] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], p2[0] - p0[0], p2[1] - p0[1],
                        p2[2] - p0[2], p3[0] - p0[0], p3[1] - p0[1], p3[2] - p0[2]};
-        orc_polar(A, R);
+        int stable = 0;
+        if (m->method == ORC_SVD) {
+            /* accumulateForceSVD (TFEM.inl:1123-1184): F = A A0^-1; an
+             * inverted or nearly flat element (det F < 1e-6) takes the
+             * stable SVD polar factor of F times the initial rotation */
+            double F[9];
+            mat_mul(A, &m->A0inv[9 * e], F);
+            if (mat_det(F) < 1e-6) {
+                double Rs[9];
+                orc_polar_stable(F, Rs);
+                mat_mul_bt(Rs, &m->R0t[9 * e], R);
+                stable = 1;
+            }
+        }
+        if (!stable) orc_polar(A, R);
     }
     double* rot = &m->rot[9 * e];
     mat_transpose(R, rot);

@@ -25,7 +25,7 @@ ERRORS = {
     -7: "not found",
     -8: "a bounded device-side wait ran out",
 }
-METHODS = {"small": 0, "large": 1, "polar": 2}
+METHODS = {"small": 0, "large": 1, "polar": 2, "svd": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1, "fp64_fma": 2}
 
 

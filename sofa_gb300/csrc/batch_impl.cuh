@@ -31,6 +31,8 @@ __device__ __forceinline__ ElemView<R> bm_elem_view(const BMeshDesc& m)
     ev.J = (const R*)m.J;
     ev.rest = (const R*)m.rest;
     ev.rest_ff = m.rest_ff;
+    ev.A0inv = nullptr;  // the batch engine admits large and polar meshes
+    ev.R0 = nullptr;
     ev.n_tets = m.n_tets;
     ev.method = m.method;
     return ev;

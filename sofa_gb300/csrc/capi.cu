@@ -101,6 +101,7 @@ static void free_mesh(TfemMesh& m)
     cudaFree(m.rest);
     cudaFree(m.rest_ff);
     cudaFree(m.R0);
+    cudaFree(m.A0inv);
     cudaFree(m.rest_pos);
     cudaFree(m.rowptr);
     cudaFree(m.slots);
@@ -135,8 +136,8 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: the mesh needs at least one node");
     if (n_tets < 0 || (n_tets > 0 && !tetrahedra_host))
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: invalid tetrahedra");
-    if (method < SGB_METHOD_SMALL || method > SGB_METHOD_POLAR)
-        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_tfem_create: method must be small, large or polar (svd is not supported)");
+    if (method < SGB_METHOD_SMALL || method > SGB_METHOD_SVD)
+        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_tfem_create: method must be small, large, polar or svd");
     const VariantOps* ops = variant_for(precision);
     if (!ops) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_create: unknown precision");
     if ((size_t)n_tets * 12 > (size_t)0x7fffffff)
@@ -227,7 +228,8 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
         (rc = dev_alloc_bytes(&m.eforce, rs * 12 * E, acc)) || (rc = dev_alloc(&m.rest_pos, 3 * (size_t)n_nodes, acc)) ||
         (rc = dev_alloc(&m.rowptr, (size_t)n_nodes + 1, acc)) || (rc = dev_alloc(&m.slots, 4 * E, acc)) ||
         (rc = dev_alloc(&m.elem_orig, E, acc)) || (rc = dev_alloc(&m.dev_flags, 1, acc)) ||
-        (precision == SGB_PRECISION_MIXED && method != SGB_METHOD_SMALL && (rc = dev_alloc(&m.rest_ff, 9 * E, acc))))
+        (precision == SGB_PRECISION_MIXED && method != SGB_METHOD_SMALL && (rc = dev_alloc(&m.rest_ff, 9 * E, acc))) ||
+        (method == SGB_METHOD_SVD && (rc = dev_alloc_bytes(&m.A0inv, rs * 9 * E, acc))))
         goto fail_out;
     if ((ce = cudaMemsetAsync(m.dev_flags, 0, sizeof(int), h->stream)) != cudaSuccess) {
         rc = cuda_fail(ce, "cudaMemsetAsync");

@@ -651,9 +651,13 @@ int Scene::init_host(std::string* err)
         if (method == "small") b.method = SGB_METHOD_SMALL;
         else if (method == "large") b.method = SGB_METHOD_LARGE;
         else if (method == "polar") b.method = SGB_METHOD_POLAR;
+        else if (method == "svd") b.method = SGB_METHOD_SVD;
         else return unsupported(err, where + "TetrahedronFEMForceField method '" + method + "' is not supported");
         if (fem->get_bool(*this, "computeGlobalMatrix") || fem->get_bool(*this, "assembling"))
             return unsupported(err, where + "computeGlobalMatrix=true (assembled matrix) is not supported");
+        if (b.method != SGB_METHOD_SMALL && fem->get_bool(*this, "updateStiffnessMatrix"))
+            return unsupported(err, where + "updateStiffnessMatrix=true (strain-displacement rebuilt every step, "
+                                            "TetrahedronFEMForceField.inl:908, 1063, 1174) is not supported");
         if (fem->get_real(*this, "plasticMaxThreshold") > 0.0)
             return unsupported(err, where + "plasticity (plasticMaxThreshold > 0) is not supported");
         if (fem->get_int(*this, "computeVonMisesStress") != 0)

@@ -10,7 +10,7 @@
 
 namespace sgb {
 
-enum Method { METHOD_SMALL = 0, METHOD_LARGE = 1, METHOD_POLAR = 2 };
+enum Method { METHOD_SMALL = 0, METHOD_LARGE = 1, METHOD_POLAR = 2, METHOD_SVD = 3 };
 enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
 
 // Blocks used by every node-parallel kernel that produces a dot product: the
@@ -34,6 +34,8 @@ struct ElemView {
     const R* J;        // 12 rows: the distinct values of the 12x6 strain-displacement matrix
     const R* rest;     // 12 rows: rotated rest coordinates (method dependent, see tfem.cu)
     const float2* rest_ff;  // mixed: rows 3..11 (b-a, c-a, d-a) as float-float pairs for the force kernel (or null)
+    const R* A0inv;         // svd: inverse rest edge matrix, 9 rows (or null)
+    const R* R0;            // svd: initial rotation rows, 9 rows (or null)
     int n_tets;
     int method;
 };
@@ -88,7 +90,8 @@ struct TfemMesh {
     void* J = nullptr;
     void* rest = nullptr;
     float2* rest_ff = nullptr;  // mixed: rest coordinates b-a, c-a, d-a (9 rows) as float-float pairs
-    void* R0 = nullptr;       // initial rotation rows (for the rotation getter)
+    void* R0 = nullptr;       // initial rotation rows (for the rotation getter; the svd method's frame)
+    void* A0inv = nullptr;    // svd: inverse rest edge matrix (9 rows)
     double* rest_pos = nullptr;  // rest positions (FP64, n_nodes*3), used by method=small
     int* rowptr = nullptr;
     int* slots = nullptr;

@@ -281,7 +281,7 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
                                 const int* __restrict__ elem_orig, int E, int method,
                                 const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
                                 int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest,
-                                float2* rest_ff, R* rot,
+                                float2* rest_ff, R* rot, R* A0inv,
                                 R* R0, double* vol)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -331,6 +331,13 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
             rotation_large(ea, eb, Rm);
         } else {
             double A[9] = {ea[0], ea[1], ea[2], eb[0], eb[1], eb[2], ec[0], ec[1], ec[2]};
+            if (method == METHOD_SVD && A0inv) {
+                // initSVD (TFEM.inl:1090-1119): the polar init plus the
+                // inverse rest edge matrix (_initialTransformation)
+                double Ai[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+                (void)invert3(A, Ai);
+                for (int i = 0; i < 9; ++i) A0inv[(size_t)i * E + s] = (R)Ai[i];
+            }
             polar3(A, Rm, 1000);
         }
         const double* P[4] = {pa, pb, pc, pd};
@@ -347,7 +354,7 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
             rr[0] = rr[1] = rr[2] = 0.0;
         }
         strain_displacement(&rr[0], &rr[3], &rr[6], &rr[9], Jd);
-        if (method == METHOD_POLAR && is_mixed<R>::value) {
+        if ((method == METHOD_POLAR || method == METHOD_SVD) && is_mixed<R>::value) {
             // mixed precision drops the rigid translation (J's columns sum to
             // zero): keep rest coordinates relative to node a
             for (int i = 1; i < 4; ++i)
@@ -387,6 +394,22 @@ __device__ __forceinline__ void store_eforce(R* eforce, int e, const R c[12])
     R* o = eforce + (size_t)e * 12;
 #pragma unroll
     for (int i = 0; i < 12; ++i) o[i] = c[i];
+}
+
+// The svd method's frame of element e from its stored inverse rest edge
+// matrix and initial rotation (svd_frame); false: the element takes the
+// polar factor of its edges, as the polar method does.
+template <typename R, typename T>
+__device__ __forceinline__ bool svd_frame_elem(const ElemView<R>& ev, size_t e, const T A[9], T Rout[9])
+{
+    const size_t En = (size_t)ev.n_tets;
+    T Ai[9], R0[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        Ai[i] = (T)ev.A0inv[i * En + e];
+        R0[i] = (T)ev.R0[i * En + e];
+    }
+    return svd_frame(A, Ai, R0, Rout);
 }
 
 // addForce element part: accumulateForceSmall / Large / Polar
@@ -436,7 +459,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
         } else {
             R ead[3] = {R(p[3][0] - p[0][0]), R(p[3][1] - p[0][1]), R(p[3][2] - p[0][2])};
             R A[9] = {eab[0], eab[1], eab[2], eac[0], eac[1], eac[2], ead[0], ead[1], ead[2]};
-            polar3(A, Rm);
+            if (!(METHOD == METHOD_SVD && svd_frame_elem(ev, (size_t)e, A, Rm))) polar3(A, Rm);
         }
         R def[12];
 #pragma unroll
@@ -495,7 +518,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
             } else {
                 float A[9] = {eg[0][0].h, eg[0][1].h, eg[0][2].h, eg[1][0].h, eg[1][1].h,
                               eg[1][2].h, eg[2][0].h, eg[2][1].h, eg[2][2].h};
-                polar3(A, X);
+                if (!(METHOD == METHOD_SVD && svd_frame_elem(ev, (size_t)e, A, X))) polar3(A, X);
             }
             orthonormalize_ff(X, dX);
 #pragma unroll
@@ -530,7 +553,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
                 rotation_large(ed[0], ed[1], Rm);
             } else {
                 R A[9] = {ed[0][0], ed[0][1], ed[0][2], ed[1][0], ed[1][1], ed[1][2], ed[2][0], ed[2][1], ed[2][2]};
-                polar3(A, Rm);
+                if (!(METHOD == METHOD_SVD && svd_frame_elem(ev, (size_t)e, A, Rm))) polar3(A, Rm);
             }
             D[0] = D[1] = D[2] = R(0);
 #pragma unroll
@@ -1840,6 +1863,8 @@ ElemView<R> view(TfemMesh* m)
     ev.J = (const R*)m->J;
     ev.rest = (const R*)m->rest;
     ev.rest_ff = m->rest_ff;
+    ev.A0inv = (const R*)m->A0inv;
+    ev.R0 = m->method == METHOD_SVD ? (const R*)m->R0 : nullptr;
     ev.n_tets = m->n_tets;
     ev.method = m->method;
     return ev;
@@ -1852,7 +1877,7 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
     if (m->n_tets == 0) return;
     k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
         m->rest_pos, m->tets, m->elem_orig, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K,
-        (R*)m->J, (R*)m->rest, m->rest_ff, (R*)m->rot, (R*)m->R0, vol);
+        (R*)m->J, (R*)m->rest, m->rest_ff, (R*)m->rot, (R*)m->A0inv, (R*)m->R0, vol);
 }
 
 template <typename R>
@@ -1865,6 +1890,8 @@ void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
         k_elem_force<R, METHOD_SMALL><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
     else if (m->method == METHOD_LARGE)
         k_elem_force<R, METHOD_LARGE><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+    else if (m->method == METHOD_SVD)
+        k_elem_force<R, METHOD_SVD><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
     else
         k_elem_force<R, METHOD_POLAR><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
 }

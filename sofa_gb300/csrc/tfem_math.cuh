@@ -228,4 +228,270 @@ __device__ __forceinline__ void element_force_nofact(T F[12], const T D[12], con
     }
 }
 
+// ---- svd method: stable polar factor through a 3x3 SVD ---------------------
+// Decompose<Real>::polarDecomposition_stable / SVD_stable /
+// eigenDecomposition_iterative / QLAlgorithm
+// (Sofa/framework/Helper/src/sofa/helper/decompose.inl:756-765, 1664-1825,
+// 1563-1608, 1488-1558), for the inverted or nearly flat elements of the svd
+// method. Row-major 3x3; operations in the reference's order.
+
+// determinant(Mat<3,3>) (Sofa/framework/Type/src/sofa/type/Mat.h:987-996)
+template <typename T>
+__device__ __forceinline__ T det3(const T m[9])
+{
+    return m[0] * m[4] * m[8] + m[3] * m[7] * m[2] + m[6] * m[1] * m[5] - m[0] * m[7] * m[5] - m[3] * m[1] * m[8] -
+           m[6] * m[4] * m[2];
+}
+
+// operator*(Mat<3,3>, Mat<3,3>) (Mat.h:1443-1481)
+template <typename T>
+__device__ __forceinline__ void mul3(const T a[9], const T b[9], T r[9])
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+}
+
+// a * b^T (Mat::multTransposed, Mat.h:623-635)
+template <typename T>
+__device__ __forceinline__ void mul3_bt(const T a[9], const T b[9], T r[9])
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T s = a[3 * i] * b[3 * j];
+            s += a[3 * i + 1] * b[3 * j + 1];
+            s += a[3 * i + 2] * b[3 * j + 2];
+            r[3 * i + j] = s;
+        }
+}
+
+// invertMatrix(Mat<3,3>) (Mat.h:1170-1192): adjugate entries over det
+template <typename T>
+__host__ __device__ inline bool invert3(const T f[9], T d[9])
+{
+    const T det = f[0] * f[4] * f[8] + f[3] * f[7] * f[2] + f[6] * f[1] * f[5] - f[0] * f[7] * f[5] -
+                  f[3] * f[1] * f[8] - f[6] * f[4] * f[2];
+    if (fabs(det) <= RealTraits<T>::eps()) return false;
+    d[0] = (f[4] * f[8] - f[7] * f[5]) / det;
+    d[3] = (f[5] * f[6] - f[8] * f[3]) / det;
+    d[6] = (f[3] * f[7] - f[6] * f[4]) / det;
+    d[1] = (f[7] * f[2] - f[1] * f[8]) / det;
+    d[4] = (f[8] * f[0] - f[2] * f[6]) / det;
+    d[7] = (f[6] * f[1] - f[0] * f[7]) / det;
+    d[2] = (f[1] * f[5] - f[4] * f[2]) / det;
+    d[5] = (f[2] * f[3] - f[5] * f[0]) / det;
+    d[8] = (f[0] * f[4] - f[3] * f[1]) / det;
+    return true;
+}
+
+// QL with implicit shifts on a symmetric tridiagonal matrix (at most 32
+// sweeps per eigenvalue), rotations accumulated into V
+template <typename T>
+__device__ inline void ql_tridiagonal(T diag[3], T sub[3], T V[9])
+{
+    for (int i0 = 0; i0 < 3; ++i0) {
+        int i1;
+        for (i1 = 0; i1 < 32; ++i1) {
+            int i2;
+            for (i2 = i0; i2 <= 1; ++i2) {
+                const T tmp = fabs(diag[i2]) + fabs(diag[i2 + 1]);
+                if (fabs(sub[i2]) + tmp == tmp) break;
+            }
+            if (i2 == i0) break;
+            T g = (diag[i0 + 1] - diag[i0]) / (T(2) * sub[i0]);
+            T r = sqrt(g * g + T(1));
+            if (g < T(0))
+                g = diag[i2] - diag[i0] + sub[i0] / (g - r);
+            else
+                g = diag[i2] - diag[i0] + sub[i0] / (g + r);
+            T sn = T(1), cs = T(1), p = T(0);
+            for (int i3 = i2 - 1; i3 >= i0; --i3) {
+                T f = sn * sub[i3];
+                const T b = cs * sub[i3];
+                if (fabs(f) >= fabs(g)) {
+                    cs = g / f;
+                    r = sqrt(cs * cs + T(1));
+                    sub[i3 + 1] = f * r;
+                    sn = T(1) / r;
+                    cs *= sn;
+                } else {
+                    sn = f / g;
+                    r = sqrt(sn * sn + T(1));
+                    sub[i3 + 1] = g * r;
+                    cs = T(1) / r;
+                    sn *= cs;
+                }
+                g = diag[i3 + 1] - p;
+                r = (diag[i3] - g) * sn + T(2) * b * cs;
+                p = sn * r;
+                diag[i3 + 1] = g + p;
+                g = cs * r - b;
+                for (int i4 = 0; i4 < 3; ++i4) {
+                    f = V[3 * i4 + i3 + 1];
+                    V[3 * i4 + i3 + 1] = sn * V[3 * i4 + i3] + cs * f;
+                    V[3 * i4 + i3] = cs * V[3 * i4 + i3] - sn * f;
+                }
+            }
+            diag[i0] -= p;
+            sub[i0] = g;
+            sub[i2] = T(0);
+        }
+        if (i1 == 32) return;
+    }
+}
+
+// Householder tridiagonalisation of the symmetric M, then QL
+template <typename T>
+__device__ inline void eigen_iterative3(const T M[9], T V[9], T diag[3])
+{
+    T sub[3];
+    T m01 = M[1], m02 = M[2];
+    const T m00 = M[0], m11 = M[4], m12 = M[5], m22 = M[8];
+    diag[0] = m00;
+    sub[2] = T(0);
+    if (m02 != T(0)) {
+        const T len = sqrt(m01 * m01 + m02 * m02);
+        const T inv = T(1) / len;
+        m01 *= inv;
+        m02 *= inv;
+        const T q = T(2) * m01 * m12 + m02 * (m22 - m11);
+        diag[1] = m11 + m02 * q;
+        diag[2] = m22 - m02 * q;
+        sub[0] = len;
+        sub[1] = m12 - m01 * q;
+        V[0] = T(1), V[1] = T(0), V[2] = T(0);
+        V[3] = T(0), V[4] = m01, V[5] = m02;
+        V[6] = T(0), V[7] = m02, V[8] = -m01;
+    } else {
+        diag[1] = m11;
+        diag[2] = m22;
+        sub[0] = m01;
+        sub[1] = m12;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? T(1) : T(0);
+    }
+    ql_tridiagonal(diag, sub, V);
+}
+
+// SVD_stable: F = U diag(S) V^T with rotations U, V. Null singular values
+// (S^2 below the zero tolerance) are rebuilt (one: cross product of the two
+// valid columns; two: a frame around the valid column, with the reference's
+// choice of components; three: identity) and an inversion goes into the
+// smallest singular value.
+template <typename T>
+__device__ inline void svd_stable3(const T F[9], T U[9], T S[3], T V[9])
+{
+    T FtF[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) FtF[3 * i + j] = F[i] * F[j] + F[3 + i] * F[3 + j] + F[6 + i] * F[6 + j];
+    eigen_iterative3(FtF, V, S);
+    if (det3(V) < T(0))
+        for (int i = 0; i < 3; ++i) V[3 * i] = -V[3 * i];
+    int degenerated = 0;
+    T S_1[3];
+    for (int i = 0; i < 3; ++i) {
+        if (S[i] < RealTraits<T>::polar_tol()) {
+            degenerated++;
+            S[i] = T(0);
+            S_1[i] = T(1);
+        } else {
+            S[i] = sqrt(S[i]);
+            S_1[i] = T(1) / S[i];
+        }
+    }
+    int o0, o1, o2;
+    if (S[0] < S[1]) {
+        if (S[0] < S[2]) {
+            o0 = 0;
+            if (S[1] < S[2]) o1 = 1, o2 = 2;
+            else o1 = 2, o2 = 1;
+        } else {
+            o0 = 2, o1 = 0, o2 = 1;
+        }
+    } else {
+        if (S[1] < S[2]) {
+            o0 = 1;
+            if (S[0] < S[2]) o1 = 0, o2 = 2;
+            else o1 = 2, o2 = 0;
+        } else {
+            o0 = 2, o1 = 1, o2 = 0;
+        }
+    }
+    if (degenerated == 3) {
+        for (int i = 0; i < 9; ++i) U[i] = (i % 4 == 0) ? T(1) : T(0);
+    } else {
+        T VS[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) VS[3 * i + j] = V[3 * i + j] * S_1[j];
+        mul3(F, VS, U);
+        if (degenerated == 1) {
+            const T a[3] = {U[o1], U[3 + o1], U[6 + o1]};
+            const T b[3] = {U[o2], U[3 + o2], U[6 + o2]};
+            T c[3];
+            cross3(a, b, c);
+            U[o0] = c[0], U[3 + o0] = c[1], U[6 + o0] = c[2];
+        } else if (degenerated == 2) {
+            const T e2[3] = {U[o2], U[3 + o0], U[6 + o0]};
+            T e0[3], e1[3];
+            const T a0 = fabs(e2[0]), a1 = fabs(e2[1]), a2 = fabs(e2[2]);
+            if (a0 > a1) {
+                if (a0 > a2) e0[0] = T(0), e0[1] = T(1), e0[2] = T(0);
+                else e0[0] = T(1), e0[1] = T(0), e0[2] = T(0);
+            } else {
+                if (a1 > a2) e0[0] = T(0), e0[1] = T(0), e0[2] = T(1);
+                else e0[0] = T(1), e0[1] = T(0), e0[2] = T(0);
+            }
+            cross3(e2, e0, e1);
+            normalize3(e1);
+            cross3(e1, e2, e0);
+            U[o0] = e0[0], U[3 + o0] = e0[1], U[6 + o0] = e0[2];
+            U[o1] = e1[0], U[3 + o1] = e1[1], U[6 + o1] = e1[2];
+        }
+    }
+    if (det3(U) < T(0)) {
+        U[o0] *= T(-1);
+        U[3 + o0] *= T(-1);
+        U[6 + o0] *= T(-1);
+        S[o0] *= T(-1);
+    }
+}
+
+// polarDecomposition_stable: Q = U V^T
+template <typename T>
+__device__ inline void polar_stable3(const T M[9], T Q[9])
+{
+    T U[9], S[3], V[9];
+    svd_stable3(M, U, S, V);
+    mul3_bt(U, V, Q);
+}
+
+// The svd method's frame (accumulateForceSVD, TFEM.inl:1123-1150): with the
+// edge rows A and the inverse rest edge matrix A0inv, F = A A0inv; when
+// det F < 1e-6 (inverted or nearly flat) R = polar_stable(F) R0 (R0 = the
+// initial rotation rows) and the function returns true; otherwise the
+// caller takes the polar factor of A, as the polar method does.
+template <typename T>
+__device__ inline bool svd_frame(const T A[9], const T A0inv[9], const T R0[9], T R[9])
+{
+    T F[9];
+    mul3(A, A0inv, F);
+    if (!(det3(F) < T(1e-6))) return false;
+    T Rs[9];
+    polar_stable3(F, Rs);
+    // Rs.multTransposed(initialRotations) with initialRotations = R0^T
+    T R0t[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) R0t[3 * i + j] = R0[3 * j + i];
+    mul3_bt(Rs, R0t, R);
+    return true;
+}
+
+
 }  // namespace sgb

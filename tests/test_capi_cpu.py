@@ -57,8 +57,8 @@ def test_create_rejects_bad_indices_before_touching_the_gpu(capi):
     assert rc == -1
     assert "out of range" in capi.last_error()
     rc = lib.sgb_tfem_create(ctypes.byref(h), 4, pos.ctypes.data_as(capi._dp), 1, tets.ctypes.data_as(capi._ip),
-                             y.ctypes.data_as(capi._dp), 1, nu.ctypes.data_as(capi._dp), 1, None, 0, 3, 0)
-    assert rc == -4  # svd is not supported
+                             y.ctypes.data_as(capi._dp), 1, nu.ctypes.data_as(capi._dp), 1, None, 0, 4, 0)
+    assert rc == -4  # no method 4
     rc = lib.sgb_tfem_create(ctypes.byref(h), 0, pos.ctypes.data_as(capi._dp), 0, None, None, 0, None, 0, None, 0,
                              1, 0)
     assert rc == -1

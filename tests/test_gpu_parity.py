@@ -60,7 +60,7 @@ def run_calls(torch, capi, mesh, method, precision, x, dx, kfactor):
     return f0, fd.cpu().double().numpy(), df0, dfd.cpu().double().numpy(), rot
 
 
-@pytest.mark.parametrize("method", ["small", "large", "polar"])
+@pytest.mark.parametrize("method", ["small", "large", "polar", "svd"])
 @pytest.mark.parametrize("precision", ["fp64", "fp64_fma", "mixed"])
 def test_add_force_add_dforce_per_call(torch_cuda, capi, oracle, method, precision):
     mesh = cases.beam_mesh()
@@ -112,6 +112,54 @@ def test_mixed_add_force_small_strain(torch_cuda, capi, oracle, method):
     f_ref = ofem.add_force(x, f0)
     err = cases.rel_err(f_gpu - f0, f_ref - f0)
     assert err <= 1e-4, err
+
+
+def _invert(mesh, x, elems, flat=()):
+    """Moves node a of each element through the opposite face (inverted,
+    det F < 0) or onto its plane (flat, det F = 0)."""
+    x = x.copy()
+    for e, s in [(e, 1.5) for e in elems] + [(e, 0.0) for e in flat]:
+        t = mesh.tetrahedra[e]
+        c = x[t[1:]].mean(0)
+        x[t[0]] = c + s * (c - x[t[0]])
+    return x
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fma", "mixed"])
+def test_svd_method_inverted_elements(torch_cuda, capi, oracle, precision):
+    """method=svd (accumulateForceSVD, TFEM.inl:1123-1184): elements whose
+    deformation gradient has det < 1e-6 take the stable SVD polar factor
+    (the oracle's restatement is pinned to the reference's bits); the
+    others the polar factor. FP64 per call is bit-identical to the oracle
+    (a flattened element included), FP64-FMA within 1e-10, mixed within
+    1e-5 (inverted elements only: a flat one sits on the FP32 / FP64
+    degeneracy thresholds)."""
+    mesh = cases.beam_mesh()
+    rng = np.random.default_rng(12)
+    x = mesh.positions + rng.normal(scale=5e-3, size=mesh.positions.shape)
+    x = _invert(mesh, x, [0, 57, 311, 900], flat=[] if precision == "mixed" else [640])
+    dx = rng.normal(scale=1e-3, size=x.shape)
+    if precision == "mixed":
+        dx = dx.astype(np.float32).astype(np.float64)
+    kfactor = -0.0011
+    ofem = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "svd")
+    f0, f_gpu, df0, df_gpu, rot = run_calls(torch_cuda, capi, mesh, "svd", precision, x, dx, kfactor)
+    f_ref = ofem.add_force(x, f0)
+    df_ref = ofem.add_dforce(dx, kfactor, df0)
+    polar = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "polar").add_force(x, f0)
+    assert not np.array_equal(polar, f_ref)  # the stable frame was taken
+    ef = cases.rel_err(f_gpu - f0, f_ref - f0)
+    ed = cases.rel_err(df_gpu - df0, df_ref - df0)
+    if precision == "fp64":
+        assert np.array_equal(f_gpu, f_ref), ef
+        assert np.array_equal(df_gpu, df_ref), ed
+    elif precision == "fp64_fma":
+        assert ef <= 1e-10 and ed <= 1e-10, (ef, ed)
+    else:
+        assert ef <= 1e-5 and ed <= 1e-5, (ef, ed)
+    ref_rot = np.stack([ofem.element(e)["rotation"] for e in (0, 57, 311, 900)])
+    tol = 0 if precision == "fp64" else (1e-12 if precision == "fp64_fma" else 1e-5)
+    np.testing.assert_allclose(rot[[0, 57, 311, 900]], ref_rot, rtol=0, atol=tol)
 
 
 def test_scene_100_steps_bit_identical_with_serial_dots(torch_cuda, capi, oracle):

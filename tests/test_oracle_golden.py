@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from sofa_gb300 import topology as topo
+from tests import cases
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -109,7 +110,7 @@ def test_small_regular_tet_forces(oracle):
     np.testing.assert_allclose(f[:, :2], 0, atol=1e-6)
 
 
-@pytest.mark.parametrize("method", ["small", "large", "polar"])
+@pytest.mark.parametrize("method", ["small", "large", "polar", "svd"])
 def test_dforce_is_derivative_of_force(oracle, method):
     """ForceField_test protocol (SolidMechanics/Testing/.../ForceFieldTestCreation.h,
     run_test): addDForce(dx) matches the finite difference of addForce under a
@@ -140,6 +141,43 @@ def test_polar_matches_reference_bits(oracle):
         q, d = oracle.polar(M)
         assert np.array_equal(q, Q), (M, q, Q)
         assert d == det
+
+
+def test_polar_stable_matches_reference_bits(oracle):
+    """The oracle's restatement of Decompose<double>::polarDecomposition_stable
+    (SVD_stable, eigenDecomposition_iterative, QLAlgorithm), used by the svd
+    method for inverted or flat elements, equals the reference's bit for bit
+    on 600 matrices covering each degenerate branch
+    (tests/golden/polar_stable_ref.npz)."""
+    g = np.load(os.path.join(GOLDEN, "polar_stable_ref.npz"))
+    for M, Q, deg in zip(g["M"], g["Q"], g["degenerate"]):
+        q, d = oracle.polar_stable(M)
+        assert np.array_equal(q, Q), (M, q, Q)
+        assert d == bool(deg)
+
+
+def test_svd_method_equals_polar_unless_inverted(oracle):
+    """accumulateForceSVD (TFEM.inl:1123-1184) takes the polar factor of the
+    edge matrix when det(A A0^-1) >= 1e-6, so on a mesh with no inverted or
+    flattened element the svd force equals the polar force bit for bit; an
+    inverted element takes the stable SVD factor instead."""
+    mesh = cases.beam_mesh()
+    rng = np.random.default_rng(3)
+    x = mesh.positions + rng.normal(scale=1e-2, size=mesh.positions.shape)
+    fp = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "polar").add_force(x)
+    fs = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "svd").add_force(x)
+    assert np.array_equal(fp, fs)
+    # invert element 0: move its node a through the opposite face
+    t = mesh.tetrahedra[0]
+    xi = x.copy()
+    c = x[t[1:]].mean(0)
+    xi[t[0]] = c + 1.5 * (c - x[t[0]])
+    fp = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "polar").add_force(xi)
+    fs = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "svd").add_force(xi)
+    assert np.all(np.isfinite(fs)) and not np.array_equal(fp, fs)
+    others = np.setdiff1d(np.arange(mesh.n_nodes), np.unique(mesh.tetrahedra[
+        np.any(np.isin(mesh.tetrahedra, t), axis=1)]))
+    assert np.array_equal(fp[others], fs[others])
 
 
 def test_euler_implicit_closed_form(oracle):

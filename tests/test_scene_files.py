@@ -150,7 +150,7 @@ def test_scene_errors(capi, case):
 
 
 @pytest.mark.parametrize("edit,msg", [
-    (('method="large"', 'method="svd"'), "svd"),
+    (('method="large"', 'method="large" updateStiffnessMatrix="1"'), "updateStiffnessMatrix"),
     (('<DiagonalMass name="mass" massDensity="1.0" />', ''), "mass"),
     (('<EulerImplicitSolver />', '<EulerImplicitSolver firstOrder="1" />'), "firstOrder"),
     (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField plasticMaxThreshold="0.1" name="FEM"'),
