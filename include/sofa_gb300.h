@@ -200,7 +200,27 @@ typedef struct sgb_scene_params {
      * (reliable-update CG: the FP32 recurrence cannot drift from the true
      * residual). 0: off. The FP64 copy doubles the force field's memory. */
     int residual_replacement;
+    /* Linear solver: SGB_SOLVER_CG (CGLinearSolver) or SGB_SOLVER_PCG
+     * (PCGLinearSolver, PCGLinearSolver.inl:194-262: starts from the previous
+     * step's solution, stops when r.z <= tolerance * b.b, no threshold test;
+     * cg_iterations / cg_tolerance are its iterations / tolerance), and its
+     * preconditioner: SGB_PRECOND_NONE or SGB_PRECOND_JACOBI
+     * (JacobiPreconditioner: z = diag(mF M + kF K)^-1 r, the diagonal
+     * re-assembled every step, fixed DOFs one). PCG runs on the unfused
+     * element-order kernels in every precision. */
+    int linear_solver;
+    int preconditioner;
+    /* PreconditionedMatrixFreeSystem assemblingRate
+     * (PreconditionedMatrixFreeSystem.inl:31-67): the preconditioner is
+     * re-assembled on the first step and every this many steps after it
+     * (0 or 1: every step). */
+    int preconditioner_rate;
 } sgb_scene_params;
+
+#define SGB_SOLVER_CG 0
+#define SGB_SOLVER_PCG 1
+#define SGB_PRECOND_NONE 0
+#define SGB_PRECOND_JACOBI 1
 
 /* Fills params with the reference Data defaults: dt 0.01, Rayleigh 0, CG
  * 25 / 1e-5 / 1e-5, gravity (0,-9.81,0), vertex mass 1, mass first. */

@@ -49,6 +49,12 @@ int sgb_sofa_scene_bodies(const sgb_sofa_scene_t* scene, int* n_bodies);
 int sgb_sofa_scene_body_info(const sgb_sofa_scene_t* scene, int body, int* n_nodes, int* n_tets, int* method,
                              int* precision, int* n_fixed);
 
+/* Linear solver of a body as assembled from the scene: SGB_SOLVER_CG or
+ * SGB_SOLVER_PCG, its preconditioner (SGB_PRECOND_*) and assembling rate,
+ * iterations and tolerance. Any output may be NULL. */
+int sgb_sofa_scene_body_solver(const sgb_sofa_scene_t* scene, int body, int* linear_solver, int* preconditioner,
+                               int* preconditioner_rate, int* iterations, double* tolerance);
+
 /* Host arrays of a body as assembled from the scene: tetrahedra (n_tets x 4),
  * lumped node masses (n_nodes; all equal to the vertex mass for a
  * UniformMass) and fixed indices (n_fixed). NULL pointers are skipped. */

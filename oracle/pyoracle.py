@@ -60,6 +60,8 @@ def _load():
     lib.orc_scene_set_external_force.argtypes = [vp, _dp]
     lib.orc_scene_set_springs.argtypes = [vp, ctypes.c_double, _dp]
     lib.orc_scene_step.argtypes = [vp, ctypes.c_int]
+    lib.orc_scene_set_solver.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.orc_scene_jacobi.argtypes = [vp, _dp]
     lib.orc_scene_compute_force.argtypes = [vp, _dp]
     lib.orc_scene_last_iterations.restype = ctypes.c_int
     lib.orc_scene_last_iterations.argtypes = [vp]
@@ -221,6 +223,19 @@ class OracleScene:
     def set_springs(self, k, anchor):
         self._anchor, p = _d(np.asarray(anchor).reshape(-1, 3))
         _load().orc_scene_set_springs(self._h, float(k), p)
+
+    def set_solver(self, solver="cg", preconditioner=None, rate=1):
+        """solver "cg" (CGLinearSolver) or "pcg" (PCGLinearSolver, warm start);
+        preconditioner None or "jacobi" (JacobiPreconditioner), re-assembled
+        every `rate` steps."""
+        _load().orc_scene_set_solver(self._h, {"cg": 0, "pcg": 1}[solver],
+                                     {None: 0, "jacobi": 1}[preconditioner], int(rate))
+
+    def jacobi(self):
+        """The last solve's inverse Jacobi diagonal (n x 3)."""
+        out = np.zeros((self.n_nodes, 3))
+        _load().orc_scene_jacobi(self._h, out.ctypes.data_as(_dp))
+        return out
 
     def step(self, n=1):
         _load().orc_scene_step(self._h, int(n))

@@ -880,6 +880,9 @@ typedef struct orc_scene {
     /* statistics of the last solve */
     int last_iters;
     double last_err;
+    /* linear solver: 0 CGLinearSolver, 1 PCGLinearSolver; Jacobi preconditioner */
+    int solver, precond, precond_rate;
+    double* dinv;
 } orc_scene;
 
 orc_scene* orc_scene_create(orc_fem* fem, int n_nodes, int mass_kind, double vertex_mass,
@@ -928,6 +931,7 @@ void orc_scene_destroy(orc_scene* s)
     free(s->node_mass);
     free(s->fixed);
     free(s->ext);
+    free(s->dinv);
     free(s->anchor);
     free(s->x);
     free(s->v);
@@ -1117,6 +1121,153 @@ static void cg_solve(orc_scene* s, double mf, double kf)
     s->last_iters = n_matvec;
 }
 
+/* ------------------------------------------------------------------------- */
+/* PCGLinearSolver (PCGLinearSolver.inl:194-262) with an optional Jacobi     */
+/* preconditioner (JacobiPreconditioner.inl:41-51: z = diag(A)^-1 r, the     */
+/* diagonal of the assembled system A = mF M + kF K with fixed DOFs set to   */
+/* one). The diagonal is re-assembled every solve from this step's           */
+/* rotations. Its summation order is this restatement's (component order,    */
+/* elements in index order); the reference assembles it through addKToMatrix */
+/* and addMToMatrix, which cannot be run here.                               */
+/* ------------------------------------------------------------------------- */
+
+/* diag(R^T S R) of node i's 3x3 stiffness block S = B^T C B of element e,
+ * with B from node i's strain-displacement values (a, b, c) and C the
+ * isotropic K3 = (k0, k1, k2); R = rot^T (rot holds rotations[e] = R^T). */
+static void element_stiffness_diag(const double* rot, const double* K3, const double* J3i, double dk[3])
+{
+    const double a = J3i[0], b = J3i[1], c = J3i[2];
+    const double k0 = K3[0], k1 = K3[1], k2 = K3[2];
+    const double k12 = k1 + k2;
+    const double S[9] = {a * a * k0 + b * b * k2 + c * c * k2, a * b * k12, a * c * k12,
+                         a * b * k12, b * b * k0 + a * a * k2 + c * c * k2, b * c * k12,
+                         a * c * k12, b * c * k12, c * c * k0 + b * b * k2 + a * a * k2};
+    for (int k = 0; k < 3; ++k) {
+        double acc = 0.0;
+        for (int p = 0; p < 3; ++p) {
+            double sr = S[3 * p] * rot[3 * k] + S[3 * p + 1] * rot[3 * k + 1] + S[3 * p + 2] * rot[3 * k + 2];
+            acc += rot[3 * k + p] * sr;
+        }
+        dk[k] = acc;
+    }
+}
+
+static void mass_diag_add(const orc_scene* s, double* d, double mf)
+{
+    for (int i = 0; i < s->n; ++i) {
+        const double m = (s->mass_kind == 1) ? s->node_mass[i] : s->vertex_mass;
+        for (int k = 0; k < 3; ++k) d[3 * i + k] += m * mf;
+    }
+}
+
+/* dinv = 1 / diag(mF M + kF K), fixed DOFs 1 */
+static void jacobi_inverse_diagonal(orc_scene* s, double mf, double kf, double* dinv)
+{
+    const long n3 = 3L * s->n;
+    memset(dinv, 0, sizeof(double) * (size_t)n3);
+    if (s->mass_first) mass_diag_add(s, dinv, mf);
+    if (s->fem) {
+        const orc_fem* m = s->fem;
+        for (int e = 0; e < m->n_tets; ++e)
+            for (int i = 0; i < 4; ++i) {
+                double dk[3];
+                element_stiffness_diag(&m->rot[9 * e], &m->K3[3 * e], &m->J3[12 * e + 3 * i], dk);
+                const int node = m->tets[4 * e + i];
+                for (int k = 0; k < 3; ++k) dinv[3 * node + k] += -kf * dk[k];
+            }
+    }
+    if (!s->mass_first) mass_diag_add(s, dinv, mf);
+    for (long i = 0; i < n3; ++i) dinv[i] = 1.0 / dinv[i];
+    if (s->fix_all) {
+        for (long i = 0; i < n3; ++i) dinv[i] = 1.0;
+    } else {
+        for (int f = 0; f < s->n_fixed; ++f)
+            if (s->fixed[f] >= 0 && s->fixed[f] < s->n)
+                for (int k = 0; k < 3; ++k) dinv[3 * s->fixed[f] + k] = 1.0;
+    }
+}
+
+/* out = a + out * f (vOp_avf, MechanicalObject.inl:1997-2011; f == 1: out += a) */
+static void vop_avf(double* out, const double* a, double f, long n3)
+{
+    if (f == 1.0)
+        for (long i = 0; i < n3; ++i) out[i] += a[i];
+    else
+        for (long i = 0; i < n3; ++i) {
+            out[i] *= f;
+            out[i] += a[i];
+        }
+}
+
+/* out += a * f (vOp_v_inc_bf; f == 1: out += a) */
+static void vop_inc(double* out, const double* a, double f, long n3)
+{
+    if (f == 1.0)
+        for (long i = 0; i < n3; ++i) out[i] += a[i];
+    else
+        for (long i = 0; i < n3; ++i) out[i] += a[i] * f;
+}
+
+static void precond_apply(const orc_scene* s, double* z, const double* r, long n3)
+{
+    if (s->precond)
+        for (long i = 0; i < n3; ++i) z[i] = s->dinv[i] * r[i];
+    else
+        memcpy(z, r, sizeof(double) * (size_t)n3);
+}
+
+/* The solution vector xs keeps the previous step's solution (the solver's
+ * x is not cleared between steps): r = b - A x starts from it. */
+static void pcg_solve(orc_scene* s, double mf, double kf)
+{
+    const int n = s->n;
+    const long n3 = 3L * n;
+    double *x = s->xs, *b = s->b, *r = s->r, *w = s->p, *sv = s->q;
+    /* PreconditionedMatrixFreeSystem assemblingRate (PreconditionedMatrixFreeSystem.inl:
+     * 48, 60-71): assembled on the first solve and every precond_rate solves */
+    if (s->precond && s->time_step_count % s->precond_rate == 0) jacobi_inverse_diagonal(s, mf, kf, s->dinv);
+    const double b_norm = vdot(b, b, n);
+    const double tol = s->cg_tol * b_norm;
+    matvec(s, r, x, mf, kf);
+    vop_avf(r, b, -1.0, n3); /* r = b - A x */
+    precond_apply(s, w, r, n3);
+    double r_norm = vdot(r, w, n);
+    int iter = 1;
+    while (iter <= s->cg_iters && r_norm > tol) {
+        matvec(s, sv, w, mf, kf);
+        const double dtq = vdot(w, sv, n);
+        const double alpha = r_norm / dtq;
+        vop_inc(x, w, alpha, n3);
+        vop_inc(r, sv, -alpha, n3);
+        precond_apply(s, sv, r, n3);
+        const double delta_old = r_norm;
+        r_norm = vdot(r, sv, n);
+        const double beta = r_norm / delta_old;
+        vop_avf(w, sv, beta, n3);
+        iter++;
+    }
+    s->last_iters = iter - 1;
+    s->last_err = (b_norm != 0.0) ? r_norm / b_norm : 0.0;
+    s->time_step_count++;
+}
+
+/* Selects the linear solver: 0 CGLinearSolver, 1 PCGLinearSolver; precond
+ * 1 = JacobiPreconditioner. */
+void orc_scene_set_solver(orc_scene* s, int solver, int precond, int precond_rate)
+{
+    s->solver = solver;
+    s->precond = precond;
+    s->precond_rate = precond_rate > 1 ? precond_rate : 1;
+    if (precond && !s->dinv) s->dinv = (double*)calloc(3 * (size_t)s->n, sizeof(double));
+}
+
+/* the last solve's Jacobi inverse diagonal (zeros before the first) */
+void orc_scene_jacobi(const orc_scene* s, double* out)
+{
+    if (s->dinv) memcpy(out, s->dinv, sizeof(double) * 3 * (size_t)s->n);
+    else memset(out, 0, sizeof(double) * 3 * (size_t)s->n);
+}
+
 /* computeForce (MappingGraphMechanicalOperations.cpp:41-92): f = 0,
  * f += externalForce, f += sum of the force fields' addForce. */
 static void scene_compute_force(orc_scene* s)
@@ -1152,7 +1303,10 @@ static void euler_step(orc_scene* s)
     /* setSystemMBKMatrix: mF = 1 + h rm, bF = -h, kF = -h (h + rs) */
     const double mf = 1 + 1.0 * h * s->rm;
     const double kf = -1.0 * h * (1.0 * h + s->rs);
-    cg_solve(s, mf, kf);
+    if (s->solver == 1)
+        pcg_solve(s, mf, kf);
+    else
+        cg_solve(s, mf, kf);
     /* vMultiOp fast path (MechanicalObject.inl:2206-2240): v += dv; x += v h */
     for (long i = 0; i < n3; ++i) {
         s->v[i] += s->xs[i];

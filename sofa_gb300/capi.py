@@ -53,6 +53,9 @@ class SceneParams(ctypes.Structure):
         ("mass_first", ctypes.c_int),
         ("serial_dots", ctypes.c_int),
         ("residual_replacement", ctypes.c_int),
+        ("linear_solver", ctypes.c_int),
+        ("preconditioner", ctypes.c_int),
+        ("preconditioner_rate", ctypes.c_int),
     ]
 
 
@@ -176,6 +179,8 @@ def load():
         "sgb_sofa_scene_body_info": (c_int, [_vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                              ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
         "sgb_sofa_scene_body_arrays": (c_int, [_vp, c_int, _ip, _dp, _ip]),
+        "sgb_sofa_scene_body_solver": (c_int, [_vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                               ctypes.POINTER(c_int), ctypes.POINTER(c_int), _dp]),
         "sgb_sofa_scene_init_device": (c_int, [_vp]),
         "sgb_sofa_scene_animate": (c_int, [_vp, c_int]),
         "sgb_sofa_scene_get_positions": (c_int, [_vp, c_int, _dp]),
@@ -303,7 +308,8 @@ class Scene:
     def __init__(self, fem: TetrahedronFEM, dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0,
                  cg_iterations=25, cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0),
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
-                 serial_dots=False, residual_replacement=0):
+                 serial_dots=False, residual_replacement=0, linear_solver="cg", preconditioner=None,
+                 preconditioner_rate=1):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -330,6 +336,9 @@ class Scene:
         p.mass_first = int(mass_first)
         p.serial_dots = int(serial_dots)
         p.residual_replacement = int(residual_replacement)
+        p.linear_solver = {"cg": 0, "pcg": 1}[linear_solver]
+        p.preconditioner = {None: 0, "jacobi": 1}[preconditioner]
+        p.preconditioner_rate = int(preconditioner_rate)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now
@@ -394,8 +403,9 @@ class Scene:
 
 def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0, cg_iterations=25,
                  cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0), vertex_mass=1.0,
-                 node_masses=None, fixed=(), fix_all=False, keep=None):
-    """A filled SceneParams; `keep` collects the numpy buffers it points to."""
+                 node_masses=None, fixed=(), fix_all=False, keep=None, linear_solver="cg", preconditioner=None):
+    """A filled SceneParams; `keep` collects the numpy buffers it points to.
+    linear_solver "cg" or "pcg"; preconditioner None or "jacobi" (PCG)."""
     lib = load()
     p = SceneParams()
     lib.sgb_scene_params_default(ctypes.byref(p))
@@ -418,6 +428,8 @@ def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.
     p.n_fixed = len(fixed)
     p.fix_all = int(fix_all)
     p.mass_first = 1
+    p.linear_solver = {"cg": 0, "pcg": 1}[linear_solver]
+    p.preconditioner = {None: 0, "jacobi": 1}[preconditioner]
     return p
 
 
@@ -644,6 +656,15 @@ class SofaScene:
         v = [ctypes.c_int() for _ in range(5)]
         check(load().sgb_sofa_scene_body_info(self._h, int(body), *[ctypes.byref(x) for x in v]))
         return dict(zip(("n_nodes", "n_tets", "method", "precision", "n_fixed"), (x.value for x in v)))
+
+    def body_solver(self, body=0) -> dict:
+        v = [ctypes.c_int() for _ in range(4)]
+        tol = ctypes.c_double()
+        check(load().sgb_sofa_scene_body_solver(self._h, int(body), *[ctypes.byref(x) for x in v], ctypes.byref(tol)))
+        names = ("linear_solver", "preconditioner", "preconditioner_rate", "iterations")
+        d = dict(zip(names, (x.value for x in v)))
+        d["tolerance"] = tol.value
+        return d
 
     def body_arrays(self, body=0):
         info = self.body_info(body)

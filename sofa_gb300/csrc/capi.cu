@@ -564,6 +564,7 @@ static void free_scene(sgb_scene* sc)
     cudaFree(s.v);
     cudaFree(s.node_mass);
     cudaFree(s.fixed);
+    cudaFree(s.dinv);
     cudaFree(s.ext);
     cudaFree(s.f);
     cudaFree(s.b);
@@ -596,6 +597,14 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: invalid fixed indices");
     if (P.residual_replacement < 0)
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: residual_replacement must be >= 0");
+    if (P.linear_solver != SGB_SOLVER_CG && P.linear_solver != SGB_SOLVER_PCG)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: unknown linear_solver");
+    if (P.preconditioner != SGB_PRECOND_NONE && P.preconditioner != SGB_PRECOND_JACOBI)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: unknown preconditioner");
+    if (P.preconditioner != SGB_PRECOND_NONE && P.linear_solver != SGB_SOLVER_PCG)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: a preconditioner needs linear_solver = PCG");
+    if (P.linear_solver == SGB_SOLVER_PCG && P.residual_replacement > 0)
+        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_create: residual replacement runs with CG only");
     if (P.residual_replacement > 0 &&
         (fem->m.precision != SGB_PRECISION_MIXED || fem->m.pl.n_patches == 0 || fem->m.method == SGB_METHOD_SMALL))
         return fail(SGB_ERR_NOT_SUPPORTED,
@@ -615,6 +624,9 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     s.prm.cg_threshold = P.cg_threshold;
     for (int k = 0; k < 3; ++k) s.prm.gravity[k] = P.gravity[k];
     s.prm.vertex_mass = P.vertex_mass;
+    s.prm.solver = P.linear_solver;
+    s.prm.precond = P.preconditioner;
+    s.prm.precond_rate = P.preconditioner_rate > 1 ? P.preconditioner_rate : 1;
     s.stream = fem->stream;
     sc->fem = fem;
     sc->ops = fem->ops;
@@ -638,6 +650,7 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
         goto fail_out;
     if (P.node_masses_host && (rc = dev_alloc(&s.node_mass, (size_t)N, acc))) goto fail_out;
     if (P.serial_dots && (rc = dev_alloc(&sc->dot_terms, (size_t)N, acc))) goto fail_out;
+    if (P.preconditioner == SGB_PRECOND_JACOBI && (rc = dev_alloc_bytes(&s.dinv, rs * 3 * N, acc))) goto fail_out;
     if (P.residual_replacement > 0) {
         // the FP64 copy of the operator, created from the force field's
         // inputs (rest positions and tetrahedra read back, caller order)

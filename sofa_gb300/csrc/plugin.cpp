@@ -98,6 +98,20 @@ int sgb_sofa_scene_body_info(const sgb_sofa_scene_t* scene, int body, int* n_nod
     return SGB_OK;
 }
 
+int sgb_sofa_scene_body_solver(const sgb_sofa_scene_t* scene, int body, int* linear_solver, int* preconditioner,
+                               int* preconditioner_rate, int* iterations, double* tolerance)
+{
+    if (!scene || body < 0 || body >= (int)scene->scene.bodies.size())
+        return fail(SGB_ERR_NOT_FOUND, "sgb_sofa_scene_body_solver: no such body");
+    const sgb_scene_params& p = scene->scene.bodies[(size_t)body].params;
+    if (linear_solver) *linear_solver = p.linear_solver;
+    if (preconditioner) *preconditioner = p.preconditioner;
+    if (preconditioner_rate) *preconditioner_rate = p.preconditioner_rate > 1 ? p.preconditioner_rate : 1;
+    if (iterations) *iterations = p.cg_iterations;
+    if (tolerance) *tolerance = p.cg_tolerance;
+    return SGB_OK;
+}
+
 int sgb_sofa_scene_body_arrays(const sgb_sofa_scene_t* scene, int body, int32_t* tetrahedra, double* node_masses,
                                int32_t* fixed)
 {

@@ -380,6 +380,36 @@ public:
     }
 };
 
+// PCGLinearSolver (PCGLinearSolver.inl:36-48): matrix-free PCG, optionally
+// preconditioned by a linked JacobiPreconditioner; PreconditionedMatrixFreeSystem
+// (PreconditionedMatrixFreeSystem.inl:31-34) sets how often the
+// preconditioner is assembled.
+class PCGLinearSolver : public PermissiveObject {
+public:
+    PCGLinearSolver() : PermissiveObject("PCGLinearSolver")
+    {
+        declare("iterations", "25", "maximum number of iterations");
+        declare("tolerance", "1e-5", "stop when r.z <= tolerance * b.b");
+        declare("use_precond", "1", "use the preconditioner");
+        declare("preconditioner", "", "link to the preconditioner (JacobiPreconditioner)");
+        declare("update_step", "1", "deprecated: assemblingRate of PreconditionedMatrixFreeSystem");
+        declare("graph", "", "");
+    }
+};
+
+class JacobiPreconditioner : public PermissiveObject {
+public:
+    JacobiPreconditioner() : PermissiveObject("JacobiPreconditioner") {}
+};
+
+class PreconditionedMatrixFreeSystem : public PermissiveObject {
+public:
+    PreconditionedMatrixFreeSystem() : PermissiveObject("PreconditionedMatrixFreeSystem")
+    {
+        declare("assemblingRate", "1", "the preconditioner is assembled every this many steps");
+    }
+};
+
 class DefaultAnimationLoop : public PermissiveObject {
 public:
     DefaultAnimationLoop() : PermissiveObject("DefaultAnimationLoop") {}
@@ -606,6 +636,7 @@ int Scene::init_host(std::string* err)
         stack.pop_back();
         for (auto it = n->children.rbegin(); it != n->children.rend(); ++it) stack.push_back(it->get());
         BaseObject *euler = nullptr, *cg = nullptr, *mo = nullptr, *topo = nullptr, *fem = nullptr, *mass = nullptr;
+        BaseObject *pcg = nullptr, *pmfs = nullptr;
         int fem_pos = -1, mass_pos = -1;
         std::vector<BaseObject*> fixed;
         for (size_t i = 0; i < n->objects.size(); ++i) {
@@ -613,6 +644,8 @@ int Scene::init_host(std::string* err)
             const std::string& c = o->class_name();
             if (c == "EulerImplicitSolver") euler = o;
             else if (c == "CGLinearSolver") cg = o;
+            else if (c == "PCGLinearSolver") pcg = o;
+            else if (c == "PreconditionedMatrixFreeSystem") pmfs = o;
             else if (c == "MechanicalObject" && !mo) mo = o;
             else if (c == "TetrahedronSetTopologyContainer" && !topo) topo = o;
             else if (c == "TetrahedronFEMForceField") {
@@ -630,7 +663,9 @@ int Scene::init_host(std::string* err)
         if (!euler) continue;
         const std::string where = "node '" + n->name + "': ";
         if (!mo) return unsupported(err, where + "EulerImplicitSolver without a MechanicalObject in the same node");
-        if (!cg) return unsupported(err, where + "EulerImplicitSolver needs a CGLinearSolver in the same node");
+        if (!cg && !pcg)
+            return unsupported(err, where + "EulerImplicitSolver needs a CGLinearSolver or PCGLinearSolver in the same node");
+        if (cg && pcg) return unsupported(err, where + "both a CGLinearSolver and a PCGLinearSolver");
         if (!fem) return unsupported(err, where + "no TetrahedronFEMForceField");
         if (!topo) return unsupported(err, where + "no TetrahedronSetTopologyContainer");
         Body b;
@@ -671,15 +706,32 @@ int Scene::init_host(std::string* err)
         // EulerImplicitSolver + CGLinearSolver
         if (euler->get_bool(*this, "firstOrder") || euler->get_bool(*this, "trapezoidalScheme"))
             return unsupported(err, where + "firstOrder / trapezoidalScheme are not supported");
-        if (cg->get_bool(*this, "warmStart")) return unsupported(err, where + "CG warmStart is not supported");
+        if (cg && cg->get_bool(*this, "warmStart")) return unsupported(err, where + "CG warmStart is not supported");
         sgb_scene_params_default(&b.params);
         b.params.dt = dt;
         b.params.rayleigh_stiffness = euler->get_real(*this, "rayleighStiffness");
         b.params.rayleigh_mass = euler->get_real(*this, "rayleighMass");
         b.params.vdamping = euler->get_real(*this, "vdamping");
-        b.params.cg_iterations = cg->get_int(*this, "iterations");
-        b.params.cg_tolerance = cg->get_real(*this, "tolerance");
-        b.params.cg_threshold = cg->get_real(*this, "threshold");
+        if (cg) {
+            b.params.cg_iterations = cg->get_int(*this, "iterations");
+            b.params.cg_tolerance = cg->get_real(*this, "tolerance");
+            b.params.cg_threshold = cg->get_real(*this, "threshold");
+        } else {
+            b.params.linear_solver = SGB_SOLVER_PCG;
+            b.params.cg_iterations = pcg->get_int(*this, "iterations");
+            b.params.cg_tolerance = pcg->get_real(*this, "tolerance");
+            const std::string link = pcg->get_string("preconditioner");
+            if (!link.empty() && pcg->get_bool(*this, "use_precond")) {
+                BaseObject* pre = resolve_object(n, link);
+                if (!pre) return unsupported(err, where + "PCGLinearSolver preconditioner '" + link + "' not found");
+                if (pre->class_name() != "JacobiPreconditioner")
+                    return unsupported(err, where + "PCGLinearSolver preconditioner " + pre->class_name() +
+                                                " is not supported (JacobiPreconditioner is)");
+                b.params.preconditioner = SGB_PRECOND_JACOBI;
+            }
+            int rate = pmfs ? pmfs->get_int(*this, "assemblingRate") : pcg->get_int(*this, "update_step");
+            b.params.preconditioner_rate = rate > 1 ? rate : 1;
+        }
         for (int k = 0; k < 3; ++k) b.params.gravity[k] = gravity[k];
         // mass
         if (!mass) return unsupported(err, where + "no mass component (UniformMass or DiagonalMass)");
@@ -820,6 +872,12 @@ void register_components(ObjectFactory& f)
                       make<TetrahedronFEMForceField>());
     f.register_object("EulerImplicitSolver", "implicit Euler integration", mod, make<EulerImplicitSolver>());
     f.register_object("CGLinearSolver", "matrix-free conjugate gradient", mod, make<CGLinearSolver>());
+    f.register_object("PCGLinearSolver", "matrix-free preconditioned conjugate gradient", mod,
+                      make<PCGLinearSolver>());
+    f.register_object("JacobiPreconditioner", "diagonal (Jacobi) preconditioner", mod,
+                      make<JacobiPreconditioner>());
+    f.register_object("PreconditionedMatrixFreeSystem", "matrix-free system with an assembled preconditioner", mod,
+                      make<PreconditionedMatrixFreeSystem>());
     f.register_object("DefaultAnimationLoop", "animation loop", mod, make<DefaultAnimationLoop>());
     f.register_object("WriteState", "state export (T= / X= / V= lines)", mod, make<WriteState>());
 }

@@ -121,6 +121,7 @@ struct CgScalars {
     double normb;
     double rho, rho_prev, den, alpha, beta;
     double last_err;
+    double bnorm2;  // PCG: b.b of the current solve
     long long time_step_count;
     int done;
     int iters;
@@ -137,6 +138,9 @@ struct SceneParams {
     double cg_tolerance = 1e-5, cg_threshold = 1e-5;
     double gravity[3] = {0.0, -9.81, 0.0};
     double vertex_mass = 1.0;
+    int solver = 0;   // 0 CGLinearSolver, 1 PCGLinearSolver
+    int precond = 0;  // PCG: 1 Jacobi
+    int precond_rate = 1;  // the preconditioner is re-assembled every this many steps
 };
 
 struct Scene {
@@ -159,6 +163,7 @@ struct Scene {
     void* p2 = nullptr;            // second CG direction buffer (patch path ping-pong)
     void* q = nullptr;
     void* r = nullptr;
+    void* dinv = nullptr;          // PCG + Jacobi: inverse diagonal of the system (3 per node)
     CgScalars* cg = nullptr;
     CgScalars* cg_h = nullptr;  // pinned mirror for reads
     cudaStream_t stream = nullptr;

@@ -608,7 +608,7 @@ __device__ __forceinline__ R cg_dir(R r, R pold, R beta)
 template <typename R, typename VIN, int METHOD, int DIR>
 __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, const VIN* __restrict__ dx,
                                                  const R* __restrict__ pold, R beta, R fact,
-                                                 R* __restrict__ eforce)
+                                                 R* __restrict__ eforce, const R* __restrict__ dinv = nullptr)
 {
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
@@ -619,6 +619,13 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
     for (int i = 0; i < 4; ++i) {
         VIN v3[3];
         ld3(dx, node[i], v3);
+        if (DIR != 0 && dinv) {
+            // PCG: the direction is built from z = diag^-1 r (Jacobi)
+            R dv[3];
+            ld3(dinv, node[i], dv);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) v3[k] = (VIN)(dv[k] * (R)v3[k]);
+        }
         if (DIR == 2) {
             R po[3];
             ld3(pold, node[i], po);
@@ -688,13 +695,14 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
 template <typename R, typename VIN, int METHOD, int DIR>
 __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, const VIN* __restrict__ dx,
                                                             const R* __restrict__ pold, const CgScalars* cg,
-                                                            R fact, R* __restrict__ eforce)
+                                                            R fact, R* __restrict__ eforce,
+                                                            const R* __restrict__ dinv)
 {
     if (DIR != 0 && cg->done) return;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ev.n_tets) return;
     const R beta = (DIR == 2) ? (R)cg->beta : R(0);
-    elem_dforce_body<R, VIN, METHOD, DIR>(ev, e, dx, pold, beta, fact, eforce);
+    elem_dforce_body<R, VIN, METHOD, DIR>(ev, e, dx, pold, beta, fact, eforce, dinv);
 }
 
 // ------------------------------------------------------------------------
@@ -764,11 +772,12 @@ __device__ __forceinline__ double dot3(const A a[3], const B b[3])
     return r;
 }
 
-enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2, FIN_REPLACE = 3 };
+enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2, FIN_REPLACE = 3, FIN_PCG_START = 4 };
 
 struct SolveConsts {
     double tol, threshold;
-    int it;  // CG iteration this kernel belongs to (1-based)
+    int it;   // CG iteration this kernel belongs to (1-based)
+    int pcg;  // 1: PCGLinearSolver bookkeeping (r.z, tolerance * b.b, no threshold test)
 };
 
 // Last-block finish of a dot product: every block writes its partial; the
@@ -810,6 +819,36 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         return;
     }
     const bool first_of_first = (sc.it == 1 && cg->time_step_count == 0);
+    if (sc.pcg) {
+        // PCGLinearSolver::solve (PCGLinearSolver.inl:194-262): r_norm = r.z,
+        // tol = tolerance * b.b, loop while r_norm > tol, no threshold test
+        const double bb = cg->bnorm2;
+        if (FIN == FIN_RHS) {
+            cg->bnorm2 = total;
+            cg->normb = sqrt(total);
+            cg->iters = 0;
+            cg->last_err = 0.0;
+            cg->done = 0;
+        } else if (FIN == FIN_PCG_START) {
+            cg->rho = total;
+            cg->last_err = bb != 0.0 ? total / bb : 0.0;
+            cg->done = (total > sc.tol * bb) ? 0 : 1;
+        } else if (FIN == FIN_DEN) {
+            cg->den = total;
+            if (total != 0.0)
+                cg->alpha = cg->rho / total;
+            else
+                cg->done = 1;
+        } else if (FIN == FIN_RHO) {
+            cg->rho_prev = cg->rho;
+            cg->rho = total;
+            cg->iters = sc.it;
+            cg->beta = total / cg->rho_prev;
+            cg->last_err = bb != 0.0 ? total / bb : 0.0;
+            cg->done = (total > sc.tol * bb) ? 0 : 1;
+        }
+        return;
+    }
     if (FIN == FIN_RHS) {
         // x = 0; r = b; normb = |b|; iteration 1 starts with rho = r.r
         cg->rho = total;
@@ -961,7 +1000,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R*
         for (int k = 0; k < 3; ++k) {
             b[3 * (size_t)n + k] = a[k];
             r[3 * (size_t)n + k] = a[k];
-            xs[3 * (size_t)n + k] = R(0);
+            if (!sc.pcg) xs[3 * (size_t)n + k] = R(0);  // PCG starts from the previous solution
         }
         double d = dot3(a, a);
         if (terms) terms[n] = d;
@@ -979,7 +1018,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const
                                                               MassArgs ma, double mf, int mass_first,
                                                               const uint8_t* __restrict__ fixed,
                                                               R* __restrict__ q, CgScalars* cg, double* terms,
-                                                              int N, SolveConsts sc)
+                                                              int N, SolveConsts sc,
+                                                              const R* __restrict__ dinv = nullptr)
 {
     if (cg->done) return;
     const R mm = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
@@ -990,6 +1030,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             R rv = r[3 * (size_t)n + k];
+            if (dinv) rv = dinv[3 * (size_t)n + k] * rv;  // PCG: z = diag^-1 r
             pp[k] = (DIR == 2) ? cg_dir(rv, p[3 * (size_t)n + k], beta) : rv;
         }
         R a[3] = {R(0), R(0), R(0)};
@@ -1020,7 +1061,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_cg_update(R* __restrict__ xs, R* __restrict__ r,
                                                           const R* __restrict__ p, const R* __restrict__ q,
-                                                          CgScalars* cg, double* terms, int N, SolveConsts sc)
+                                                          CgScalars* cg, double* terms, int N, SolveConsts sc,
+                                                          const R* __restrict__ dinv = nullptr)
 {
     if (cg->done) return;
     const R alpha = (R)cg->alpha;
@@ -1037,11 +1079,132 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_update(R* __restrict__ xs, R*
             rr[k] = r[i] + u;
             r[i] = rr[k];
         }
-        double d = dot3(rr, rr);
+        R zz[3] = {rr[0], rr[1], rr[2]};
+        if (dinv)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) zz[k] = dinv[3 * (size_t)n + k] * rr[k];
+        double d = dot3(rr, zz);
         if (terms) terms[n] = d;
         local += d;
     }
     finish_dot<FIN_RHO>(local, cg, terms, N, sc);
+}
+
+// ---- PCGLinearSolver with the Jacobi preconditioner ------------------------
+// (PCGLinearSolver.inl:194-262, JacobiPreconditioner.inl:41-51) on the
+// element-order kernels.
+
+// Jacobi diagonal, element part: for node i of element e the diagonal of
+// R^T S R, S = B_i^T C B_i its 3x3 stiffness block (B_i from the node's
+// strain-displacement values, C the isotropic material matrix), times -kF:
+// the element's contribution to diag(mF M + kF K).
+template <typename R, int METHOD>
+__global__ void __launch_bounds__(kElemBlock) k_elem_jacobi(ElemView<R> ev, R nkf, R* __restrict__ eforce,
+                                                             const CgScalars* cg, int rate)
+{
+    if (cg->time_step_count % rate != 0) return;  // assembled on the first step and every `rate` steps
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ev.n_tets) return;
+    R K[3], J[12], Rm[9];
+    load_KJ(ev, (size_t)e, K, J);
+    if (METHOD == METHOD_SMALL) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rm[i] = (i % 4 == 0) ? R(1) : R(0);
+    } else {
+        load_rot(ev, (size_t)e, Rm);
+    }
+    const R k0 = K[0], k1 = K[1], k2 = K[2], k12 = k1 + k2;
+    R c[12];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const R a = J[3 * i], b = J[3 * i + 1], cc = J[3 * i + 2];
+        const R S[9] = {a * a * k0 + b * b * k2 + cc * cc * k2, a * b * k12, a * cc * k12,
+                        a * b * k12, b * b * k0 + a * a * k2 + cc * cc * k2, b * cc * k12,
+                        a * cc * k12, b * cc * k12, cc * cc * k0 + b * b * k2 + a * a * k2};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            R acc = R(0);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                const R sr = S[3 * p] * Rm[k] + S[3 * p + 1] * Rm[3 + k] + S[3 * p + 2] * Rm[6 + k];
+                acc += Rm[3 * p + k] * sr;
+            }
+            c[3 * i + k] = nkf * acc;
+        }
+    }
+    store_eforce(eforce, e, c);
+}
+
+// Jacobi diagonal, node part: dinv = 1 / (mF m + element terms in element
+// order; mass first or last as in the node), fixed DOFs one.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_gather_jacobi(NodeCSR csr, const R* __restrict__ eforce, MassArgs ma,
+                                                              double mf, int mass_first,
+                                                              const uint8_t* __restrict__ fixed,
+                                                              R* __restrict__ dinv, int N, const CgScalars* cg,
+                                                              int rate)
+{
+    if (cg->time_step_count % rate != 0) return;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const R mm = (R)((ma.node_mass ? ma.node_mass[n] : ma.vertex_mass) * mf);
+        R d[3] = {R(0), R(0), R(0)};
+        if (mass_first)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) d[k] += mm;
+        for (int s = csr.rowptr[n]; s < csr.rowptr[n + 1]; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            d[0] += c[0];
+            d[1] += c[1];
+            d[2] += c[2];
+        }
+        if (!mass_first)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) d[k] += mm;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dinv[3 * (size_t)n + k] = fixed[n] ? R(1) : R(1) / d[k];
+    }
+}
+
+// PCG start: r = b - A x with x the previous step's solution (its K terms
+// in eforce), z = diag^-1 r (or r), r.z.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_pcg_start(NodeCSR csr, const R* __restrict__ eforce,
+                                                          const R* __restrict__ xs, const R* __restrict__ b,
+                                                          MassArgs ma, double mf, int mass_first,
+                                                          const uint8_t* __restrict__ fixed,
+                                                          const R* __restrict__ dinv, R* __restrict__ r,
+                                                          CgScalars* cg, double* terms, int N, SolveConsts sc)
+{
+    const R mm = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    double local = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R pp[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) pp[k] = xs[3 * (size_t)n + k];
+        R a[3] = {R(0), R(0), R(0)};
+        if (mass_first) add_mdx(a, pp, ma, mf, mm, n);
+        for (int s = csr.rowptr[n]; s < csr.rowptr[n + 1]; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            a[0] -= c[0];
+            a[1] -= c[1];
+            a[2] -= c[2];
+        }
+        if (!mass_first) add_mdx(a, pp, ma, mf, mm, n);
+        if (fixed[n]) a[0] = a[1] = a[2] = R(0);
+        R rr[3], z[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const size_t i = 3 * (size_t)n + k;
+            R t = a[k] * R(-1);  // r = b + (A x) * -1 (vOp_avf)
+            rr[k] = t + b[i];
+            r[i] = rr[k];
+            z[k] = dinv ? dinv[i] * rr[k] : rr[k];
+        }
+        double d = dot3(rr, z);
+        if (terms) terms[n] = d;
+        local += d;
+    }
+    finish_dot<FIN_PCG_START>(local, cg, terms, N, sc);
 }
 
 // Euler update (MechanicalObject::vMultiOp fast path, MechanicalObject.inl:
@@ -1897,15 +2060,18 @@ void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
 }
 
 template <typename R, typename VIN, int DIR>
-void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScalars* cg, R fact, cudaStream_t s)
+void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScalars* cg, R fact, cudaStream_t s,
+                        const R* dinv = nullptr)
 {
     if (m->n_tets == 0) return;
     ElemView<R> ev = view<R>(m);
     const int g = elem_grid(m->n_tets);
     if (m->method == METHOD_SMALL)
-        k_elem_dforce<R, VIN, METHOD_SMALL, DIR><<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce);
+        k_elem_dforce<R, VIN, METHOD_SMALL, DIR>
+            <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, dinv);
     else
-        k_elem_dforce<R, VIN, METHOD_LARGE, DIR><<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce);
+        k_elem_dforce<R, VIN, METHOD_LARGE, DIR>
+            <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, dinv);
 }
 
 inline PatchView patch_view(TfemMesh* m)
@@ -2101,7 +2267,9 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     R* p = (R*)sc->p;
     R* q = (R*)sc->q;
     R* xs = (R*)sc->xs;
-    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1};
+    const bool pcg = P.solver == 1;
+    R* dinv = pcg ? (R*)sc->dinv : nullptr;  // null: no preconditioner
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0};
     // f = F(x)
     launch_elem_force<R>(m, sc->x, s);
     k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
@@ -2110,21 +2278,42 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)kf_rhs, s);
     k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass, mass_first,
                                               h, sc->fixed, b, r, xs, sc->cg, dot_terms, N, cons);
-    // CG on (mF M + kF K) dv = b
+    // CG (or PCG) on (mF M + kF K) dv = b
     const double mf = 1 + 1.0 * h * P.rayleigh_mass;
     const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    if (pcg) {
+        if (dinv) {
+            // Jacobi diagonal from this step's rotations
+            ElemView<R> ev = view<R>(m);
+            const int ge = elem_grid(m->n_tets);
+            if (m->n_tets > 0) {
+                if (m->method == METHOD_SMALL)
+                    k_elem_jacobi<R, METHOD_SMALL>
+                        <<<ge, kElemBlock, 0, s>>>(ev, (R)(-kf), (R*)m->eforce, sc->cg, P.precond_rate);
+                else
+                    k_elem_jacobi<R, METHOD_LARGE>
+                        <<<ge, kElemBlock, 0, s>>>(ev, (R)(-kf), (R*)m->eforce, sc->cg, P.precond_rate);
+            }
+            k_gather_jacobi<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, ma, mf, mass_first, sc->fixed,
+                                                         dinv, N, sc->cg, P.precond_rate);
+        }
+        // r = b - A x from the previous step's solution
+        launch_elem_dforce<R, R, 0>(m, xs, nullptr, sc->cg, (R)kf, s);
+        k_pcg_start<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, xs, b, ma, mf, mass_first, sc->fixed,
+                                                 dinv, r, sc->cg, dot_terms, N, cons);
+    }
     for (int it = 1; it <= P.cg_iterations; ++it) {
         cons.it = it;
         if (it == 1) {
-            launch_elem_dforce<R, R, 1>(m, r, p, sc->cg, (R)kf, s);
+            launch_elem_dforce<R, R, 1>(m, r, p, sc->cg, (R)kf, s, dinv);
             k_gather_matvec<R, 1><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf, mass_first,
-                                                            sc->fixed, q, sc->cg, dot_terms, N, cons);
+                                                            sc->fixed, q, sc->cg, dot_terms, N, cons, dinv);
         } else {
-            launch_elem_dforce<R, R, 2>(m, r, p, sc->cg, (R)kf, s);
+            launch_elem_dforce<R, R, 2>(m, r, p, sc->cg, (R)kf, s, dinv);
             k_gather_matvec<R, 2><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf, mass_first,
-                                                            sc->fixed, q, sc->cg, dot_terms, N, cons);
+                                                            sc->fixed, q, sc->cg, dot_terms, N, cons, dinv);
         }
-        k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons);
+        k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons, dinv);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);

@@ -26,13 +26,15 @@ def oracle_scene(oracle, mesh, method="large", cfg=BEAM_SMALL, young=None, poiss
 
 
 def gpu_scene(capi, mesh, method="large", precision="fp64", cfg=BEAM_SMALL, serial_dots=False, young=None,
-              poisson=None):
+              poisson=None, **solver):
+    """`solver`: linear_solver / preconditioner / preconditioner_rate of capi.Scene."""
     fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, cfg["young"] if young is None else young,
                               cfg["poisson"] if poisson is None else poisson, method, precision)
     return capi.Scene(fem, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"], rayleigh_mass=cfg["rm"],
                       cg_iterations=cfg["cg_iterations"], cg_tolerance=cfg["cg_tolerance"],
                       cg_threshold=cfg["cg_threshold"], gravity=cfg["gravity"],
-                      vertex_mass=cfg["total_mass"] / mesh.n_nodes, fixed=mesh.fixed, serial_dots=serial_dots)
+                      vertex_mass=cfg["total_mass"] / mesh.n_nodes, fixed=mesh.fixed, serial_dots=serial_dots,
+                      **solver)
 
 
 def rel_err(a, b):

@@ -104,3 +104,29 @@ def test_write_state_records(capi, tmp_path):
     rec2 = _records(timed)
     assert [t for t, _ in rec2] == pytest.approx([0.02, 0.05, 0.08])
     assert set(rec2[0][1]) == {"X"}
+
+
+def test_pcg_jacobi_scene_file_against_oracle(capi, oracle):
+    """The known-answer grid scene with PCGLinearSolver + JacobiPreconditioner
+    (assembled every 4 steps) instead of CG: 30 steps against the oracle's PCG
+    on the same inputs (30 iterations every step, tolerance 0: no stopping
+    test that dot-product rounding could move)."""
+    text = _read("grid_fem_4x10x4.scn").replace(
+        '<CGLinearSolver iterations="20" tolerance="1e-5" threshold="1e-6" />',
+        '<PreconditionedMatrixFreeSystem assemblingRate="4"/>\n'
+        '        <PCGLinearSolver iterations="30" tolerance="0" preconditioner="@precond"/>\n'
+        '        <JacobiPreconditioner name="precond"/>')
+    s = capi.SofaScene(text)
+    s.animate(30)
+    x = s.positions(0)
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+    osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01, cg_iterations=30,
+                             cg_tolerance=0.0, cg_threshold=1e-6)
+    osc.set_solver("pcg", "jacobi", 4)
+    osc.step(30)
+    xo, _ = osc.state()
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+    assert np.max(np.abs(xo - pos)) > 1e-3

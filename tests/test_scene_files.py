@@ -161,3 +161,24 @@ def test_unsupported_component_settings(capi, edit, msg):
     with pytest.raises(capi.SgbError) as e:
         capi.SofaScene(xml)
     assert e.value.code == -4 and msg in str(e.value)
+
+
+PCG_SCENE = ('<CGLinearSolver iterations="20" tolerance="1e-5" threshold="1e-6" />',
+             '<PreconditionedMatrixFreeSystem assemblingRate="4"/>\n'
+             '        <PCGLinearSolver name="PCG" iterations="30" tolerance="1e-9" preconditioner="@precond"/>\n'
+             '        <JacobiPreconditioner name="precond" template="DiagonalMatrix"/>')
+
+
+def test_pcg_jacobi_scene(capi):
+    """PCGLinearSolver + JacobiPreconditioner (+ PreconditionedMatrixFreeSystem
+    assemblingRate), as in the reference's FEMBAR_PCG_JacobiPreconditioner.scn."""
+    s = capi.SofaScene(_read("grid_fem_4x10x4.scn").replace(*PCG_SCENE))
+    assert s.body_solver(0) == {"linear_solver": 1, "preconditioner": 1, "preconditioner_rate": 4,
+                                "iterations": 30, "tolerance": pytest.approx(1e-9)}
+    plain = capi.SofaScene(_read("grid_fem_4x10x4.scn").replace(
+        PCG_SCENE[0], '<PCGLinearSolver iterations="12" use_precond="0" preconditioner="@p"/><JacobiPreconditioner name="p"/>'))
+    assert plain.body_solver(0)["preconditioner"] == 0
+    with pytest.raises(capi.SgbError) as e:
+        capi.SofaScene(_read("grid_fem_4x10x4.scn").replace(
+            PCG_SCENE[0], '<PCGLinearSolver preconditioner="@p"/><BlockJacobiPreconditioner name="p"/>'))
+    assert e.value.code in (-4,)
