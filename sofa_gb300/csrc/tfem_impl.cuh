@@ -605,7 +605,7 @@ __device__ __forceinline__ R cg_dir(R r, R pold, R beta)
 // addDForce element part: applyStiffnessSmall / applyStiffnessCorotational
 // (TFEM.inl:721-749, 1193-1237). Writes the corner terms R K (R^T dx) fact
 // that the gather subtracts.
-template <typename R, typename VIN, int METHOD, int DIR>
+template <typename R, typename VIN, int METHOD, int DIR, int PC = 0>
 __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, const VIN* __restrict__ dx,
                                                  const R* __restrict__ pold, R beta, R fact,
                                                  R* __restrict__ eforce, const R* __restrict__ dinv = nullptr)
@@ -619,7 +619,7 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
     for (int i = 0; i < 4; ++i) {
         VIN v3[3];
         ld3(dx, node[i], v3);
-        if (DIR != 0 && dinv) {
+        if constexpr (PC != 0 && DIR != 0) {
             // PCG: the direction is built from z = diag^-1 r (Jacobi)
             R dv[3];
             ld3(dinv, node[i], dv);
@@ -692,7 +692,7 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
     store_eforce(eforce, e, c);
 }
 
-template <typename R, typename VIN, int METHOD, int DIR>
+template <typename R, typename VIN, int METHOD, int DIR, int PC = 0>
 __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, const VIN* __restrict__ dx,
                                                             const R* __restrict__ pold, const CgScalars* cg,
                                                             R fact, R* __restrict__ eforce,
@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, cons
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ev.n_tets) return;
     const R beta = (DIR == 2) ? (R)cg->beta : R(0);
-    elem_dforce_body<R, VIN, METHOD, DIR>(ev, e, dx, pold, beta, fact, eforce, dinv);
+    elem_dforce_body<R, VIN, METHOD, DIR, PC>(ev, e, dx, pold, beta, fact, eforce, dinv);
 }
 
 // ------------------------------------------------------------------------
@@ -1012,7 +1012,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R*
 // q = A p for GraphScatteredMatrix::apply (GraphScatteredTypes.cpp:33-45):
 // q = mF M p - (K p terms), projected; also stores the direction p and
 // the dot p.q.
-template <typename R, int DIR>
+template <typename R, int DIR, int PC = 0>
 __global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const R* __restrict__ eforce,
                                                               const R* __restrict__ r, R* __restrict__ p,
                                                               MassArgs ma, double mf, int mass_first,
@@ -1030,7 +1030,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             R rv = r[3 * (size_t)n + k];
-            if (dinv) rv = dinv[3 * (size_t)n + k] * rv;  // PCG: z = diag^-1 r
+            if constexpr (PC != 0) rv = dinv[3 * (size_t)n + k] * rv;  // PCG: z = diag^-1 r
             pp[k] = (DIR == 2) ? cg_dir(rv, p[3 * (size_t)n + k], beta) : rv;
         }
         R a[3] = {R(0), R(0), R(0)};
@@ -1058,7 +1058,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_matvec(NodeCSR csr, const
 
 // cgstep_alpha (CGLinearSolver.cpp:47-63): x += alpha p; r += -alpha q; then
 // rho = r.r for the next iteration.
-template <typename R>
+template <typename R, int PC = 0>
 __global__ void __launch_bounds__(kNodeBlock) k_cg_update(R* __restrict__ xs, R* __restrict__ r,
                                                           const R* __restrict__ p, const R* __restrict__ q,
                                                           CgScalars* cg, double* terms, int N, SolveConsts sc,
@@ -1079,11 +1079,15 @@ __global__ void __launch_bounds__(kNodeBlock) k_cg_update(R* __restrict__ xs, R*
             rr[k] = r[i] + u;
             r[i] = rr[k];
         }
-        R zz[3] = {rr[0], rr[1], rr[2]};
-        if (dinv)
+        double d;
+        if constexpr (PC != 0) {
+            R zz[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) zz[k] = dinv[3 * (size_t)n + k] * rr[k];
-        double d = dot3(rr, zz);
+            d = dot3(rr, zz);
+        } else {
+            d = dot3(rr, rr);
+        }
         if (terms) terms[n] = d;
         local += d;
     }
@@ -2066,12 +2070,23 @@ void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScala
     if (m->n_tets == 0) return;
     ElemView<R> ev = view<R>(m);
     const int g = elem_grid(m->n_tets);
-    if (m->method == METHOD_SMALL)
-        k_elem_dforce<R, VIN, METHOD_SMALL, DIR>
-            <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, dinv);
-    else
-        k_elem_dforce<R, VIN, METHOD_LARGE, DIR>
-            <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, dinv);
+    // the preconditioned variant is a separate instantiation: the CG
+    // kernels carry no test for it
+    if (m->method == METHOD_SMALL) {
+        if (dinv)
+            k_elem_dforce<R, VIN, METHOD_SMALL, DIR, 1>
+                <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, dinv);
+        else
+            k_elem_dforce<R, VIN, METHOD_SMALL, DIR, 0>
+                <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, nullptr);
+    } else {
+        if (dinv)
+            k_elem_dforce<R, VIN, METHOD_LARGE, DIR, 1>
+                <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, dinv);
+        else
+            k_elem_dforce<R, VIN, METHOD_LARGE, DIR, 0>
+                <<<g, kElemBlock, 0, s>>>(ev, dx, pold, cg, fact, (R*)m->eforce, nullptr);
+    }
 }
 
 inline PatchView patch_view(TfemMesh* m)
@@ -2306,14 +2321,27 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
         cons.it = it;
         if (it == 1) {
             launch_elem_dforce<R, R, 1>(m, r, p, sc->cg, (R)kf, s, dinv);
-            k_gather_matvec<R, 1><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf, mass_first,
-                                                            sc->fixed, q, sc->cg, dot_terms, N, cons, dinv);
+            if (dinv)
+                k_gather_matvec<R, 1, 1><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf,
+                                                                   mass_first, sc->fixed, q, sc->cg, dot_terms, N,
+                                                                   cons, dinv);
+            else
+                k_gather_matvec<R, 1><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf,
+                                                                mass_first, sc->fixed, q, sc->cg, dot_terms, N, cons);
         } else {
             launch_elem_dforce<R, R, 2>(m, r, p, sc->cg, (R)kf, s, dinv);
-            k_gather_matvec<R, 2><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf, mass_first,
-                                                            sc->fixed, q, sc->cg, dot_terms, N, cons, dinv);
+            if (dinv)
+                k_gather_matvec<R, 2, 1><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf,
+                                                                   mass_first, sc->fixed, q, sc->cg, dot_terms, N,
+                                                                   cons, dinv);
+            else
+                k_gather_matvec<R, 2><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, r, p, ma, mf,
+                                                                mass_first, sc->fixed, q, sc->cg, dot_terms, N, cons);
         }
-        k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons, dinv);
+        if (dinv)
+            k_cg_update<R, 1><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons, dinv);
+        else
+            k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);
