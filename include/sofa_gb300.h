@@ -109,6 +109,17 @@ int sgb_tfem_add_dforce_f32(sgb_tfem_t* fem, const float* dx_dev, float* df_dev,
  * getActualTetraRotation / getInitialTetraRotation). Synchronous. */
 int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* initial_rotations_host);
 
+/* The assembled stiffness df/dx at the current rotations (those of the last
+ * addForce), as TetrahedronFEMForceField::buildStiffnessMatrix assembles it
+ * (TetrahedronFEMForceField.inl:1965-1993): block-sparse rows of 3x3 blocks,
+ * block (i, j) = - sum over the elements holding nodes i and j (in element
+ * order) of R^T S_ij R. rowptr_host: n_nodes + 1 entries; cols_host and
+ * values_host (9 doubles per block, row-major): n_blocks entries. Call with
+ * NULL arrays to get n_blocks; the pattern is built on the first call.
+ * Synchronous. df/dx times dx equals addDForce with kFactor 1. */
+int sgb_tfem_stiffness_bsr(sgb_tfem_t* fem, int* n_blocks, int32_t* rowptr_host, int32_t* cols_host,
+                           double* values_host);
+
 /* Reads and clears the force field's sticky device error flag (synchronises
  * the device). SGB_OK, or SGB_ERR_DEVICE_TIMEOUT when a bounded device-side
  * wait of an earlier add_dforce (the completion of the bulk copies that

@@ -138,6 +138,7 @@ def load():
         "sgb_tfem_add_dforce": (c_int, [_vp, _vp, _vp, c_double, _vp]),
         "sgb_tfem_add_dforce_f32": (c_int, [_vp, _vp, _vp, c_float, _vp]),
         "sgb_tfem_get_rotations": (c_int, [_vp, _dp, _dp]),
+        "sgb_tfem_stiffness_bsr": (c_int, [_vp, ctypes.POINTER(c_int), _ip, _ip, _dp]),
         "sgb_tfem_check_device": (c_int, [_vp]),
         "sgb_tfem_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                   ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_size_t)]),
@@ -294,6 +295,18 @@ class TetrahedronFEM:
         r0 = np.zeros((self.n_tets, 3, 3))
         check(load().sgb_tfem_get_rotations(self._h, r.ctypes.data_as(_dp), r0.ctypes.data_as(_dp)))
         return r, r0
+
+    def stiffness_bsr(self):
+        """The assembled df/dx at the current rotations as (rowptr, cols,
+        blocks[n_blocks, 3, 3]) (buildStiffnessMatrix)."""
+        nb = ctypes.c_int()
+        check(load().sgb_tfem_stiffness_bsr(self._h, ctypes.byref(nb), None, None, None))
+        rowptr = np.zeros(self.n_nodes + 1, np.int32)
+        cols = np.zeros(max(nb.value, 1), np.int32)
+        vals = np.zeros((max(nb.value, 1), 3, 3))
+        check(load().sgb_tfem_stiffness_bsr(self._h, ctypes.byref(nb), rowptr.ctypes.data_as(_ip),
+                                             cols.ctypes.data_as(_ip), vals.ctypes.data_as(_dp)))
+        return rowptr, cols[: nb.value], vals[: nb.value]
 
     def device_bytes(self):
         b = ctypes.c_size_t()

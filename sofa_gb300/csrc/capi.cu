@@ -94,6 +94,9 @@ const VariantOps* variant_for(int precision)
 
 static void free_mesh(TfemMesh& m)
 {
+    cudaFree(m.bsr_cptr);
+    cudaFree(m.bsr_contrib);
+    cudaFree(m.bsr_values);
     cudaFree(m.tets);
     cudaFree(m.rot);
     cudaFree(m.K);
@@ -395,6 +398,87 @@ int sgb_tfem_add_dforce_f32(sgb_tfem_t* fem, const float* dx_dev, float* df_dev,
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_add_dforce_f32: FP64 handle, use sgb_tfem_add_dforce");
     fem->ops->add_dforce(&fem->m, dx_dev, df_dev, (double)kfactor, pick(fem, stream));
     SGB_CUDA_TRY(cudaGetLastError());
+    return SGB_OK;
+}
+
+int sgb_tfem_stiffness_bsr(sgb_tfem_t* fem, int* n_blocks, int32_t* rowptr_host, int32_t* cols_host,
+                           double* values_host)
+{
+    if (!fem || !n_blocks) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_stiffness_bsr: NULL argument");
+    TfemMesh& m = fem->m;
+    const int N = m.n_nodes, E = m.n_tets;
+    if ((size_t)E * 16 >= ((size_t)1 << 31) || (size_t)E >= ((size_t)1 << 27))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_stiffness_bsr: too many tetrahedra");
+    if (m.bsr_rowptr_h.empty()) {
+        // pattern: per node row, the nodes sharing an element with it
+        // (itself included), ascending; per block, its contributions in the
+        // caller's element order
+        std::vector<int32_t> st((size_t)E * 4);
+        if (E > 0) SGB_CUDA_TRY(cudaMemcpy(st.data(), m.tets, sizeof(int32_t) * st.size(), cudaMemcpyDeviceToHost));
+        std::vector<int> inv((size_t)E);
+        for (int s = 0; s < E; ++s) inv[(size_t)m.perm_h[(size_t)s]] = s;
+        std::vector<std::vector<int>> adj((size_t)N);
+        for (int s = 0; s < E; ++s)
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) adj[(size_t)st[4 * (size_t)s + a]].push_back(st[4 * (size_t)s + b]);
+        std::vector<int> rowptr((size_t)N + 1, 0), cols;
+        for (int n = 0; n < N; ++n) {
+            auto& v = adj[(size_t)n];
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            rowptr[(size_t)n + 1] = rowptr[(size_t)n] + (int)v.size();
+            cols.insert(cols.end(), v.begin(), v.end());
+            std::vector<int>().swap(v);
+        }
+        const int nb = rowptr[(size_t)N];
+        auto block_of = [&](int r, int c) {
+            auto b0 = cols.begin() + rowptr[(size_t)r], b1 = cols.begin() + rowptr[(size_t)r + 1];
+            return (int)(std::lower_bound(b0, b1, c) - cols.begin());
+        };
+        std::vector<int> cptr((size_t)nb + 1, 0), contrib((size_t)E * 16);
+        for (int s = 0; s < E; ++s)
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) cptr[(size_t)block_of(st[4 * (size_t)s + a], st[4 * (size_t)s + b]) + 1]++;
+        for (int k = 0; k < nb; ++k) cptr[(size_t)k + 1] += cptr[(size_t)k];
+        std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+        for (int e = 0; e < E; ++e) {  // caller order
+            const int s = inv[(size_t)e];
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) {
+                    const int k = block_of(st[4 * (size_t)s + a], st[4 * (size_t)s + b]);
+                    contrib[(size_t)fill[(size_t)k]++] = (s << 4) | (a << 2) | b;
+                }
+        }
+        size_t acc = 0;
+        int rc;
+        if ((rc = dev_alloc(&m.bsr_cptr, (size_t)nb + 1, &acc)) ||
+            (rc = dev_alloc(&m.bsr_contrib, std::max<size_t>(contrib.size(), 1), &acc)) ||
+            (rc = dev_alloc(&m.bsr_values, std::max<size_t>((size_t)nb * 9, 1), &acc))) {
+            cudaFree(m.bsr_cptr);
+            cudaFree(m.bsr_contrib);
+            cudaFree(m.bsr_values);
+            m.bsr_cptr = m.bsr_contrib = nullptr;
+            m.bsr_values = nullptr;
+            return rc;
+        }
+        SGB_CUDA_TRY(cudaMemcpy(m.bsr_cptr, cptr.data(), sizeof(int) * cptr.size(), cudaMemcpyHostToDevice));
+        if (!contrib.empty())
+            SGB_CUDA_TRY(
+                cudaMemcpy(m.bsr_contrib, contrib.data(), sizeof(int) * contrib.size(), cudaMemcpyHostToDevice));
+        m.bsr_rowptr_h.assign(rowptr.begin(), rowptr.end());
+        m.bsr_cols_h.swap(cols);
+    }
+    const int nb = (int)m.bsr_cols_h.size();
+    *n_blocks = nb;
+    if (rowptr_host) std::memcpy(rowptr_host, m.bsr_rowptr_h.data(), sizeof(int32_t) * ((size_t)N + 1));
+    if (cols_host && nb) std::memcpy(cols_host, m.bsr_cols_h.data(), sizeof(int32_t) * (size_t)nb);
+    if (values_host && nb) {
+        fem->ops->stiffness_blocks(&m, m.bsr_cptr, m.bsr_contrib, nb, m.bsr_values, fem->stream);
+        SGB_CUDA_TRY(cudaGetLastError());
+        SGB_CUDA_TRY(cudaMemcpyAsync(values_host, m.bsr_values, sizeof(double) * 9 * (size_t)nb,
+                                     cudaMemcpyDeviceToHost, fem->stream));
+        SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
+    }
     return SGB_OK;
 }
 

@@ -97,6 +97,12 @@ struct TfemMesh {
     int* slots = nullptr;
     int* elem_orig = nullptr;      // original element index of each storage position
     std::vector<int> perm_h;       // storage position -> original element index
+    // assembled stiffness pattern (built on first use): BSR rows / columns on
+    // the host, per-block contribution lists on the device
+    std::vector<int> bsr_rowptr_h, bsr_cols_h;
+    int* bsr_cptr = nullptr;
+    int* bsr_contrib = nullptr;
+    double* bsr_values = nullptr;
     PatchLayout pl;
     int max_valence = 0;
     void* eforce = nullptr;   // scratch: 12 reals per element (corner forces)

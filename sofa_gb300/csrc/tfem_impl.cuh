@@ -2089,6 +2089,71 @@ void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScala
     }
 }
 
+// ---- assembled stiffness (buildStiffnessMatrix, TFEM.inl:1965-1993) --------
+// One thread per 3x3 block (row node n1, column node n2) of df/dx: minus the
+// sum, over the elements holding both nodes in element index order, of
+// R^T S R with S = B1^T C B2 the element's coupling block in its frame (B
+// from the nodes' strain-displacement values, C isotropic; R the element's
+// current rotation rows, identity for method small). contrib holds the
+// element storage slot << 4 | n1 << 2 | n2 per contribution.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_stiffness_blocks(ElemView<R> ev, int small,
+                                                                 const int* __restrict__ cptr,
+                                                                 const int* __restrict__ contrib, int n_blocks,
+                                                                 double* __restrict__ out)
+{
+    for (int blk = blockIdx.x * blockDim.x + threadIdx.x; blk < n_blocks; blk += gridDim.x * blockDim.x) {
+        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int c = cptr[blk]; c < cptr[blk + 1]; ++c) {
+            const int code = contrib[c];
+            const size_t e = (size_t)(code >> 4);
+            const int n1 = (code >> 2) & 3, n2 = code & 3;
+            R K[3], J[12], Rm[9];
+            load_KJ(ev, e, K, J);
+            if (small) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Rm[i] = (i % 4 == 0) ? R(1) : R(0);
+            } else {
+                load_rot(ev, e, Rm);
+            }
+            const R k0 = K[0], k1 = K[1], k2 = K[2];
+            const R a1 = J[3 * n1], b1 = J[3 * n1 + 1], c1 = J[3 * n1 + 2];
+            const R a2 = J[3 * n2], b2 = J[3 * n2 + 1], c2 = J[3 * n2 + 2];
+            const R S[9] = {a1 * k0 * a2 + b1 * k2 * b2 + c1 * k2 * c2, a1 * k1 * b2 + b1 * k2 * a2,
+                            a1 * k1 * c2 + c1 * k2 * a2,
+                            b1 * k1 * a2 + a1 * k2 * b2, b1 * k0 * b2 + a1 * k2 * a2 + c1 * k2 * c2,
+                            b1 * k1 * c2 + c1 * k2 * b2,
+                            c1 * k1 * a2 + a1 * k2 * c2, c1 * k1 * b2 + b1 * k2 * c2,
+                            c1 * k0 * c2 + b1 * k2 * b2 + a1 * k2 * a2};
+            // W = R^T S R (world frame)
+            R SR[9];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    SR[3 * i + j] = S[3 * i] * Rm[j] + S[3 * i + 1] * Rm[3 + j] + S[3 * i + 2] * Rm[6 + j];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const R w = Rm[i] * SR[j] + Rm[3 + i] * SR[3 + j] + Rm[6 + i] * SR[6 + j];
+                    acc[3 * i + j] -= (double)w;
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[9 * (size_t)blk + i] = acc[i];
+    }
+}
+
+template <typename R>
+void launch_stiffness_blocks(TfemMesh* m, const int* cptr, const int* contrib, int n_blocks, double* out,
+                             cudaStream_t s)
+{
+    if (n_blocks <= 0) return;
+    k_stiffness_blocks<R><<<node_grid(n_blocks), kNodeBlock, 0, s>>>(view<R>(m), m->method == METHOD_SMALL, cptr,
+                                                                     contrib, n_blocks, out);
+}
+
 inline PatchView patch_view(TfemMesh* m)
 {
     PatchView pv;

@@ -46,11 +46,16 @@ static void v_batch_record(const BatchLaunch& b, cudaStream_t s) { batch_record_
 static int (*const v_batch_prepare)(int, int*) = nullptr;
 static void (*const v_batch_record)(const BatchLaunch&, cudaStream_t) = nullptr;
 #endif
+static void v_stiffness_blocks(TfemMesh* m, const int* cptr, const int* contrib, int n_blocks, double* out,
+                               cudaStream_t s)
+{
+    launch_stiffness_blocks<SGB_REAL>(m, cptr, contrib, n_blocks, out, s);
+}
 }  // namespace SGB_NS
 
 namespace sgb {
 const VariantOps SGB_TABLE = {SGB_VARIANT_NAME,     sizeof(SGB_REAL),     SGB_USES_PATCHES,
                               SGB_NS::v_init,       SGB_NS::v_add_force,  SGB_NS::v_add_dforce,
                               SGB_NS::v_scene_step, SGB_NS::v_prepare,   SGB_NS::v_batch_prepare,
-                              SGB_NS::v_batch_record};
+                              SGB_NS::v_batch_record, SGB_NS::v_stiffness_blocks};
 }

@@ -19,6 +19,9 @@ struct VariantOps {
     // batch engine (null for the reference-rounding variant)
     int (*batch_prepare)(int pe, int* grid_patch);  // returns the SM count, -1 on failure
     void (*batch_record)(const BatchLaunch&, cudaStream_t);
+    // assembled stiffness blocks (BSR, 3x3) at the current rotations
+    void (*stiffness_blocks)(TfemMesh*, const int* cptr, const int* contrib, int n_blocks, double* out,
+                             cudaStream_t);
 };
 
 extern const VariantOps ops_fp64_exact;

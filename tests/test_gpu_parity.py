@@ -296,3 +296,31 @@ def test_empty_and_isolated_nodes(torch_cuda, capi):
     sc.step(3)
     x, v = sc.state()
     assert np.array_equal(x, mesh.positions) and not v.any()
+
+
+@pytest.mark.parametrize("method", ["small", "large", "polar", "svd"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp64_fma", 1e-12), ("mixed", 1e-5)])
+def test_assembled_stiffness(torch_cuda, capi, oracle, method, precision, tol):
+    """sgb_tfem_stiffness_bsr (buildStiffnessMatrix, TFEM.inl:1965-1993): the
+    block-sparse df/dx at the rotations of the last addForce times a vector
+    equals the oracle's addDForce with kFactor 1; the matrix is symmetric."""
+    sp = pytest.importorskip("scipy.sparse")
+    mesh = cases.beam_mesh()
+    x, _ = deformed_state(oracle, mesh, "large" if method == "small" else method)
+    fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, method, precision)
+    dt = torch_cuda.float32 if precision == "mixed" else torch_cuda.float64
+    xd = torch_cuda.tensor(x, dtype=torch_cuda.float64, device="cuda")
+    fd = torch_cuda.zeros(x.shape, dtype=dt, device="cuda")
+    fem.add_force(xd.data_ptr(), fd.data_ptr())
+    rowptr, cols, blocks = fem.stiffness_bsr()
+    fem.close()
+    n3 = 3 * mesh.n_nodes
+    Kb = sp.bsr_matrix((blocks, cols, rowptr), shape=(n3, n3))
+    v = np.random.default_rng(8).normal(size=x.shape)
+    ofem = oracle.OracleFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, method)
+    ofem.add_force(x)
+    ref = ofem.add_dforce(v, 1.0)
+    got = (Kb @ v.reshape(-1)).reshape(-1, 3)
+    assert cases.rel_err(got, ref) <= tol
+    # symmetric to the rounding of the element products (FP32 in mixed)
+    assert abs(Kb - Kb.T).max() <= (1e-6 if precision == "mixed" else 1e-12) * abs(Kb).max()
