@@ -324,3 +324,49 @@ def test_assembled_stiffness(torch_cuda, capi, oracle, method, precision, tol):
     assert cases.rel_err(got, ref) <= tol
     # symmetric to the rounding of the element products (FP32 in mixed)
     assert abs(Kb - Kb.T).max() <= (1e-6 if precision == "mixed" else 1e-12) * abs(Kb).max()
+
+
+@pytest.mark.parametrize("method", ["large", "polar"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 0.0), ("fp64_fma", 1e-10), ("mixed", 1e-5)])
+def test_ragged_materials_and_isolated_nodes(torch_cuda, capi, oracle, method, precision, tol):
+    """Ragged per-element data (getVecRealInElement,
+    BaseLinearElasticityFEMForceField.inl:114-144: entry e when the vector is
+    longer than e, else entry 0): a Young's modulus vector of 37 entries, a
+    Poisson vector of E entries, a local stiffness factor of 5 entries; plus
+    nodes that belong to no element, interleaved with the mesh's nodes (the
+    patch layout must leave them out). Per call against the oracle."""
+    mesh = cases.beam_mesh((4, 4, 9), seed=3)
+    rng = np.random.default_rng(21)
+    n0 = mesh.n_nodes
+    # interleave isolated nodes: old node i -> 2 i, odd slots unused
+    pos = np.zeros((2 * n0, 3))
+    pos[0::2] = mesh.positions
+    pos[1::2] = rng.normal(size=(n0, 3)) * 10.0
+    tets = 2 * mesh.tetrahedra
+    E = tets.shape[0]
+    young = 10 ** rng.uniform(3, 4, size=37)
+    poisson = rng.uniform(0.3, 0.45, size=E)
+    lsf = rng.uniform(0.5, 2.0, size=5)
+    x = pos + rng.normal(scale=2e-2, size=pos.shape)
+    dx = rng.normal(scale=1e-3, size=pos.shape)
+    fem = capi.TetrahedronFEM(pos, tets, young, poisson, method, precision, local_stiffness_factor=lsf)
+    dt = torch_cuda.float32 if precision == "mixed" else torch_cuda.float64
+    if precision == "mixed":
+        dx = dx.astype(np.float32).astype(np.float64)
+    xd = torch_cuda.tensor(x, dtype=torch_cuda.float64, device="cuda")
+    fd = torch_cuda.zeros(x.shape, dtype=dt, device="cuda")
+    fem.add_force(xd.data_ptr(), fd.data_ptr())
+    dxd = torch_cuda.tensor(dx, dtype=dt, device="cuda")
+    dfd = torch_cuda.zeros(x.shape, dtype=dt, device="cuda")
+    fem.add_dforce(dxd.data_ptr(), dfd.data_ptr(), -0.01)
+    torch_cuda.cuda.synchronize()
+    fem.close()
+    ofem = oracle.OracleFEM(pos, tets, young, poisson, method, local_stiffness_factor=lsf)
+    f_ref = ofem.add_force(x)
+    df_ref = ofem.add_dforce(dx, -0.01)
+    f, df = fd.cpu().double().numpy(), dfd.cpu().double().numpy()
+    assert not f[1::2].any() and not df[1::2].any()  # isolated nodes untouched
+    if tol == 0.0:
+        assert np.array_equal(f, f_ref) and np.array_equal(df, df_ref)
+    else:
+        assert cases.rel_err(f, f_ref) <= tol and cases.rel_err(df, df_ref) <= tol
