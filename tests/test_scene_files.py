@@ -182,3 +182,33 @@ def test_pcg_jacobi_scene(capi):
         capi.SofaScene(_read("grid_fem_4x10x4.scn").replace(
             PCG_SCENE[0], '<PCGLinearSolver preconditioner="@p"/><BlockJacobiPreconditioner name="p"/>'))
     assert e.value.code in (-4,)
+
+
+DIAG_MASS_SCENE = """<Node name="Root" gravity="0 0 0">
+    <RegularGridTopology name="grid" n="2 2 2" min="0 0 0" max="2 2 2" p0="0 0 0" />
+    <Node name="Tetra">
+        <EulerImplicitSolver />
+        <CGLinearSolver />
+        <MechanicalObject position="@../grid.position" />
+        <TetrahedronSetTopologyContainer name="Container" />
+        <Hexa2TetraTopologicalMapping name="default28" input="@../grid" output="@Container" />
+        <DiagonalMass name="m_mass" {mass} />
+        <TetrahedronFEMForceField />
+    </Node>
+</Node>"""
+
+
+@pytest.mark.parametrize("mass,total,first", [
+    ('massDensity="1.0"', 8.0, [1.66667, 1.0, 1.0, 0.333333]),
+    ('totalMass="10.0"', 10.0, [2.08333, 1.25, 1.25, 0.416667]),
+])
+def test_diagonal_mass_known_answers(capi, mass, total, first):
+    """DiagonalMass on the 2x2x2 grid split into tetrahedra
+    (DiagonalMass_test.cpp checkTotalMassFromMassDensity_Tetra and
+    checkMassDensityFromTotalMass_Tetra): total mass and the first four
+    lumped node masses, to the reference test's 1e-4."""
+    s = capi.SofaScene(DIAG_MASS_SCENE.format(mass=mass))
+    _, masses, _ = s.body_arrays(0)
+    assert len(masses) == 8
+    assert masses.sum() == pytest.approx(total, abs=1e-4)
+    np.testing.assert_allclose(masses[:4], first, atol=1e-4)
