@@ -370,3 +370,20 @@ def test_ragged_materials_and_isolated_nodes(torch_cuda, capi, oracle, method, p
         assert np.array_equal(f, f_ref) and np.array_equal(df, df_ref)
     else:
         assert cases.rel_err(f, f_ref) <= tol and cases.rel_err(df, df_ref) <= tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fma", "mixed"])
+def test_fixed_constraint_constant_force_known_answer(torch_cuda, capi, precision):
+    """The reference's FixedProjectiveConstraint_test known answer on the GPU
+    (a force field with no tetrahedra, the constant force as the external
+    force): x[3][0] = 4.32231 and x[4][0] = 5.32231 after two steps of 0.1,
+    fixed points unchanged."""
+    x0 = np.array([[i + 0.1 * k for k in range(3)] for i in range(5)])
+    fem = capi.TetrahedronFEM(x0, np.zeros((0, 4), np.int32), 5000.0, 0.45, "large", precision)
+    sc = capi.Scene(fem, dt=0.1, rayleigh_stiffness=0.01, rayleigh_mass=1.0, cg_iterations=25, cg_tolerance=1e-5,
+                    cg_threshold=1e-5, gravity=(0.0, 0.0, 0.0), vertex_mass=0.2, fixed=[0, 1, 2])
+    sc.set_external_force(np.full((5, 3), 10.0))
+    sc.step(2)
+    x, _ = sc.state()
+    assert np.array_equal(x[:3], x0[:3])
+    np.testing.assert_allclose([x[3, 0], x[4, 0]], [4.32231, 5.32231], atol=1e-4)

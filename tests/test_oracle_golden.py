@@ -212,3 +212,22 @@ def test_uniform_mass_rules(oracle):
     f = scene.compute_force()
     np.testing.assert_array_equal(f[:, 1], np.full(n, -9.81 * (1.0 / n)))
     assert np.all(f[:, [0, 2]] == 0)
+
+
+def test_fixed_constraint_constant_force_known_answer(oracle):
+    """FixedProjectiveConstraint_test.cpp testTopologicalChanges (before the
+    topology change): 5 points at x_i = i + 0.1 k, UniformMass totalMass 1, a
+    constant force (10, 10, 10) on every point, points 0-2 fixed,
+    EulerImplicitSolver rayleighStiffness 0.01 / rayleighMass 1.0 with CG
+    25 / 1e-5 / 1e-5 (SceneCreator createEulerSolverNode), two steps of 0.1:
+    x[3][0] = 4.32231, x[4][0] = 5.32231, fixed points unchanged."""
+    x0 = np.array([[i + 0.1 * k for k in range(3)] for i in range(5)])
+    sc = oracle.OracleScene(None, n_nodes=5, vertex_mass=1.0 / 5, gravity=(0.0, 0.0, 0.0), fixed=[0, 1, 2],
+                            dt=0.1, rayleigh_stiffness=0.01, rayleigh_mass=1.0, cg_iterations=25,
+                            cg_tolerance=1e-5, cg_threshold=1e-5)
+    sc.set_state(x0, np.zeros_like(x0))
+    sc.set_external_force(np.full((5, 3), 10.0))
+    sc.step(2)
+    x, _ = sc.state()
+    assert np.array_equal(x[:3], x0[:3])
+    np.testing.assert_allclose([x[3, 0], x[4, 0]], [4.32231, 5.32231], atol=1e-4)
