@@ -1355,11 +1355,12 @@ struct PatchArgs {
     const uint8_t* __restrict__ fixed;
     R* __restrict__ qout;
     R* __restrict__ partials;
+    const R* __restrict__ dinv;  // PCG: Jacobi inverse diagonal (PC = 1)
 };
 
 // One patch of the fused matvec, executed by the whole block (it contains
 // block barriers). Returns this thread's share of the patch's p^T A p.
-template <typename R, int MODE>
+template <typename R, int MODE, int PC = 0>
 __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& ev, int P, const PatchArgs<R>& a, R* ef,
                                         R* lp, uint16_t* sl, int* lr)
 {
@@ -1384,7 +1385,8 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         R v[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const R rv = a.rin[3 * (size_t)g + k];
+            R rv = a.rin[3 * (size_t)g + k];
+            if constexpr (PC != 0) rv = a.dinv[3 * (size_t)g + k] * rv;  // PCG: z = diag^-1 r
             v[k] = (MODE == 2) ? cg_dir(rv, a.pold[3 * (size_t)g + k], a.beta) : rv;
             lp[3 * l + k] = v[k];
         }
@@ -1448,14 +1450,15 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
     return pen;
 }
 
-template <typename R, int MODE>
+template <typename R, int MODE, int PC = 0>
 __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv, ElemView<R> ev,
                                                                    const R* __restrict__ rin,
                                                                    const R* __restrict__ pold, R* __restrict__ pnew,
                                                                    CgScalars* cg, R kf, MassArgs ma, double mf,
                                                                    const uint8_t* __restrict__ fixed,
                                                                    R* __restrict__ qout, R* __restrict__ partials,
-                                                                   SolveConsts sc, int prefetch)
+                                                                   SolveConsts sc, int prefetch,
+                                                                   const R* __restrict__ dinv = nullptr)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* ef;
@@ -1469,13 +1472,13 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
     if (MODE == 0 && cg && cg->iters != sc.it) return;
     const R beta = (MODE == 2) ? (R)cg->beta : R(0);
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
-    const PatchArgs<R> args{rin, pold, pnew, beta, kf, mmu, ma, mf, fixed, qout, partials};
+    const PatchArgs<R> args{rin, pold, pnew, beta, kf, mmu, ma, mf, fixed, qout, partials, dinv};
     double energy = 0.0;  // FP64 across patches; FP32 within one patch
     for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
         if constexpr (is_mixed<R>::value)
             if (prefetch && threadIdx.x == 0 && P + (int)gridDim.x < pv.n_patches)
                 prefetch_patch(pv, ev, P + gridDim.x);
-        energy += (double)patch_body<R, MODE>(pv, ev, P, args, ef, lp, sl, lr);
+        energy += (double)patch_body<R, MODE, PC>(pv, ev, P, args, ef, lp, sl, lr);
     }
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
@@ -1497,7 +1500,7 @@ __global__ void __launch_bounds__(kPatchThreads, sizeof(R) == 4 ? 10 : 1)
     patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
     if (gate && gate->iters != gate_it) return;
     const PatchArgs<R> args{dx, nullptr, nullptr, R(0), kf, R(0), {nullptr, 0.0, {0.0, 0.0, 0.0}}, 1.0, nullptr, df,
-                            partials};
+                            partials, nullptr};
     for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) (void)patch_body<R, 0>(pv, ev, P, args, ef, lp, sl, lr);
 }
 
@@ -1762,12 +1765,14 @@ __global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restric
 
 // CG update of one node after a patch matvec: completes q on a shared node
 // (mass term minus the patches' partial sums, projected), then x += alpha p,
-// r += -alpha q. Returns the node's r.r (three-term sum in R).
-template <typename R>
+// r += -alpha q. Returns the node's r.r, or r.z with z = diag^-1 r for PCG
+// (three-term sum in R).
+template <typename R, int PC = 0>
 __device__ __forceinline__ R cg_update1(size_t n, R* __restrict__ xs, R* __restrict__ r, const R* __restrict__ p,
                                         const R* __restrict__ q, const R* __restrict__ partials,
                                         const int* __restrict__ bnd_rowptr, const double* __restrict__ node_mass,
-                                        R mmu, double mf, const uint8_t* __restrict__ fixed, R alpha)
+                                        R mmu, double mf, const uint8_t* __restrict__ fixed, R alpha,
+                                        const R* __restrict__ dinv = nullptr)
 {
     const size_t i3 = 3 * n;
     const R pp[3] = {p[i3], p[i3 + 1], p[i3 + 2]};
@@ -1798,6 +1803,12 @@ __device__ __forceinline__ R cg_update1(size_t n, R* __restrict__ xs, R* __restr
         rr[k] = r[i3 + k] + qq[k] * nalpha;
         r[i3 + k] = rr[k];
     }
+    if constexpr (PC != 0) {
+        R zz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) zz[k] = dinv[i3 + k] * rr[k];
+        return rr[0] * zz[0] + rr[1] * zz[1] + rr[2] * zz[2];
+    }
     return rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
 }
 
@@ -1820,13 +1831,15 @@ __device__ __forceinline__ void st12(float* __restrict__ a, size_t n0, const flo
 
 // The same update for four consecutive nodes n0..n0+3 (n0 a multiple of 4)
 // with 16-byte loads, every load of the group issued before the first use.
-// Returns the group's r.r: the twelve squares summed in FP32 in node order
-// (the caller's running sum is FP64).
+// Returns the group's r.r (PCG: r.z, z = diag^-1 r): the twelve products
+// summed in FP32 in node order (the caller's running sum is FP64).
+template <int PC = 0>
 __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, float* __restrict__ r,
                                              const float* __restrict__ p, const float* __restrict__ q,
                                              const float* __restrict__ partials, const int* __restrict__ bnd_rowptr,
                                              const double* __restrict__ node_mass, float mmu, double mf,
-                                             const uint8_t* __restrict__ fixed, float alpha)
+                                             const uint8_t* __restrict__ fixed, float alpha,
+                                             const float* __restrict__ dinv = nullptr)
 {
     float pp[12], qq[12], xx[12], rr[12];
     ld12(p, n0, pp);
@@ -1872,38 +1885,49 @@ __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, 
     }
     st12(xs, n0, xx);
     st12(r, n0, rr);
+    float zz[12];
+    if constexpr (PC != 0) {
+        ld12(dinv, n0, zz);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) zz[k] = zz[k] * rr[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) zz[k] = rr[k];
+    }
     float local = 0.f;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-        local += rr[3 * j] * rr[3 * j] + rr[3 * j + 1] * rr[3 * j + 1] + rr[3 * j + 2] * rr[3 * j + 2];
+        local += rr[3 * j] * zz[3 * j] + rr[3 * j + 1] * zz[3 * j + 1] + rr[3 * j + 2] * zz[3 * j + 2];
     return (double)local;
 }
 
-template <typename R>
+template <typename R, int PC>
 __device__ __forceinline__ double cg_update4g(size_t n0, R* xs, R* r, const R* p, const R* q, const R* partials,
                                               const int* bnd_rowptr, const double* node_mass, R mmu, double mf,
-                                              const uint8_t* fixed, R alpha)
+                                              const uint8_t* fixed, R alpha, const R* dinv)
 {
     if constexpr (is_mixed<R>::value) {
-        return cg_update4(n0, xs, r, p, q, partials, bnd_rowptr, node_mass, mmu, mf, fixed, alpha);
+        return cg_update4<PC>(n0, xs, r, p, q, partials, bnd_rowptr, node_mass, mmu, mf, fixed, alpha, dinv);
     } else {
         double local = 0.0;
         for (int j = 0; j < 4; ++j)
-            local += (double)cg_update1<R>(n0 + j, xs, r, p, q, partials, bnd_rowptr, node_mass, mmu, mf, fixed, alpha);
+            local += (double)cg_update1<R, PC>(n0 + j, xs, r, p, q, partials, bnd_rowptr, node_mass, mmu, mf, fixed,
+                                               alpha, dinv);
         return local;
     }
 }
 
-// CG update after a patch matvec over all nodes, then rho = r.r. FP32: one
-// thread per group of four nodes (16-byte loads), the N % 4 last nodes one
-// per thread.
-template <typename R, int MINB>
+// CG update after a patch matvec over all nodes, then rho = r.r (PCG: r.z).
+// FP32: one thread per group of four nodes (16-byte loads), the N % 4 last
+// nodes one per thread.
+template <typename R, int MINB, int PC = 0>
 __global__ void __launch_bounds__(kNodeBlock, MINB) k_cg_update_patch(R* __restrict__ xs, R* __restrict__ r,
                                                                 const R* __restrict__ p, const R* __restrict__ q,
                                                                 const R* __restrict__ partials,
                                                                 const int* __restrict__ bnd_rowptr, MassArgs ma,
                                                                 double mf, const uint8_t* __restrict__ fixed,
-                                                                CgScalars* cg, int N, SolveConsts sc, int vec4)
+                                                                CgScalars* cg, int N, SolveConsts sc, int vec4,
+                                                                const R* __restrict__ dinv = nullptr)
 {
     if (cg->done) return;
     const R alpha = (R)cg->alpha;
@@ -1913,14 +1937,15 @@ __global__ void __launch_bounds__(kNodeBlock, MINB) k_cg_update_patch(R* __restr
     if (is_mixed<R>::value && vec4) {
         const int G4 = N >> 2;
         for (int g = tid; g < G4; g += stride)
-            local += cg_update4g(4 * (size_t)g, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf, fixed, alpha);
+            local += cg_update4g<R, PC>(4 * (size_t)g, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf,
+                                        fixed, alpha, dinv);
         for (int n = 4 * G4 + tid; n < N; n += stride)
-            local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf, fixed,
-                                           alpha);
+            local += (double)cg_update1<R, PC>((size_t)n, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf,
+                                               fixed, alpha, dinv);
     } else {
         for (int n = tid; n < N; n += stride)
-            local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf, fixed,
-                                           alpha);
+            local += (double)cg_update1<R, PC>((size_t)n, xs, r, p, q, partials, bnd_rowptr, ma.node_mass, mmu, mf,
+                                               fixed, alpha, dinv);
     }
     finish_dot<FIN_RHO>(local, cg, nullptr, N, sc);
 }
@@ -2179,15 +2204,15 @@ size_t patch_smem_bytes(const TfemMesh* m)
 
 // The CG update with the register cap chosen at preparation (MINB resident
 // CTAs of kNodeBlock threads per SM).
-template <typename R, typename... A>
+template <typename R, int PC = 0, typename... A>
 void launch_cg_update(const TfemMesh* m, int grid, cudaStream_t s, A... a)
 {
     if (m->update_minb == 2)
-        k_cg_update_patch<R, 2><<<grid, kNodeBlock, 0, s>>>(a...);
+        k_cg_update_patch<R, 2, PC><<<grid, kNodeBlock, 0, s>>>(a...);
     else if (m->update_minb == 3)
-        k_cg_update_patch<R, 3><<<grid, kNodeBlock, 0, s>>>(a...);
+        k_cg_update_patch<R, 3, PC><<<grid, kNodeBlock, 0, s>>>(a...);
     else
-        k_cg_update_patch<R, 4><<<grid, kNodeBlock, 0, s>>>(a...);
+        k_cg_update_patch<R, 4, PC><<<grid, kNodeBlock, 0, s>>>(a...);
 }
 
 // Sets the shared-memory attribute of the patch kernels and returns the grid
@@ -2234,6 +2259,8 @@ int prepare_patch(TfemMesh* m)
     }
     cudaFuncSetAttribute(k_patch_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_patch_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_matvec<R, 1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_patch_matvec<R, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, threads, smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, threads, smem);
     int nb = nb1;
@@ -2326,6 +2353,40 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
                                                                                  m->n_nodes);
 }
 
+// PCG before its first iteration (PCGLinearSolver.inl:194-214): the Jacobi
+// diagonal from this step's rotations when a preconditioner is set (it
+// returns at once on the steps between re-assemblies), then r = b - A x from
+// the previous step's solution and r.z. Element-order kernels: once per step.
+template <typename R>
+void pcg_begin(Scene* sc, int mass_first, double mf, double kf, const SolveConsts& cons, double* dot_terms,
+               cudaStream_t s)
+{
+    TfemMesh* m = sc->mesh;
+    const int N = sc->n;
+    const SceneParams& P = sc->prm;
+    NodeCSR csr{m->rowptr, m->slots};
+    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const int ng = node_grid(N);
+    R* dinv = (R*)sc->dinv;  // null: no preconditioner
+    if (dinv) {
+        ElemView<R> ev = view<R>(m);
+        const int ge = elem_grid(m->n_tets);
+        if (m->n_tets > 0) {
+            if (m->method == METHOD_SMALL)
+                k_elem_jacobi<R, METHOD_SMALL>
+                    <<<ge, kElemBlock, 0, s>>>(ev, (R)(-kf), (R*)m->eforce, sc->cg, P.precond_rate);
+            else
+                k_elem_jacobi<R, METHOD_LARGE>
+                    <<<ge, kElemBlock, 0, s>>>(ev, (R)(-kf), (R*)m->eforce, sc->cg, P.precond_rate);
+        }
+        k_gather_jacobi<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, ma, mf, mass_first, sc->fixed, dinv,
+                                                     N, sc->cg, P.precond_rate);
+    }
+    launch_elem_dforce<R, R, 0>(m, (const R*)sc->xs, nullptr, sc->cg, (R)kf, s);
+    k_pcg_start<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->xs, (const R*)sc->b, ma, mf,
+                                             mass_first, sc->fixed, dinv, (R*)sc->r, sc->cg, dot_terms, N, cons);
+}
+
 // One implicit Euler step of a scene (EulerImplicitSolver::solve,
 // Sofa/Component/ODESolver/Backward/src/sofa/component/odesolver/backward/
 // EulerImplicitSolver.cpp:83-341) as a fixed sequence of launches: the CG
@@ -2361,27 +2422,7 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     // CG (or PCG) on (mF M + kF K) dv = b
     const double mf = 1 + 1.0 * h * P.rayleigh_mass;
     const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
-    if (pcg) {
-        if (dinv) {
-            // Jacobi diagonal from this step's rotations
-            ElemView<R> ev = view<R>(m);
-            const int ge = elem_grid(m->n_tets);
-            if (m->n_tets > 0) {
-                if (m->method == METHOD_SMALL)
-                    k_elem_jacobi<R, METHOD_SMALL>
-                        <<<ge, kElemBlock, 0, s>>>(ev, (R)(-kf), (R*)m->eforce, sc->cg, P.precond_rate);
-                else
-                    k_elem_jacobi<R, METHOD_LARGE>
-                        <<<ge, kElemBlock, 0, s>>>(ev, (R)(-kf), (R*)m->eforce, sc->cg, P.precond_rate);
-            }
-            k_gather_jacobi<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, ma, mf, mass_first, sc->fixed,
-                                                         dinv, N, sc->cg, P.precond_rate);
-        }
-        // r = b - A x from the previous step's solution
-        launch_elem_dforce<R, R, 0>(m, xs, nullptr, sc->cg, (R)kf, s);
-        k_pcg_start<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, xs, b, ma, mf, mass_first, sc->fixed,
-                                                 dinv, r, sc->cg, dot_terms, N, cons);
-    }
+    if (pcg) pcg_begin<R>(sc, mass_first, mf, kf, cons, dot_terms, s);
     for (int it = 1; it <= P.cg_iterations; ++it) {
         cons.it = it;
         if (it == 1) {
@@ -2414,6 +2455,9 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
 
 // The same step with the fused patch matvec: two launches per CG iteration
 // (patch matvec + update), the CG direction p ping-pongs between two buffers.
+// PCG (linear_solver = PCG) adds the warm start of pcg_begin and, with the
+// Jacobi preconditioner, the PC = 1 kernels (z = diag^-1 r where the direction
+// is formed, r.z in the update).
 template <typename R>
 void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
 {
@@ -2431,7 +2475,9 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     R* q = (R*)sc->q;
     R* xs = (R*)sc->xs;
     R* partials = (R*)m->pl.partials;
-    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1};
+    const bool pcg = P.solver == 1;
+    const R* dinv = pcg ? (const R*)sc->dinv : nullptr;
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0};
     launch_elem_force<R>(m, sc->x, s);
     k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
     const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
@@ -2440,14 +2486,30 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
                                               h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons);
     const double mf = 1 + 1.0 * h * P.rayleigh_mass;
     const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    if (pcg) pcg_begin<R>(sc, mass_first, mf, kf, cons, nullptr, s);
     PatchView pv = patch_view(m);
     ElemView<R> ev = view<R>(m);
     const size_t smem = patch_smem_bytes<R>(m);
     const int ng_update = is_mixed<R>::value ? node_grid((N + 3) / 4) : ng;
+    const int gu = m->update_grid > 0 ? m->update_grid : (m->update_vec4 ? ng_update : ng);
     for (int it = 1; it <= P.cg_iterations; ++it) {
         cons.it = it;
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
+        if (dinv) {
+            if (it == 1)
+                k_patch_matvec<R, 1, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
+                    pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch,
+                    dinv);
+            else
+                k_patch_matvec<R, 2, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
+                    pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch,
+                    dinv);
+            launch_cg_update<R, 1>(m, gu, s, xs, r, (const R*)pnew, (const R*)q, (const R*)partials,
+                                   (const int*)m->pl.bnd_rowptr, ma, mf, (const uint8_t*)sc->fixed, sc->cg, N, cons,
+                                   m->update_vec4, dinv);
+            continue;
+        }
         bool done = false;
         if constexpr (is_mixed<R>::value) {
             if (m->staged) {
@@ -2471,9 +2533,9 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
         else
             k_patch_matvec<R, 2><<<m->patch_grid, m->patch_threads, smem, s>>>(
                 pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
-        launch_cg_update<R>(m, m->update_grid > 0 ? m->update_grid : (m->update_vec4 ? ng_update : ng), s, xs, r,
-                            (const R*)pnew, (const R*)q, (const R*)partials, (const int*)m->pl.bnd_rowptr, ma, mf,
-                            (const uint8_t*)sc->fixed, sc->cg, N, cons, m->update_vec4);
+        launch_cg_update<R>(m, gu, s, xs, r, (const R*)pnew, (const R*)q, (const R*)partials,
+                            (const int*)m->pl.bnd_rowptr, ma, mf, (const uint8_t*)sc->fixed, sc->cg, N, cons,
+                            m->update_vec4);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);

@@ -22,11 +22,11 @@ static void v_add_dforce(TfemMesh* m, const void* dx, void* df, double k, cudaSt
 }
 static void v_scene_step(Scene* sc, double* terms, int mass_first, cudaStream_t s)
 {
-    // FP32 runs the fused patch matvec; FP64 (FMA) is bound by the FP64 issue
-    // rate, where the element-order path with its plain gather is faster
-    // PCG runs on the element-order kernels in every precision
+    // FP32 runs the fused patch matvec (CG and PCG); FP64 (FMA) is bound by
+    // the FP64 issue rate, where the element-order path with its plain gather
+    // is faster
     if (SGB_USES_PATCHES && sizeof(SGB_REAL) == 4 && sc->mesh->pl.n_patches > 0 &&
-        sc->mesh->method != METHOD_SMALL && sc->prm.solver == 0) {
+        sc->mesh->method != METHOD_SMALL) {
         if (sc->replace_every > 0 && sc->shadow && sc->shadow->pl.n_patches > 0)
             scene_step_refined<SGB_REAL>(sc, mass_first, s);
         else

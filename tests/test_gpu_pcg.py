@@ -1,8 +1,8 @@
 """PCGLinearSolver (+ JacobiPreconditioner) on the GPU against the oracle:
 FP64 reference rounding with serial dots bit-identical over 20 steps (with
 and without the preconditioner, and with the preconditioner re-assembled
-every 3 steps), FP64-FMA within 1e-10, mixed within 1e-4 of the positions;
-Jacobi cuts the iterations on a stiff inclusion."""
+every 3 steps), FP64-FMA within 1e-10, mixed (fused patch kernels) within
+1e-4 of the positions; Jacobi cuts the iterations on a stiff inclusion."""
 import numpy as np
 import pytest
 
@@ -66,14 +66,50 @@ def test_pcg_jacobi_other_precisions(capi, oracle, precision, tol, method):
     assert np.linalg.norm(xo - mesh.positions) > 1e-3  # it moved
 
 
-def test_pcg_jacobi_fewer_iterations_on_a_stiff_inclusion(capi):
+@pytest.mark.parametrize("pre,rate", [(None, 1), ("jacobi", 3)])
+def test_pcg_mixed_patch_kernels(capi, oracle, pre, rate):
+    """Mixed precision runs PCG on the fused patch kernels (z = diag^-1 r where
+    the direction is formed, r.z in the update); the beam has several patches,
+    so shared nodes go through the partial sums."""
+    mesh = cases.beam_mesh()
+    cfg = dict(PCG, cg_iterations=30, cg_tolerance=0.0)
+    osc = _oracle(oracle, mesh, "polar", pre, rate, cfg=cfg)
+    osc.step(20)
+    sc = cases.gpu_scene(capi, mesh, "polar", "mixed", cfg=cfg, linear_solver="pcg", preconditioner=pre,
+                         preconditioner_rate=rate)
+    sc.step(20)
+    x, _ = sc.state()
+    xo, _ = osc.state()
+    assert cases.rel_err(x, xo) <= 1e-4
+    assert np.linalg.norm(xo - mesh.positions) > 1e-3
+
+
+def test_pcg_mixed_stops_on_tolerance(capi, oracle):
+    """r.z <= tolerance b.b ends the mixed solve early, as in the oracle."""
+    mesh = cases.beam_mesh()
+    cfg = dict(PCG, cg_iterations=300, cg_tolerance=1e-5)  # the oracle stops after 130-180 iterations
+    osc = _oracle(oracle, mesh, "large", "jacobi", cfg=cfg)
+    sc = cases.gpu_scene(capi, mesh, "large", "mixed", cfg=cfg, linear_solver="pcg", preconditioner="jacobi")
+    for _ in range(5):
+        osc.step(1)
+        sc.step(1)
+        it, _ = sc.sync()
+        oi = osc.last_iterations
+        assert oi < 300 and abs(it - oi) <= max(3, oi // 20), (it, oi)
+    x, _ = sc.state()
+    xo, _ = osc.state()
+    assert cases.rel_err(x, xo) <= 1e-4
+
+
+@pytest.mark.parametrize("precision", ["fp64_fma", "mixed"])
+def test_pcg_jacobi_fewer_iterations_on_a_stiff_inclusion(capi, precision):
     mesh = cases.beam_mesh(n=(6, 6, 21))
     c = mesh.positions[mesh.tetrahedra].mean(1)
     young = np.where(np.linalg.norm(c - c.mean(0), axis=1) < 1.0, 1e6, 1e3)
     cfg = dict(PCG, cg_iterations=1000, cg_tolerance=1e-16)
     its = {}
     for pre in (None, "jacobi"):
-        sc = cases.gpu_scene(capi, mesh, "large", "fp64_fma", cfg=cfg, young=young, linear_solver="pcg",
+        sc = cases.gpu_scene(capi, mesh, "large", precision, cfg=cfg, young=young, linear_solver="pcg",
                              preconditioner=pre)
         sc.step(1)
         its[pre], _ = sc.sync()
