@@ -109,6 +109,23 @@ int sgb_tfem_add_dforce_f32(sgb_tfem_t* fem, const float* dx_dev, float* df_dev,
  * getActualTetraRotation / getInitialTetraRotation). Synchronous. */
 int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* initial_rotations_host);
 
+/* Plasticity of the addForce strain: the Data plasticMaxThreshold,
+ * plasticYieldThreshold and plasticCreep of TetrahedronFEMForceField
+ * (TetrahedronFEMForceField.inl:51-53; the update in computeForce, :357-370).
+ * max_threshold > 0 turns it on; every add_force call (and every scene step,
+ * through its force computation) then updates the per-element plastic
+ * strain. The strain starts at zero when first turned on; max_threshold = 0
+ * turns it off and keeps the strain. Thresholds are 2-norms of the 6-vector
+ * strain. Synchronous on the handle's stream when first turned on. */
+int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_threshold, double creep);
+/* Zeroes the plastic strain (TetrahedronFEMForceField::reset, .inl:1382-1390).
+ * Stream-ordered on the handle's stream. */
+int sgb_tfem_reset_plasticity(sgb_tfem_t* fem);
+/* The plastic strain, 6 doubles per element in the caller's element order
+ * (Voigt: xx, yy, zz, then the three shear terms of J^T D); zeros when
+ * plasticity was never turned on. Synchronous. */
+int sgb_tfem_get_plastic_strain(sgb_tfem_t* fem, double* plastic_strain_host);
+
 /* The assembled stiffness df/dx at the current rotations (those of the last
  * addForce), as TetrahedronFEMForceField::buildStiffnessMatrix assembles it
  * (TetrahedronFEMForceField.inl:1965-1993): block-sparse rows of 3x3 blocks,

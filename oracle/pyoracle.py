@@ -44,6 +44,8 @@ def _load():
     lib.orc_fem_element.argtypes = [vp, ctypes.c_int, _dp]
     lib.orc_fem_rest_volume.restype = ctypes.c_double
     lib.orc_fem_rest_volume.argtypes = [vp]
+    lib.orc_fem_set_plasticity.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.orc_fem_plastic_strain.argtypes = [vp, _dp]
     lib.orc_polar.restype = ctypes.c_double
     lib.orc_polar.argtypes = [_dp, _dp]
     lib.orc_polar_stable.restype = ctypes.c_int
@@ -154,6 +156,16 @@ class OracleFEM:
     @property
     def rest_volume(self):
         return _load().orc_fem_rest_volume(self._h)
+
+    def set_plasticity(self, max_threshold, yield_threshold=1e-4, creep=0.9):
+        """plasticMaxThreshold / plasticYieldThreshold / plasticCreep."""
+        _load().orc_fem_set_plasticity(self._h, max_threshold, yield_threshold, creep)
+
+    def plastic_strain(self):
+        """(n_tets, 6) plastic strain."""
+        out, pout = _d(np.zeros(6 * self.n_tets))
+        _load().orc_fem_plastic_strain(self._h, pout)
+        return out.reshape(-1, 6)
 
 
 def full_K(K3):

@@ -437,12 +437,19 @@ static void strain_displacement(const double* a, const double* b, const double* 
     J3[11] = pdet(a[0], b[0], c[0], a[1], b[1], c[1]);
 }
 
-/* computeForce (TFEM.inl:293-415 without plasticity, and :417-521 with
- * `fact`): F = J K J^T D using only J's non-zero pattern, in the
- * reference's term order. K3 = {K(0,0), K(0,1), K(3,3)}. fact is applied to
- * K J^T D when use_fact is set. */
-static void compute_force(double F[12], const double D[12], const double K3[3], const double J3[12],
-                          int use_fact, double fact)
+/* Plasticity settings of computeForce (TFEM.inl:51-53): max_threshold > 0
+ * turns the plastic step on. */
+typedef struct {
+    double max_threshold, yield_threshold, creep;
+} orc_plastic;
+
+/* computeForce (TFEM.inl:293-415, and :417-521 with `fact`): F = J K J^T D
+ * using only J's non-zero pattern, in the reference's term order.
+ * K3 = {K(0,0), K(0,1), K(3,3)}. fact is applied to K J^T D when use_fact is
+ * set. With `ps` (the element's plastic strain) and plasticity on, the
+ * plastic step of :357-370 updates ps and the force uses J^T D - ps. */
+static void compute_force_pl(double F[12], const double D[12], const double K3[3], const double J3[12],
+                             int use_fact, double fact, double* ps, const orc_plastic* pl)
 {
 #define JA(i) J3[3 * (i) + 0]
 #define JB(i) J3[3 * (i) + 1]
@@ -457,6 +464,22 @@ static void compute_force(double F[12], const double D[12], const double K3[3], 
              JC(3) * D[10] + JB(3) * D[11];
     JtD[5] = JC(0) * D[0] + JA(0) * D[2] + JC(1) * D[3] + JA(1) * D[5] + JC(2) * D[6] + JA(2) * D[8] +
              JC(3) * D[9] + JA(3) * D[11];
+
+    if (ps && pl && pl->max_threshold > 0) {
+        double el[6], n2, p2;
+        for (int i = 0; i < 6; ++i) el[i] = JtD[i] - ps[i]; /* elasticStrain = JtD - plasticStrain */
+        n2 = el[0] * el[0];                                  /* Vec::norm2 (Vec.h:483-493) */
+        for (int i = 1; i < 6; ++i) n2 += el[i] * el[i];
+        if (n2 > pl->yield_threshold * pl->yield_threshold)
+            for (int i = 0; i < 6; ++i) ps[i] += el[i] * pl->creep;
+        p2 = ps[0] * ps[0];
+        for (int i = 1; i < 6; ++i) p2 += ps[i] * ps[i];
+        if (p2 > pl->max_threshold * pl->max_threshold) {
+            const double s = pl->max_threshold / sqrt(p2); /* helper::rsqrt(double) is sqrt (rmath.h:131-138) */
+            for (int i = 0; i < 6; ++i) ps[i] *= s;
+        }
+        for (int i = 0; i < 6; ++i) JtD[i] -= ps[i];
+    }
 
     const double k0 = K3[0], k1 = K3[1], k2 = K3[2];
     KJtD[0] = k0 * JtD[0] + k1 * JtD[1] + k1 * JtD[2];
@@ -476,6 +499,12 @@ static void compute_force(double F[12], const double D[12], const double K3[3], 
 #undef JA
 #undef JB
 #undef JC
+}
+
+static void compute_force(double F[12], const double D[12], const double K3[3], const double J3[12],
+                          int use_fact, double fact)
+{
+    compute_force_pl(F, D, K3, J3, use_fact, fact, NULL, NULL);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -545,6 +574,8 @@ typedef struct orc_fem {
     double* rest_rot;  /* _rotatedInitialElements, 12 per element */
     double* A0inv;     /* svd: _initialTransformation (inverse rest edge matrix), 9 per element */
     double rest_volume;
+    double* plastic;   /* _plasticStrains, 6 per element (NULL until plasticity is turned on) */
+    orc_plastic pl;
     double* tl_buf;    /* thread-local force buffers for the threaded mode */
     int tl_threads;
 } orc_fem;
@@ -651,6 +682,7 @@ void orc_fem_destroy(orc_fem* m)
     free(m->rot);
     free(m->rest_rot);
     free(m->A0inv);
+    free(m->plastic);
     free(m->tl_buf);
     free(m);
 }
@@ -671,7 +703,7 @@ static void element_force(orc_fem* m, int e, const double* p, double* f)
         for (int i = 1; i < 4; ++i)
             for (int k = 0; k < 3; ++k)
                 D[3 * i + k] = ip[3 * t[i] + k] - ip[3 * a + k] - p[3 * t[i] + k] + p[3 * a + k];
-        compute_force(F, D, K3, J3, 0, 0.0);
+        compute_force_pl(F, D, K3, J3, 0, 0.0, m->plastic ? &m->plastic[6 * e] : NULL, &m->pl);
         for (int i = 0; i < 4; ++i)
             for (int k = 0; k < 3; ++k) f[3 * t[i] + k] += F[3 * i + k];
         return;
@@ -721,7 +753,7 @@ static void element_force(orc_fem* m, int e, const double* p, double* f)
     } else {
         for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
     }
-    compute_force(F, D, K3, J3, 0, 0.0);
+    compute_force_pl(F, D, K3, J3, 0, 0.0, m->plastic ? &m->plastic[6 * e] : NULL, &m->pl);
     for (int i = 0; i < 4; ++i) {
         double r3[3];
         mat_vec(rot, &F[3 * i], r3);
@@ -848,6 +880,22 @@ void orc_fem_element(const orc_fem* m, int e, double* out)
 }
 
 double orc_fem_rest_volume(const orc_fem* m) { return m->rest_volume; }
+
+/* plasticMaxThreshold / plasticYieldThreshold / plasticCreep; the plastic
+ * strain starts at zero when plasticity is first turned on. */
+void orc_fem_set_plasticity(orc_fem* m, double max_threshold, double yield_threshold, double creep)
+{
+    if (max_threshold > 0 && !m->plastic) m->plastic = (double*)calloc(6 * (size_t)m->n_tets + 1, sizeof(double));
+    m->pl.max_threshold = max_threshold;
+    m->pl.yield_threshold = yield_threshold;
+    m->pl.creep = creep;
+}
+
+/* _plasticStrains, 6 per element (zeros before plasticity is turned on). */
+void orc_fem_plastic_strain(const orc_fem* m, double* out)
+{
+    for (size_t i = 0; i < 6 * (size_t)m->n_tets; ++i) out[i] = m->plastic ? m->plastic[i] : 0.0;
+}
 
 /* ------------------------------------------------------------------------- */
 /* Scene: MechanicalObject + mass + force fields + projective constraint,    */

@@ -138,6 +138,9 @@ def load():
         "sgb_tfem_add_dforce": (c_int, [_vp, _vp, _vp, c_double, _vp]),
         "sgb_tfem_add_dforce_f32": (c_int, [_vp, _vp, _vp, c_float, _vp]),
         "sgb_tfem_get_rotations": (c_int, [_vp, _dp, _dp]),
+        "sgb_tfem_set_plasticity": (c_int, [_vp, c_double, c_double, c_double]),
+        "sgb_tfem_reset_plasticity": (c_int, [_vp]),
+        "sgb_tfem_get_plastic_strain": (c_int, [_vp, _dp]),
         "sgb_tfem_stiffness_bsr": (c_int, [_vp, ctypes.POINTER(c_int), _ip, _ip, _dp]),
         "sgb_tfem_check_device": (c_int, [_vp]),
         "sgb_tfem_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
@@ -295,6 +298,21 @@ class TetrahedronFEM:
         r0 = np.zeros((self.n_tets, 3, 3))
         check(load().sgb_tfem_get_rotations(self._h, r.ctypes.data_as(_dp), r0.ctypes.data_as(_dp)))
         return r, r0
+
+    def set_plasticity(self, max_threshold, yield_threshold=1e-4, creep=0.9):
+        """plasticMaxThreshold / plasticYieldThreshold / plasticCreep: with
+        max_threshold > 0 every addForce updates the per-element plastic
+        strain (TetrahedronFEMForceField::computeForce)."""
+        check(load().sgb_tfem_set_plasticity(self._h, float(max_threshold), float(yield_threshold), float(creep)))
+
+    def reset_plasticity(self):
+        check(load().sgb_tfem_reset_plasticity(self._h))
+
+    def plastic_strain(self):
+        """(n_tets, 6) plastic strain in the caller's element order."""
+        out = np.zeros((self.n_tets, 6))
+        check(load().sgb_tfem_get_plastic_strain(self._h, out.ctypes.data_as(_dp)))
+        return out
 
     def stiffness_bsr(self):
         """The assembled df/dx at the current rotations as (rowptr, cols,

@@ -94,6 +94,8 @@ const VariantOps* variant_for(int precision)
 
 static void free_mesh(TfemMesh& m)
 {
+    cudaFree(m.plastic);
+    cudaFree(m.plastic_scale);
     cudaFree(m.bsr_cptr);
     cudaFree(m.bsr_contrib);
     cudaFree(m.bsr_values);
@@ -527,6 +529,92 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
     return SGB_OK;
 }
 
+int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_threshold, double creep)
+{
+    if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_set_plasticity: NULL handle");
+    if (!(max_threshold >= 0.0) || !(yield_threshold >= 0.0) || !std::isfinite(max_threshold) ||
+        !std::isfinite(yield_threshold) || !std::isfinite(creep))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_set_plasticity: thresholds must be finite and >= 0");
+    TfemMesh& m = fem->m;
+    const size_t E = (size_t)m.n_tets;
+    if (max_threshold > 0.0 && !m.plastic && E > 0) {
+        // first enabled: zero plastic strain; mixed also computes its
+        // per-element strain scale
+        SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
+        SGB_CUDA_TRY(cudaMalloc(&m.plastic, m.real_size * 6 * E));
+        m.device_bytes += m.real_size * 6 * E;
+        SGB_CUDA_TRY(cudaMemsetAsync(m.plastic, 0, m.real_size * 6 * E, fem->stream));
+        if (m.real_size == sizeof(float)) {
+            SGB_CUDA_TRY(cudaMalloc(&m.plastic_scale, sizeof(float) * E));
+            m.device_bytes += sizeof(float) * E;
+            double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr;
+            cudaError_t ce = cudaMalloc(&d_y, sizeof(double) * m.young_h.size());
+            if (ce == cudaSuccess) ce = cudaMalloc(&d_p, sizeof(double) * m.poisson_h.size());
+            if (ce == cudaSuccess) ce = cudaMalloc(&d_l, sizeof(double) * std::max<size_t>(m.lsf_h.size(), 1));
+            if (ce == cudaSuccess)
+                ce = cudaMemcpy(d_y, m.young_h.data(), sizeof(double) * m.young_h.size(), cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpy(d_p, m.poisson_h.data(), sizeof(double) * m.poisson_h.size(),
+                                cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess && !m.lsf_h.empty())
+                ce = cudaMemcpy(d_l, m.lsf_h.data(), sizeof(double) * m.lsf_h.size(), cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess) {
+                fem->ops->plastic_scale(&m, d_y, (int)m.young_h.size(), d_p, (int)m.poisson_h.size(), d_l,
+                                        (int)m.lsf_h.size(), fem->stream);
+                ce = cudaGetLastError();
+            }
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(fem->stream);
+            cudaFree(d_y);
+            cudaFree(d_p);
+            cudaFree(d_l);
+            if (ce != cudaSuccess) return cuda_fail(ce, "sgb_tfem_set_plasticity");
+        }
+    }
+    m.plastic_max = max_threshold;
+    m.plastic_yield = yield_threshold;
+    m.plastic_creep = creep;
+    m.plastic_version++;
+    return SGB_OK;
+}
+
+int sgb_tfem_reset_plasticity(sgb_tfem_t* fem)
+{
+    if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_reset_plasticity: NULL handle");
+    if (fem->m.plastic)
+        SGB_CUDA_TRY(cudaMemsetAsync(fem->m.plastic, 0, fem->m.real_size * 6 * (size_t)fem->m.n_tets, fem->stream));
+    return SGB_OK;
+}
+
+int sgb_tfem_get_plastic_strain(sgb_tfem_t* fem, double* plastic_strain_host)
+{
+    if (!fem || !plastic_strain_host)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_get_plastic_strain: NULL argument");
+    TfemMesh& m = fem->m;
+    const size_t E = (size_t)m.n_tets, rs = m.real_size;
+    if (!m.plastic) {
+        std::fill(plastic_strain_host, plastic_strain_host + 6 * E, 0.0);
+        return SGB_OK;
+    }
+    std::vector<unsigned char> buf(rs * 6 * std::max<size_t>(E, 1));
+    std::vector<float> scale;
+    SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
+    SGB_CUDA_TRY(cudaMemcpy(buf.data(), m.plastic, rs * 6 * E, cudaMemcpyDeviceToHost));
+    if (m.plastic_scale) {
+        scale.resize(E);
+        SGB_CUDA_TRY(cudaMemcpy(scale.data(), m.plastic_scale, sizeof(float) * E, cudaMemcpyDeviceToHost));
+    }
+    for (size_t e = 0; e < E; ++e) {
+        const size_t o = (size_t)m.perm_h[e];
+        for (int i = 0; i < 6; ++i) {
+            const size_t k = (size_t)i * E + e;
+            double v = (rs == 8) ? ((double*)buf.data())[k] : (double)((float*)buf.data())[k];
+            if (!scale.empty()) v /= (double)scale[e];  // mixed keeps it in J's scaling
+            plastic_strain_host[6 * o + i] = v;
+        }
+    }
+    return SGB_OK;
+}
+
 int sgb_tfem_check_device(sgb_tfem_t* fem)
 {
     if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_check_device: NULL handle");
@@ -804,7 +892,16 @@ int sgb_scene_step(sgb_scene_t* scene, int n_steps)
 {
     if (!scene || n_steps < 0) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_step: invalid argument");
     Scene& s = scene->s;
+    const TfemMesh& fm = *s.mesh;
+    if (s.replace_every > 0 && fm.plastic && fm.plastic_max > 0.0)
+        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_step: plasticity runs without residual replacement");
+    if (s.graph_valid && s.graph_plastic_version != fm.plastic_version) s.graph_valid = false;
     if (!s.graph_valid) {
+        if (s.graph) {
+            cudaGraphExecDestroy(s.graph);
+            s.graph = nullptr;
+        }
+        s.graph_plastic_version = fm.plastic_version;
         cudaGraph_t g;
         SGB_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
         scene->ops->scene_step(&s, scene->dot_terms, scene->mass_first, s.stream);

@@ -693,8 +693,11 @@ int Scene::init_host(std::string* err)
         if (b.method != SGB_METHOD_SMALL && fem->get_bool(*this, "updateStiffnessMatrix"))
             return unsupported(err, where + "updateStiffnessMatrix=true (strain-displacement rebuilt every step, "
                                             "TetrahedronFEMForceField.inl:908, 1063, 1174) is not supported");
-        if (fem->get_real(*this, "plasticMaxThreshold") > 0.0)
-            return unsupported(err, where + "plasticity (plasticMaxThreshold > 0) is not supported");
+        b.plastic_max = fem->get_real(*this, "plasticMaxThreshold");
+        b.plastic_yield = fem->get_real(*this, "plasticYieldThreshold");
+        b.plastic_creep = fem->get_real(*this, "plasticCreep");
+        if (b.plastic_max > 0.0 && b.plastic_yield < 0.0)
+            return unsupported(err, where + "plasticYieldThreshold must be >= 0");
         if (fem->get_int(*this, "computeVonMisesStress") != 0)
             return unsupported(err, where + "computeVonMisesStress is not supported");
         if (fem->get_real(*this, "rayleighStiffness") != 0.0)
@@ -778,6 +781,12 @@ int Scene::init_device(std::string* err)
                                  b.poisson.data(), (int)b.poisson.size(), nullptr, 0, b.method, b.precision);
         if (rc) {
             *err = sgb_last_error();
+            return rc;
+        }
+        if (b.plastic_max > 0.0 &&
+            (rc = sgb_tfem_set_plasticity(fem, b.plastic_max, b.plastic_yield, b.plastic_creep))) {
+            *err = sgb_last_error();
+            sgb_tfem_destroy(fem);
             return rc;
         }
         sgb_scene_params p = b.params;

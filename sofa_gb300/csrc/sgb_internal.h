@@ -117,6 +117,12 @@ struct TfemMesh {
     int staged_grid = 0;      // CTAs of the staged patch kernels
     int* dev_flags = nullptr; // sticky device error flag: 1 = a bounded device wait ran out
     double rest_volume = 0.0;
+    // plasticity (plasticMaxThreshold > 0): 6 plastic strain rows per
+    // element (allocated when first enabled); mixed: per-element sqrt(K(0,0))
+    void* plastic = nullptr;
+    void* plastic_scale = nullptr;
+    double plastic_max = 0.0, plastic_yield = 1e-4, plastic_creep = 0.9;
+    int plastic_version = 0;  // bumped by every change of the settings (a captured step re-records)
     std::vector<double> young_h, poisson_h;  // as given (for inspection)
     std::vector<double> lsf_h;               // localStiffnessFactor as given
     size_t device_bytes = 0;
@@ -176,6 +182,7 @@ struct Scene {
     bool own_stream = false;
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    int graph_plastic_version = 0;  // the force field's plasticity settings the graph was recorded with
     int graph_steps = 0;
     size_t device_bytes = 0;
     // residual replacement (FP32 scenes): every `replace_every` CG iterations

@@ -276,23 +276,15 @@ __device__ __forceinline__ void load_KJ(const ElemView<R>& ev, size_t e, R K[3],
 // initSmall/initLarge/initPolar TFEM.inl:526-532, 835-868, 993-1023) and
 // stored in R.
 // ------------------------------------------------------------------------
-template <typename R>
-__global__ void k_init_elements(const double* __restrict__ rest_pos, const int4* __restrict__ tets,
-                                const int* __restrict__ elem_orig, int E, int method,
-                                const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
-                                int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest,
-                                float2* rest_ff, R* rot, R* A0inv,
-                                R* R0, double* vol)
+// computeMaterialStiffness (TFEM.inl:256-291) of element s (storage order;
+// e its index in the caller's order): K(0,0), K(0,1), K(3,3) divided by
+// 36 V, and V.
+__device__ __forceinline__ void material_stiffness(const double pa[3], const double pb[3], const double pc[3],
+                                                   const double pd[3], int e, int E,
+                                                   const double* __restrict__ young, int n_young,
+                                                   const double* __restrict__ poisson, int n_poisson,
+                                                   const double* __restrict__ lsf, int n_lsf, double k[3], double* vol)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= E) return;
-    const int e = elem_orig[s];  // material data is indexed by the caller's element order
-    const int4 t = tets[s];
-    double pa[3], pb[3], pc[3], pd[3];
-    ld3(rest_pos, t.x, pa);
-    ld3(rest_pos, t.y, pb);
-    ld3(rest_pos, t.z, pc);
-    ld3(rest_pos, t.w, pd);
     // getVecRealInElement (BaseLinearElasticityFEMForceField.inl:114-132)
     double Ey = (n_young > e) ? young[e] : young[0];
     double nu = (n_poisson > e) ? poisson[e] : poisson[0];
@@ -312,10 +304,35 @@ __global__ void k_init_elements(const double* __restrict__ rest_pos, const int4*
     dt += cr[1] * ec[1];
     dt += cr[2] * ec[2];
     double v = fabs(dt / 6.0);
-    vol[s] = v;
-    k0 /= v * 36;
-    k1 /= v * 36;
-    k2 /= v * 36;
+    *vol = v;
+    k[0] = k0 / (v * 36);
+    k[1] = k1 / (v * 36);
+    k[2] = k2 / (v * 36);
+}
+
+template <typename R>
+__global__ void k_init_elements(const double* __restrict__ rest_pos, const int4* __restrict__ tets,
+                                const int* __restrict__ elem_orig, int E, int method,
+                                const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
+                                int n_poisson, const double* __restrict__ lsf, int n_lsf, R* K, R* J, R* rest,
+                                float2* rest_ff, R* rot, R* A0inv,
+                                R* R0, double* vol)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= E) return;
+    const int e = elem_orig[s];  // material data is indexed by the caller's element order
+    const int4 t = tets[s];
+    double pa[3], pb[3], pc[3], pd[3];
+    ld3(rest_pos, t.x, pa);
+    ld3(rest_pos, t.y, pb);
+    ld3(rest_pos, t.z, pc);
+    ld3(rest_pos, t.w, pd);
+    double kk[3];
+    material_stiffness(pa, pb, pc, pd, e, E, young, n_young, poisson, n_poisson, lsf, n_lsf, kk, &vol[s]);
+    const double k0 = kk[0], k1 = kk[1], k2 = kk[2];
+    double ea[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+    double eb[3] = {pc[0] - pa[0], pc[1] - pa[1], pc[2] - pa[2]};
+    double ec[3] = {pd[0] - pa[0], pd[1] - pa[1], pd[2] - pa[2]};
     const size_t En = (size_t)E;
     K[0 * En + s] = (R)k0;
     K[1 * En + s] = (R)k1;
@@ -412,12 +429,82 @@ __device__ __forceinline__ bool svd_frame_elem(const ElemView<R>& ev, size_t e, 
     return svd_frame(A, Ai, R0, Rout);
 }
 
+// Plasticity of the addForce strain (plasticMaxThreshold > 0): per element
+// six plastic strain components that every addForce call updates.
+// FP64 stores the strain as the reference does; mixed precision stores it in
+// the scaling of its strain-displacement values (J sqrt(K(0,0)), so J^T D is
+// sqrt(K(0,0)) times the strain) and scales the thresholds by the same
+// per-element factor.
+template <typename R>
+struct PlasticArgs {
+    R* strain = nullptr;         // 6 rows x n_tets; null: plasticity off
+    const R* scale = nullptr;    // mixed: sqrt(K(0,0)) per element; null for FP64
+    R max_threshold = R(0), yield_threshold = R(0), creep = R(0);
+};
+
+// computeForce's plastic step (TFEM.inl:357-370): the elastic part of the
+// strain J^T D minus the plastic strain; above the yield threshold the
+// plastic strain creeps towards it, it is clamped to the maximum norm, and
+// the force uses the strain minus the plastic strain.
+template <typename R>
+__device__ __forceinline__ void plastic_step(R jd[6], const PlasticArgs<R>& pl, size_t e, size_t En)
+{
+    R ps[6], el[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        ps[i] = pl.strain[i * En + e];
+        el[i] = jd[i] - ps[i];
+    }
+    R yield = pl.yield_threshold, mx = pl.max_threshold;
+    if (pl.scale) {
+        const R k = pl.scale[e];
+        yield = yield * k;
+        mx = mx * k;
+    }
+    R n2 = el[0] * el[0];
+#pragma unroll
+    for (int i = 1; i < 6; ++i) n2 += el[i] * el[i];
+    if (n2 > yield * yield) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const R c = el[i] * pl.creep;
+            ps[i] += c;
+        }
+    }
+    R p2 = ps[0] * ps[0];
+#pragma unroll
+    for (int i = 1; i < 6; ++i) p2 += ps[i] * ps[i];
+    if (p2 > mx * mx) {
+        const R f = mx / sqrt(p2);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) ps[i] *= f;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        pl.strain[i * En + e] = ps[i];
+        jd[i] -= ps[i];
+    }
+}
+
+// computeForce of addForce (TFEM.inl:293-415), with the plastic step when
+// plasticity is on.
+template <typename R>
+__device__ __forceinline__ void addforce_element(R F[12], const R D[12], const R K[3], const R J[12],
+                                                 const PlasticArgs<R>& pl, size_t e, size_t En)
+{
+    R jd[6];
+    strain_jtd(D, J, jd);
+    if (pl.strain) plastic_step(jd, pl, e, En);
+    force_from_strain(F, jd, K, J);
+}
+
 // addForce element part: accumulateForceSmall / Large / Polar
 // (TFEM.inl:534-623, 870-986, 1025-1079). Writes rotations and the corner
 // forces R^T F (method=small: F).
 template <typename R, int METHOD>
 __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, const double* __restrict__ x,
-                                                const double* __restrict__ rest_pos, R* __restrict__ eforce)
+                                                const double* __restrict__ rest_pos, R* __restrict__ eforce,
+                                                const PlasticArgs<R>& pl = PlasticArgs<R>{})
 {
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
@@ -440,7 +527,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
         for (int i = 1; i < 4; ++i)
 #pragma unroll
             for (int k = 0; k < 3; ++k) D[3 * i + k] = (R)(q[i][k] - q[0][k] - p[i][k] + p[0][k]);
-        element_force_nofact(F, D, K, J);
+        addforce_element(F, D, K, J, pl, (size_t)e, En);
 #pragma unroll
         for (int i = 0; i < 12; ++i) c[i] = F[i];
         store_eforce(eforce, e, c);
@@ -567,7 +654,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
         }
     }
     store_rot(ev, (size_t)e, Rm);
-    element_force_nofact(F, D, K, J);
+    addforce_element(F, D, K, J, pl, (size_t)e, En);
     // f[node] += rotations[e] * F_node, rotations[e] = R^T
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -584,11 +671,11 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
 template <typename R, int METHOD>
 __global__ void __launch_bounds__(kElemBlock) k_elem_force(ElemView<R> ev, const double* __restrict__ x,
                                                            const double* __restrict__ rest_pos,
-                                                           R* __restrict__ eforce)
+                                                           R* __restrict__ eforce, PlasticArgs<R> pl)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ev.n_tets) return;
-    elem_force_body<R, METHOD>(ev, e, x, rest_pos, eforce);
+    elem_force_body<R, METHOD>(ev, e, x, rest_pos, eforce, pl);
 }
 
 // Direction of the CG step for the matvec element pass. DIR 0: the input
@@ -2072,20 +2159,58 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
         (R*)m->J, (R*)m->rest, m->rest_ff, (R*)m->rot, (R*)m->A0inv, (R*)m->R0, vol);
 }
 
+// Mixed precision: the per-element factor sqrt(K(0,0)) of the stored
+// strain-displacement values, for the plastic thresholds.
+template <typename R>
+__global__ void k_plastic_scale(const double* __restrict__ rest_pos, const int4* __restrict__ tets,
+                                const int* __restrict__ elem_orig, int E, const double* __restrict__ young,
+                                int n_young, const double* __restrict__ poisson, int n_poisson,
+                                const double* __restrict__ lsf, int n_lsf, R* __restrict__ scale)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= E) return;
+    const int4 t = tets[s];
+    double pa[3], pb[3], pc[3], pd[3], k[3], v;
+    ld3(rest_pos, t.x, pa);
+    ld3(rest_pos, t.y, pb);
+    ld3(rest_pos, t.z, pc);
+    ld3(rest_pos, t.w, pd);
+    material_stiffness(pa, pb, pc, pd, elem_orig[s], E, young, n_young, poisson, n_poisson, lsf, n_lsf, k, &v);
+    scale[s] = (R)sqrt(k[0]);
+}
+
+template <typename R>
+void launch_plastic_scale(TfemMesh* m, const double* young, int ny, const double* poisson, int np, const double* lsf,
+                          int nl, cudaStream_t s)
+{
+    if (m->n_tets == 0 || !m->plastic_scale) return;
+    k_plastic_scale<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(m->rest_pos, m->tets, m->elem_orig, m->n_tets,
+                                                                   young, ny, poisson, np, lsf, nl,
+                                                                   (R*)m->plastic_scale);
+}
+
 template <typename R>
 void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
 {
     if (m->n_tets == 0) return;
     ElemView<R> ev = view<R>(m);
     const int g = elem_grid(m->n_tets);
+    PlasticArgs<R> pl;
+    if (m->plastic && m->plastic_max > 0.0) {
+        pl.strain = (R*)m->plastic;
+        pl.scale = (const R*)m->plastic_scale;
+        pl.max_threshold = (R)m->plastic_max;
+        pl.yield_threshold = (R)m->plastic_yield;
+        pl.creep = (R)m->plastic_creep;
+    }
     if (m->method == METHOD_SMALL)
-        k_elem_force<R, METHOD_SMALL><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+        k_elem_force<R, METHOD_SMALL><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
     else if (m->method == METHOD_LARGE)
-        k_elem_force<R, METHOD_LARGE><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+        k_elem_force<R, METHOD_LARGE><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
     else if (m->method == METHOD_SVD)
-        k_elem_force<R, METHOD_SVD><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+        k_elem_force<R, METHOD_SVD><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
     else
-        k_elem_force<R, METHOD_POLAR><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce);
+        k_elem_force<R, METHOD_POLAR><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
 }
 
 template <typename R, typename VIN, int DIR>

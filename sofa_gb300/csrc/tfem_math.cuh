@@ -200,25 +200,31 @@ __device__ __forceinline__ void element_force(T F[12], const T D[12], const T K[
     }
 }
 
-// computeForce without the factor (the addForce variant, TFEM.inl:293-415,
-// plasticity off).
+// J^T D on J's sparsity pattern (computeForce, TFEM.inl:329-355): the six
+// strain components in the reference's term order.
 template <typename T>
-__device__ __forceinline__ void element_force_nofact(T F[12], const T D[12], const T K[3], const T J[12])
+__device__ __forceinline__ void strain_jtd(const T D[12], const T J[12], T jd[6])
 {
-    T jd0 = J[0] * D[0] + J[3] * D[3] + J[6] * D[6] + J[9] * D[9];
-    T jd1 = J[1] * D[1] + J[4] * D[4] + J[7] * D[7] + J[10] * D[10];
-    T jd2 = J[2] * D[2] + J[5] * D[5] + J[8] * D[8] + J[11] * D[11];
-    T jd3 = J[1] * D[0] + J[0] * D[1] + J[4] * D[3] + J[3] * D[4] + J[7] * D[6] + J[6] * D[7] + J[10] * D[9] +
+    jd[0] = J[0] * D[0] + J[3] * D[3] + J[6] * D[6] + J[9] * D[9];
+    jd[1] = J[1] * D[1] + J[4] * D[4] + J[7] * D[7] + J[10] * D[10];
+    jd[2] = J[2] * D[2] + J[5] * D[5] + J[8] * D[8] + J[11] * D[11];
+    jd[3] = J[1] * D[0] + J[0] * D[1] + J[4] * D[3] + J[3] * D[4] + J[7] * D[6] + J[6] * D[7] + J[10] * D[9] +
             J[9] * D[10];
-    T jd4 = J[2] * D[1] + J[1] * D[2] + J[5] * D[4] + J[4] * D[5] + J[8] * D[7] + J[7] * D[8] + J[11] * D[10] +
+    jd[4] = J[2] * D[1] + J[1] * D[2] + J[5] * D[4] + J[4] * D[5] + J[8] * D[7] + J[7] * D[8] + J[11] * D[10] +
             J[10] * D[11];
-    T jd5 = J[2] * D[0] + J[0] * D[2] + J[5] * D[3] + J[3] * D[5] + J[8] * D[6] + J[6] * D[8] + J[11] * D[9] +
+    jd[5] = J[2] * D[0] + J[0] * D[2] + J[5] * D[3] + J[3] * D[5] + J[8] * D[6] + J[6] * D[8] + J[11] * D[9] +
             J[9] * D[11];
+}
+
+// F = J K jd (computeForce, TFEM.inl:374-412) without the factor.
+template <typename T>
+__device__ __forceinline__ void force_from_strain(T F[12], const T jd[6], const T K[3], const T J[12])
+{
     const T k0 = K[0], k1 = K[1], k2 = K[2];
-    T s0 = k0 * jd0 + k1 * jd1 + k1 * jd2;
-    T s1 = k1 * jd0 + k0 * jd1 + k1 * jd2;
-    T s2 = k1 * jd0 + k1 * jd1 + k0 * jd2;
-    T s3 = k2 * jd3, s4 = k2 * jd4, s5 = k2 * jd5;
+    T s0 = k0 * jd[0] + k1 * jd[1] + k1 * jd[2];
+    T s1 = k1 * jd[0] + k0 * jd[1] + k1 * jd[2];
+    T s2 = k1 * jd[0] + k1 * jd[1] + k0 * jd[2];
+    T s3 = k2 * jd[3], s4 = k2 * jd[4], s5 = k2 * jd[5];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const T a = J[3 * i], b = J[3 * i + 1], c = J[3 * i + 2];
@@ -226,6 +232,16 @@ __device__ __forceinline__ void element_force_nofact(T F[12], const T D[12], con
         F[3 * i + 1] = b * s1 + a * s3 + c * s4;
         F[3 * i + 2] = c * s2 + b * s4 + a * s5;
     }
+}
+
+// computeForce without the factor (the addForce variant, TFEM.inl:293-415,
+// plasticity off).
+template <typename T>
+__device__ __forceinline__ void element_force_nofact(T F[12], const T D[12], const T K[3], const T J[12])
+{
+    T jd[6];
+    strain_jtd(D, J, jd);
+    force_from_strain(F, jd, K, J);
 }
 
 // ---- svd method: stable polar factor through a 3x3 SVD ---------------------

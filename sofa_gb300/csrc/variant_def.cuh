@@ -51,11 +51,16 @@ static void v_stiffness_blocks(TfemMesh* m, const int* cptr, const int* contrib,
 {
     launch_stiffness_blocks<SGB_REAL>(m, cptr, contrib, n_blocks, out, s);
 }
+static void v_plastic_scale(TfemMesh* m, const double* y, int ny, const double* p, int np, const double* l, int nl,
+                            cudaStream_t s)
+{
+    launch_plastic_scale<SGB_REAL>(m, y, ny, p, np, l, nl, s);
+}
 }  // namespace SGB_NS
 
 namespace sgb {
 const VariantOps SGB_TABLE = {SGB_VARIANT_NAME,     sizeof(SGB_REAL),     SGB_USES_PATCHES,
                               SGB_NS::v_init,       SGB_NS::v_add_force,  SGB_NS::v_add_dforce,
                               SGB_NS::v_scene_step, SGB_NS::v_prepare,   SGB_NS::v_batch_prepare,
-                              SGB_NS::v_batch_record, SGB_NS::v_stiffness_blocks};
+                              SGB_NS::v_batch_record, SGB_NS::v_stiffness_blocks, SGB_NS::v_plastic_scale};
 }

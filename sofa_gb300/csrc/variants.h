@@ -22,6 +22,9 @@ struct VariantOps {
     // assembled stiffness blocks (BSR, 3x3) at the current rotations
     void (*stiffness_blocks)(TfemMesh*, const int* cptr, const int* contrib, int n_blocks, double* out,
                              cudaStream_t);
+    // mixed plasticity: per-element scale of the stored strain (plastic_scale)
+    void (*plastic_scale)(TfemMesh*, const double* young, int ny, const double* poisson, int np, const double* lsf,
+                          int nl, cudaStream_t);
 };
 
 extern const VariantOps ops_fp64_exact;

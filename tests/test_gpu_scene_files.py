@@ -130,3 +130,33 @@ def test_pcg_jacobi_scene_file_against_oracle(capi, oracle):
     xo, _ = osc.state()
     assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
     assert np.max(np.abs(xo - pos)) > 1e-3
+
+
+def test_plasticity_scene_file_against_oracle(capi, oracle):
+    """The known-answer grid scene with the plasticity settings of the
+    reference's TetrahedronFEMForceField_plasticity.scn (yield 0.005, maximum
+    0.025, creep 1): 50 steps against the oracle with the same settings."""
+    text = _read("grid_fem_4x10x4.scn").replace(
+        '<TetrahedronFEMForceField name="FEM"',
+        '<TetrahedronFEMForceField plasticYieldThreshold="0.005" plasticMaxThreshold="0.025" plasticCreep="1" '
+        'name="FEM"')
+    s = capi.SofaScene(text)
+    s.animate(50)
+    x = s.positions(0)
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    runs = []
+    for plastic in (True, False):
+        fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+        if plastic:
+            fem.set_plasticity(0.025, 0.005, 1.0)
+        osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01,
+                                 cg_iterations=20, cg_tolerance=1e-5, cg_threshold=1e-6)
+        osc.step(50)
+        runs.append(osc.state()[0])
+        if plastic:
+            assert np.abs(fem.plastic_strain()).max() > 0
+    xo, xe = runs
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+    assert np.max(np.abs(xe - xo)) > 1e-3 * np.max(np.abs(xo - pos))  # plasticity changed the motion

@@ -153,8 +153,8 @@ def test_scene_errors(capi, case):
     (('method="large"', 'method="large" updateStiffnessMatrix="1"'), "updateStiffnessMatrix"),
     (('<DiagonalMass name="mass" massDensity="1.0" />', ''), "mass"),
     (('<EulerImplicitSolver />', '<EulerImplicitSolver firstOrder="1" />'), "firstOrder"),
-    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField plasticMaxThreshold="0.1" name="FEM"'),
-     "plastic"),
+    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="1" name="FEM"'),
+     "computeVonMisesStress"),
 ])
 def test_unsupported_component_settings(capi, edit, msg):
     xml = _read("grid_fem_4x10x4.scn").replace(*edit)
