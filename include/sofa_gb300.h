@@ -118,6 +118,21 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
  * turns it off and keeps the strain. Thresholds are 2-norms of the 6-vector
  * strain. Synchronous on the handle's stream when first turned on. */
 int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_threshold, double creep);
+/* von Mises stress (TetrahedronFEMForceField::computeVonMisesStress,
+ * TetrahedronFEMForceField.inl:2197-2374; Data computeVonMisesStress,
+ * vonMisesPerElement, vonMisesPerNode) at positions x_dev (n_nodes xyz
+ * doubles, device). mode 1: from the corotational strain (methods large,
+ * polar, svd; small is refused as in the reference, :1441-1445); mode 2:
+ * from the Green strain. per_element_dev: n_tets doubles in the caller's
+ * element order; per_node_dev (may be NULL): n_nodes doubles, the mean over
+ * each node's elements. FP64 for every precision. The reference also
+ * overwrites the element rotations in mode 1; this call leaves them as the
+ * last add_force computed them. The first call computes and keeps the
+ * elements' Lame coefficients (16 B per element), synchronously; later calls
+ * are stream-ordered. */
+int sgb_tfem_von_mises(sgb_tfem_t* fem, int mode, const double* x_dev, double* per_element_dev,
+                       double* per_node_dev, void* stream);
+
 /* Zeroes the plastic strain (TetrahedronFEMForceField::reset, .inl:1382-1390).
  * Stream-ordered on the handle's stream. */
 int sgb_tfem_reset_plasticity(sgb_tfem_t* fem);
@@ -268,6 +283,12 @@ int sgb_scene_step(sgb_scene_t* scene, int n_steps);
  * run, last relative residual |r|/|b|, and SGB_ERR_NUMERICAL if a
  * non-finite value was met. */
 int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual);
+
+/* von Mises stress of the scene's force field at its current positions
+ * (sgb_tfem_von_mises; TetrahedronFEMForceField computes it at the end of
+ * each step, TetrahedronFEMForceField.inl:2008-2031), into host arrays:
+ * n_tets per element, n_nodes per node (may be NULL). Synchronous. */
+int sgb_scene_von_mises(sgb_scene_t* scene, int mode, double* per_element_host, double* per_node_host);
 
 /* State access (FP64). get_* synchronise; set_* are stream-ordered: from
  * pinned host memory the copies run asynchronously, and the caller keeps the

@@ -73,6 +73,14 @@ int sgb_sofa_scene_animate(sgb_sofa_scene_t* scene, int n_steps);
  * device is initialised, else the initial positions. */
 int sgb_sofa_scene_get_positions(sgb_sofa_scene_t* scene, int body, double* x_host);
 
+/* vonMisesPerElement / vonMisesPerNode of a body whose
+ * TetrahedronFEMForceField sets computeVonMisesStress (1 or 2), at its
+ * current state (TetrahedronFEMForceField.inl:2197-2374); per_node_host may be
+ * NULL. SGB_ERR_INVALID_ARGUMENT when the force field does not compute it or
+ * the device is not initialised yet. Synchronous. */
+int sgb_sofa_scene_get_von_mises(sgb_sofa_scene_t* scene, int body, double* per_element_host,
+                                 double* per_node_host);
+
 /* Simulated time (steps x dt). */
 int sgb_sofa_scene_time(const sgb_sofa_scene_t* scene, double* t);
 

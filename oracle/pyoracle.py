@@ -46,6 +46,8 @@ def _load():
     lib.orc_fem_rest_volume.argtypes = [vp]
     lib.orc_fem_set_plasticity.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
     lib.orc_fem_plastic_strain.argtypes = [vp, _dp]
+    lib.orc_fem_von_mises.restype = ctypes.c_int
+    lib.orc_fem_von_mises.argtypes = [vp, ctypes.c_int, _dp, _dp, _dp]
     lib.orc_polar.restype = ctypes.c_double
     lib.orc_polar.argtypes = [_dp, _dp]
     lib.orc_polar_stable.restype = ctypes.c_int
@@ -160,6 +162,15 @@ class OracleFEM:
     def set_plasticity(self, max_threshold, yield_threshold=1e-4, creep=0.9):
         """plasticMaxThreshold / plasticYieldThreshold / plasticCreep."""
         _load().orc_fem_set_plasticity(self._h, max_threshold, yield_threshold, creep)
+
+    def von_mises(self, x, mode):
+        """computeVonMisesStress at x: (per element, per node)."""
+        x, px = _d(np.asarray(x).reshape(-1, 3))
+        e, pe = _d(np.zeros(self.n_tets))
+        n, pn = _d(np.zeros(self.n_nodes))
+        if _load().orc_fem_von_mises(self._h, int(mode), px, pe, pn) != 0:
+            raise ValueError("von Mises mode 1 needs method large, polar or svd")
+        return e, n
 
     def plastic_strain(self):
         """(n_tets, 6) plastic strain."""

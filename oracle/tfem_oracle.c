@@ -35,6 +35,7 @@
  * ParallelTetrahedronFEMForceField.inl:53-124); its sums are reordered, so it
  * is used for timing, not as the parity reference.
  */
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -575,6 +576,7 @@ typedef struct orc_fem {
     double* A0inv;     /* svd: _initialTransformation (inverse rest edge matrix), 9 per element */
     double rest_volume;
     double* plastic;   /* _plasticStrains, 6 per element (NULL until plasticity is turned on) */
+    double* lame;      /* elemLambda, elemMu (TFEM.inl:278-282), 2 per element */
     orc_plastic pl;
     double* tl_buf;    /* thread-local force buffers for the threaded mode */
     int tl_threads;
@@ -607,6 +609,7 @@ orc_fem* orc_fem_create(int n_nodes, const double* rest, int n_tets, const int32
     m->rot = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
     m->rest_rot = (double*)calloc(12 * (size_t)n_tets, sizeof(double));
     if (method == ORC_SVD) m->A0inv = (double*)calloc(9 * (size_t)n_tets, sizeof(double));
+    m->lame = (double*)calloc(2 * (size_t)n_tets + 1, sizeof(double));
 
     for (int e = 0; e < n_tets; ++e) {
         const int32_t* t = &tets[4 * e];
@@ -622,6 +625,8 @@ orc_fem* orc_fem_create(int n_nodes, const double* rest, int n_tets, const int32
         k0 *= s;
         k1 *= s;
         k2 *= s;
+        m->lame[2 * e] = k1; /* elemLambda = K(0,1), elemMu = K(3,3) before the volume division */
+        m->lame[2 * e + 1] = k2;
         /* geometry::Tetrahedron::volume (Geometry/.../Tetrahedron.h:55-83) */
         double ea[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
         double eb[3] = {pc[0] - pa[0], pc[1] - pa[1], pc[2] - pa[2]};
@@ -683,6 +688,7 @@ void orc_fem_destroy(orc_fem* m)
     free(m->rest_rot);
     free(m->A0inv);
     free(m->plastic);
+    free(m->lame);
     free(m->tl_buf);
     free(m);
 }
@@ -889,6 +895,157 @@ void orc_fem_set_plasticity(orc_fem* m, double max_threshold, double yield_thres
     m->pl.max_threshold = max_threshold;
     m->pl.yield_threshold = yield_threshold;
     m->pl.creep = creep;
+}
+
+/* invertMatrix, general square case (Sofa/framework/Type/src/sofa/type/
+ * Mat.h:1102-1168), for 4x4: Gauss-Jordan with full pivoting. Returns 0 when
+ * a pivot is within machine epsilon of zero (equalsZero, Mat.h:46-49). */
+static int invert4(const double from[16], double dest[16])
+{
+    double m1[16], m2[16];
+    int r[4] = {0}, c[4] = {0}, row[4] = {0}, col[4] = {0};
+    for (int i = 0; i < 16; ++i) {
+        m1[i] = from[i];
+        m2[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    }
+    for (int k = 0; k < 4; ++k) {
+        double pivot = 0;
+        for (int i = 0; i < 4; ++i) {
+            if (row[i]) continue;
+            for (int j = 0; j < 4; ++j) {
+                double t;
+                if (col[j]) continue;
+                t = m1[4 * i + j];
+                if (t < 0) t = -t;
+                if (t > pivot) {
+                    pivot = t;
+                    r[k] = i;
+                    c[k] = j;
+                }
+            }
+        }
+        if (fabs(pivot) <= DBL_EPSILON) return 0;
+        row[r[k]] = col[c[k]] = 1;
+        pivot = m1[4 * r[k] + c[k]];
+        for (int j = 0; j < 4; ++j) m1[4 * r[k] + j] /= pivot;
+        m1[4 * r[k] + c[k]] = 1;
+        for (int j = 0; j < 4; ++j) m2[4 * r[k] + j] /= pivot;
+        for (int i = 0; i < 4; ++i) {
+            if (i == r[k]) continue;
+            double f = m1[4 * i + c[k]];
+            for (int j = 0; j < 4; ++j) m1[4 * i + j] -= m1[4 * r[k] + j] * f;
+            m1[4 * i + c[k]] = 0;
+            for (int j = 0; j < 4; ++j) m2[4 * i + j] -= m2[4 * r[k] + j] * f;
+        }
+    }
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            if (c[j] == i) row[i] = r[j];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) dest[4 * i + j] = m2[4 * row[i] + j];
+    return 1;
+}
+
+/* computeVonMisesStress (TFEM.inl:2197-2374): per element von Mises stress
+ * from the corotational strain (mode 1, large/polar/svd) or the Green strain
+ * (mode 2), and per node the mean over the node's elements in element order.
+ * vmn may be NULL. Returns 0, or -1 for mode 1 with method small (the
+ * reference marks the component invalid, :1441-1445). */
+int orc_fem_von_mises(const orc_fem* m, int mode, const double* X, double* vme, double* vmn)
+{
+    if (mode == 1 && m->method == ORC_SMALL) return -1;
+    for (int el = 0; el < m->n_tets; ++el) {
+        const int32_t* t = &m->tets[4 * el];
+        double mv[16], shf[16] = {0}, g[9], strain[9], v[6], sg[6], tr = 0.0, q;
+        /* elemShapeFun (:1527-1541) */
+        for (int k = 0; k < 4; ++k) {
+            mv[4 * k] = 1.0;
+            for (int l = 1; l < 4; ++l) mv[4 * k + l] = m->rest[3 * t[k] + l - 1];
+        }
+        if (!invert4(mv, shf)) memset(shf, 0, sizeof(shf));
+        if (mode == 2) {
+            double U[4][3];
+            for (int i = 0; i < 4; ++i)
+                for (int k = 0; k < 3; ++k) U[i][k] = X[3 * t[i] + k] - m->rest[3 * t[i] + k];
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    g[3 * k + l] = 0.0;
+                    for (int i = 0; i < 4; ++i) g[3 * k + l] += shf[4 * (l + 1) + i] * U[i][k];
+                }
+            /* 0.5 (gradU + gradU^T + gradU^T gradU) */
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double sym = g[3 * i + j] + g[3 * j + i];
+                    double tt = g[i] * g[j] + g[3 + i] * g[3 + j] + g[6 + i] * g[6 + j];
+                    strain[3 * i + j] = 0.5 * (sym + tt);
+                }
+        } else {
+            double R[9], def[12], D[12];
+            const double* rr = &m->rest_rot[12 * el];
+            const double *p0 = &X[3 * t[0]], *p1 = &X[3 * t[1]], *p2 = &X[3 * t[2]], *p3 = &X[3 * t[3]];
+            if (m->method == ORC_LARGE) {
+                rotation_large(p0, p1, p2, R);
+            } else {
+                double A[9] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], p2[0] - p0[0], p2[1] - p0[1],
+                               p2[2] - p0[2], p3[0] - p0[0], p3[1] - p0[1], p3[2] - p0[2]};
+                orc_polar(A, R);
+            }
+            for (int i = 0; i < 4; ++i) mat_vec(R, &X[3 * t[i]], &def[3 * i]);
+            if (m->method == ORC_LARGE) {
+                def[3] -= def[0];
+                def[6] -= def[0];
+                def[7] -= def[1];
+                def[9] -= def[0];
+                def[10] -= def[1];
+                def[11] -= def[2];
+                for (int i = 0; i < 12; ++i) D[i] = 0.0;
+                D[3] = rr[3] - def[3];
+                D[6] = rr[6] - def[6];
+                D[7] = rr[7] - def[7];
+                D[9] = rr[9] - def[9];
+                D[10] = rr[10] - def[10];
+                D[11] = rr[11] - def[11];
+            } else {
+                for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
+            }
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    g[3 * k + l] = 0.0;
+                    for (int i = 0; i < 4; ++i) g[3 * k + l] += shf[4 * (l + 1) + i] * D[3 * i + k];
+                }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) strain[3 * i + j] = 0.5 * (g[3 * i + j] + g[3 * j + i]);
+        }
+        v[0] = strain[0];
+        v[1] = strain[4];
+        v[2] = strain[8];
+        v[3] = strain[5];
+        v[4] = strain[2];
+        v[5] = strain[1];
+        for (int k = 0; k < 3; ++k) {
+            tr += v[k];
+            sg[k] = v[k] * 2 * m->lame[2 * el + 1];
+        }
+        for (int k = 3; k < 6; ++k) sg[k] = v[k] * 2 * m->lame[2 * el + 1];
+        for (int k = 0; k < 3; ++k) sg[k] += m->lame[2 * el] * tr;
+        q = sg[0] * sg[0] + sg[1] * sg[1] + sg[2] * sg[2] - sg[0] * sg[1] - sg[1] * sg[2] - sg[2] * sg[0] +
+            3 * sg[3] * sg[3] + 3 * sg[4] * sg[4] + 3 * sg[5] * sg[5];
+        vme[el] = sqrt(q);
+        if (vme[el] < 1e-10) vme[el] = 0.0;
+    }
+    if (vmn) {
+        int* cnt = (int*)calloc((size_t)m->n_nodes + 1, sizeof(int));
+        memset(vmn, 0, sizeof(double) * (size_t)m->n_nodes);
+        for (int el = 0; el < m->n_tets; ++el)
+            for (int c = 0; c < 4; ++c) {
+                vmn[m->tets[4 * el + c]] += vme[el];
+                cnt[m->tets[4 * el + c]]++;
+            }
+        for (int n = 0; n < m->n_nodes; ++n)
+            if (cnt[n]) vmn[n] /= (double)cnt[n];
+        free(cnt);
+    }
+    return 0;
 }
 
 /* _plasticStrains, 6 per element (zeros before plasticity is turned on). */

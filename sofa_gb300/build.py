@@ -30,6 +30,7 @@ UNITS = {
     "capi.cu": [],
     "mesh_layout.cu": [],
     "noalloc.cu": [],
+    "von_mises.cu": ["-fmad=false"],
     "batch.cu": [],
     "server.cu": [],
     "scene_graph.cpp": [],

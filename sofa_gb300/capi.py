@@ -150,6 +150,8 @@ def load():
         "sgb_scene_destroy": (c_int, [_vp]),
         "sgb_scene_step": (c_int, [_vp, c_int]),
         "sgb_scene_sync": (c_int, [_vp, ctypes.POINTER(c_int), _dp]),
+        "sgb_scene_von_mises": (c_int, [_vp, c_int, _dp, _dp]),
+        "sgb_tfem_von_mises": (c_int, [_vp, c_int, _vp, _vp, _vp, _vp]),
         "sgb_scene_get_state": (c_int, [_vp, _dp, _dp]),
         "sgb_scene_set_state": (c_int, [_vp, _dp, _dp]),
         "sgb_scene_set_external_force": (c_int, [_vp, _dp]),
@@ -188,6 +190,7 @@ def load():
         "sgb_sofa_scene_init_device": (c_int, [_vp]),
         "sgb_sofa_scene_animate": (c_int, [_vp, c_int]),
         "sgb_sofa_scene_get_positions": (c_int, [_vp, c_int, _dp]),
+        "sgb_sofa_scene_get_von_mises": (c_int, [_vp, c_int, _dp, _dp]),
         "sgb_sofa_scene_time": (c_int, [_vp, _dp]),
         "sgb_object_factory_new": (_vp, []),
         "sgb_object_factory_delete": (None, [_vp]),
@@ -305,6 +308,10 @@ class TetrahedronFEM:
         strain (TetrahedronFEMForceField::computeForce)."""
         check(load().sgb_tfem_set_plasticity(self._h, float(max_threshold), float(yield_threshold), float(creep)))
 
+    def von_mises(self, x_dev, mode, per_element_dev, per_node_dev=None, stream=None):
+        """computeVonMisesStress at positions x_dev (device pointers, FP64)."""
+        check(load().sgb_tfem_von_mises(self._h, int(mode), x_dev, per_element_dev, per_node_dev, stream))
+
     def reset_plasticity(self):
         check(load().sgb_tfem_reset_plasticity(self._h))
 
@@ -391,6 +398,14 @@ class Scene:
 
     def step(self, n=1):
         check(load().sgb_scene_step(self._h, int(n)))
+
+    def von_mises(self, mode=1):
+        """(per element, per node) von Mises stress at the current positions
+        (computeVonMisesStress mode 1: corotational strain, 2: Green strain)."""
+        e = np.zeros(self.fem.n_tets)
+        n = np.zeros(self.n_nodes)
+        check(load().sgb_scene_von_mises(self._h, int(mode), e.ctypes.data_as(_dp), n.ctypes.data_as(_dp)))
+        return e, n
 
     def sync(self):
         it = ctypes.c_int()
@@ -716,6 +731,16 @@ class SofaScene:
         x = np.zeros((self.body_info(body)["n_nodes"], 3), np.float64)
         check(load().sgb_sofa_scene_get_positions(self._h, int(body), x.ctypes.data_as(_dp)))
         return x
+
+    def von_mises(self, body=0):
+        """vonMisesPerElement, vonMisesPerNode of a body whose force field sets
+        computeVonMisesStress."""
+        info = self.body_info(body)
+        e = np.zeros(info["n_tets"])
+        n = np.zeros(info["n_nodes"])
+        check(load().sgb_sofa_scene_get_von_mises(self._h, int(body), e.ctypes.data_as(_dp),
+                                                  n.ctypes.data_as(_dp)))
+        return e, n
 
     @property
     def time(self) -> float:

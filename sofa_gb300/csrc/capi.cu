@@ -96,6 +96,7 @@ static void free_mesh(TfemMesh& m)
 {
     cudaFree(m.plastic);
     cudaFree(m.plastic_scale);
+    cudaFree(m.vm_lame);
     cudaFree(m.bsr_cptr);
     cudaFree(m.bsr_contrib);
     cudaFree(m.bsr_values);
@@ -529,6 +530,24 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
     return SGB_OK;
 }
 
+// Temporary device copies of the material vectors as given at creation
+// (Young's moduli, Poisson ratios, localStiffnessFactor), for kernels that
+// recompute per-element material values after initialisation. The caller
+// frees all three, also on failure.
+static cudaError_t upload_materials(const TfemMesh& m, double** d_y, double** d_p, double** d_l)
+{
+    cudaError_t ce = cudaMalloc(d_y, sizeof(double) * m.young_h.size());
+    if (ce == cudaSuccess) ce = cudaMalloc(d_p, sizeof(double) * m.poisson_h.size());
+    if (ce == cudaSuccess) ce = cudaMalloc(d_l, sizeof(double) * std::max<size_t>(m.lsf_h.size(), 1));
+    if (ce == cudaSuccess)
+        ce = cudaMemcpy(*d_y, m.young_h.data(), sizeof(double) * m.young_h.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpy(*d_p, m.poisson_h.data(), sizeof(double) * m.poisson_h.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && !m.lsf_h.empty())
+        ce = cudaMemcpy(*d_l, m.lsf_h.data(), sizeof(double) * m.lsf_h.size(), cudaMemcpyHostToDevice);
+    return ce;
+}
+
 int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_threshold, double creep)
 {
     if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_set_plasticity: NULL handle");
@@ -548,16 +567,7 @@ int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_
             SGB_CUDA_TRY(cudaMalloc(&m.plastic_scale, sizeof(float) * E));
             m.device_bytes += sizeof(float) * E;
             double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr;
-            cudaError_t ce = cudaMalloc(&d_y, sizeof(double) * m.young_h.size());
-            if (ce == cudaSuccess) ce = cudaMalloc(&d_p, sizeof(double) * m.poisson_h.size());
-            if (ce == cudaSuccess) ce = cudaMalloc(&d_l, sizeof(double) * std::max<size_t>(m.lsf_h.size(), 1));
-            if (ce == cudaSuccess)
-                ce = cudaMemcpy(d_y, m.young_h.data(), sizeof(double) * m.young_h.size(), cudaMemcpyHostToDevice);
-            if (ce == cudaSuccess)
-                ce = cudaMemcpy(d_p, m.poisson_h.data(), sizeof(double) * m.poisson_h.size(),
-                                cudaMemcpyHostToDevice);
-            if (ce == cudaSuccess && !m.lsf_h.empty())
-                ce = cudaMemcpy(d_l, m.lsf_h.data(), sizeof(double) * m.lsf_h.size(), cudaMemcpyHostToDevice);
+            cudaError_t ce = upload_materials(m, &d_y, &d_p, &d_l);
             if (ce == cudaSuccess) {
                 fem->ops->plastic_scale(&m, d_y, (int)m.young_h.size(), d_p, (int)m.poisson_h.size(), d_l,
                                         (int)m.lsf_h.size(), fem->stream);
@@ -574,6 +584,44 @@ int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_
     m.plastic_yield = yield_threshold;
     m.plastic_creep = creep;
     m.plastic_version++;
+    return SGB_OK;
+}
+
+int sgb_tfem_von_mises(sgb_tfem_t* fem, int mode, const double* x_dev, double* per_element_dev,
+                       double* per_node_dev, void* stream)
+{
+    if (!fem || !x_dev || !per_element_dev)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_von_mises: NULL argument");
+    if (mode != 1 && mode != 2)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_von_mises: mode must be 1 (corotational) or 2 (Green)");
+    TfemMesh& m = fem->m;
+    if (mode == 1 && m.method == METHOD_SMALL)
+        return fail(SGB_ERR_NOT_SUPPORTED,
+                    "sgb_tfem_von_mises: method small computes von Mises stress with the Green strain only (mode 2)");
+    const size_t E = (size_t)m.n_tets;
+    if (!m.vm_lame && E > 0) {
+        SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
+        SGB_CUDA_TRY(cudaMalloc(&m.vm_lame, sizeof(double) * 2 * E));
+        m.device_bytes += sizeof(double) * 2 * E;
+        double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr;
+        cudaError_t ce = upload_materials(m, &d_y, &d_p, &d_l);
+        if (ce == cudaSuccess) {
+            launch_lame(&m, d_y, (int)m.young_h.size(), d_p, (int)m.poisson_h.size(), d_l, (int)m.lsf_h.size(),
+                        m.vm_lame, fem->stream);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(fem->stream);
+        cudaFree(d_y);
+        cudaFree(d_p);
+        cudaFree(d_l);
+        if (ce != cudaSuccess) {
+            cudaFree(m.vm_lame);
+            m.vm_lame = nullptr;
+            return cuda_fail(ce, "sgb_tfem_von_mises");
+        }
+    }
+    launch_von_mises(&m, mode, x_dev, m.vm_lame, per_element_dev, per_node_dev, pick(fem, stream));
+    SGB_CUDA_TRY(cudaGetLastError());
     return SGB_OK;
 }
 
@@ -915,6 +963,32 @@ int sgb_scene_step(sgb_scene_t* scene, int n_steps)
         s.graph_valid = true;
     }
     for (int i = 0; i < n_steps; ++i) SGB_CUDA_TRY(cudaGraphLaunch(s.graph, s.stream));
+    return SGB_OK;
+}
+
+int sgb_scene_von_mises(sgb_scene_t* scene, int mode, double* per_element_host, double* per_node_host)
+{
+    if (!scene || !per_element_host) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_von_mises: NULL argument");
+    const TfemMesh& m = scene->fem->m;
+    const size_t E = (size_t)m.n_tets, N = (size_t)m.n_nodes;
+    double *d_e = nullptr, *d_n = nullptr;
+    cudaError_t ce = cudaMalloc(&d_e, sizeof(double) * std::max<size_t>(E, 1));
+    if (ce == cudaSuccess && per_node_host) ce = cudaMalloc(&d_n, sizeof(double) * std::max<size_t>(N, 1));
+    int rc = SGB_OK;
+    if (ce == cudaSuccess) {
+        rc = sgb_tfem_von_mises(scene->fem, mode, scene->s.x, d_e, d_n, scene->s.stream);
+        if (rc == SGB_OK) {
+            ce = cudaMemcpyAsync(per_element_host, d_e, sizeof(double) * E, cudaMemcpyDeviceToHost, scene->s.stream);
+            if (ce == cudaSuccess && per_node_host)
+                ce = cudaMemcpyAsync(per_node_host, d_n, sizeof(double) * N, cudaMemcpyDeviceToHost,
+                                     scene->s.stream);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(scene->s.stream);
+        }
+    }
+    cudaFree(d_e);
+    cudaFree(d_n);
+    if (rc != SGB_OK) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "sgb_scene_von_mises");
     return SGB_OK;
 }
 

@@ -168,6 +168,19 @@ int sgb_sofa_scene_get_positions(sgb_sofa_scene_t* scene, int body, double* x_ho
     return SGB_OK;
 }
 
+int sgb_sofa_scene_get_von_mises(sgb_sofa_scene_t* scene, int body, double* per_element_host,
+                                 double* per_node_host)
+{
+    if (!scene || !per_element_host || body < 0 || body >= (int)scene->scene.bodies.size())
+        return fail(SGB_ERR_NOT_FOUND, "sgb_sofa_scene_get_von_mises: no such body");
+    sgb::scn::Body& b = scene->scene.bodies[(size_t)body];
+    if (b.von_mises_mode == 0)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_get_von_mises: computeVonMisesStress is 0");
+    if (!b.scene)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_get_von_mises: the device is not initialised yet");
+    return sgb_scene_von_mises(b.scene, b.von_mises_mode, per_element_host, per_node_host);
+}
+
 int sgb_sofa_scene_time(const sgb_sofa_scene_t* scene, double* t)
 {
     if (!scene || !t) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_time: NULL argument");

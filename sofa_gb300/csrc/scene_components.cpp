@@ -698,8 +698,12 @@ int Scene::init_host(std::string* err)
         b.plastic_creep = fem->get_real(*this, "plasticCreep");
         if (b.plastic_max > 0.0 && b.plastic_yield < 0.0)
             return unsupported(err, where + "plasticYieldThreshold must be >= 0");
-        if (fem->get_int(*this, "computeVonMisesStress") != 0)
-            return unsupported(err, where + "computeVonMisesStress is not supported");
+        b.von_mises_mode = fem->get_int(*this, "computeVonMisesStress");
+        if (b.von_mises_mode < 0 || b.von_mises_mode > 2)
+            return unsupported(err, where + "computeVonMisesStress must be 0, 1 or 2");
+        if (b.von_mises_mode == 1 && b.method == SGB_METHOD_SMALL)
+            return unsupported(err, where + "computeVonMisesStress=1 (corotational strain) needs method large, polar "
+                                            "or svd (TetrahedronFEMForceField.inl:1441-1445)");
         if (fem->get_real(*this, "rayleighStiffness") != 0.0)
             return unsupported(err, where + "a force-field rayleighStiffness is not supported (use the solver's)");
         b.young = fem->get_reals(*this, "youngModulus");

@@ -123,6 +123,7 @@ struct TfemMesh {
     void* plastic_scale = nullptr;
     double plastic_max = 0.0, plastic_yield = 1e-4, plastic_creep = 0.9;
     int plastic_version = 0;  // bumped by every change of the settings (a captured step re-records)
+    double* vm_lame = nullptr;  // von Mises: lambda, mu per element (2 rows, computed on first use)
     std::vector<double> young_h, poisson_h;  // as given (for inspection)
     std::vector<double> lsf_h;               // localStiffnessFactor as given
     size_t device_bytes = 0;
@@ -276,5 +277,12 @@ struct BatchLaunch {
     int prefetch;  // FP32 matvec: prefetch the block's next patch into L2
     int* err;    // sticky device error flag of the batch
 };
+
+// von Mises stress (von_mises.cu): per-element lambda and mu, then the
+// per-element values (caller's order) and the per-node means.
+void launch_lame(const TfemMesh* m, const double* young, int ny, const double* poisson, int np, const double* lsf,
+                 int nl, double* lame, cudaStream_t s);
+void launch_von_mises(const TfemMesh* m, int mode, const double* x, const double* lame, double* per_element,
+                      double* per_node, cudaStream_t s);
 
 }  // namespace sgb

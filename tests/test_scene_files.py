@@ -153,7 +153,7 @@ def test_scene_errors(capi, case):
     (('method="large"', 'method="large" updateStiffnessMatrix="1"'), "updateStiffnessMatrix"),
     (('<DiagonalMass name="mass" massDensity="1.0" />', ''), "mass"),
     (('<EulerImplicitSolver />', '<EulerImplicitSolver firstOrder="1" />'), "firstOrder"),
-    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="1" name="FEM"'),
+    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="3" name="FEM"'),
      "computeVonMisesStress"),
 ])
 def test_unsupported_component_settings(capi, edit, msg):
