@@ -249,8 +249,8 @@ typedef struct sgb_scene_params {
      * cg_iterations / cg_tolerance are its iterations / tolerance), and its
      * preconditioner: SGB_PRECOND_NONE or SGB_PRECOND_JACOBI
      * (JacobiPreconditioner: z = diag(mF M + kF K)^-1 r, the diagonal
-     * re-assembled every step, fixed DOFs one). PCG runs on the unfused
-     * element-order kernels in every precision. */
+     * re-assembled every step, fixed DOFs one). FP64 PCG runs on the
+     * element-order kernels, mixed PCG on the fused patch kernels. */
     int linear_solver;
     int preconditioner;
     /* PreconditionedMatrixFreeSystem assemblingRate
@@ -258,6 +258,10 @@ typedef struct sgb_scene_params {
      * re-assembled on the first step and every this many steps after it
      * (0 or 1: every step). */
     int preconditioner_rate;
+    /* CGLinearSolver warmStart (CGLinearSolver.inl:95-104): 1 starts each
+     * solve from the previous step's solution, r = b - A x, instead of
+     * x = 0, r = b. PCG always starts from it. */
+    int warm_start;
 } sgb_scene_params;
 
 #define SGB_SOLVER_CG 0

@@ -65,6 +65,7 @@ def _load():
     lib.orc_scene_set_springs.argtypes = [vp, ctypes.c_double, _dp]
     lib.orc_scene_step.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_set_solver.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.orc_scene_set_warm_start.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_jacobi.argtypes = [vp, _dp]
     lib.orc_scene_compute_force.argtypes = [vp, _dp]
     lib.orc_scene_last_iterations.restype = ctypes.c_int
@@ -246,6 +247,10 @@ class OracleScene:
     def set_springs(self, k, anchor):
         self._anchor, p = _d(np.asarray(anchor).reshape(-1, 3))
         _load().orc_scene_set_springs(self._h, float(k), p)
+
+    def set_warm_start(self, on=True):
+        """CGLinearSolver warmStart."""
+        _load().orc_scene_set_warm_start(self._h, int(on))
 
     def set_solver(self, solver="cg", preconditioner=None, rate=1):
         """solver "cg" (CGLinearSolver) or "pcg" (PCGLinearSolver, warm start);

@@ -1087,6 +1087,7 @@ typedef struct orc_scene {
     double last_err;
     /* linear solver: 0 CGLinearSolver, 1 PCGLinearSolver; Jacobi preconditioner */
     int solver, precond, precond_rate;
+    int warm_start; /* CGLinearSolver warmStart */
     double* dinv;
 } orc_scene;
 
@@ -1273,14 +1274,22 @@ static void matvec(orc_scene* s, double* q, const double* p, double mf, double k
 
 /* CGLinearSolver::solve (CGLinearSolver.inl:72-315) with the GraphScattered
  * cgstep_beta / cgstep_alpha (CGLinearSolver.cpp:40-63), warmStart off. */
+static void vop_avf(double* out, const double* a, double f, long n3);
+
 static void cg_solve(orc_scene* s, double mf, double kf)
 {
     const int n = s->n;
     const long n3 = 3L * n;
     double *x = s->xs, *b = s->b, *p = s->p, *q = s->q, *r = s->r;
     double rho, rho_1 = 0.0, alpha, beta;
-    memset(x, 0, sizeof(double) * (size_t)n3);
-    memcpy(r, b, sizeof(double) * (size_t)n3);
+    if (s->warm_start) {
+        /* CGLinearSolver.inl:95-99: r = A x; r = b + r * -1 */
+        matvec(s, r, x, mf, kf);
+        vop_avf(r, b, -1.0, n3);
+    } else {
+        memset(x, 0, sizeof(double) * (size_t)n3);
+        memcpy(r, b, sizeof(double) * (size_t)n3);
+    }
     const double normb = sqrt(vdot(b, b, n));
     int nb_iter = 0, n_matvec = 0;
     s->last_err = 0.0;
@@ -1465,6 +1474,9 @@ void orc_scene_set_solver(orc_scene* s, int solver, int precond, int precond_rat
     s->precond_rate = precond_rate > 1 ? precond_rate : 1;
     if (precond && !s->dinv) s->dinv = (double*)calloc(3 * (size_t)s->n, sizeof(double));
 }
+
+/* CGLinearSolver warmStart: each CG solve starts from the previous solution. */
+void orc_scene_set_warm_start(orc_scene* s, int on) { s->warm_start = on ? 1 : 0; }
 
 /* the last solve's Jacobi inverse diagonal (zeros before the first) */
 void orc_scene_jacobi(const orc_scene* s, double* out)

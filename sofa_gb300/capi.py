@@ -56,6 +56,7 @@ class SceneParams(ctypes.Structure):
         ("linear_solver", ctypes.c_int),
         ("preconditioner", ctypes.c_int),
         ("preconditioner_rate", ctypes.c_int),
+        ("warm_start", ctypes.c_int),
     ]
 
 
@@ -347,7 +348,7 @@ class Scene:
                  cg_iterations=25, cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0),
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
                  serial_dots=False, residual_replacement=0, linear_solver="cg", preconditioner=None,
-                 preconditioner_rate=1):
+                 preconditioner_rate=1, warm_start=False):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -377,6 +378,7 @@ class Scene:
         p.linear_solver = {"cg": 0, "pcg": 1}[linear_solver]
         p.preconditioner = {None: 0, "jacobi": 1}[preconditioner]
         p.preconditioner_rate = int(preconditioner_rate)
+        p.warm_start = int(warm_start)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now

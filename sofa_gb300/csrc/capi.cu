@@ -823,6 +823,8 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: unknown preconditioner");
     if (P.preconditioner != SGB_PRECOND_NONE && P.linear_solver != SGB_SOLVER_PCG)
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: a preconditioner needs linear_solver = PCG");
+    if (P.warm_start && P.residual_replacement > 0)
+        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_create: residual replacement starts each solve from x = 0");
     if (P.linear_solver == SGB_SOLVER_PCG && P.residual_replacement > 0)
         return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_create: residual replacement runs with CG only");
     if (P.residual_replacement > 0 &&
@@ -847,6 +849,7 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     s.prm.solver = P.linear_solver;
     s.prm.precond = P.preconditioner;
     s.prm.precond_rate = P.preconditioner_rate > 1 ? P.preconditioner_rate : 1;
+    s.prm.warm_start = P.warm_start ? 1 : 0;
     s.stream = fem->stream;
     sc->fem = fem;
     sc->ops = fem->ops;

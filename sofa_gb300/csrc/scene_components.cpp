@@ -713,7 +713,6 @@ int Scene::init_host(std::string* err)
         // EulerImplicitSolver + CGLinearSolver
         if (euler->get_bool(*this, "firstOrder") || euler->get_bool(*this, "trapezoidalScheme"))
             return unsupported(err, where + "firstOrder / trapezoidalScheme are not supported");
-        if (cg && cg->get_bool(*this, "warmStart")) return unsupported(err, where + "CG warmStart is not supported");
         sgb_scene_params_default(&b.params);
         b.params.dt = dt;
         b.params.rayleigh_stiffness = euler->get_real(*this, "rayleighStiffness");
@@ -723,6 +722,7 @@ int Scene::init_host(std::string* err)
             b.params.cg_iterations = cg->get_int(*this, "iterations");
             b.params.cg_tolerance = cg->get_real(*this, "tolerance");
             b.params.cg_threshold = cg->get_real(*this, "threshold");
+            b.params.warm_start = cg->get_bool(*this, "warmStart") ? 1 : 0;
         } else {
             b.params.linear_solver = SGB_SOLVER_PCG;
             b.params.cg_iterations = pcg->get_int(*this, "iterations");

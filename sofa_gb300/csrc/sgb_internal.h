@@ -154,6 +154,7 @@ struct SceneParams {
     int solver = 0;   // 0 CGLinearSolver, 1 PCGLinearSolver
     int precond = 0;  // PCG: 1 Jacobi
     int precond_rate = 1;  // the preconditioner is re-assembled every this many steps
+    int warm_start = 0;    // CG: start from the previous solution (warmStart)
 };
 
 struct Scene {

@@ -859,12 +859,13 @@ __device__ __forceinline__ double dot3(const A a[3], const B b[3])
     return r;
 }
 
-enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2, FIN_REPLACE = 3, FIN_PCG_START = 4 };
+enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2, FIN_REPLACE = 3, FIN_PCG_START = 4, FIN_WARM_START = 5 };
 
 struct SolveConsts {
     double tol, threshold;
     int it;   // CG iteration this kernel belongs to (1-based)
     int pcg;  // 1: PCGLinearSolver bookkeeping (r.z, tolerance * b.b, no threshold test)
+    int warm; // 1: CG warmStart (the solve starts from the previous solution)
 };
 
 // Last-block finish of a dot product: every block writes its partial; the
@@ -968,6 +969,15 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         double err = sqrt(total) / cg->normb;
         cg->last_err = err;
         if (err <= sc.tol) cg->done = 1;
+    } else if (FIN == FIN_WARM_START) {
+        // warmStart (CGLinearSolver.inl:95-99): r = b - A x; iteration 1
+        // starts with rho = r.r; b = 0 runs no iteration and keeps x
+        if (cg->normb != 0.0) {
+            cg->rho = total;
+            double err = sqrt(total) / cg->normb;
+            cg->last_err = err;
+            cg->done = (err <= sc.tol && !first_of_first) ? 1 : 0;
+        }
     } else {
         // residual replacement after the update of iteration sc.it: the true
         // residual's r.r replaces the recurrence's, for beta and for the
@@ -1087,7 +1097,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R*
         for (int k = 0; k < 3; ++k) {
             b[3 * (size_t)n + k] = a[k];
             r[3 * (size_t)n + k] = a[k];
-            if (!sc.pcg) xs[3 * (size_t)n + k] = R(0);  // PCG starts from the previous solution
+            if (!sc.pcg && !sc.warm) xs[3 * (size_t)n + k] = R(0);  // PCG / warmStart keep the previous solution
         }
         double d = dot3(a, a);
         if (terms) terms[n] = d;
@@ -1257,8 +1267,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_jacobi(NodeCSR csr, const
 }
 
 // PCG start: r = b - A x with x the previous step's solution (its K terms
-// in eforce), z = diag^-1 r (or r), r.z.
-template <typename R>
+// in eforce), z = diag^-1 r (or r), r.z; FIN_WARM_START: the same start for
+// CG with warmStart (r.r).
+template <typename R, int FIN = FIN_PCG_START>
 __global__ void __launch_bounds__(kNodeBlock) k_pcg_start(NodeCSR csr, const R* __restrict__ eforce,
                                                           const R* __restrict__ xs, const R* __restrict__ b,
                                                           MassArgs ma, double mf, int mass_first,
@@ -1295,7 +1306,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_pcg_start(NodeCSR csr, const R* 
         if (terms) terms[n] = d;
         local += d;
     }
-    finish_dot<FIN_PCG_START>(local, cg, terms, N, sc);
+    finish_dot<FIN>(local, cg, terms, N, sc);
 }
 
 // Euler update (MechanicalObject::vMultiOp fast path, MechanicalObject.inl:
@@ -2481,7 +2492,9 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
 // PCG before its first iteration (PCGLinearSolver.inl:194-214): the Jacobi
 // diagonal from this step's rotations when a preconditioner is set (it
 // returns at once on the steps between re-assemblies), then r = b - A x from
-// the previous step's solution and r.z. Element-order kernels: once per step.
+// the previous step's solution and r.z. CG with warmStart
+// (CGLinearSolver.inl:95-99): the same start with r.r. Element-order
+// kernels: once per step.
 template <typename R>
 void pcg_begin(Scene* sc, int mass_first, double mf, double kf, const SolveConsts& cons, double* dot_terms,
                cudaStream_t s)
@@ -2493,6 +2506,13 @@ void pcg_begin(Scene* sc, int mass_first, double mf, double kf, const SolveConst
     MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
     const int ng = node_grid(N);
     R* dinv = (R*)sc->dinv;  // null: no preconditioner
+    if (P.solver != 1) {
+        launch_elem_dforce<R, R, 0>(m, (const R*)sc->xs, nullptr, sc->cg, (R)kf, s);
+        k_pcg_start<R, FIN_WARM_START><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->xs,
+                                                                 (const R*)sc->b, ma, mf, mass_first, sc->fixed,
+                                                                 nullptr, (R*)sc->r, sc->cg, dot_terms, N, cons);
+        return;
+    }
     if (dinv) {
         ElemView<R> ev = view<R>(m);
         const int ge = elem_grid(m->n_tets);
@@ -2535,7 +2555,7 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     R* xs = (R*)sc->xs;
     const bool pcg = P.solver == 1;
     R* dinv = pcg ? (R*)sc->dinv : nullptr;  // null: no preconditioner
-    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0};
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0, P.warm_start};
     // f = F(x)
     launch_elem_force<R>(m, sc->x, s);
     k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
@@ -2547,7 +2567,7 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     // CG (or PCG) on (mF M + kF K) dv = b
     const double mf = 1 + 1.0 * h * P.rayleigh_mass;
     const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
-    if (pcg) pcg_begin<R>(sc, mass_first, mf, kf, cons, dot_terms, s);
+    if (pcg || P.warm_start) pcg_begin<R>(sc, mass_first, mf, kf, cons, dot_terms, s);
     for (int it = 1; it <= P.cg_iterations; ++it) {
         cons.it = it;
         if (it == 1) {
@@ -2602,7 +2622,7 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     R* partials = (R*)m->pl.partials;
     const bool pcg = P.solver == 1;
     const R* dinv = pcg ? (const R*)sc->dinv : nullptr;
-    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0};
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0, P.warm_start};
     launch_elem_force<R>(m, sc->x, s);
     k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
     const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
@@ -2611,7 +2631,7 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
                                               h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons);
     const double mf = 1 + 1.0 * h * P.rayleigh_mass;
     const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
-    if (pcg) pcg_begin<R>(sc, mass_first, mf, kf, cons, nullptr, s);
+    if (pcg || P.warm_start) pcg_begin<R>(sc, mass_first, mf, kf, cons, nullptr, s);
     PatchView pv = patch_view(m);
     ElemView<R> ev = view<R>(m);
     const size_t smem = patch_smem_bytes<R>(m);

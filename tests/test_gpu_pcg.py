@@ -125,3 +125,27 @@ def test_pcg_parameter_errors(capi):
         fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, "large", "mixed")
         capi.Scene(fem, linear_solver="pcg", residual_replacement=10)
     assert e.value.code == -4
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 0.0), ("mixed", 1e-4)])
+def test_cg_warm_start_against_oracle(capi, oracle, precision, tol):
+    """CGLinearSolver warmStart: FP64 reference rounding with serial dots is
+    bit-identical to the oracle over 20 steps, iteration counts included;
+    mixed is within 1e-4 of the positions."""
+    mesh = cases.beam_mesh()
+    cfg = dict(cases.BEAM_SMALL, cg_iterations=40, cg_tolerance=1e-8)
+    _, osc = cases.oracle_scene(oracle, mesh, "large", cfg=cfg)
+    osc.set_warm_start(True)
+    sc = cases.gpu_scene(capi, mesh, "large", precision, cfg=cfg, serial_dots=(tol == 0.0), warm_start=True)
+    for step in range(20):
+        osc.step(1)
+        sc.step(1)
+        it, _ = sc.sync()
+        if tol == 0.0:
+            assert it == osc.last_iterations, step
+    x, _ = sc.state()
+    xo, _ = osc.state()
+    if tol == 0.0:
+        assert np.array_equal(x, xo), np.abs(x - xo).max()
+    else:
+        assert cases.rel_err(x, xo) <= tol

@@ -160,3 +160,24 @@ def test_plasticity_scene_file_against_oracle(capi, oracle):
     xo, xe = runs
     assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
     assert np.max(np.abs(xe - xo)) > 1e-3 * np.max(np.abs(xo - pos))  # plasticity changed the motion
+
+
+def test_cg_warm_start_scene_file_against_oracle(capi, oracle):
+    """The known-answer grid scene with CGLinearSolver warmStart="1": 30 steps
+    against the oracle with warm starts."""
+    text = _read("grid_fem_4x10x4.scn").replace(
+        '<CGLinearSolver iterations="20" tolerance="1e-5" threshold="1e-6" />',
+        '<CGLinearSolver iterations="20" tolerance="1e-5" threshold="1e-6" warmStart="1" />')
+    s = capi.SofaScene(text)
+    s.animate(30)
+    x = s.positions(0)
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+    osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01, cg_iterations=20,
+                             cg_tolerance=1e-5, cg_threshold=1e-6)
+    osc.set_warm_start(True)
+    osc.step(30)
+    xo, _ = osc.state()
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
