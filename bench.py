@@ -55,6 +55,10 @@ def parse():
                     help="profiling run: build the mixed scene, run warm-up + steps, print a short line")
     ap.add_argument("--profile-batched", action="store_true",
                     help="profiling run of the batched workload alone: admission, warm-up + steps, a short line")
+    ap.add_argument("--profile-pcg", action="store_true",
+                    help="profiling run of mixed Jacobi-PCG on the stiff-inclusion block: warm-up + steps of "
+                         "--pcg-iterations iterations, a short line")
+    ap.add_argument("--pcg-iterations", type=int, default=100)
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-beam batched workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--no-ill-conditioned", action="store_true", help="skip the stiff-inclusion workload")
@@ -514,6 +518,20 @@ def main():
         b.step(args.warmup + args.steps)
         b.sync()
         print(json.dumps({"profile_run": True, "batched": b.info()}))
+        return 0
+    if args.profile_pcg:
+        from sofa_gb300 import topology as topo
+
+        ib = topo.inclusion_beam(ILL["n"], seed=ILL["seed"], young_out=ILL["young_out"], young_in=ILL["young_in"])
+        m = ib.mesh
+        fem = capi.TetrahedronFEM(m.positions, m.tetrahedra, ib.young, ILL["poisson"], ILL["method"], "mixed")
+        sc = capi.Scene(fem, dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=args.pcg_iterations,
+                        cg_tolerance=1e-20, cg_threshold=1e-20, gravity=(0.0, -9.81, 0.0),
+                        vertex_mass=1.0 / m.n_nodes, fixed=m.fixed, linear_solver="pcg", preconditioner="jacobi")
+        sc.set_external_force(ib.tip_force)
+        sc.step(args.warmup + args.steps)
+        it, res = sc.sync()
+        print(json.dumps({"profile_run": True, "pcg": {"n_tets": m.n_tets, "iterations": it, "r.z/b.b": res}}))
         return 0
     mesh = make_mesh(cfg)
     E, N = mesh.n_tets, mesh.n_nodes
