@@ -36,9 +36,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-CONFIG = dict(n=(64, 64, 257), spacing=0.5, jitter=0.05, seed=0, young=5000.0, poisson=0.45, method="polar",
-              dt=0.01, rs=0.1, rm=0.1, cg_iterations=50, cg_tolerance=1e-7, cg_threshold=1e-9, total_mass=1.0,
-              gravity=(0.0, -9.81, 0.0))
+from sofa_gb300 import workloads as wl  # noqa: E402
+
+CONFIG = wl.SINGLE_BEAM
 
 
 def parse():
@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--n", default=None, help="override node grid, e.g. 32,32,129")
     ap.add_argument("--error-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-single-thread", action="store_true", help="skip the single-thread CPU baseline step")
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: build the mixed scene, run warm-up + steps, print a short line")
@@ -64,6 +65,7 @@ def parse():
     ap.add_argument("--no-ill-conditioned", action="store_true", help="skip the stiff-inclusion workload")
     ap.add_argument("--ill-steps", type=int, default=50)
     ap.add_argument("--beams", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=50, help="timed steps of the batched workload")
     ap.add_argument("--requests", type=int, default=150, help="requests per arrival rate in the serving sample")
     return ap.parse_args()
 
@@ -138,17 +140,12 @@ def peaks():
 
 
 def make_mesh(cfg):
-    from sofa_gb300 import topology as topo
-
-    return topo.beam(cfg["n"], spacing=cfg["spacing"], jitter=cfg["jitter"], seed=cfg["seed"], split=5)
+    return wl.single_beam_mesh(cfg)
 
 
-def make_scene(capi, mesh, cfg, precision):
+def make_scene(capi, mesh, cfg, precision, **extra):
     fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, cfg["young"], cfg["poisson"], cfg["method"], precision)
-    return capi.Scene(fem, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"], rayleigh_mass=cfg["rm"],
-                      cg_iterations=cfg["cg_iterations"], cg_tolerance=cfg["cg_tolerance"],
-                      cg_threshold=cfg["cg_threshold"], gravity=cfg["gravity"],
-                      vertex_mass=cfg["total_mass"] / mesh.n_nodes, fixed=mesh.fixed)
+    return capi.Scene(fem, **wl.single_beam_solver(cfg, mesh), **extra)
 
 
 def replica_barrier(torch, world):
@@ -240,40 +237,27 @@ def e2e_steps(torch, capi, scene, mesh, steps):
     return t1 - t0, xh.nbytes + vh.nbytes, xo.nbytes
 
 
-def beam_population(n, seed):
-    """Beams of the batched/serving workloads: node counts log-uniform in
-    [1e3, 2e5], aspect z:x uniform in [2, 8], youngModulus log-uniform in
-    [1e3, 1e5], poissonRatio uniform in [0.3, 0.49], method large or polar at
-    50/50; dt 0.01, Rayleigh 0.1/0.1, CG 25 iterations with the reference's
-    default tolerance and threshold (1e-5), total mass 1, z = 0 fixed."""
-    from sofa_gb300 import topology as topo
-
-    rng = np.random.default_rng(seed)
-    out = []
-    for i in range(n):
-        nn = 10 ** rng.uniform(3.0, np.log10(2e5))
-        dims = topo.beam_dims(nn, rng.uniform(2.0, 8.0))
-        kw = dict(young=float(10 ** rng.uniform(3, 5)), poisson=float(rng.uniform(0.3, 0.49)),
-                  method="large" if rng.random() < 0.5 else "polar")
-        mesh = topo.beam(dims, 0.5, 0.05, seed * 100003 + i)
-        kw.update(dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=25, cg_tolerance=1e-5,
-                  cg_threshold=1e-5, total_mass=1.0, fixed=mesh.fixed)
-        out.append((mesh, kw))
-    return out
+def beam_population(n, seed, members=None):
+    return wl.beam_population(n, seed, members)
 
 
 def run_batched(torch, capi, args, plain_best):
+    """The batched workload: 256 beams of the population in one batch, mixed
+    precision, warm-up steps then BATCH_STEPS timed steps (CUDA events on the
+    batch stream). Every beam's positions after all those steps are compared
+    with the same beams batched in FP64 (FMA)."""
     beams = beam_population(args.beams, seed=3)
     tets = sum(m.n_tets for m, _ in beams)
     nodes = sum(m.n_nodes for m, _ in beams)
+    threads = min(16, host_threads())
     b = capi.Batch("mixed", budget_bytes=int(60e9), max_meshes=args.beams + 8, max_cg_iterations=25)
     t0 = time.perf_counter()
-    b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=min(16, host_threads()))
+    slots = b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=threads)
     admit_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(b.stream)
     b.step(args.warmup)
     b.sync()
-    k = max(2, min(args.steps, 10))
+    k = args.batch_steps
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -282,31 +266,34 @@ def run_batched(torch, capi, args, plain_best):
     e1.synchronize()
     t = e0.elapsed_time(e1) / 1e3
     info = b.info()
+    tuning = b.tuning()
+    xm = [b.state(s_)[0] for s_ in slots]
+    its_m = [b.stats(s_)[0] for s_ in slots]
     b.close()
     value = tets * k / t
-    # position error of mixed vs FP64 (FMA) after 100 steps on a subset
-    sub = beams[:: max(1, len(beams) // 8)][:8]
+    # every beam against the FP64 (FMA) batch after the same number of steps
+    bb = capi.Batch("fp64_fma", budget_bytes=int(60e9), max_meshes=args.beams + 8, max_cg_iterations=25)
+    slots64 = bb.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=threads)
+    bb.step(args.warmup + k)
+    x64 = [bb.state(s_)[0] for s_ in slots64]
+    its_64 = [bb.stats(s_)[0] for s_ in slots64]
+    bb.close()
     errs, derrs = [], []
-    for prec in ("mixed", "fp64_fma"):
-        bb = capi.Batch(prec, budget_bytes=int(20e9), max_meshes=len(sub) + 1, max_cg_iterations=25)
-        slots = bb.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in sub], threads=min(16, host_threads()))
-        bb.step(100)
-        res = [bb.state(s_)[0] for s_ in slots]
-        bb.close()
-        if prec == "mixed":
-            xm = res
-        else:
-            for (m, _), a, r in zip(sub, xm, res):
-                errs.append(float(np.linalg.norm(a - r) / np.linalg.norm(r)))
-                d = np.linalg.norm(r - m.positions)
-                derrs.append(float(np.linalg.norm(a - r) / d) if d > 0 else 0.0)
+    for (m, _), a, r in zip(beams, xm, x64):
+        errs.append(float(np.linalg.norm(a - r) / np.linalg.norm(r)))
+        d = np.linalg.norm(r - m.positions)
+        derrs.append(float(np.linalg.norm(a - r) / d) if d > 0 else 0.0)
     return {"workload": f"{len(beams)} beams, {nodes} nodes, {tets} tets, mixed precision, one launch per phase, "
                         "CUDA-graph steps", "tet_steps_per_s": value, "ms_per_step": t / k * 1e3, "steps": k,
-            "admission_s": admit_s, "budget_used_bytes": info["budget_used"],
+            "admission_s": admit_s, "budget_used_bytes": info["budget_used"], "tiles": tuning,
             "speedup_vs_plain_fp64_single_mesh": value / plain_best,
-            "position_error_100_steps": {"beams_checked": len(sub), "rel_l2_position_max": max(errs),
-                                        "rel_l2_displacement_max": max(derrs),
-                                        "reference": "the same beams batched in FP64 (FMA)"}}
+            "position_error": {"steps": args.warmup + k, "beams_checked": len(beams),
+                               "rel_l2_position_max": max(errs), "rel_l2_position_median": float(np.median(errs)),
+                               "rel_l2_displacement_max": max(derrs),
+                               "rel_l2_displacement_median": float(np.median(derrs)),
+                               "beams_with_other_cg_iteration_count_last_step":
+                                   int(sum(a != c for a, c in zip(its_m, its_64))),
+                               "reference": "the same beams batched in FP64 (FMA)"}}
 
 
 def run_serving(torch, capi, args, plain_best):
@@ -366,8 +353,7 @@ def run_serving(torch, capi, args, plain_best):
             "speedup_vs_plain_fp64_single_mesh": best / plain_best}
 
 
-ILL = dict(n=(48, 48, 193), young_out=1e3, young_in=1e6, poisson=0.49, method="polar", cg_iterations=200,
-           cg_tolerance=1e-10, replace_every=20, seed=0)
+ILL = wl.INCLUSION
 
 
 def run_ill_conditioned(torch, capi, args):
@@ -425,19 +411,76 @@ def run_ill_conditioned(torch, capi, args):
             "mixed_plain": arm(xm, tm, im, rm)}
 
 
-def cpu_baseline(mesh, cfg, threads, steps=1):
+def oracle_scene(pyoracle, fem, mesh, cfg):
+    return pyoracle.OracleScene(fem, vertex_mass=cfg["total_mass"] / mesh.n_nodes, gravity=cfg["gravity"],
+                                fixed=mesh.fixed, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"],
+                                rayleigh_mass=cfg["rm"], cg_iterations=cfg["cg_iterations"],
+                                cg_tolerance=cfg["cg_tolerance"], cg_threshold=cfg["cg_threshold"])
+
+
+def cpu_baseline_leg(capi, mesh, cfg, threads, parity_steps=3, single_thread=True):
+    """The CPU baseline: the oracle (an FP64 restatement of the reference's
+    CPU path) timed on the host cores, one full step with `threads` threads
+    (thread-local force buffers, as the MultiThreading plugin) and one with a
+    single thread (the reference's serial loops). The same oracle, run
+    `parity_steps` steps in its exact parallel mode (bit-identical to one
+    thread), is the checker of the GPU arms on this workload: FP64 reference
+    rounding with serial dots must be bit-identical; FP64-FMA and mixed are
+    reported on both norms."""
     from oracle import pyoracle
 
-    pyoracle.set_threads(threads)
-    fem = pyoracle.OracleFEM(mesh.positions, mesh.tetrahedra, cfg["young"], cfg["poisson"], cfg["method"])
-    sc = pyoracle.OracleScene(fem, vertex_mass=cfg["total_mass"] / mesh.n_nodes, gravity=cfg["gravity"],
-                              fixed=mesh.fixed, dt=cfg["dt"], rayleigh_stiffness=cfg["rs"],
-                              rayleigh_mass=cfg["rm"], cg_iterations=cfg["cg_iterations"],
-                              cg_tolerance=cfg["cg_tolerance"], cg_threshold=cfg["cg_threshold"])
+    pyoracle.build()
+    ofem = pyoracle.OracleFEM(mesh.positions, mesh.tetrahedra, cfg["young"], cfg["poisson"], cfg["method"])
+    pyoracle.set_threads(threads, exact=True)
+    sc = oracle_scene(pyoracle, ofem, mesh, cfg)
     t0 = time.perf_counter()
-    sc.step(steps)
-    dt = time.perf_counter() - t0
-    return mesh.n_tets * steps / dt, dt
+    sc.step(parity_steps)
+    t_exact = time.perf_counter() - t0
+    xr, vr = sc.state()
+    it_ref = sc.last_iterations
+    del sc
+    pyoracle.set_threads(threads)
+    sc = oracle_scene(pyoracle, ofem, mesh, cfg)
+    t0 = time.perf_counter()
+    sc.step(1)
+    t_mt = time.perf_counter() - t0
+    del sc
+    t_1 = None
+    if single_thread:
+        pyoracle.set_threads(1)
+        sc = oracle_scene(pyoracle, ofem, mesh, cfg)
+        t0 = time.perf_counter()
+        sc.step(1)
+        t_1 = time.perf_counter() - t0
+        del sc
+    pyoracle.set_threads(1)
+    del ofem
+    E = mesh.n_tets
+    base = {"value": E / t_mt, "unit": "tet-steps/s", "cores": threads, "kind": "port",
+            "sample": f"1 full step of the workload ({E} tets, CG {cfg['cg_iterations']}), FP64 CPU oracle with "
+                      f"{threads} threads and thread-local force buffers, {t_mt:.1f} s"}
+    if t_1 is not None:
+        base["single_thread"] = {"value": E / t_1, "unit": "tet-steps/s", "cores": 1,
+                                 "sample": f"1 full step, one thread (the reference's serial loops), {t_1:.1f} s"}
+    # the GPU arms against the oracle's trajectory
+    d = np.linalg.norm(xr - mesh.positions)
+    parity = {"steps": parity_steps, "checker": f"CPU oracle, exact parallel mode on {threads} threads "
+                                                f"({t_exact:.1f} s), bit-identical to one thread"}
+    for prec, extra in (("fp64", dict(serial_dots=True)), ("fp64_fma", {}), ("mixed", {})):
+        g = make_scene(capi, mesh, cfg, prec, **extra)
+        g.step(parity_steps)
+        it, _ = g.sync()
+        x, v = g.state()
+        g.close()
+        arm = {"rel_l2_position": float(np.linalg.norm(x - xr) / np.linalg.norm(xr)),
+               "rel_l2_displacement": float(np.linalg.norm(x - xr) / d) if d > 0 else None,
+               "cg_iterations_equal": bool(it == it_ref)}
+        if prec == "fp64":
+            arm["bit_identical"] = bool(np.array_equal(x, xr) and np.array_equal(v, vr))
+            parity["fp64_reference_rounding_serial_dots"] = arm
+        else:
+            parity[prec] = arm
+    return base, parity
 
 
 def host_threads():
@@ -575,29 +618,41 @@ def main():
         plain[prec] = {"tet_steps_per_s": E * k / t, "ms_per_step": t / k * 1e3}
         sc.close()
 
-    # position error of mixed vs FP64 after error-steps steps
+    # position error of mixed vs FP64 after error-steps steps, and along the
+    # way: the GPU FP64 reference-rounding run is the reference, the FP64-FMA
+    # run against it shows how far two FP64 roundings drift on this workload
     err = None
     if not args.no_error and rank == 0:
-        ref = make_scene(capi, mesh, cfg, "fp64_fma")
-        ref.step(args.error_steps)
-        xr, _ = ref.state()
-        ref.close()
-        mx = make_scene(capi, mesh, cfg, "mixed")
-        mx.step(args.error_steps)
-        xm, _ = mx.state()
-        mx.close()
-        d = np.linalg.norm(xr - mesh.positions)
-        err = {"steps": args.error_steps, "rel_l2_position": float(np.linalg.norm(xm - xr) / np.linalg.norm(xr)),
-               "rel_l2_displacement": float(np.linalg.norm(xm - xr) / d) if d > 0 else None,
-               "target_uses": "rel_l2_position", "reference": "GPU FP64 (FMA) run of the same workload"}
+        marks = sorted({1, 20, args.error_steps})
+        runs = {}
+        for prec in ("fp64", "fp64_fma", "mixed"):
+            sc_ = make_scene(capi, mesh, cfg, prec)
+            done, xs_ = 0, {}
+            for mk in marks:
+                sc_.step(mk - done)
+                done = mk
+                xs_[mk] = sc_.state()[0]
+            sc_.close()
+            runs[prec] = xs_
+
+        def norms(a, b):
+            d_ = np.linalg.norm(b - mesh.positions)
+            return {"rel_l2_position": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                    "rel_l2_displacement": float(np.linalg.norm(a - b) / d_) if d_ > 0 else None}
+
+        last = args.error_steps
+        err = dict(steps=last, **norms(runs["mixed"][last], runs["fp64"][last]), target_uses="rel_l2_position",
+                   reference="GPU FP64 run of the same workload in the reference's rounding (no FMA)")
+        err["by_step"] = {str(mk): {"mixed_vs_fp64": norms(runs["mixed"][mk], runs["fp64"][mk]),
+                                    "fp64_fma_vs_fp64": norms(runs["fp64_fma"][mk], runs["fp64"][mk])}
+                          for mk in marks}
+        del runs
 
     cpu = None
+    oracle_parity = None
     if not args.no_cpu_baseline and rank == 0:
-        threads = host_threads()
-        v, dt = cpu_baseline(mesh, cfg, threads, steps=1)
-        cpu = {"value": v, "unit": "tet-steps/s", "cores": threads, "kind": "port",
-               "sample": f"1 full step of the workload ({E} tets, CG {cfg['cg_iterations']}), FP64 CPU oracle "
-                         f"with {threads} threads, {dt:.1f} s"}
+        cpu, oracle_parity = cpu_baseline_leg(capi, mesh, cfg, host_threads(),
+                                              single_thread=not args.no_single_thread)
 
     plain_best = max(p["tet_steps_per_s"] for p in plain.values())
     batched = None
@@ -636,6 +691,7 @@ def main():
         "batched": batched,
         "serving": serving,
         "position_error": err,
+        "oracle_parity": oracle_parity,
         "ill_conditioned": ill,
         "roofline": {"kernel": "addDForce (element + gather kernels, mixed)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,

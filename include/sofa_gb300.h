@@ -175,7 +175,10 @@ int sgb_tfem_info(const sgb_tfem_t* fem, int* n_nodes, int* n_tets, int* method,
  * calls that overlap on the GPU (unordered streams) race and give wrong
  * results; order them on one stream. The first call on a device looks up
  * the array's device address once for that device; make that first call
- * before any stream capture. This entry point has no counterpart in the
+ * before any stream capture, and make no call after a cudaDeviceReset in
+ * the same process (the array may move). Out-of-range node or slot indices
+ * are skipped by the kernels (no access outside the arrays; df is then
+ * wrong for the nodes concerned). This entry point has no counterpart in the
  * reference: it is a variant of sgb_tfem_add_dforce_f32 for such callers.
  * Computes df -= kfactor R K R^T dx per tetrahedron, FP32, with arrays:
  *   tetrahedra_dev        4 int32 per tetrahedron (node indices < n_nodes), 16-byte aligned
@@ -339,7 +342,12 @@ typedef struct sgb_mesh_desc {
 int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, int max_meshes,
                      int max_cg_iterations);
 int sgb_batch_destroy(sgb_batch_t* batch);
-/* Bytes a mesh would take in the budget (host-side planning only). */
+/* Bytes a mesh would take in the budget (host-side planning only; with
+ * batch NULL, for a mixed-precision batch with the default patch size).
+ * Runs the admission checks: the batch engine runs cold-start
+ * CGLinearSolver with block-ordered dot products, so a mesh whose params
+ * ask for PCG, a preconditioner, warmStart, residual replacement or serial
+ * dots is refused with SGB_ERR_NOT_SUPPORTED, here and at admission. */
 int sgb_batch_mesh_bytes(const sgb_batch_t* batch, const sgb_mesh_desc* mesh, size_t* bytes);
 /* Admission: SGB_ERR_BUDGET when the mesh does not fit or no slot is free.
  * Synchronous; positions start at rest, velocities at zero. */

@@ -53,6 +53,7 @@ def _load():
     lib.orc_polar_stable.restype = ctypes.c_int
     lib.orc_polar_stable.argtypes = [_dp, _dp]
     lib.orc_set_threads.argtypes = [ctypes.c_int]
+    lib.orc_set_exact_parallel.argtypes = [ctypes.c_int]
     lib.orc_get_threads.restype = ctypes.c_int
     lib.orc_scene_create.restype = vp
     lib.orc_scene_create.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp, _ip, ctypes.c_int,
@@ -86,8 +87,15 @@ def _i(a):
     return a, a.ctypes.data_as(_ip)
 
 
-def set_threads(n):
-    _load().orc_set_threads(int(n))
+def set_threads(n, exact=False):
+    """Threads of the oracle's element loops and vector operations. exact:
+    element terms gathered per node in element order, bit-identical to one
+    thread (the parity checker for large meshes); otherwise thread-local
+    force buffers merged after the loop, as the MultiThreading plugin does
+    (the CPU timing baseline)."""
+    lib = _load()
+    lib.orc_set_threads(int(n))
+    lib.orc_set_exact_parallel(1 if exact else 0)
 
 
 def polar(M):
@@ -284,10 +292,12 @@ class OracleScene:
 
 def ref_math_lib():
     """The reference's own polar decomposition, compiled from the reference
-    sources by oracle/ref/Makefile (only where the reference tree exists)."""
+    sources by oracle/ref/Makefile. The reference tree is named by the
+    SOFA_REFERENCE_ROOT environment variable; without it (or without the
+    tree) this returns None unless the library was built before."""
     if not os.path.exists(_REF_LIB):
-        ref = os.environ.get("SOFA_REFERENCE_ROOT", "/root/reference")
-        if not os.path.isdir(ref):
+        ref = os.environ.get("SOFA_REFERENCE_ROOT", "")
+        if not ref or not os.path.isdir(ref):
             return None
         try:
             subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref"), f"REF={ref}"], check=True)

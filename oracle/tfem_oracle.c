@@ -33,7 +33,14 @@
  * after the element loop, applications/plugins/MultiThreading/src/
  * MultiThreading/component/solidmechanics/fem/elastic/
  * ParallelTetrahedronFEMForceField.inl:53-124); its sums are reordered, so it
- * is used for timing, not as the parity reference.
+ * is used for timing, not as the parity reference. The exact parallel mode
+ * (orc_set_exact_parallel(1) with orc_set_threads > 1) computes each
+ * element's corner terms in parallel into a per-element buffer and then lets
+ * every node add its terms in element order, which is the serial loop's
+ * order: its results are bit-identical to one thread, so it checks large
+ * meshes. In both modes the element-wise vector operations of the solver run
+ * in parallel (they have no reductions, so their bits do not change) and the
+ * dot products stay serial, as MechanicalObject::vDot computes them.
  */
 #include <float.h>
 #include <math.h>
@@ -513,9 +520,11 @@ static void compute_force(double F[12], const double D[12], const double K3[3], 
 /* ------------------------------------------------------------------------- */
 
 static int g_threads = 1;
+static int g_exact = 0;
 
 void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
 int orc_get_threads(void) { return g_threads; }
+void orc_set_exact_parallel(int on) { g_exact = on ? 1 : 0; }
 
 typedef void (*orc_task_fn)(void* ctx, int tid, int nthreads);
 typedef struct {
@@ -580,6 +589,9 @@ typedef struct orc_fem {
     orc_plastic pl;
     double* tl_buf;    /* thread-local force buffers for the threaded mode */
     int tl_threads;
+    double* ebuf;      /* exact parallel mode: 12 corner terms per element */
+    int32_t* nrow;     /* exact parallel mode: node -> (element*4 + corner) CSR, */
+    int32_t* nslot;    /* rows in increasing order */
 } orc_fem;
 
 /* BaseLinearElasticityFEMForceField::getVecRealInElement
@@ -690,12 +702,16 @@ void orc_fem_destroy(orc_fem* m)
     free(m->plastic);
     free(m->lame);
     free(m->tl_buf);
+    free(m->ebuf);
+    free(m->nrow);
+    free(m->nslot);
     free(m);
 }
 
-/* Element e's contribution to addForce, added into f (TFEM.inl:534-623 small,
- * :870-986 large, :1025-1079 polar). Also stores rotations[e]. */
-static void element_force(orc_fem* m, int e, const double* p, double* f)
+/* Element e's contribution to addForce (TFEM.inl:534-623 small, :870-986
+ * large, :1025-1079 polar): out[3i+k] is what the element adds to f at its
+ * node i. Also stores rotations[e]. */
+static void element_force_terms(orc_fem* m, int e, const double* p, double out[12])
 {
     const int32_t* t = &m->tets[4 * e];
     const double* K3 = &m->K3[3 * e];
@@ -710,8 +726,7 @@ static void element_force(orc_fem* m, int e, const double* p, double* f)
             for (int k = 0; k < 3; ++k)
                 D[3 * i + k] = ip[3 * t[i] + k] - ip[3 * a + k] - p[3 * t[i] + k] + p[3 * a + k];
         compute_force_pl(F, D, K3, J3, 0, 0.0, m->plastic ? &m->plastic[6 * e] : NULL, &m->pl);
-        for (int i = 0; i < 4; ++i)
-            for (int k = 0; k < 3; ++k) f[3 * t[i] + k] += F[3 * i + k];
+        memcpy(out, F, sizeof(double) * 12);
         return;
     }
     double R[9], def[12];
@@ -760,18 +775,24 @@ static void element_force(orc_fem* m, int e, const double* p, double* f)
         for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
     }
     compute_force_pl(F, D, K3, J3, 0, 0.0, m->plastic ? &m->plastic[6 * e] : NULL, &m->pl);
-    for (int i = 0; i < 4; ++i) {
-        double r3[3];
-        mat_vec(rot, &F[3 * i], r3);
-        f[3 * t[i] + 0] += r3[0];
-        f[3 * t[i] + 1] += r3[1];
-        f[3 * t[i] + 2] += r3[2];
-    }
+    for (int i = 0; i < 4; ++i) mat_vec(rot, &F[3 * i], &out[3 * i]);
+}
+
+/* f += element e's addForce terms, node by node in corner order */
+static void element_force(orc_fem* m, int e, const double* p, double* f)
+{
+    const int32_t* t = &m->tets[4 * e];
+    double c[12];
+    element_force_terms(m, e, p, c);
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 3; ++k) f[3 * t[i] + k] += c[3 * i + k];
 }
 
 /* applyStiffnessSmall / applyStiffnessCorotational (TFEM.inl:721-749,
- * 1193-1237): df -= R K (R^T dx) * fact for element e. */
-static void element_dforce(const orc_fem* m, int e, const double* x, double* df, double fact)
+ * 1193-1237): R K (R^T dx) * fact for element e; out[3i+k] is what the
+ * element subtracts from df at its node i (df += -F for small is the same
+ * operation: x + (-y) and x - y round alike). */
+static void element_dforce_terms(const orc_fem* m, int e, const double* x, double fact, double out[12])
 {
     const int32_t* t = &m->tets[4 * e];
     const double* K3 = &m->K3[3 * e];
@@ -781,8 +802,7 @@ static void element_dforce(const orc_fem* m, int e, const double* x, double* df,
         for (int i = 0; i < 4; ++i)
             for (int k = 0; k < 3; ++k) X[3 * i + k] = x[3 * t[i] + k];
         compute_force(F, X, K3, J3, 1, fact);
-        for (int i = 0; i < 4; ++i)
-            for (int k = 0; k < 3; ++k) df[3 * t[i] + k] += -F[3 * i + k];
+        memcpy(out, F, sizeof(double) * 12);
         return;
     }
     const double* r = &m->rot[9 * e]; /* rotations[i] = R^T */
@@ -791,11 +811,19 @@ static void element_dforce(const orc_fem* m, int e, const double* x, double* df,
         for (int k = 0; k < 3; ++k) X[3 * i + k] = r[0 * 3 + k] * xi[0] + r[1 * 3 + k] * xi[1] + r[2 * 3 + k] * xi[2];
     }
     compute_force(F, X, K3, J3, 1, fact);
-    for (int i = 0; i < 4; ++i) {
-        double* fi = &df[3 * t[i]];
+    for (int i = 0; i < 4; ++i)
         for (int k = 0; k < 3; ++k)
-            fi[k] -= r[k * 3 + 0] * F[3 * i + 0] + r[k * 3 + 1] * F[3 * i + 1] + r[k * 3 + 2] * F[3 * i + 2];
-    }
+            out[3 * i + k] = r[k * 3 + 0] * F[3 * i + 0] + r[k * 3 + 1] * F[3 * i + 1] + r[k * 3 + 2] * F[3 * i + 2];
+}
+
+/* df -= element e's addDForce terms, node by node in corner order */
+static void element_dforce(const orc_fem* m, int e, const double* x, double* df, double fact)
+{
+    const int32_t* t = &m->tets[4 * e];
+    double c[12];
+    element_dforce_terms(m, e, x, fact, c);
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 3; ++k) df[3 * t[i] + k] -= c[3 * i + k];
 }
 
 typedef struct {
@@ -853,9 +881,77 @@ static void fem_threaded(orc_fem* m, const double* in, double* out, double fact,
     parallel_run(merge_job_run, &mj, nt);
 }
 
+/* Exact parallel mode: element terms into ebuf (parallel over elements),
+ * then each node adds or subtracts its terms in increasing (element, corner)
+ * order (parallel over nodes) -- the serial element loop's order for every
+ * node, so the sums are bit-identical to one thread. */
+typedef struct {
+    orc_fem* m;
+    const double* in;
+    double* out;
+    double fact;
+    int dforce;
+} exact_job;
+
+static void exact_elem_run(void* ctx, int tid, int n)
+{
+    exact_job* j = (exact_job*)ctx;
+    long b, e;
+    chunk(j->m->n_tets, tid, n, &b, &e);
+    for (long i = b; i < e; ++i) {
+        if (j->dforce)
+            element_dforce_terms(j->m, (int)i, j->in, j->fact, &j->m->ebuf[12 * (size_t)i]);
+        else
+            element_force_terms(j->m, (int)i, j->in, &j->m->ebuf[12 * (size_t)i]);
+    }
+}
+
+static void exact_node_run(void* ctx, int tid, int n)
+{
+    exact_job* j = (exact_job*)ctx;
+    const orc_fem* m = j->m;
+    long b, e;
+    chunk(m->n_nodes, tid, n, &b, &e);
+    for (long v = b; v < e; ++v) {
+        double* o = &j->out[3 * (size_t)v];
+        for (int32_t s = m->nrow[v]; s < m->nrow[v + 1]; ++s) {
+            const double* c = &m->ebuf[3 * (size_t)m->nslot[s]];
+            for (int k = 0; k < 3; ++k) {
+                if (j->dforce)
+                    o[k] -= c[k];
+                else
+                    o[k] += c[k];
+            }
+        }
+    }
+}
+
+static void fem_exact(orc_fem* m, const double* in, double* out, double fact, int dforce)
+{
+    if (!m->ebuf) {
+        const size_t E = (size_t)m->n_tets, N = (size_t)m->n_nodes;
+        m->ebuf = (double*)malloc(sizeof(double) * 12 * E + 1);
+        m->nrow = (int32_t*)calloc(N + 1, sizeof(int32_t));
+        m->nslot = (int32_t*)malloc(sizeof(int32_t) * 4 * E + 1);
+        for (size_t s = 0; s < 4 * E; ++s) m->nrow[m->tets[s] + 1]++;
+        for (size_t v = 0; v < N; ++v) m->nrow[v + 1] += m->nrow[v];
+        int32_t* fill = (int32_t*)malloc(sizeof(int32_t) * (N + 1));
+        memcpy(fill, m->nrow, sizeof(int32_t) * (N + 1));
+        for (size_t s = 0; s < 4 * E; ++s) m->nslot[fill[m->tets[s]]++] = (int32_t)s;
+        free(fill);
+    }
+    exact_job j = {m, in, out, fact, dforce};
+    parallel_run(exact_elem_run, &j, g_threads);
+    parallel_run(exact_node_run, &j, g_threads);
+}
+
 /* addForce (TFEM.inl:1548-1604): f += internal forces at positions x. */
 void orc_fem_add_force(orc_fem* m, const double* x, double* f)
 {
+    if (g_threads > 1 && g_exact) {
+        fem_exact(m, x, f, 0.0, 0);
+        return;
+    }
     if (g_threads > 1) {
         fem_threaded(m, x, f, 0.0, 0);
         return;
@@ -866,6 +962,10 @@ void orc_fem_add_force(orc_fem* m, const double* x, double* f)
 /* addDForce (TFEM.inl:1606-1636): df += -kFactor K dx. */
 void orc_fem_add_dforce(orc_fem* m, const double* dx, double* df, double kfactor)
 {
+    if (g_threads > 1 && g_exact) {
+        fem_exact(m, dx, df, kfactor, 1);
+        return;
+    }
     if (g_threads > 1) {
         fem_threaded(m, dx, df, kfactor, 1);
         return;
@@ -1182,6 +1282,72 @@ void orc_scene_set_springs(orc_scene* s, double k, const double* anchor)
 int orc_scene_last_iterations(const orc_scene* s) { return s->last_iters; }
 double orc_scene_last_error(const orc_scene* s) { return s->last_err; }
 
+/* Element-wise vector operations (MechanicalObject::vOp,
+ * MechanicalObject.inl:1999-2205), split over the threads for long vectors:
+ * each entry is computed by the same expression whatever the split. */
+enum { VOP_COPY, VOP_ZERO, VOP_AVF, VOP_INC, VOP_INTEGRATE };
+typedef struct {
+    int kind;
+    double* out;
+    const double* a;
+    double* x; /* VOP_INTEGRATE: positions (out = v, a = dv) */
+    double f;
+    long n3;
+} vop_job;
+
+static void vop_range(const vop_job* j, long b, long e)
+{
+    double* out = j->out;
+    const double* a = j->a;
+    const double f = j->f;
+    switch (j->kind) {
+    case VOP_COPY:
+        memcpy(out + b, a + b, sizeof(double) * (size_t)(e - b));
+        break;
+    case VOP_ZERO:
+        memset(out + b, 0, sizeof(double) * (size_t)(e - b));
+        break;
+    case VOP_AVF: /* out = out * f + a (f == 1: out += a) */
+        if (f == 1.0)
+            for (long i = b; i < e; ++i) out[i] += a[i];
+        else
+            for (long i = b; i < e; ++i) {
+                out[i] *= f;
+                out[i] += a[i];
+            }
+        break;
+    case VOP_INC: /* out += a * f (f == 1: out += a) */
+        if (f == 1.0)
+            for (long i = b; i < e; ++i) out[i] += a[i];
+        else
+            for (long i = b; i < e; ++i) out[i] += a[i] * f;
+        break;
+    case VOP_INTEGRATE: /* v += dv; x += v h */
+        for (long i = b; i < e; ++i) {
+            out[i] += a[i];
+            j->x[i] += out[i] * f;
+        }
+        break;
+    }
+}
+
+static void vop_job_run(void* ctx, int tid, int n)
+{
+    const vop_job* j = (const vop_job*)ctx;
+    long b, e;
+    chunk(j->n3, tid, n, &b, &e);
+    vop_range(j, b, e);
+}
+
+static void vop_run(int kind, double* out, const double* a, double f, long n3, double* x)
+{
+    vop_job j = {kind, out, a, x, f, n3};
+    if (g_threads > 1 && n3 >= (1L << 17))
+        parallel_run(vop_job_run, &j, g_threads);
+    else
+        vop_range(&j, 0, n3);
+}
+
 /* UniformMass::addForce (UniformMass.inl:471-496) / DiagonalMass::addForce
  * (DiagonalMass.inl:1393-1413): f += m g. */
 static void mass_add_force(const orc_scene* s, double* f)
@@ -1203,7 +1369,7 @@ static void mass_add_mdx(const orc_scene* s, double* res, const double* dx, doub
     if (s->mass_kind == 0) {
         double m = s->vertex_mass;
         if (factor != 1.0) m *= factor;
-        for (long i = 0; i < 3L * s->n; ++i) res[i] += dx[i] * m;
+        vop_run(VOP_INC, res, dx, m, 3L * s->n, NULL);
     } else if (factor == 1.0) {
         for (int i = 0; i < s->n; ++i)
             for (int k = 0; k < 3; ++k) res[3 * i + k] += dx[3 * i + k] * s->node_mass[i];
@@ -1267,7 +1433,7 @@ static void add_mbkdx(orc_scene* s, double* df, const double* dx, double mf, dou
  * q = (mF M + kF K) p, then projected. */
 static void matvec(orc_scene* s, double* q, const double* p, double mf, double kf)
 {
-    memset(q, 0, sizeof(double) * 3 * (size_t)s->n);
+    vop_run(VOP_ZERO, q, NULL, 0.0, 3L * s->n, NULL);
     add_mbkdx(s, q, p, mf, kf);
     project_response(s, q);
 }
@@ -1287,8 +1453,8 @@ static void cg_solve(orc_scene* s, double mf, double kf)
         matvec(s, r, x, mf, kf);
         vop_avf(r, b, -1.0, n3);
     } else {
-        memset(x, 0, sizeof(double) * (size_t)n3);
-        memcpy(r, b, sizeof(double) * (size_t)n3);
+        vop_run(VOP_ZERO, x, NULL, 0.0, n3, NULL);
+        vop_run(VOP_COPY, r, b, 0.0, n3, NULL);
     }
     const double normb = sqrt(vdot(b, b, n));
     int nb_iter = 0, n_matvec = 0;
@@ -1302,17 +1468,11 @@ static void cg_solve(orc_scene* s, double mf, double kf)
                 if (!(nb_iter == 1 && s->time_step_count == 0)) break;
             }
             if (nb_iter == 1) {
-                memcpy(p, r, sizeof(double) * (size_t)n3);
+                vop_run(VOP_COPY, p, r, 0.0, n3, NULL);
             } else {
                 beta = rho / rho_1;
                 /* vOp_avf (MechanicalObject.inl:1999-2013): p *= beta; p += r */
-                if (beta == 1.0)
-                    for (long i = 0; i < n3; ++i) p[i] += r[i];
-                else
-                    for (long i = 0; i < n3; ++i) {
-                        p[i] *= beta;
-                        p[i] += r[i];
-                    }
+                vop_run(VOP_AVF, p, r, beta, n3, NULL);
             }
             matvec(s, q, p, mf, kf);
             n_matvec++;
@@ -1322,9 +1482,9 @@ static void cg_solve(orc_scene* s, double mf, double kf)
                     if (!(nb_iter == 1 && s->time_step_count == 0)) break;
                 }
                 alpha = rho / den;
-                /* vOp_v_inc_bf (MechanicalObject.inl:2018-2032), alpha != 1 */
-                for (long i = 0; i < n3; ++i) x[i] += p[i] * alpha;
-                for (long i = 0; i < n3; ++i) r[i] += q[i] * -alpha;
+                /* vOp_v_inc_bf (MechanicalObject.inl:2018-2032) */
+                vop_run(VOP_INC, x, p, alpha, n3, NULL);
+                vop_run(VOP_INC, r, q, -alpha, n3, NULL);
             } else {
                 break;
             }
@@ -1525,10 +1685,7 @@ static void euler_step(orc_scene* s)
     else
         cg_solve(s, mf, kf);
     /* vMultiOp fast path (MechanicalObject.inl:2206-2240): v += dv; x += v h */
-    for (long i = 0; i < n3; ++i) {
-        s->v[i] += s->xs[i];
-        s->x[i] += s->v[i] * h;
-    }
+    vop_run(VOP_INTEGRATE, s->v, s->xs, h, n3, s->x);
     if (s->vdamping != 0.0) {
         const double d = exp(-h * s->vdamping);
         for (long i = 0; i < n3; ++i) s->v[i] *= d;

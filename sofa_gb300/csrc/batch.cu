@@ -298,14 +298,29 @@ static int validate_mesh(const sgb_mesh_desc* m)
         return bfail(SGB_ERR_INVALID_ARGUMENT, "invalid solver parameters");
     if (p.n_fixed < 0 || (p.n_fixed > 0 && !p.fixed_host))
         return bfail(SGB_ERR_INVALID_ARGUMENT, "invalid fixed indices");
+    // the batch kernels run plain cold-start CGLinearSolver with block-ordered
+    // dot products: options that would change the solve are refused rather
+    // than ignored
+    if (p.linear_solver != SGB_SOLVER_CG)
+        return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes use CGLinearSolver (linear_solver = SGB_SOLVER_CG)");
+    if (p.preconditioner != SGB_PRECOND_NONE)
+        return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes take no preconditioner");
+    if (p.warm_start) return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not support CG warmStart");
+    if (p.residual_replacement > 0)
+        return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not support residual replacement");
+    if (p.serial_dots)
+        return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes sum dot products per block, not serially (serial_dots)");
     return SGB_OK;
 }
 
 int sgb_batch_mesh_bytes(const sgb_batch_t* B, const sgb_mesh_desc* m, size_t* bytes)
 {
-    if (!B || !bytes) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_mesh_bytes: NULL argument");
+    if (!bytes) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_mesh_bytes: NULL argument");
+    // no batch: plan for a mixed-precision batch with the default patch size
+    const int pe = B ? B->pe : 512;
+    const size_t rs = B ? B->rs : sizeof(float);
     PreparedMesh pm;
-    int rc = prepare_mesh(m, B->pe, B->rs, pm);
+    int rc = prepare_mesh(m, pe, rs, pm);
     if (rc) return rc;
     *bytes = pm.bytes;
     return SGB_OK;

@@ -17,6 +17,15 @@
 // has to start at zero, because the element pass overwrites every entry the
 // gather then reads. Two calls that overlap on the GPU (different streams,
 // no ordering between them) race on the array and give wrong results.
+// The array's device address is looked up once per device and kept; a
+// cudaDeviceReset (or any teardown of the primary context) in the same
+// process reloads the module and may move the array, so this entry point
+// is not to be called again after one.
+//
+// Node and slot indices come from the caller. The kernels check them
+// against n_nodes and 4*n_tets before any access: an out-of-range entry is
+// skipped (it contributes nothing), so a bad table gives a wrong df but
+// never an access outside the caller's arrays or the scratch.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -35,12 +44,13 @@ static __device__ __align__(256) float g_noalloc_corner_terms[12 * kNoAllocMaxTe
 
 std::mutex g_setup_mutex;
 void* g_scratch_addr[kMaxDevices] = {nullptr};
+int g_sm_count[kMaxDevices] = {0};
 
 
 // Once per device, with that device current: the device address of the
 // array. In host code the array's name is only a host-side stand-in, so the
 // kernels receive this address instead.
-cudaError_t scratch_for_current_device(float** out)
+cudaError_t scratch_for_current_device(float** out, int* sm_count)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -51,15 +61,20 @@ cudaError_t scratch_for_current_device(float** out)
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_corner_terms);
         if (e != cudaSuccess) return e;
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        g_sm_count[dev] = sms > 0 ? sms : 1;
         g_scratch_addr[dev] = p;
     }
     *out = (float*)g_scratch_addr[dev];
+    *sm_count = g_sm_count[dev];
     return cudaSuccess;
 }
 
 // Element pass: corner terms R K (R^T dx) kfactor of the corotational
 // stiffness (applyStiffnessCorotational, TetrahedronFEMForceField.inl:1193-1237).
-__global__ void __launch_bounds__(128) k_noalloc_elements(int n_tets, const int4* __restrict__ tets,
+__global__ void __launch_bounds__(128) k_noalloc_elements(int n_nodes, int n_tets, const int4* __restrict__ tets,
                                                           const float* __restrict__ rot,
                                                           const float* __restrict__ K,
                                                           const float* __restrict__ J,
@@ -71,6 +86,10 @@ __global__ void __launch_bounds__(128) k_noalloc_elements(int n_tets, const int4
     const size_t En = (size_t)n_tets;
     const int4 t = tets[e];
     const int node[4] = {t.x, t.y, t.z, t.w};
+    // a node index outside [0, n_nodes) reads nothing: its values count as zero
+    bool ok[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ok[i] = (unsigned)node[i] < (unsigned)n_nodes;
     float Rm[9], Ke[3], Je[12], X[12], F[12];
 #pragma unroll
     for (int i = 0; i < 9; ++i) Rm[i] = rot[i * En + e];
@@ -82,7 +101,7 @@ __global__ void __launch_bounds__(128) k_noalloc_elements(int n_tets, const int4
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) d[i][k] = dx[3 * (size_t)node[i] + k];
+        for (int k = 0; k < 3; ++k) d[i][k] = ok[i] ? dx[3 * (size_t)node[i] + k] : 0.f;
     // values relative to node a: J^T annihilates translations
 #pragma unroll
     for (int i = 3; i >= 0; --i)
@@ -103,14 +122,18 @@ __global__ void __launch_bounds__(128) k_noalloc_elements(int n_tets, const int4
 
 // Node gather: each node subtracts its (tetrahedron, corner) terms in slot
 // order, no atomics.
-__global__ void __launch_bounds__(256) k_noalloc_gather(int n_nodes, const int* __restrict__ rowptr,
+__global__ void __launch_bounds__(256) k_noalloc_gather(int n_nodes, int n_slots, const int* __restrict__ rowptr,
                                                         const int* __restrict__ slots,
                                                         const float* __restrict__ scratch, float* __restrict__ df)
 {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < n_nodes; n += gridDim.x * blockDim.x) {
         float a0 = df[3 * (size_t)n], a1 = df[3 * (size_t)n + 1], a2 = df[3 * (size_t)n + 2];
-        for (int s = rowptr[n]; s < rowptr[n + 1]; ++s) {
-            const float* c = scratch + 3 * (size_t)slots[s];
+        // row bounds outside [0, n_slots] and slots outside [0, 4 n_tets) are skipped
+        const int s0 = max(rowptr[n], 0), s1 = min(rowptr[n + 1], n_slots);
+        for (int s = s0; s < s1; ++s) {
+            const int slot = slots[s];
+            if ((unsigned)slot >= (unsigned)n_slots) continue;
+            const float* c = scratch + 3 * (size_t)slot;
             a0 -= c[0];
             a1 -= c[1];
             a2 -= c[2];
@@ -155,18 +178,20 @@ extern "C" int sgb_tfem_add_dforce_f32_noalloc(int n_nodes, int n_tets, const in
     }
     if (n_tets == 0) return SGB_OK;
     float* scratch = nullptr;
-    cudaError_t e = scratch_for_current_device(&scratch);
+    int sms = 1;
+    cudaError_t e = scratch_for_current_device(&scratch, &sms);
     if (e != cudaSuccess) {
         sgb::set_last_error(std::string("sgb_tfem_add_dforce_f32_noalloc: scratch set-up: ") + cudaGetErrorString(e));
         return SGB_ERR_CUDA;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    k_noalloc_elements<<<(n_tets + 127) / 128, 128, 0, s>>>(n_tets, (const int4*)tetrahedra_dev, rotations_dev,
+    k_noalloc_elements<<<(n_tets + 127) / 128, 128, 0, s>>>(n_nodes, n_tets, (const int4*)tetrahedra_dev, rotations_dev,
                                                            stiffness_dev, strain_displacement_dev, dx_dev, kfactor,
                                                            scratch);
+    // grid-stride gather: at most 8 resident 256-thread CTAs per SM
     int grid = (n_nodes + 255) / 256;
-    if (grid > 152 * 8) grid = 152 * 8;
-    k_noalloc_gather<<<grid, 256, 0, s>>>(n_nodes, node_rowptr_dev, node_slots_dev, scratch, df_dev);
+    if (grid > sms * 8) grid = sms * 8;
+    k_noalloc_gather<<<grid, 256, 0, s>>>(n_nodes, 4 * n_tets, node_rowptr_dev, node_slots_dev, scratch, df_dev);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         sgb::set_last_error(std::string("sgb_tfem_add_dforce_f32_noalloc: launch: ") + cudaGetErrorString(e));

@@ -5,7 +5,8 @@ the reference sources by oracle/ref/Makefile, on seeded 3x3 matrices shaped
 like the edge matrices of deformed tetrahedra (rotation x stretch x shear),
 plus generic random ones.
 
-Run where the reference tree is present:  python tests/golden/make_polar_golden.py
+Run with SOFA_REFERENCE_ROOT naming the SOFA source tree:
+    SOFA_REFERENCE_ROOT=<tree> python tests/golden/make_polar_golden.py
 """
 import ctypes
 import os

@@ -6,7 +6,8 @@ matrices covering each branch the svd method reaches: regular, inverted,
 nearly inverted, flat (rank 2), collapsed to an edge (rank 1) and to a
 point, and flat or inverted deformation gradients of tetrahedra.
 
-Run where the reference tree is present:  python tests/golden/make_polar_stable_golden.py
+Run with SOFA_REFERENCE_ROOT naming the SOFA source tree:
+    SOFA_REFERENCE_ROOT=<tree> python tests/golden/make_polar_stable_golden.py
 """
 import ctypes
 import os

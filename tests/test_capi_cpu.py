@@ -107,3 +107,24 @@ def test_patch_layout_random_soup(capi):
     rc = lib.sgb_patch_layout_check(300, pos.ctypes.data_as(capi._dp), 2000, tets.ctypes.data_as(capi._ip), 128, 100,
                                     stats)
     assert rc == 0, capi.last_error()
+
+
+@pytest.mark.parametrize("field,value", [("linear_solver", 1), ("preconditioner", 1), ("warm_start", 1),
+                                         ("residual_replacement", 20), ("serial_dots", 1)])
+def test_batch_admission_refuses_solver_options_it_does_not_run(capi, field, value):
+    """The batch engine runs cold-start CG with block-ordered dots; a mesh
+    that asks for PCG, a preconditioner, warmStart, residual replacement or
+    serial dots is refused (SGB_ERR_NOT_SUPPORTED) instead of being run as
+    plain CG. Planning with a NULL batch runs the same checks host-side."""
+    from sofa_gb300 import topology as topo
+
+    lib = capi.load()
+    mesh = topo.beam((3, 3, 5), spacing=0.5, jitter=0.05, seed=0)
+    d, keep = capi.Batch.mesh_desc(mesh.positions, mesh.tetrahedra, method="polar", fixed=mesh.fixed)
+    b = ctypes.c_size_t()
+    assert lib.sgb_batch_mesh_bytes(None, ctypes.byref(d), ctypes.byref(b)) == 0
+    assert b.value > 0
+    setattr(d.params, field, value)
+    rc = lib.sgb_batch_mesh_bytes(None, ctypes.byref(d), ctypes.byref(b))
+    assert rc == -4, (rc, capi.last_error())
+    assert "batched meshes" in capi.last_error()

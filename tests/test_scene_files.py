@@ -12,7 +12,10 @@ from sofa_gb300 import topology as topo
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SCENES = os.path.join(HERE, "scenes")
-REF_BENCH = "/root/reference/applications/plugins/SofaCUDA/scenes/benchmarks"
+# the reference's own benchmark scenes, read in place from the SOFA source
+# tree named by SOFA_REFERENCE_ROOT (tests that need them skip without it)
+REF_BENCH = os.path.join(os.environ.get("SOFA_REFERENCE_ROOT", ""),
+                         "applications/plugins/SofaCUDA/scenes/benchmarks")
 
 
 @pytest.fixture(scope="module")
@@ -105,7 +108,7 @@ def test_reference_scene_with_an_out_of_scope_force_field(capi):
     class it does not know."""
     path = os.path.join(REF_BENCH, "TetrahedronFEMForceField_beam16x16x76_gpu.scn")
     if not os.path.exists(path):
-        pytest.skip("reference tree not present")
+        pytest.skip("SOFA_REFERENCE_ROOT does not name the reference tree")
     with open(path) as f, pytest.raises(capi.SgbError) as e:
         capi.SofaScene(f.read())
     assert e.value.code == -4 and "PlaneForceField" in str(e.value)
@@ -118,7 +121,7 @@ def test_reference_benchmark_scene_files(capi, name, precision):
     tree is present, load unchanged."""
     path = os.path.join(REF_BENCH, name)
     if not os.path.exists(path):
-        pytest.skip("reference tree not present")
+        pytest.skip("SOFA_REFERENCE_ROOT does not name the reference tree")
     with open(path) as f:
         s = capi.SofaScene(f.read())
     assert s.n_bodies == 1
