@@ -39,7 +39,8 @@ extern "C" {
 #define SGB_ERR_NUMERICAL -5   /* a non-finite value was met in the CG solve */
 #define SGB_ERR_BUDGET -6      /* admission refused: HBM budget exceeded */
 #define SGB_ERR_NOT_FOUND -7
-#define SGB_ERR_DEVICE_TIMEOUT -8 /* a bounded device-side wait (bulk copy completion) ran out */
+#define SGB_ERR_DEVICE_TIMEOUT -8 /* a bounded device-side wait ran out */
+#define SGB_ERR_CANCELLED -9   /* the request was cancelled (sgb_server_cancel) */
 
 /* TetrahedronFEMForceField Data "method"
  * (TetrahedronFEMForceField.inl:45): small, large (QR frame), polar, svd
@@ -154,8 +155,10 @@ int sgb_tfem_stiffness_bsr(sgb_tfem_t* fem, int* n_blocks, int32_t* rowptr_host,
 
 /* Reads and clears the force field's sticky device error flag (synchronises
  * the device). SGB_OK, or SGB_ERR_DEVICE_TIMEOUT when a bounded device-side
- * wait of an earlier add_dforce (the completion of the bulk copies that
- * stage element data) ran out; that call's df is then incomplete. */
+ * wait of an earlier call ran out. No kernel of this version waits on the
+ * device (the reductions take no locks and never spin), so it returns
+ * SGB_OK after any call that completed; the flag is kept so that callers
+ * need no change when a kernel with a bounded wait is added. */
 int sgb_tfem_check_device(sgb_tfem_t* fem);
 
 /* Sizes and device footprint of the force field. */
@@ -265,6 +268,23 @@ typedef struct sgb_scene_params {
      * solve from the previous step's solution, r = b - A x, instead of
      * x = 0, r = b. PCG always starts from it. */
     int warm_start;
+    /* The components' own Rayleigh coefficients: the force field's
+     * rayleighStiffness (BaseForceField.cpp:34) and the mass's rayleighMass
+     * (BaseMass.cpp:33-34). They enter the system matrix only, as
+     * kFactorIncludingRayleighDamping = kF + bF * ff_rayleigh_stiffness and
+     * mFactorIncludingRayleighDamping = mF - bF * mass_rayleigh_mass
+     * (MechanicalParams.h:62-64, BaseForceField.cpp:38-47, Mass.inl:94-104);
+     * the right-hand side is built with bF = 0. */
+    double ff_rayleigh_stiffness;
+    double mass_rayleigh_mass;
+    /* EulerImplicitSolver firstOrder (EulerImplicitSolver.cpp:138-171): b = f,
+     * (M - h K) v_new = b, x += h v_new; the Rayleigh and bF terms vanish. */
+    int first_order;
+    /* FixedProjectiveConstraint activate_projectVelocity
+     * (FixedProjectiveConstraint.inl:237-261): after each step the velocity
+     * of the fixed nodes is set to zero (DefaultAnimationLoop's
+     * projectPositionAndVelocity, DefaultAnimationLoop.cpp:228-233, 293). */
+    int project_velocity;
 } sgb_scene_params;
 
 #define SGB_SOLVER_CG 0
@@ -345,9 +365,11 @@ int sgb_batch_destroy(sgb_batch_t* batch);
 /* Bytes a mesh would take in the budget (host-side planning only; with
  * batch NULL, for a mixed-precision batch with the default patch size).
  * Runs the admission checks: the batch engine runs cold-start
- * CGLinearSolver with block-ordered dot products, so a mesh whose params
- * ask for PCG, a preconditioner, warmStart, residual replacement or serial
- * dots is refused with SGB_ERR_NOT_SUPPORTED, here and at admission. */
+ * CGLinearSolver with block-ordered dot products and the second-order
+ * Euler scheme, so a mesh whose params ask for PCG, a preconditioner,
+ * warmStart, residual replacement, serial dots, firstOrder or
+ * project_velocity is refused with SGB_ERR_NOT_SUPPORTED, here and at
+ * admission. The components' Rayleigh coefficients are supported. */
 int sgb_batch_mesh_bytes(const sgb_batch_t* batch, const sgb_mesh_desc* mesh, size_t* bytes);
 /* Admission: SGB_ERR_BUDGET when the mesh does not fit or no slot is free.
  * Synchronous; positions start at rest, velocities at zero. */
@@ -365,9 +387,46 @@ int sgb_batch_get_state(sgb_batch_t* batch, int slot, double* x_host, double* v_
 /* Queues the copy of a mesh's positions on the batch stream (no wait). */
 int sgb_batch_get_positions_async(sgb_batch_t* batch, int slot, double* x_host);
 int sgb_batch_set_state(sgb_batch_t* batch, int slot, const double* x_host, const double* v_host);
+/* What carries a mesh from one step to the next -- positions, velocities and
+ * its time-step count -- saved to host memory and put back, so that a mesh
+ * removed from a batch and admitted again (into this or another batch of the
+ * same precision, from the same description) continues bit-exactly; the
+ * counterpart of MechanicalObject::writeState / readState
+ * (Sofa/Component/StateContainer/src/sofa/component/statecontainer/
+ * MechanicalObject.inl:1229-1340) for this library's state. x_host and v_host
+ * hold 3 n_nodes doubles. Synchronous. */
+int sgb_batch_save_mesh(sgb_batch_t* batch, int slot, double* x_host, double* v_host, long long* steps);
+int sgb_batch_restore_mesh(sgb_batch_t* batch, int slot, const double* x_host, const double* v_host,
+                           long long steps);
 int sgb_batch_info(const sgb_batch_t* batch, int* active_meshes, long long* active_tets, size_t* budget_used,
                    size_t* budget_total);
 void* sgb_batch_stream(sgb_batch_t* batch);
+
+/* Launch tiles of the batch step, picked by timing the admitted mix (an
+ * autotuner of this library; the reference sets its equivalent knobs by hand:
+ * gatherPt / gatherBsize of SofaCUDA's TetrahedronFEMForceField,
+ * applications/plugins/SofaCUDA/Component/src/SofaCUDA/component/
+ * solidmechanics/fem/elastic/CudaTetrahedronFEMForceField.h:258-266). The
+ * tiles are the matvec's resident CTAs per SM (5, 6 or 8: its register cap),
+ * the CG update's nodes per thread (1, 2 or 4) and CTAs per SM, the element
+ * kernels' CTAs per SM, and an L2 prefetch of each block's next patch. No
+ * tile changes a result bit: every per-mesh reduction is formed per work item
+ * in an order fixed by the item. sgb_batch_tune times candidates one tile at
+ * a time, each over steps_per_trial whole steps from the same saved state,
+ * restores every mesh's state afterwards and keeps the fastest; with
+ * use_cache it first looks for the choice made for a mix with the same
+ * size histogram in this process. Patches keep the size fixed at creation
+ * (elements per patch: 512 mixed, 256 FP64), because it fixes each node's
+ * gather order. Synchronous. */
+int sgb_batch_tune(sgb_batch_t* batch, int steps_per_trial, int use_cache);
+/* tiles: matvec CTAs per SM, update nodes per thread, update CTAs per SM,
+ * element CTAs per SM, prefetch (0 / 1). */
+int sgb_batch_set_tiles(sgb_batch_t* batch, const int tiles[5]);
+/* tiles[6]: elements per patch, then the five tiles above; default_ms and
+ * best_ms: step time of the starting and the chosen tiles in the last tuning
+ * (0 before any), trials: configurations it timed (0 when the cache
+ * answered). Any output but tiles may be NULL. */
+int sgb_batch_get_tiles(const sgb_batch_t* batch, int tiles[6], double* default_ms, double* best_ms, int* trials);
 
 /* ------------------------------------------------------------------ */
 /* Serving: continuous batching of simulate-K-steps requests            */
@@ -402,9 +461,13 @@ typedef struct sgb_completion {
 typedef struct sgb_server_stats {
     long long submitted, completed, failed;
     long long tet_steps;      /* completed requests: tets x steps */
-    double p50_ms, p99_ms, max_ms;
+    double p50_ms, p99_ms, max_ms;  /* request latency: submission -> positions copied */
     double busy_s;            /* time spent in batch launches */
     double wall_s;            /* since the first submission */
+    /* step latency: each launch of k steps over the admitted meshes counts k
+     * steps of (launch wall time) / k, outputs copied included */
+    double step_p50_ms, step_p99_ms;
+    long long launches, cancelled, evicted;
 } sgb_server_stats;
 
 int sgb_server_create(sgb_server_t** out, int precision, size_t hbm_budget_bytes, int max_meshes,
@@ -415,6 +478,19 @@ int sgb_server_poll(sgb_server_t* server, sgb_completion* out, int max_out, int*
 /* Blocks until every submitted request has completed (or timeout_s passes). */
 int sgb_server_wait_idle(sgb_server_t* server, double timeout_s);
 int sgb_server_get_stats(sgb_server_t* server, sgb_server_stats* stats);
+/* Cancels a request: one still queued (being prepared or waiting for
+ * admission) is dropped at once, a running one at the next launch boundary
+ * (its slot and memory are freed). Its completion carries
+ * SGB_ERR_CANCELLED. SGB_ERR_NOT_FOUND when the id is unknown or the request
+ * already completed. */
+int sgb_server_cancel(sgb_server_t* server, uint64_t id);
+/* Evicts a running request at the next launch boundary: its state
+ * (sgb_batch_save_mesh) goes to host memory and its slot and HBM are freed;
+ * it re-enters the queue behind the requests already waiting and, once
+ * admitted again, continues from where it stopped, bit-exactly. Its latency
+ * still counts from the first submission. SGB_ERR_NOT_FOUND when the
+ * request is not running. */
+int sgb_server_evict(sgb_server_t* server, uint64_t id);
 int sgb_server_destroy(sgb_server_t* server);
 
 #ifdef __cplusplus

@@ -69,6 +69,24 @@ int sgb_sofa_scene_init_device(sgb_sofa_scene_t* scene);
  * needed. Stream-ordered; sgb_sofa_scene_get_positions synchronises. */
 int sgb_sofa_scene_animate(sgb_sofa_scene_t* scene, int n_steps);
 
+/* SofaPhysicsAPI::reset (applications/projects/SofaPhysicsAPI/src/
+ * SofaPhysicsAPI/SofaPhysicsAPI.h:98-99; sofa::simulation::node::reset):
+ * every body's positions back to their initial values and velocities to
+ * their initial values (zero unless the scene set them), as
+ * MechanicalObject::reset does (Sofa/Component/StateContainer/src/sofa/
+ * component/statecontainer/MechanicalObject.inl:1204-1225); plastic strains
+ * cleared (TetrahedronFEMForceField.inl:1382-1388); WriteState rewound; time
+ * 0. The solvers keep their own state (the reference's CGLinearSolver has no
+ * reset). Device objects are kept; synchronous. */
+int sgb_sofa_scene_reset(sgb_sofa_scene_t* scene);
+
+/* SofaPhysicsAPI::unload (SofaPhysicsAPI.h:74-75) for the device: releases
+ * every body's GPU objects (device memory) and keeps the parsed scene; the
+ * next sgb_sofa_scene_animate (or init_device) creates them again and starts
+ * from the initial state. Destroy the scene itself with
+ * sgb_sofa_scene_destroy. */
+int sgb_sofa_scene_unload(sgb_sofa_scene_t* scene);
+
 /* Positions of a body (n_nodes x 3 doubles): the current state once the
  * device is initialised, else the initial positions. */
 int sgb_sofa_scene_get_positions(sgb_sofa_scene_t* scene, int body, double* x_host);

@@ -1189,6 +1189,12 @@ typedef struct orc_scene {
     int solver, precond, precond_rate;
     int warm_start; /* CGLinearSolver warmStart */
     double* dinv;
+    /* the components' own Rayleigh coefficients (force field rayleighStiffness,
+     * mass rayleighMass), EulerImplicitSolver firstOrder,
+     * FixedProjectiveConstraint activate_projectVelocity */
+    double ff_rs, mass_rm;
+    int first_order, project_velocity;
+    double cur_bf; /* bFactor of the matrix being applied (0 for the right-hand side) */
 } orc_scene;
 
 orc_scene* orc_scene_create(orc_fem* fem, int n_nodes, int mass_kind, double vertex_mass,
@@ -1414,16 +1420,18 @@ static double vdot(const double* a, const double* b, int n)
 
 /* addMBKdx with the forcefield order of the node: mass (Mass::addMBKdx,
  * Mass.inl:94-104) and the FEM (BaseForceField::addMBKdx,
- * BaseForceField.cpp:38-47). The force fields' own Rayleigh coefficients are
- * zero in every scene here, so kFactorIncludingRayleighDamping = k and
- * mFactorIncludingRayleighDamping = m (MechanicalParams.h:62-64). */
+ * BaseForceField.cpp:38-47). mf and kf are the factors each component
+ * applies, their own Rayleigh terms already folded in
+ * (k/mFactorIncludingRayleighDamping, MechanicalParams.h:62-64); the force
+ * field runs when its factor or the matrix's bFactor is non-zero. */
 static void add_mbkdx(orc_scene* s, double* df, const double* dx, double mf, double kf)
 {
+    const int ff = (kf != 0.0 || s->cur_bf != 0.0) && s->fem;
     if (s->mass_first) {
         if (mf != 0.0) mass_add_mdx(s, df, dx, mf);
-        if (kf != 0.0 && s->fem) orc_fem_add_dforce(s->fem, dx, df, kf);
+        if (ff) orc_fem_add_dforce(s->fem, dx, df, kf);
     } else {
-        if (kf != 0.0 && s->fem) orc_fem_add_dforce(s->fem, dx, df, kf);
+        if (ff) orc_fem_add_dforce(s->fem, dx, df, kf);
         if (mf != 0.0) mass_add_mdx(s, df, dx, mf);
     }
     if (kf != 0.0) spring_add_dforce(s, dx, df, kf);
@@ -1638,6 +1646,17 @@ void orc_scene_set_solver(orc_scene* s, int solver, int precond, int precond_rat
 /* CGLinearSolver warmStart: each CG solve starts from the previous solution. */
 void orc_scene_set_warm_start(orc_scene* s, int on) { s->warm_start = on ? 1 : 0; }
 
+/* The components' own Rayleigh coefficients, EulerImplicitSolver firstOrder and
+ * FixedProjectiveConstraint activate_projectVelocity. */
+void orc_scene_set_options(orc_scene* s, double ff_rayleigh_stiffness, double mass_rayleigh_mass, int first_order,
+                           int project_velocity)
+{
+    s->ff_rs = ff_rayleigh_stiffness;
+    s->mass_rm = mass_rayleigh_mass;
+    s->first_order = first_order ? 1 : 0;
+    s->project_velocity = project_velocity ? 1 : 0;
+}
+
 /* the last solve's Jacobi inverse diagonal (zeros before the first) */
 void orc_scene_jacobi(const orc_scene* s, double* out)
 {
@@ -1670,26 +1689,54 @@ static void scene_compute_force(orc_scene* s)
 static void euler_step(orc_scene* s)
 {
     const long n3 = 3L * s->n;
-    const double h = s->dt;
+    const double h = s->dt, tr = 1.0;
     scene_compute_force(s);
-    /* b = f; b += (-rm M + (h + rs) K) v; b *= h; project(b) */
     memcpy(s->b, s->f, sizeof(double) * (size_t)n3);
-    add_mbkdx(s, s->b, s->v, -s->rm, h * 1.0 + s->rs);
-    for (long i = 0; i < n3; ++i) s->b[i] *= h;
+    if (!s->first_order) {
+        /* b = f; b += (-rm M + (h + rs) K) v with bFactor 0; b *= h
+         * (EulerImplicitSolver.cpp:141-158); firstOrder: b = f (:137-140) */
+        s->cur_bf = 0.0;
+        add_mbkdx(s, s->b, s->v, -s->rm, h * tr + s->rs);
+        for (long i = 0; i < n3; ++i) s->b[i] *= h;
+    }
     project_response(s, s->b);
-    /* setSystemMBKMatrix: mF = 1 + h rm, bF = -h, kF = -h (h + rs) */
-    const double mf = 1 + 1.0 * h * s->rm;
-    const double kf = -1.0 * h * (1.0 * h + s->rs);
+    /* setSystemMBKMatrix (EulerImplicitSolver.cpp:165-171): second order
+     * mF = 1 + h rm, bF = -h, kF = -h (h + rs); first order mF = 1, bF = 0,
+     * kF = -h. Each component adds its own Rayleigh term to its factor. */
+    double mf, bf, kf;
+    if (s->first_order) {
+        mf = 1;
+        bf = 0;
+        kf = -h * tr;
+    } else {
+        mf = 1 + tr * h * s->rm;
+        bf = -tr * h;
+        kf = -tr * h * (tr * h + s->rs);
+    }
+    const double kf_ff = kf + bf * s->ff_rs;
+    const double mf_mass = mf - bf * s->mass_rm;
+    s->cur_bf = bf;
     if (s->solver == 1)
-        pcg_solve(s, mf, kf);
+        pcg_solve(s, mf_mass, kf_ff);
     else
-        cg_solve(s, mf, kf);
-    /* vMultiOp fast path (MechanicalObject.inl:2206-2240): v += dv; x += v h */
-    vop_run(VOP_INTEGRATE, s->v, s->xs, h, n3, s->x);
+        cg_solve(s, mf_mass, kf_ff);
+    if (s->first_order) {
+        /* v = x; x = x + v h (the generic vMultiOp, :248-256) */
+        vop_run(VOP_COPY, s->v, s->xs, 0.0, n3, NULL);
+        vop_run(VOP_INC, s->x, s->v, h, n3, NULL);
+    } else {
+        /* vMultiOp fast path (MechanicalObject.inl:2206-2240): v += dv; x += v h */
+        vop_run(VOP_INTEGRATE, s->v, s->xs, h, n3, s->x);
+    }
     if (s->vdamping != 0.0) {
         const double d = exp(-h * s->vdamping);
         for (long i = 0; i < n3; ++i) s->v[i] *= d;
     }
+    /* DefaultAnimationLoop::projectPositionAndVelocity (DefaultAnimationLoop.cpp:
+     * 228-233, 293): FixedProjectiveConstraint::projectVelocity
+     * (FixedProjectiveConstraint.inl:237-261) zeroes the fixed nodes' velocity
+     * when activate_projectVelocity is set; projectPosition does nothing */
+    if (s->project_velocity) project_response(s, s->v);
 }
 
 void orc_scene_step(orc_scene* s, int n_steps)

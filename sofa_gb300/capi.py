@@ -57,6 +57,10 @@ class SceneParams(ctypes.Structure):
         ("preconditioner", ctypes.c_int),
         ("preconditioner_rate", ctypes.c_int),
         ("warm_start", ctypes.c_int),
+        ("ff_rayleigh_stiffness", ctypes.c_double),
+        ("mass_rayleigh_mass", ctypes.c_double),
+        ("first_order", ctypes.c_int),
+        ("project_velocity", ctypes.c_int),
     ]
 
 
@@ -108,6 +112,11 @@ class ServerStats(ctypes.Structure):
         ("max_ms", ctypes.c_double),
         ("busy_s", ctypes.c_double),
         ("wall_s", ctypes.c_double),
+        ("step_p50_ms", ctypes.c_double),
+        ("step_p99_ms", ctypes.c_double),
+        ("launches", ctypes.c_longlong),
+        ("cancelled", ctypes.c_longlong),
+        ("evicted", ctypes.c_longlong),
     ]
 
 
@@ -173,14 +182,23 @@ def load():
         "sgb_batch_info": (c_int, [_vp, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong),
                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
         "sgb_batch_stream": (_vp, [_vp]),
+        "sgb_batch_tune": (c_int, [_vp, c_int, c_int]),
+        "sgb_batch_set_tiles": (c_int, [_vp, ctypes.POINTER(c_int)]),
+        "sgb_batch_get_tiles": (c_int, [_vp, ctypes.POINTER(c_int), _dp, _dp, ctypes.POINTER(c_int)]),
         "sgb_server_create": (c_int, [ctypes.POINTER(_vp), c_int, ctypes.c_size_t, c_int, c_int, c_int, c_int]),
         "sgb_server_submit": (c_int, [_vp, ctypes.POINTER(Request)]),
         "sgb_server_poll": (c_int, [_vp, ctypes.POINTER(Completion), c_int, ctypes.POINTER(c_int)]),
         "sgb_server_wait_idle": (c_int, [_vp, c_double]),
         "sgb_server_get_stats": (c_int, [_vp, ctypes.POINTER(ServerStats)]),
         "sgb_server_destroy": (c_int, [_vp]),
+        "sgb_server_cancel": (c_int, [_vp, ctypes.c_uint64]),
+        "sgb_server_evict": (c_int, [_vp, ctypes.c_uint64]),
+        "sgb_batch_save_mesh": (c_int, [_vp, c_int, _dp, _dp, ctypes.POINTER(ctypes.c_longlong)]),
+        "sgb_batch_restore_mesh": (c_int, [_vp, c_int, _dp, _dp, ctypes.c_longlong]),
         "sgb_sofa_scene_load": (c_int, [ctypes.POINTER(_vp), ctypes.c_char_p, c_int]),
         "sgb_sofa_scene_destroy": (c_int, [_vp]),
+        "sgb_sofa_scene_reset": (c_int, [_vp]),
+        "sgb_sofa_scene_unload": (c_int, [_vp]),
         "sgb_sofa_scene_describe": (c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "sgb_sofa_scene_bodies": (c_int, [_vp, ctypes.POINTER(c_int)]),
         "sgb_sofa_scene_body_info": (c_int, [_vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
@@ -348,7 +366,8 @@ class Scene:
                  cg_iterations=25, cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0),
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
                  serial_dots=False, residual_replacement=0, linear_solver="cg", preconditioner=None,
-                 preconditioner_rate=1, warm_start=False):
+                 preconditioner_rate=1, warm_start=False, ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0,
+                 first_order=False, project_velocity=False):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -379,6 +398,10 @@ class Scene:
         p.preconditioner = {None: 0, "jacobi": 1}[preconditioner]
         p.preconditioner_rate = int(preconditioner_rate)
         p.warm_start = int(warm_start)
+        p.ff_rayleigh_stiffness = float(ff_rayleigh_stiffness)
+        p.mass_rayleigh_mass = float(mass_rayleigh_mass)
+        p.first_order = int(first_order)
+        p.project_velocity = int(project_velocity)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now
@@ -451,7 +474,8 @@ class Scene:
 
 def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0, cg_iterations=25,
                  cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0), vertex_mass=1.0,
-                 node_masses=None, fixed=(), fix_all=False, keep=None, linear_solver="cg", preconditioner=None):
+                 node_masses=None, fixed=(), fix_all=False, keep=None, linear_solver="cg", preconditioner=None,
+                 ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0):
     """A filled SceneParams; `keep` collects the numpy buffers it points to.
     linear_solver "cg" or "pcg"; preconditioner None or "jacobi" (PCG)."""
     lib = load()
@@ -478,6 +502,8 @@ def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.
     p.mass_first = 1
     p.linear_solver = {"cg": 0, "pcg": 1}[linear_solver]
     p.preconditioner = {None: 0, "jacobi": 1}[preconditioner]
+    p.ff_rayleigh_stiffness = float(ff_rayleigh_stiffness)
+    p.mass_rayleigh_mass = float(mass_rayleigh_mass)
     return p
 
 
@@ -588,6 +614,43 @@ class Batch:
         va, pv = _d(np.asarray(v).reshape(-1, 3)) if v is not None else (None, _dp())
         check(load().sgb_batch_set_state(self._h, int(slot), px, pv))
 
+    def save_mesh(self, slot):
+        """(x, v, steps) of a mesh: what carries it from one step to the next."""
+        n = self.n_nodes[slot]
+        x = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        st = ctypes.c_longlong()
+        check(load().sgb_batch_save_mesh(self._h, int(slot), x.ctypes.data_as(_dp), v.ctypes.data_as(_dp),
+                                         ctypes.byref(st)))
+        return x, v, st.value
+
+    def restore_mesh(self, slot, x, v, steps):
+        xa, px = _d(np.asarray(x).reshape(-1, 3))
+        va, pv = _d(np.asarray(v).reshape(-1, 3))
+        check(load().sgb_batch_restore_mesh(self._h, int(slot), px, pv, int(steps)))
+
+    def tune(self, steps_per_trial=2, use_cache=True):
+        """Picks the batch step's launch tiles by timing the admitted mix
+        (state is restored; results do not change)."""
+        check(load().sgb_batch_tune(self._h, int(steps_per_trial), int(use_cache)))
+        return self.tuning()
+
+    def set_tiles(self, matvec_ctas_per_sm=6, update_nodes_per_thread=4, update_ctas_per_sm=4,
+                  elem_ctas_per_sm=4, prefetch=0):
+        t = (ctypes.c_int * 5)(matvec_ctas_per_sm, update_nodes_per_thread, update_ctas_per_sm, elem_ctas_per_sm,
+                               prefetch)
+        check(load().sgb_batch_set_tiles(self._h, t))
+
+    def tuning(self):
+        t = (ctypes.c_int * 6)()
+        d = ctypes.c_double()
+        b = ctypes.c_double()
+        n = ctypes.c_int()
+        check(load().sgb_batch_get_tiles(self._h, t, ctypes.byref(d), ctypes.byref(b), ctypes.byref(n)))
+        return {"elements_per_patch": t[0], "matvec_ctas_per_sm": t[1], "update_nodes_per_thread": t[2],
+                "update_ctas_per_sm": t[3], "elem_ctas_per_sm": t[4], "prefetch": t[5],
+                "default_ms_per_step": d.value, "tuned_ms_per_step": b.value, "trials": n.value}
+
     def info(self):
         n = ctypes.c_int()
         t = ctypes.c_longlong()
@@ -655,6 +718,16 @@ class Server:
 
     def wait_idle(self, timeout_s=600.0):
         check(load().sgb_server_wait_idle(self._h, float(timeout_s)))
+
+    def cancel(self, rid):
+        """Cancels a queued or running request; raises SgbError(-7) when it
+        is neither (already completed or unknown)."""
+        check(load().sgb_server_cancel(self._h, int(rid)))
+
+    def evict(self, rid):
+        """Moves a running request's state to host memory and frees its slot;
+        it re-enters the queue and continues bit-exactly."""
+        check(load().sgb_server_evict(self._h, int(rid)))
 
     def stats(self):
         st = ServerStats()
@@ -725,6 +798,14 @@ class SofaScene:
 
     def init_device(self):
         check(load().sgb_sofa_scene_init_device(self._h))
+
+    def reset(self):
+        """SofaPhysicsAPI::reset: initial state, plastic strains cleared, time 0."""
+        check(load().sgb_sofa_scene_reset(self._h))
+
+    def unload(self):
+        """Releases the device objects; the next animate starts again."""
+        check(load().sgb_sofa_scene_unload(self._h))
 
     def animate(self, n_steps=1):
         check(load().sgb_sofa_scene_animate(self._h, int(n_steps)))

@@ -7,9 +7,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <thread>
 #include <string>
 #include <vector>
@@ -232,7 +234,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
             const int v = atoi(e);
             if (v >= 64 && v <= 512 && v % 2 == 0) B->pe = v;
         }
-    if (const char* e = getenv("SGB_BATCH_PREFETCH")) B->prefetch = (e[0] == '1');
+    if (const char* e = getenv("SGB_BATCH_PREFETCH")) B->tiles.prefetch = (e[0] == '1');
     B->max_slots = max_meshes;
     B->max_iterations = max_cg_iterations;
     B->slots.resize((size_t)max_meshes);
@@ -251,7 +253,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
     }
     B->arena.reset(B->arena_mem, hbm_budget_bytes);
     B->device_bytes = hbm_budget_bytes + sizeof(BMeshDesc) * max_meshes;
-    B->sms = ops->batch_prepare(B->pe, &B->grid_patch);
+    B->sms = ops->batch_prepare(B->pe, B->grid_patch_v);
     if (B->sms <= 0) {
         sgb_batch_destroy(B);
         return bfail(SGB_ERR_CUDA, "sgb_batch_create: kernel attributes");
@@ -310,6 +312,11 @@ static int validate_mesh(const sgb_mesh_desc* m)
         return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not support residual replacement");
     if (p.serial_dots)
         return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes sum dot products per block, not serially (serial_dots)");
+    if (p.first_order) return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes run the second-order Euler scheme");
+    if (p.project_velocity)
+        return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not support activate_projectVelocity");
+    if (!std::isfinite(p.ff_rayleigh_stiffness) || !std::isfinite(p.mass_rayleigh_mass))
+        return bfail(SGB_ERR_INVALID_ARGUMENT, "non-finite component Rayleigh coefficient");
     return SGB_OK;
 }
 
@@ -494,10 +501,19 @@ int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot_out)
     d.cg_iterations = std::min(P.cg_iterations, B->max_iterations);
     const double h = P.dt;
     d.h = h;
-    d.kf_rhs = h * 1.0 + P.rayleigh_stiffness;
+    // solver factors with the components' own Rayleigh terms folded in
+    // (kFactor/mFactorIncludingRayleighDamping, MechanicalParams.h:62-64)
+    SceneParams sp;
+    sp.dt = h;
+    sp.rayleigh_stiffness = P.rayleigh_stiffness;
+    sp.rayleigh_mass = P.rayleigh_mass;
+    sp.ff_rs = P.ff_rayleigh_stiffness;
+    sp.mass_rm = P.mass_rayleigh_mass;
+    const StepFactors F = step_factors(sp);
+    d.kf_rhs = F.kf_rhs;
     d.rm_factor = -P.rayleigh_mass;
-    d.mf = 1 + 1.0 * h * P.rayleigh_mass;
-    d.kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    d.mf = F.mf_mass;
+    d.kf = F.kf_ff;
     d.vdamp = (P.vdamping != 0.0) ? std::exp(-h * P.vdamping) : 1.0;
     d.tol = P.cg_tolerance;
     d.thr = P.cg_threshold;
@@ -580,14 +596,19 @@ int sgb_batch_step(sgb_batch_t* B, int n_steps)
         L.meshes = B->d_meshes;
         for (int k = 0; k < 3; ++k) L.items[k] = B->d_items[k];
         L.counts = B->d_counts;
-        L.grid_patch = B->grid_patch;
-        L.grid_elem = B->sms * 4;
+        const BatchTiles& T = B->tiles;
+        const int mi = T.matvec_minb == kBatchMatvecMinb[0] ? 0 : (T.matvec_minb == kBatchMatvecMinb[2] ? 2 : 1);
+        L.grid_patch = B->grid_patch_v[mi];
+        L.matvec_minb = kBatchMatvecMinb[mi];
+        L.grid_elem = B->sms * T.elem_ctas;
         L.grid_node = B->sms * 4;
+        L.grid_update = B->sms * T.update_ctas;
+        L.update_npt = T.update_npt;
         L.n_slots = B->max_slots;
         L.grid_slots = std::min(B->max_slots, B->sms * 8);
         L.pe = B->pe;
         L.max_iterations = B->max_iterations;
-        L.prefetch = B->prefetch;
+        L.prefetch = T.prefetch;
         L.err = B->d_err;
         cudaGraph_t g;
         BTRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
@@ -663,6 +684,244 @@ int sgb_batch_set_state(sgb_batch_t* B, int slot, const double* x_host, const do
     if (x_host) BTRY(cudaMemcpyAsync(hm.d.x, x_host, bytes, cudaMemcpyHostToDevice, B->stream));
     if (v_host) BTRY(cudaMemcpyAsync(hm.d.v, v_host, bytes, cudaMemcpyHostToDevice, B->stream));
     BTRY(cudaStreamSynchronize(B->stream));
+    return SGB_OK;
+}
+
+// ---- launch-tile tuner ------------------------------------------------------
+// The batch step's launch tiles (the matvec's register cap, the CG update's
+// nodes per thread and grid, the element kernels' grid, the L2 prefetch) are
+// picked by timing the admitted mix: one coordinate at a time from the
+// current choice, each candidate timed with CUDA events over a few whole
+// steps that all start from the same saved state, which is put back
+// afterwards. Every tile is rounding-neutral, so tuning changes no result.
+// The reference sets its equivalent knobs by hand (gatherPt / gatherBsize of
+// SofaCUDA's TetrahedronFEMForceField). Choices are cached per process by the
+// mix's size histogram, so a batch with the same kind of mix skips the timing.
+
+namespace {
+
+std::mutex g_tile_cache_mutex;
+std::map<std::string, BatchTiles> g_tile_cache;
+
+std::string mix_key(const sgb_batch* B)
+{
+    // meshes per power-of-two size class of their tetrahedron count, the
+    // counts themselves rounded to powers of two
+    int hist[40] = {0};
+    for (auto& m : B->slots)
+        if (m.active) {
+            int b = 0;
+            while (b < 39 && (1LL << (b + 1)) <= (long long)m.n_tets) ++b;
+            hist[b]++;
+        }
+    std::string key = std::to_string(B->precision) + "/" + std::to_string(B->pe) + "/" + std::to_string(B->sms) + ":";
+    for (int b = 0; b < 40; ++b)
+        if (hist[b]) {
+            int q = 0;
+            while ((1 << (q + 1)) <= hist[b]) ++q;
+            key += std::to_string(b) + "x" + std::to_string(q) + ",";
+        }
+    return key;
+}
+
+// What a step changes: every mesh's positions and velocities, the device
+// descriptors (time-step counts, CG scalars, status), the host step counters
+// and the device error flag.
+struct BatchSnapshot {
+    std::vector<BMeshDesc> desc;
+    std::vector<std::vector<double>> x, v;
+    std::vector<long long> steps;
+    int err = 0;
+};
+
+int snapshot_take(sgb_batch* B, BatchSnapshot& S)
+{
+    BTRY(cudaStreamSynchronize(B->stream));
+    S.desc.resize((size_t)B->max_slots);
+    BTRY(cudaMemcpy(S.desc.data(), B->d_meshes, sizeof(BMeshDesc) * B->max_slots, cudaMemcpyDeviceToHost));
+    BTRY(cudaMemcpy(&S.err, B->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    S.x.assign((size_t)B->max_slots, {});
+    S.v.assign((size_t)B->max_slots, {});
+    S.steps.assign((size_t)B->max_slots, 0);
+    for (int i = 0; i < B->max_slots; ++i) {
+        const BatchMeshHost& m = B->slots[(size_t)i];
+        if (!m.active) continue;
+        const size_t n = 3 * (size_t)m.n_nodes;
+        S.x[(size_t)i].resize(n);
+        S.v[(size_t)i].resize(n);
+        BTRY(cudaMemcpy(S.x[(size_t)i].data(), m.d.x, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        BTRY(cudaMemcpy(S.v[(size_t)i].data(), m.d.v, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        S.steps[(size_t)i] = m.steps;
+    }
+    return SGB_OK;
+}
+
+int snapshot_restore(sgb_batch* B, const BatchSnapshot& S)
+{
+    BTRY(cudaStreamSynchronize(B->stream));
+    BTRY(cudaMemcpy(B->d_meshes, S.desc.data(), sizeof(BMeshDesc) * B->max_slots, cudaMemcpyHostToDevice));
+    BTRY(cudaMemcpy(B->d_err, &S.err, sizeof(int), cudaMemcpyHostToDevice));
+    for (int i = 0; i < B->max_slots; ++i) {
+        BatchMeshHost& m = B->slots[(size_t)i];
+        if (!m.active) continue;
+        const size_t n = 3 * (size_t)m.n_nodes;
+        BTRY(cudaMemcpy(m.d.x, S.x[(size_t)i].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        BTRY(cudaMemcpy(m.d.v, S.v[(size_t)i].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        m.steps = S.steps[(size_t)i];
+    }
+    return SGB_OK;
+}
+
+int valid_tiles(const BatchTiles& t)
+{
+    const bool minb = t.matvec_minb == kBatchMatvecMinb[0] || t.matvec_minb == kBatchMatvecMinb[1] ||
+                      t.matvec_minb == kBatchMatvecMinb[2];
+    const bool npt = t.update_npt == 1 || t.update_npt == 2 || t.update_npt == 4;
+    return minb && npt && t.update_ctas >= 1 && t.update_ctas <= 16 && t.elem_ctas >= 1 && t.elem_ctas <= 16 &&
+           (t.prefetch == 0 || t.prefetch == 1);
+}
+
+}  // namespace
+
+int sgb_batch_set_tiles(sgb_batch_t* B, const int tiles[5])
+{
+    if (!B || !tiles) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_set_tiles: NULL argument");
+    BatchTiles t;
+    t.matvec_minb = tiles[0];
+    t.update_npt = tiles[1];
+    t.update_ctas = tiles[2];
+    t.elem_ctas = tiles[3];
+    t.prefetch = tiles[4];
+    if (!valid_tiles(t))
+        return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_set_tiles: matvec CTAs per SM must be 5, 6 or 8, update "
+                                               "nodes per thread 1, 2 or 4, grids 1..16 CTAs per SM, prefetch 0 or 1");
+    B->tiles = t;
+    B->graph_valid = false;
+    return SGB_OK;
+}
+
+int sgb_batch_get_tiles(const sgb_batch_t* B, int tiles[6], double* default_ms, double* best_ms, int* trials)
+{
+    if (!B || !tiles) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_get_tiles: NULL argument");
+    tiles[0] = B->pe;
+    tiles[1] = B->tiles.matvec_minb;
+    tiles[2] = B->tiles.update_npt;
+    tiles[3] = B->tiles.update_ctas;
+    tiles[4] = B->tiles.elem_ctas;
+    tiles[5] = B->tiles.prefetch;
+    if (default_ms) *default_ms = B->tune_default_ms;
+    if (best_ms) *best_ms = B->tune_best_ms;
+    if (trials) *trials = B->tune_trials;
+    return SGB_OK;
+}
+
+int sgb_batch_tune(sgb_batch_t* B, int steps_per_trial, int use_cache)
+{
+    if (!B || steps_per_trial < 1) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_tune: invalid argument");
+    bool any = false;
+    for (auto& m : B->slots) any = any || m.active;
+    if (!any) return SGB_OK;  // nothing admitted: nothing to time
+    const std::string key = mix_key(B);
+    if (use_cache) {
+        std::lock_guard<std::mutex> lk(g_tile_cache_mutex);
+        auto it = g_tile_cache.find(key);
+        if (it != g_tile_cache.end()) {
+            B->tiles = it->second;
+            B->graph_valid = false;
+            B->tune_trials = 0;
+            return SGB_OK;
+        }
+    }
+    BatchSnapshot S;
+    int rc = snapshot_take(B, S);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    BTRY(cudaEventCreate(&e0));
+    BTRY(cudaEventCreate(&e1));
+    int trials = 0;
+    auto trial = [&](const BatchTiles& t, double* ms) -> int {
+        B->tiles = t;
+        B->graph_valid = false;
+        int r = snapshot_restore(B, S);
+        if (!r) r = sgb_batch_step(B, 1);  // records the graph of these tiles; warms up
+        if (!r) r = snapshot_restore(B, S);
+        if (r) return r;
+        BTRY(cudaEventRecord(e0, B->stream));
+        if ((r = sgb_batch_step(B, steps_per_trial))) return r;
+        BTRY(cudaEventRecord(e1, B->stream));
+        BTRY(cudaEventSynchronize(e1));
+        float f = 0.f;
+        BTRY(cudaEventElapsedTime(&f, e0, e1));
+        *ms = (double)f / steps_per_trial;
+        trials++;
+        return SGB_OK;
+    };
+    const BatchTiles start = B->tiles;
+    BatchTiles best = start;
+    double best_ms = 0.0, default_ms = 0.0;
+    rc = trial(best, &best_ms);
+    default_ms = best_ms;
+    // one coordinate at a time; a candidate must win by 1 % to be taken
+    const int minbs[3] = {kBatchMatvecMinb[0], kBatchMatvecMinb[1], kBatchMatvecMinb[2]};
+    const int npts[3] = {4, 2, 1};
+    const int ctas[3] = {2, 4, 8};
+    for (int knob = 0; knob < 5 && !rc; ++knob) {
+        const int n = knob == 4 ? 2 : 3;
+        for (int c = 0; c < n && !rc; ++c) {
+            BatchTiles t = best;
+            if (knob == 0) t.matvec_minb = minbs[c];
+            if (knob == 1) t.update_npt = npts[c];
+            if (knob == 2) t.update_ctas = ctas[c];
+            if (knob == 3) t.elem_ctas = ctas[c];
+            if (knob == 4) t.prefetch = c;
+            if (std::memcmp(&t, &best, sizeof(t)) == 0) continue;
+            double ms = 0.0;
+            rc = trial(t, &ms);
+            if (!rc && ms < 0.99 * best_ms) {
+                best = t;
+                best_ms = ms;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->tiles = rc ? start : best;
+    B->graph_valid = false;
+    const int rr = snapshot_restore(B, S);
+    if (rc) return rc;
+    if (rr) return rr;
+    B->tune_default_ms = default_ms;
+    B->tune_best_ms = best_ms;
+    B->tune_trials = trials;
+    {
+        std::lock_guard<std::mutex> lk(g_tile_cache_mutex);
+        g_tile_cache[key] = best;
+    }
+    return SGB_OK;
+}
+
+int sgb_batch_save_mesh(sgb_batch_t* B, int slot, double* x_host, double* v_host, long long* steps)
+{
+    if (!B || !x_host || !v_host || !steps || slot < 0 || slot >= B->max_slots || !B->slots[(size_t)slot].active)
+        return bfail(SGB_ERR_NOT_FOUND, "sgb_batch_save_mesh: no mesh in that slot, or a NULL output");
+    int rc = sgb_batch_get_state(B, slot, x_host, v_host);
+    if (rc) return rc;
+    *steps = B->slots[(size_t)slot].steps;
+    return SGB_OK;
+}
+
+int sgb_batch_restore_mesh(sgb_batch_t* B, int slot, const double* x_host, const double* v_host, long long steps)
+{
+    if (!B || !x_host || !v_host || steps < 0 || slot < 0 || slot >= B->max_slots ||
+        !B->slots[(size_t)slot].active)
+        return bfail(SGB_ERR_NOT_FOUND, "sgb_batch_restore_mesh: no mesh in that slot, or an invalid argument");
+    int rc = sgb_batch_set_state(B, slot, x_host, v_host);
+    if (rc) return rc;
+    // the solver's time-step count (CGLinearSolver exempts the very first
+    // iteration of the first time step from its tests)
+    BTRY(cudaMemcpy((char*)&B->d_meshes[slot] + offsetof(BMeshDesc, tsc), &steps, sizeof(long long),
+                    cudaMemcpyHostToDevice));
+    B->slots[(size_t)slot].steps = steps;
     return SGB_OK;
 }
 

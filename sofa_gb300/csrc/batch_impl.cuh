@@ -8,7 +8,10 @@
 // mesh's CG scalars (CGLinearSolver::solve, Sofa/Component/LinearSolver/
 // Iterative/src/sofa/component/linearsolver/iterative/CGLinearSolver.inl:
 // 102-272); the once-per-step start of CG reduces with a per-mesh ticket.
-// Meshes whose CG has stopped skip their items.
+// Meshes whose CG has stopped skip their items. Every partial belongs to one
+// work item (a patch or a node chunk) and is formed in an order fixed by the
+// item alone, so neither the grid sizes nor the register caps and nodes per
+// thread the tile tuner picks change a single bit of the results.
 //
 // Included by the variant translation units after tfem_impl.cuh, inside
 // SGB_NS, for R = float (mixed) and R = double (FP64 with FMA).
@@ -17,9 +20,6 @@
 namespace SGB_NS {
 
 constexpr int kBatchThreads = 256;
-#ifndef KB_MATVEC_MIN_BLOCKS
-#define KB_MATVEC_MIN_BLOCKS 6
-#endif
 
 template <typename R>
 __device__ __forceinline__ ElemView<R> bm_elem_view(const BMeshDesc& m)
@@ -60,6 +60,41 @@ __device__ __forceinline__ bool bm_cg_skip(const BMeshDesc& m, int it)
     return m.done || it > m.cg_iterations || !m.active;
 }
 
+// Canonical sum of a node chunk's per-node terms: the terms of nodes
+// 32g .. 32g+31 (chunk-local) are added as a balanced pairwise tree,
+// neighbours first, and the chunk's group sums are then added in group order.
+// A thread holding NPT consecutive nodes adds the first log2(NPT) tree levels
+// itself and the warp butterfly adds the rest, so every group sum -- and the
+// chunk sum -- is the same for NPT = 1, 2 or 4 (IEEE addition is
+// commutative). group_tree_store: this thread's NPT terms (node order) of
+// the pass starting at chunk-local node `base`; every thread of the block
+// calls it. Groups past the chunk's end hold zeros.
+template <int NPT>
+__device__ __forceinline__ void group_tree_store(const double t[NPT], int base, double* gsum)
+{
+    double v;
+    if constexpr (NPT == 4)
+        v = (t[0] + t[1]) + (t[2] + t[3]);
+    else if constexpr (NPT == 2)
+        v = t[0] + t[1];
+    else
+        v = t[0];
+    constexpr int lanes = 32 / NPT;  // lanes holding one group of 32 nodes
+#pragma unroll
+    for (int o = 1; o < lanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x % lanes) == 0) gsum[(base + (int)threadIdx.x * NPT) / 32] = v;
+}
+
+// The chunk sum from its group sums, in group order (thread 0), after a
+// block barrier.
+__device__ __forceinline__ double groups_sum(const double* gsum, int n_groups)
+{
+    double total = 0.0;
+    if (threadIdx.x == 0)
+        for (int g = 0; g < n_groups; ++g) total += gsum[g];
+    return total;
+}
+
 // Block-wide: store this item's partial, take the mesh's ticket; when this
 // is the mesh's last item, returns true in every thread with the mesh total
 // in `total` (valid in thread 0).
@@ -84,46 +119,12 @@ __device__ __forceinline__ bool bm_ticket_sum(double mine, double* partials, int
     return true;
 }
 
-// A block's share of one mesh's dot product. Each mesh's items are
-// contiguous in every work list and blocks stride through a list by the grid
-// size, so the items a block takes of one mesh are consecutive in its loop:
-// the block reduces once per mesh, into partial slot `first` (the mesh-local
-// index of its first item of that mesh, which is below min(grid, items of
-// the mesh)). The mesh's ticket counts min(grid, items) arrivals, and the
-// last arrival adds the partials in index order.
-struct BlockRun {
-    int slot;
-    int first;
-    double acc;  // this thread's share
-    __device__ BlockRun() : slot(-1), first(0), acc(0.0) {}
-    __device__ void open(int s, int f)
-    {
-        slot = s;
-        first = f;
-        acc = 0.0;
-    }
-};
-
-__device__ __forceinline__ bool bm_run_sum(const BlockRun& run, double* partials, unsigned int* ticket, int count,
-                                           double* total)
-{
-    const int arrivals = count < (int)gridDim.x ? count : (int)gridDim.x;
-    return bm_ticket_sum(run.acc, partials, run.first, ticket, arrivals, total);
-}
-
-// Stores the block's share of a run at partial slot `first` (no ticket: a
-// later kernel adds the mesh's min(grid, items) partials).
-__device__ __forceinline__ void bm_run_store(const BlockRun& run, double* partials)
-{
-    const double tot = block_sum(run.acc);
-    if (threadIdx.x == 0) partials[run.first] = tot;
-}
-
-// CG start: rho = r.r, |b| (every block that took items of the mesh calls it)
-__device__ __forceinline__ void rhs_done(BMeshDesc& m, const BlockRun& run)
+// CG start: rho = r.r, |b|. Every node chunk of the mesh calls it with its
+// share; the last one to arrive adds the chunk partials in chunk order.
+__device__ __forceinline__ void rhs_done(BMeshDesc& m, int chunk, double mine)
 {
     double total;
-    if (bm_run_sum(run, m.chunk_sum, &m.ticket_rhs, m.n_chunks, &total) && threadIdx.x == 0) {
+    if (bm_ticket_sum(mine, m.chunk_sum, chunk, &m.ticket_rhs, m.n_chunks, &total) && threadIdx.x == 0) {
         m.rho = total;
         m.normb = sqrt(total);
         m.iters = 0;
@@ -226,14 +227,8 @@ __global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, con
                                                                const int* __restrict__ counts)
 {
     const int L = counts[WL_NODE];
-    BlockRun run;
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem it = items[w];
-        if (run.slot >= 0 && it.slot != run.slot) {
-            rhs_done(M[run.slot], run);
-            run.slot = -1;
-        }
-        if (run.slot < 0) run.open(it.slot, it.c);
         BMeshDesc& m = M[it.slot];
         const R* ef = (const R*)m.eforce;
         const R* f = (const R*)m.f;
@@ -269,14 +264,15 @@ __global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, con
             }
             dlocal += (double)(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
         }
-        run.acc += dlocal;
+        rhs_done(m, it.c, dlocal);  // the chunk's partial at its own index
     }
-    if (run.slot >= 0) rhs_done(M[run.slot], run);
 }
 
 // ---- CG matvec over patches ------------------------------------------------
-template <typename R, int MODE>
-__global__ void __launch_bounds__(kPatchThreads, KB_MATVEC_MIN_BLOCKS) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
+// MINB: resident CTAs per SM the register cap is set for (a tile of the
+// tuner; the arithmetic is the same for every value)
+template <typename R, int MODE, int MINB>
+__global__ void __launch_bounds__(kPatchThreads, MINB) kb_matvec(BMeshDesc* M, const WorkItem* __restrict__ items,
                                                            const int* __restrict__ counts, int it, int pe,
                                                            int prefetch)
 {
@@ -291,17 +287,13 @@ __global__ void __launch_bounds__(kPatchThreads, KB_MATVEC_MIN_BLOCKS) kb_matvec
     __shared__ ElemView<R> sev;
     __shared__ PatchArgs<R> sa;
     const int L = counts[WL_PATCH];
-    BlockRun run;
+    int open_slot = -1;
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem wi = items[w];
-        if (run.slot >= 0 && wi.slot != run.slot) {
-            bm_run_store(run, M[run.slot].patch_energy);
-            run.slot = -1;
-        }
         BMeshDesc& m = M[wi.slot];
         if (bm_cg_skip(m, it)) continue;  // uniform over the block
-        if (run.slot < 0) {
-            run.open(wi.slot, wi.a);
+        if (open_slot != wi.slot) {
+            open_slot = wi.slot;
             // the previous patch ended with a block barrier: no thread still
             // reads the shared copies
             if (threadIdx.x == 0) {
@@ -331,27 +323,23 @@ __global__ void __launch_bounds__(kPatchThreads, KB_MATVEC_MIN_BLOCKS) kb_matvec
                 prefetch_patch(bm_patch_view(nm, pe), bm_elem_view<R>(nm), ni.a);
             }
         }
-        run.acc += (double)patch_body<R, MODE>(spv, sev, wi.a, sa, ef, lp, sl, lr);
+        // the patch's p^T A p share, stored at the patch's own index
+        const double e = block_sum((double)patch_body<R, MODE>(spv, sev, wi.a, sa, ef, lp, sl, lr));
+        if (threadIdx.x == 0) m.patch_energy[wi.a] = e;
     }
-    if (run.slot >= 0) bm_run_store(run, M[run.slot].patch_energy);
 }
 
 // ---- CG update: shared-node q, x += alpha p, r -= alpha q, rho -------------
-template <typename R>
+template <typename R, int NPT>
 __global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const WorkItem* __restrict__ items,
                                                            const int* __restrict__ counts, int it)
 {
+    __shared__ double gsum[kBatchNodeChunk / 32];
     const int L = counts[WL_NODE];
-    BlockRun run;
     for (int w = blockIdx.x; w < L; w += gridDim.x) {
         const WorkItem wi = items[w];
-        if (run.slot >= 0 && wi.slot != run.slot) {
-            bm_run_store(run, M[run.slot].chunk_sum);
-            run.slot = -1;
-        }
         BMeshDesc& m = M[wi.slot];
-        if (bm_cg_skip(m, it)) continue;
-        if (run.slot < 0) run.open(wi.slot, wi.c);
+        if (bm_cg_skip(m, it)) continue;  // uniform over the block
         const R alpha = (R)m.alpha;
         const R* p = (const R*)((it & 1) ? m.p0 : m.p1);
         const R* q = (const R*)m.q;
@@ -360,25 +348,37 @@ __global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const W
         R* r = (R*)m.r;
         const double mf = m.mf;
         const R mmu = (R)(mf != 1.0 ? m.vertex_mass * mf : m.vertex_mass);
-        double local = 0.0;
-        if constexpr (is_mixed<R>::value) {
-            // chunks start at multiples of 4 nodes: groups of four, then the
-            // chunk's last N % 4 nodes one per thread
-            const int g0 = wi.a >> 2, g1 = wi.b >> 2;
-            for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x)
-                local += cg_update4(4 * (size_t)g, xs, r, p, q, partials, m.bnd_rowptr, m.node_mass, mmu, mf, m.fixed,
-                                    alpha);
-            for (int n = 4 * g1 + threadIdx.x; n < wi.b; n += blockDim.x)
-                local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, m.bnd_rowptr, m.node_mass, mmu, mf,
-                                               m.fixed, alpha);
-        } else {
-            for (int n = wi.a + threadIdx.x; n < wi.b; n += blockDim.x)
-                local += (double)cg_update1<R>((size_t)n, xs, r, p, q, partials, m.bnd_rowptr, m.node_mass, mmu, mf,
-                                               m.fixed, alpha);
+        // chunk-local passes of blockDim * NPT nodes; thread t takes NPT
+        // consecutive nodes of each pass
+        for (int base = 0; base < kBatchNodeChunk; base += kBatchThreads * NPT) {
+            const int n0 = wi.a + base + (int)threadIdx.x * NPT;
+            double t[NPT];
+            if constexpr (is_mixed<R>::value && NPT == 4) {
+                if (n0 + 4 <= wi.b) {
+                    cg_update4_terms(4 * (size_t)(n0 >> 2), xs, r, p, q, partials, m.bnd_rowptr, m.node_mass, mmu, mf,
+                                     m.fixed, alpha, t);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        t[j] = (n0 + j < wi.b)
+                                   ? (double)cg_update1<R>((size_t)(n0 + j), xs, r, p, q, partials, m.bnd_rowptr,
+                                                           m.node_mass, mmu, mf, m.fixed, alpha)
+                                   : 0.0;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < NPT; ++j)
+                    t[j] = (n0 + j < wi.b) ? (double)cg_update1<R>((size_t)(n0 + j), xs, r, p, q, partials,
+                                                                   m.bnd_rowptr, m.node_mass, mmu, mf, m.fixed, alpha)
+                                           : 0.0;
+            }
+            group_tree_store<NPT>(t, base, gsum);
         }
-        run.acc += local;
+        __syncthreads();
+        const double tot = groups_sum(gsum, kBatchNodeChunk / 32);
+        if (threadIdx.x == 0) m.chunk_sum[wi.c] = tot;  // the chunk's partial at its own index
+        __syncthreads();
     }
-    if (run.slot >= 0) bm_run_store(run, M[run.slot].chunk_sum);
 }
 
 // ---- per-mesh CG scalars of one iteration ----------------------------------
@@ -390,14 +390,14 @@ __global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const W
 // WHAT 0, after the matvec: den = p.Ap, the threshold test, alpha.
 // WHAT 1, after the update: rho = r.r, beta, the tolerance and iteration tests.
 template <int WHAT>
-__global__ void __launch_bounds__(kBatchThreads) kb_cg_scalars(BMeshDesc* M, int n_slots, int it, int grid_items)
+__global__ void __launch_bounds__(kBatchThreads) kb_cg_scalars(BMeshDesc* M, int n_slots, int it)
 {
     for (int s = blockIdx.x; s < n_slots; s += gridDim.x) {
         BMeshDesc& m = M[s];
         if (bm_cg_skip(m, it)) continue;  // uniform over the block
         const double* part = (WHAT == 0) ? m.patch_energy : m.chunk_sum;
         const int items_m = (WHAT == 0) ? m.n_patches : m.n_chunks;
-        const int n = items_m < grid_items ? items_m : grid_items;  // one partial per block run
+        const int n = items_m;  // one partial per item
         // thread t adds entries t, t + blockDim, ... in that order; eight
         // loads are issued before their additions
         double v = 0.0;
@@ -478,27 +478,68 @@ size_t batch_patch_smem(int pe)
     return patch_smem_size<R>(pe, kBatchMaxLocalNodes);
 }
 
+// Kernel attributes of the batch step; grid_patch[i]: resident matvec CTAs
+// over the device for the register-cap variant kBatchMatvecMinb[i]. Returns
+// the SM count, -1 on failure.
+template <typename R, int MINB>
+int matvec_grid(size_t smem, int sms)
+{
+    int nb1 = 0, nb2 = 0;
+    if (cudaFuncSetAttribute(kb_matvec<R, 1, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(kb_matvec<R, 2, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return -1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, kb_matvec<R, 1, MINB>, kPatchThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, kb_matvec<R, 2, MINB>, kPatchThreads, smem);
+    const int nb = nb1 < nb2 ? nb1 : nb2;
+    return (nb < 1 ? 1 : nb) * sms;
+}
+
 template <typename R>
 int batch_prepare(int pe, int* grid_patch)
 {
     const size_t smem = batch_patch_smem<R>(pe);
-    int dev = 0, sms = 0, nb1 = 0, nb2 = 0;
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaFuncSetAttribute(kb_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaFuncSetAttribute(kb_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return -1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, kb_matvec<R, 1>, kPatchThreads, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, kb_matvec<R, 2>, kPatchThreads, smem);
-    int nb = nb1 < nb2 ? nb1 : nb2;
-    *grid_patch = (nb < 1 ? 1 : nb) * sms;
+    grid_patch[0] = matvec_grid<R, kBatchMatvecMinb[0]>(smem, sms);
+    grid_patch[1] = matvec_grid<R, kBatchMatvecMinb[1]>(smem, sms);
+    grid_patch[2] = matvec_grid<R, kBatchMatvecMinb[2]>(smem, sms);
+    if (grid_patch[0] < 0 || grid_patch[1] < 0 || grid_patch[2] < 0) return -1;
     return sms;
+}
+
+template <typename R, int MODE>
+void launch_kb_matvec(const BatchLaunch& B, size_t smem, int it, cudaStream_t s)
+{
+    const WorkItem* pit = B.items[WL_PATCH];
+    if (B.matvec_minb == kBatchMatvecMinb[0])
+        kb_matvec<R, MODE, kBatchMatvecMinb[0]>
+            <<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe, B.prefetch);
+    else if (B.matvec_minb == kBatchMatvecMinb[2])
+        kb_matvec<R, MODE, kBatchMatvecMinb[2]>
+            <<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe, B.prefetch);
+    else
+        kb_matvec<R, MODE, kBatchMatvecMinb[1]>
+            <<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe, B.prefetch);
+}
+
+template <typename R>
+void launch_kb_update(const BatchLaunch& B, int it, cudaStream_t s)
+{
+    const WorkItem* nit = B.items[WL_NODE];
+    if (B.update_npt == 1)
+        kb_update<R, 1><<<B.grid_update, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
+    else if (B.update_npt == 2)
+        kb_update<R, 2><<<B.grid_update, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
+    else
+        kb_update<R, 4><<<B.grid_update, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
 }
 
 template <typename R>
 void batch_record_step(const BatchLaunch& B, cudaStream_t s)
 {
-    const WorkItem* pit = B.items[WL_PATCH];
     const WorkItem* eit = B.items[WL_ELEM];
     const WorkItem* nit = B.items[WL_NODE];
     kb_force_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
@@ -508,14 +549,12 @@ void batch_record_step(const BatchLaunch& B, cudaStream_t s)
     const size_t smem = batch_patch_smem<R>(B.pe);
     for (int it = 1; it <= B.max_iterations; ++it) {
         if (it == 1)
-            kb_matvec<R, 1><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe,
-                                                                      B.prefetch);
+            launch_kb_matvec<R, 1>(B, smem, it, s);
         else
-            kb_matvec<R, 2><<<B.grid_patch, kPatchThreads, smem, s>>>(B.meshes, pit, B.counts, it, B.pe,
-                                                                      B.prefetch);
-        kb_cg_scalars<0><<<B.grid_slots, kBatchThreads, 0, s>>>(B.meshes, B.n_slots, it, B.grid_patch);
-        kb_update<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts, it);
-        kb_cg_scalars<1><<<B.grid_slots, kBatchThreads, 0, s>>>(B.meshes, B.n_slots, it, B.grid_node);
+            launch_kb_matvec<R, 2>(B, smem, it, s);
+        kb_cg_scalars<0><<<B.grid_slots, kBatchThreads, 0, s>>>(B.meshes, B.n_slots, it);
+        launch_kb_update<R>(B, it, s);
+        kb_cg_scalars<1><<<B.grid_slots, kBatchThreads, 0, s>>>(B.meshes, B.n_slots, it);
     }
     kb_euler<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
 }

@@ -70,8 +70,11 @@ struct sgb_batch {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
-    int sms = 152, grid_patch = 152;
-    int prefetch = 0;  // FP32 matvec: the block's next patch into L2 while this one computes (measured slower)
+    int sms = 152;
+    int grid_patch_v[3] = {152, 152, 152};  // resident matvec CTAs per register-cap variant (kBatchMatvecMinb)
+    sgb::BatchTiles tiles;                  // launch tiles (set by sgb_batch_tune / sgb_batch_set_tiles)
+    double tune_default_ms = 0.0, tune_best_ms = 0.0;  // last tuning: step time of the default and chosen tiles
+    int tune_trials = 0;                    // configurations timed by the last tuning (0: from the cache)
     size_t device_bytes = 0;
 };
 

@@ -123,6 +123,10 @@ static void free_mesh(TfemMesh& m)
     cudaFree(m.pl.bnd_rowptr);
     cudaFree(m.pl.partials);
     cudaFree(m.dev_flags);
+    cudaFree(m.rotq);
+    cudaFree(m.emat);
+    cudaFree(m.nrest_hi);
+    cudaFree(m.nrest_lo);
     m = TfemMesh();
 }
 
@@ -240,6 +244,20 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     if ((ce = cudaMemsetAsync(m.dev_flags, 0, sizeof(int), h->stream)) != cudaSuccess) {
         rc = cuda_fail(ce, "cudaMemsetAsync");
         goto fail_out;
+    }
+    // compact FP32 matvec (mixed large / polar with patches; SGB_MATVEC_COMPACT=0
+    // keeps the stored 64-byte element format in the matvec)
+    if (precision == SGB_PRECISION_MIXED && !L.elem_start.empty() &&
+        (method == SGB_METHOD_LARGE || method == SGB_METHOD_POLAR)) {
+        const char* e = getenv("SGB_MATVEC_COMPACT");
+        m.compact = (e && e[0] == '0') ? 0 : 1;
+    }
+    if (m.compact) {
+        const bool uniform = E_h.size() == 1 && nu_h.size() == 1 && n_lsf == 0;
+        if ((rc = dev_alloc(&m.rotq, E, acc)) || (rc = dev_alloc(&m.nrest_hi, (size_t)n_nodes, acc)) ||
+            (rc = dev_alloc(&m.nrest_lo, (size_t)n_nodes, acc)) || (!uniform && (rc = dev_alloc(&m.emat, E, acc))))
+            goto fail_out;
+        if (uniform) m.cmat = compact_material(E_h[0], nu_h[0]);
     }
     if (!L.elem_start.empty()) {
         PatchLayout& pl = m.pl;
@@ -825,6 +843,10 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
         return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: a preconditioner needs linear_solver = PCG");
     if (P.warm_start && P.residual_replacement > 0)
         return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_create: residual replacement starts each solve from x = 0");
+    if (P.first_order && P.residual_replacement > 0)
+        return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_create: residual replacement runs the second-order scheme");
+    if (!std::isfinite(P.ff_rayleigh_stiffness) || !std::isfinite(P.mass_rayleigh_mass))
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_create: non-finite component Rayleigh coefficient");
     if (P.linear_solver == SGB_SOLVER_PCG && P.residual_replacement > 0)
         return fail(SGB_ERR_NOT_SUPPORTED, "sgb_scene_create: residual replacement runs with CG only");
     if (P.residual_replacement > 0 &&
@@ -850,6 +872,10 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     s.prm.precond = P.preconditioner;
     s.prm.precond_rate = P.preconditioner_rate > 1 ? P.preconditioner_rate : 1;
     s.prm.warm_start = P.warm_start ? 1 : 0;
+    s.prm.ff_rs = P.ff_rayleigh_stiffness;
+    s.prm.mass_rm = P.mass_rayleigh_mass;
+    s.prm.first_order = P.first_order ? 1 : 0;
+    s.prm.project_velocity = P.project_velocity ? 1 : 0;
     s.stream = fem->stream;
     sc->fem = fem;
     sc->ops = fem->ops;

@@ -151,6 +151,20 @@ int sgb_sofa_scene_animate(sgb_sofa_scene_t* scene, int n_steps)
     return rc ? fail(rc, err) : SGB_OK;
 }
 
+int sgb_sofa_scene_reset(sgb_sofa_scene_t* scene)
+{
+    if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_reset: NULL scene");
+    std::string err;
+    int rc = scene->scene.reset(&err);
+    return rc ? fail(rc, err) : SGB_OK;
+}
+
+int sgb_sofa_scene_unload(sgb_sofa_scene_t* scene)
+{
+    if (!scene) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_unload: NULL scene");
+    return scene->scene.unload();
+}
+
 int sgb_sofa_scene_get_positions(sgb_sofa_scene_t* scene, int body, double* x_host)
 {
     if (!scene || !x_host || body < 0 || body >= (int)scene->scene.bodies.size())

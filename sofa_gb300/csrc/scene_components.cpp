@@ -504,6 +504,14 @@ public:
         if (path.empty()) path = "defaultExportFile";
     }
 
+    // WriteState::reset (WriteState.inl:231-238): the next record is again
+    // the first export time
+    void rewind()
+    {
+        next = 0;
+        last_time = 0.0;
+    }
+
     // AnimateBeginEvent at simulation time t: writes the state if due.
     int begin_step(Scene& s, double t, std::string* err)
     {
@@ -704,17 +712,19 @@ int Scene::init_host(std::string* err)
         if (b.von_mises_mode == 1 && b.method == SGB_METHOD_SMALL)
             return unsupported(err, where + "computeVonMisesStress=1 (corotational strain) needs method large, polar "
                                             "or svd (TetrahedronFEMForceField.inl:1441-1445)");
-        if (fem->get_real(*this, "rayleighStiffness") != 0.0)
-            return unsupported(err, where + "a force-field rayleighStiffness is not supported (use the solver's)");
         b.young = fem->get_reals(*this, "youngModulus");
         b.poisson = fem->get_reals(*this, "poissonRatio");
         const int fallback = precision_of(fem->template_name, SGB_PRECISION_FP64);
         b.precision = precision_override >= 0 ? precision_override : precision_of(mo->template_name, fallback);
         // EulerImplicitSolver + CGLinearSolver
-        if (euler->get_bool(*this, "firstOrder") || euler->get_bool(*this, "trapezoidalScheme"))
-            return unsupported(err, where + "firstOrder / trapezoidalScheme are not supported");
+        if (euler->get_bool(*this, "trapezoidalScheme"))
+            return unsupported(err, where + "trapezoidalScheme is not supported");
         sgb_scene_params_default(&b.params);
         b.params.dt = dt;
+        b.params.first_order = euler->get_bool(*this, "firstOrder") ? 1 : 0;
+        // the force field's own rayleighStiffness (BaseForceField.cpp:34): its
+        // addDForce factor is kFactorIncludingRayleighDamping
+        b.params.ff_rayleigh_stiffness = fem->get_real(*this, "rayleighStiffness");
         b.params.rayleigh_stiffness = euler->get_real(*this, "rayleighStiffness");
         b.params.rayleigh_mass = euler->get_real(*this, "rayleighMass");
         b.params.vdamping = euler->get_real(*this, "vdamping");
@@ -742,8 +752,9 @@ int Scene::init_host(std::string* err)
         for (int k = 0; k < 3; ++k) b.params.gravity[k] = gravity[k];
         // mass
         if (!mass) return unsupported(err, where + "no mass component (UniformMass or DiagonalMass)");
-        if (mass->get_real(*this, "rayleighMass") != 0.0)
-            return unsupported(err, where + "a mass-component rayleighMass is not supported (use the solver's)");
+        // the mass's own rayleighMass (BaseMass.cpp:33-34): its addMDx factor
+        // is mFactorIncludingRayleighDamping
+        b.params.mass_rayleigh_mass = mass->get_real(*this, "rayleighMass");
         if (mass->class_name() == "UniformMass") {
             // UniformMass::init: totalMass wins over vertexMass when both are
             // set; neither set is an error (UniformMass.inl:233-268)
@@ -759,14 +770,20 @@ int Scene::init_host(std::string* err)
         b.params.mass_first = mass_pos < fem_pos ? 1 : 0;
         // fixed points
         std::set<int> fx;
+        int n_project = 0;
         for (BaseObject* f : fixed) {
             if (f->get_bool(*this, "fixAll")) b.params.fix_all = 1;
-            if (f->get_bool(*this, "activate_projectVelocity"))
-                return unsupported(err, where + "activate_projectVelocity is not supported");
+            if (f->get_bool(*this, "activate_projectVelocity")) n_project++;
             for (int i : f->out_ints["indices"])
                 if (i >= 0 && (size_t)i < N) fx.insert(i);
         }
         b.fixed.assign(fx.begin(), fx.end());
+        // projectVelocity zeroes the velocity of a component's own indices; the
+        // library applies it to every fixed node, so the components must agree
+        if (n_project > 0 && n_project < (int)fixed.size())
+            return unsupported(err, where + "activate_projectVelocity must be set on every "
+                                            "FixedProjectiveConstraint of the node or on none");
+        b.params.project_velocity = n_project > 0 ? 1 : 0;
         auto fe = mo->out_reals.find("externalForce");
         if (fe != mo->out_reals.end()) b.external_force = fe->second;
         if (x0.size() == b.rest.size() && x0 != b.rest) mo->out_reals["initial_position"] = x0;
@@ -803,6 +820,7 @@ int Scene::init_device(std::string* err)
             sgb_tfem_destroy(fem);
             return rc;
         }
+        b.fem = fem;
         if (!b.external_force.empty() && (rc = sgb_scene_set_external_force(b.scene, b.external_force.data()))) {
             *err = sgb_last_error();
             return rc;
@@ -829,6 +847,63 @@ static void collect_writers(Node* n, std::vector<WriteState*>& out)
     for (auto& o : n->objects)
         if (auto* w = dynamic_cast<WriteState*>(o.get())) out.push_back(w);
     for (auto& c : n->children) collect_writers(c.get(), out);
+}
+
+// The reset state of a body's MechanicalObject (MechanicalObject::
+// storeResetState, MechanicalObject.inl:1180-1200): its initial positions, and
+// its initial velocities when they are not all zero (else zero).
+static void reset_state(const Body& b, std::vector<double>& x, std::vector<double>& v)
+{
+    x = b.rest;
+    v.assign(b.rest.size(), 0.0);
+    for (auto& o : b.node->objects)
+        if (o->class_name() == "MechanicalObject") {
+            auto it = o->out_reals.find("initial_position");
+            if (it != o->out_reals.end() && it->second.size() == x.size()) x = it->second;
+            auto iv = o->out_reals.find("velocity");
+            if (iv != o->out_reals.end() && iv->second.size() == v.size()) v = iv->second;
+            break;
+        }
+}
+
+int Scene::reset(std::string* err)
+{
+    // MechanicalObject::reset (MechanicalObject.inl:1204-1225), the force
+    // field's plastic strains (TetrahedronFEMForceField::reset,
+    // TetrahedronFEMForceField.inl:1382-1388), WriteState::reset
+    // (WriteState.inl:231-238). The solvers keep their own state, as the
+    // reference's CGLinearSolver (which has no reset) keeps its time-step count.
+    for (auto& b : bodies) {
+        if (!b.scene) continue;
+        std::vector<double> x, v;
+        reset_state(b, x, v);
+        int rc = sgb_scene_set_state(b.scene, x.data(), v.data());
+        if (!rc && b.plastic_max > 0.0 && b.fem) rc = sgb_tfem_reset_plasticity(b.fem);
+        if (rc) {
+            *err = sgb_last_error();
+            return rc;
+        }
+    }
+    std::vector<WriteState*> writers;
+    if (root) collect_writers(root.get(), writers);
+    for (WriteState* w : writers) w->rewind();
+    time = 0.0;
+    return SGB_OK;
+}
+
+int Scene::unload()
+{
+    for (auto& b : bodies) {
+        if (b.scene) sgb_scene_destroy(b.scene);
+        b.scene = nullptr;
+        b.fem = nullptr;
+    }
+    device_ready = false;
+    time = 0.0;
+    std::vector<WriteState*> writers;
+    if (root) collect_writers(root.get(), writers);
+    for (WriteState* w : writers) w->rewind();
+    return SGB_OK;
 }
 
 int Scene::animate(int n_steps, std::string* err)

@@ -141,6 +141,7 @@ struct Body {
     std::vector<int32_t> fixed;
     std::vector<double> external_force;  // n x 3 or empty
     sgb_scene_t* scene = nullptr;
+    sgb_tfem_t* fem = nullptr;  // the scene's force field (owned by the scene)
 };
 
 // A parsed scene: the node tree, its host initialisation and the bodies.
@@ -170,6 +171,13 @@ public:
     int init_host(std::string* err);
     int init_device(std::string* err);
     int animate(int n_steps, std::string* err);
+    // sofa::simulation::node::reset: states back to their reset values, plastic
+    // strains cleared, writers rewound, time 0 (device objects kept)
+    int reset(std::string* err);
+    // sofa::simulation::node::unload's counterpart for the device: every
+    // body's GPU objects released; the parsed scene stays and the next
+    // animate starts again from the initial state
+    int unload();
     std::string describe() const;
 };
 

@@ -10,6 +10,16 @@
 // and memory freed, and its latency (submission to completion) recorded;
 // requests that arrive meanwhile join at the next launch boundary. The batch
 // handle is used by the scheduler thread only.
+//
+// Admission policy: strict arrival order with head-of-line blocking -- the
+// oldest waiting request is admitted as soon as a slot and a contiguous
+// block of the HBM budget fit it, and nothing behind it is admitted first
+// (a request larger than the whole budget fails instead of blocking).
+// Requests can be cancelled (dropped from the queue at once, or removed from
+// the GPU at the next launch boundary) and evicted (their state saved to host
+// memory and their slot freed at the next launch boundary; they re-enter the
+// queue behind the waiting requests and continue bit-exactly once admitted
+// again).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,6 +30,7 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -43,9 +54,17 @@ struct Pending {
     int prep_rc = SGB_OK;
     std::string prep_err;
     bool prepared = false;
+    bool in_worker = false;  // a preparation worker holds it
+    bool cancelled = false;
+    // an evicted request: the state to resume from and the steps left
+    bool resume = false;
+    std::vector<double> sx, sv;
+    long long saved_steps = 0;
+    int remaining = 0;
 };
 
 struct Running {
+    sgb_request req;
     uint64_t id = 0;
     int slot = -1;
     int remaining = 0;
@@ -73,8 +92,11 @@ struct sgb_server {
     std::vector<Running> running;          // scheduler thread only
     std::vector<sgb_completion> done;      // completions not yet polled
     std::vector<double> latencies;         // all completions
+    std::vector<double> step_ms;           // one entry per step of every launch
+    std::set<uint64_t> running_ids;        // requests on the GPU (kept by the scheduler)
+    std::set<uint64_t> cancel_running, evict_running;  // asked for, done at the next launch boundary
     long long tet_steps = 0;
-    long long completed = 0, failed = 0, submitted = 0;
+    long long completed = 0, failed = 0, submitted = 0, launches = 0, cancelled = 0, evicted = 0;
     double busy_s = 0.0;
     Clock::time_point first_submit;
     bool have_first = false;
@@ -83,6 +105,9 @@ struct sgb_server {
     std::thread scheduler;
     std::atomic<int> in_flight{0};
 };
+
+static void complete(sgb_server* S, uint64_t id, int status, Clock::time_point submitted, Clock::time_point admitted,
+                     int iters, long long tets, int steps);
 
 static void prep_worker(sgb_server* S)
 {
@@ -94,14 +119,26 @@ static void prep_worker(sgb_server* S)
             if (S->stop && S->incoming.empty()) return;
             p = S->incoming.front();
             S->incoming.pop_front();
+            p->in_worker = true;
         }
         const int rc = prepare_mesh(&p->req.mesh, S->batch->pe, S->batch->rs, p->pm);
         std::string err = rc ? std::string(sgb_last_error()) : std::string();
+        bool drop = false;
         {
             std::lock_guard<std::mutex> lk(S->mu);
             p->prep_rc = rc;
             p->prep_err = err;
             p->prepared = true;
+            p->in_worker = false;
+            if (p->cancelled) {  // cancelled while it was being prepared
+                S->ordered.erase(p->seq);
+                drop = true;
+            }
+        }
+        if (drop) {
+            complete(S, p->req.id, SGB_ERR_CANCELLED, p->submitted, Clock::now(), 0, 0, 0);
+            delete p;
+            continue;
         }
         S->cv_sched.notify_one();
     }
@@ -126,6 +163,8 @@ static void complete(sgb_server* S, uint64_t id, int status, Clock::time_point s
             S->latencies.push_back(c.latency_ms);
             S->completed++;
             S->tet_steps += tets * steps;
+        } else if (status == SGB_ERR_CANCELLED) {
+            S->cancelled++;
         } else {
             S->failed++;
         }
@@ -134,10 +173,69 @@ static void complete(sgb_server* S, uint64_t id, int status, Clock::time_point s
     S->cv_idle.notify_all();
 }
 
+// Cancellations and evictions of running requests, at a launch boundary
+// (scheduler thread).
+static void handle_running_requests(sgb_server* S)
+{
+    sgb_batch* B = S->batch;
+    std::set<uint64_t> cancel, evict;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        cancel.swap(S->cancel_running);
+        evict.swap(S->evict_running);
+    }
+    if (cancel.empty() && evict.empty()) return;
+    std::vector<Running> keep;
+    for (auto& r : S->running) {
+        if (cancel.count(r.id)) {
+            sgb_batch_remove_mesh(B, r.slot);
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->running_ids.erase(r.id);
+            }
+            complete(S, r.id, SGB_ERR_CANCELLED, r.submitted, r.admitted, 0, r.tets, 0);
+        } else if (evict.count(r.id)) {
+            Pending* p = new Pending();
+            p->req = r.req;
+            p->submitted = r.submitted;
+            p->resume = true;
+            p->remaining = r.remaining;
+            p->sx.resize(3 * (size_t)r.req.mesh.n_nodes);
+            p->sv.resize(3 * (size_t)r.req.mesh.n_nodes);
+            const int rc = sgb_batch_save_mesh(B, r.slot, p->sx.data(), p->sv.data(), &p->saved_steps);
+            sgb_batch_remove_mesh(B, r.slot);
+            if (rc != SGB_OK) {
+                delete p;
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->running_ids.erase(r.id);
+                }
+                complete(S, r.id, rc, r.submitted, r.admitted, 0, r.tets, 0);
+                continue;
+            }
+            {
+                // back into the queue, behind the requests already waiting;
+                // the mesh layout is prepared again from its description
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->running_ids.erase(r.id);
+                p->seq = S->next_seq++;
+                S->ordered[p->seq] = p;
+                S->incoming.push_back(p);
+                S->evicted++;
+            }
+            S->cv_prep.notify_one();
+        } else {
+            keep.push_back(r);
+        }
+    }
+    S->running.swap(keep);
+}
+
 static void scheduler_loop(sgb_server* S)
 {
     sgb_batch* B = S->batch;
     for (;;) {
+        handle_running_requests(S);
         // admission, in arrival order, while the head fits
         std::vector<Pending*> to_admit;
         {
@@ -182,20 +280,27 @@ static void scheduler_loop(sgb_server* S)
                 continue;
             }
             int slot = -1;
-            const int rc = admit_prepared(B, p->pm, &slot);
+            int rc = admit_prepared(B, p->pm, &slot);
+            if (rc == SGB_OK && p->resume) {
+                rc = sgb_batch_restore_mesh(B, slot, p->sx.data(), p->sv.data(), p->saved_steps);
+                if (rc != SGB_OK) sgb_batch_remove_mesh(B, slot);
+            }
             if (rc != SGB_OK) {
                 complete(S, p->req.id, rc, p->submitted, t_admit, 0, 0, 0);
             } else {
                 Running r;
+                r.req = p->req;
                 r.id = p->req.id;
                 r.slot = slot;
-                r.remaining = p->req.n_steps;
+                r.remaining = p->resume ? p->remaining : p->req.n_steps;
                 r.n_steps = p->req.n_steps;
                 r.tets = p->pm.E;
                 r.out = p->req.positions_out_host;
                 r.submitted = p->submitted;
                 r.admitted = t_admit;
                 S->running.push_back(r);
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->running_ids.insert(r.id);
             }
             delete p;
         }
@@ -219,6 +324,9 @@ static void scheduler_loop(sgb_server* S)
         {
             std::lock_guard<std::mutex> lk(S->mu);
             S->busy_s += std::chrono::duration<double>(t1 - t0).count();
+            S->launches++;
+            const double per_step = ms_between(t0, t1) / k;
+            for (int i = 0; i < k; ++i) S->step_ms.push_back(per_step);
         }
         for (size_t i = 0; i < finished.size(); ++i) {
             long long steps = 0;
@@ -230,6 +338,10 @@ static void scheduler_loop(sgb_server* S)
                 iters[i] = it;
             }
             sgb_batch_remove_mesh(B, finished[i].slot);
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->running_ids.erase(finished[i].id);
+            }
             complete(S, finished[i].id, st, finished[i].submitted, finished[i].admitted, iters[i], finished[i].tets,
                      finished[i].n_steps);
         }
@@ -238,6 +350,10 @@ static void scheduler_loop(sgb_server* S)
             // a failed launch fails every running request; the server keeps serving new ones
             for (auto& r : S->running) {
                 sgb_batch_remove_mesh(B, r.slot);
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->running_ids.erase(r.id);
+                }
                 complete(S, r.id, SGB_ERR_CUDA, r.submitted, r.admitted, 0, r.tets, 0);
             }
             S->running.clear();
@@ -343,6 +459,62 @@ int sgb_server_get_stats(sgb_server_t* S, sgb_server_stats* st)
     st->max_ms = l.empty() ? 0.0 : l.back();
     st->busy_s = S->busy_s;
     st->wall_s = S->have_first ? std::chrono::duration<double>(Clock::now() - S->first_submit).count() : 0.0;
+    std::vector<double> sm = S->step_ms;
+    std::sort(sm.begin(), sm.end());
+    auto spct = [&](double q) {
+        if (sm.empty()) return 0.0;
+        size_t i = (size_t)std::ceil(q * (double)sm.size()) - 1;
+        return sm[std::min(i, sm.size() - 1)];
+    };
+    st->step_p50_ms = spct(0.50);
+    st->step_p99_ms = spct(0.99);
+    st->launches = S->launches;
+    st->cancelled = S->cancelled;
+    st->evicted = S->evicted;
+    return SGB_OK;
+}
+
+int sgb_server_cancel(sgb_server_t* S, uint64_t id)
+{
+    if (!S) return (set_last_error("sgb_server_cancel: NULL server"), SGB_ERR_INVALID_ARGUMENT);
+    Pending* drop = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (auto it = S->ordered.begin(); it != S->ordered.end(); ++it) {
+            Pending* p = it->second;
+            if (p->req.id != id || p->cancelled) continue;
+            if (p->in_worker) {
+                p->cancelled = true;  // the worker completes it when it is done preparing
+                return SGB_OK;
+            }
+            auto q = std::find(S->incoming.begin(), S->incoming.end(), p);
+            if (q != S->incoming.end()) S->incoming.erase(q);
+            S->ordered.erase(it);
+            drop = p;
+            break;
+        }
+        if (!drop) {
+            if (S->running_ids.count(id) && !S->cancel_running.count(id)) {
+                S->cancel_running.insert(id);
+                return SGB_OK;
+            }
+            return (set_last_error("sgb_server_cancel: no queued or running request with that id"),
+                    SGB_ERR_NOT_FOUND);
+        }
+    }
+    complete(S, drop->req.id, SGB_ERR_CANCELLED, drop->submitted, Clock::now(), 0, 0, 0);
+    delete drop;
+    S->cv_sched.notify_one();
+    return SGB_OK;
+}
+
+int sgb_server_evict(sgb_server_t* S, uint64_t id)
+{
+    if (!S) return (set_last_error("sgb_server_evict: NULL server"), SGB_ERR_INVALID_ARGUMENT);
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (!S->running_ids.count(id) || S->cancel_running.count(id))
+        return (set_last_error("sgb_server_evict: no running request with that id"), SGB_ERR_NOT_FOUND);
+    S->evict_running.insert(id);
     return SGB_OK;
 }
 

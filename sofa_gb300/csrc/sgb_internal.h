@@ -38,6 +38,34 @@ struct ElemView {
     const R* R0;            // svd: initial rotation rows, 9 rows (or null)
     int n_tets;
     int method;
+    // compact FP32 matvec (or null): the force kernel also writes the
+    // quaternion of Q = R0^T R, from the initial rotation rows R0rows
+    float4* rotq = nullptr;
+    const R* R0rows = nullptr;
+};
+
+// Compact FP32 element format of the matvec: per element only the rotation
+// Q = R0^T R from the rest frame to the current element frame (a unit
+// quaternion, 16 B), the strain-displacement values being formed from the
+// nodes' rest positions in the world frame (float-float, per node) -- for an
+// isotropic material K_e(R0 p) = R0 K_e(p) R0^T, so the rotated rest frame
+// of the reference and the world frame give the same stiffness.
+// The compact matvec's material factors of one element: sqrt(s / 6) with s
+// the isotropic scale of computeMaterialStiffness (TFEM.inl:256-291), so that
+// sqrt(K(0,0)) = sqrt(s / 6) / sqrt(|det|) for K(0,0) = s / (36 V), and the
+// ratios K(0,1)/K(0,0), K(3,3)/K(0,0).
+__host__ __device__ inline float4 compact_material(double Ey, double nu)
+{
+    const double sc = (Ey * (1 - nu)) / ((1 + nu) * (1 - 2 * nu));
+    return make_float4((float)sqrt(sc / 6.0), (float)(nu / (1 - nu)), (float)((1 - 2 * nu) / (2 * (1 - nu))), 0.f);
+}
+
+struct CompactView {
+    const float4* rotq;      // per element: quaternion of Q
+    const float4* emat;      // per element {sqrt(s/6), K(0,1)/K(0,0), K(3,3)/K(0,0), 0}, or null: uniform
+    const float4* nrest_hi;  // per node: rest position, high float parts
+    const float4* nrest_lo;  // per node: rest position, low float parts
+    float4 mat;              // the uniform material factors
 };
 
 // Node -> (element*4 + corner) incidence in CSR form, each row sorted by slot.
@@ -113,8 +141,14 @@ struct TfemMesh {
     int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads
     int update_minb = 4;      // CG update: resident CTAs per SM the register cap is set for
     int update_grid = 0;      // CG update grid; 0: one thread per group of four nodes
-    bool staged = false;      // FP32: the patch kernels stage element data with bulk copies
-    int staged_grid = 0;      // CTAs of the staged patch kernels
+    // compact FP32 matvec (mixed large / polar meshes with patches)
+    int compact = 0;
+    float4* rotq = nullptr;      // per element: quaternion of Q = R0^T R
+    float4* emat = nullptr;      // per element material factors (null when uniform)
+    float4* nrest_hi = nullptr;  // per node: rest position as float-float, high parts
+    float4* nrest_lo = nullptr;  // low parts
+    float4 cmat = {0.f, 0.f, 0.f, 0.f};  // uniform material factors
+    int patch_grid_c = 0, adddforce_grid_c = 0;  // CTAs of the compact kernels
     int* dev_flags = nullptr; // sticky device error flag: 1 = a bounded device wait ran out
     double rest_volume = 0.0;
     // plasticity (plasticMaxThreshold > 0): 6 plastic strain rows per
@@ -142,6 +176,12 @@ struct CgScalars {
     int pad;
     unsigned int ticket;
     unsigned int pad2;
+    // residual replacement: the largest recurrence residual norm since the
+    // solve started or was last replaced, and the iteration whose update is
+    // followed by a replacement (0: none yet)
+    double rmax;
+    int replace_it;
+    int pad3;
     double partials[kMaxDotBlocks];
 };
 
@@ -155,7 +195,42 @@ struct SceneParams {
     int precond = 0;  // PCG: 1 Jacobi
     int precond_rate = 1;  // the preconditioner is re-assembled every this many steps
     int warm_start = 0;    // CG: start from the previous solution (warmStart)
+    double ff_rs = 0.0;    // the force field's own rayleighStiffness
+    double mass_rm = 0.0;  // the mass's own rayleighMass
+    int first_order = 0;   // EulerImplicitSolver firstOrder
+    int project_velocity = 0;  // FixedProjectiveConstraint activate_projectVelocity
 };
+
+// Factors of one EulerImplicitSolver step (EulerImplicitSolver.cpp:138-171,
+// trapezoidal factor tr = 1): the system matrix mF M + bF B + kF K, with the
+// components' Rayleigh terms folded into the factors each component applies
+// (MechanicalParams::k/mFactorIncludingRayleighDamping, MechanicalParams.h:
+// 62-64), and the right-hand side's stiffness factor h + rs (bF = 0 there).
+struct StepFactors {
+    double mf, bf, kf;  // solver factors
+    double kf_ff;       // kF + bF * force-field rayleighStiffness: what the force field's addDForce uses
+    double mf_mass;     // mF - bF * mass rayleighMass: what the mass's addMDx uses
+    double kf_rhs;      // h + rs, the right-hand side's K factor (second order)
+};
+
+inline StepFactors step_factors(const SceneParams& P)
+{
+    const double h = P.dt, tr = 1.0;
+    StepFactors f;
+    if (P.first_order) {
+        f.mf = 1;
+        f.bf = 0;
+        f.kf = -h * tr;
+    } else {
+        f.mf = 1 + tr * h * P.rayleigh_mass;
+        f.bf = -tr * h;
+        f.kf = -tr * h * (tr * h + P.rayleigh_stiffness);
+    }
+    f.kf_ff = f.kf + f.bf * P.ff_rs;
+    f.mf_mass = f.mf - f.bf * P.mass_rm;
+    f.kf_rhs = h * tr + P.rayleigh_stiffness;
+    return f;
+}
 
 struct Scene {
     TfemMesh* mesh = nullptr;
@@ -266,12 +341,28 @@ struct BMeshDesc {
     unsigned int ticket_rhs, ticket_den, ticket_rho, ticket_pad;
 };
 
+// The register-cap variants of the batch matvec (resident CTAs per SM).
+constexpr int kBatchMatvecMinb[3] = {5, 6, 8};
+
+// Launch tiles of a batch step. None of them changes a result bit: every
+// per-mesh reduction is formed per work item in an order fixed by the item.
+struct BatchTiles {
+    int matvec_minb = 6;  // the matvec's register cap: resident CTAs per SM (kBatchMatvecMinb)
+    int update_npt = 4;   // nodes per thread of the CG update (1, 2 or 4)
+    int update_ctas = 4;  // CG-update CTAs per SM
+    int elem_ctas = 4;    // element-kernel CTAs per SM
+    int prefetch = 0;     // matvec: L2 prefetch of a block's next patch
+};
+
 // Everything a precision variant needs to record one batch step.
 struct BatchLaunch {
     BMeshDesc* meshes;
     const WorkItem* items[3];
     const int* counts;
     int grid_patch, grid_elem, grid_node, grid_slots;
+    int grid_update;   // CTAs of the CG update
+    int matvec_minb;   // register-cap variant of the matvec
+    int update_npt;    // nodes per thread of the CG update
     int n_slots;  // mesh slots of the batch (the CG scalar kernels take one block per slot)
     int pe;
     int max_iterations;

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <type_traits>
 
@@ -654,6 +655,20 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
         }
     }
     store_rot(ev, (size_t)e, Rm);
+    if constexpr (is_mixed<R>::value) {
+        if (ev.rotq) {
+            // Q = R0^T R for the compact matvec
+            float R0m[9], Q[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) R0m[i] = ev.R0rows[i * En + e];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    Q[3 * i + j] = R0m[i] * Rm[j] + R0m[3 + i] * Rm[3 + j] + R0m[6 + i] * Rm[6 + j];
+            ev.rotq[e] = rot_to_quat(Q);
+        }
+    }
     addforce_element(F, D, K, J, pl, (size_t)e, En);
     // f[node] += rotations[e] * F_node, rotations[e] = R^T
 #pragma unroll
@@ -866,7 +881,20 @@ struct SolveConsts {
     int it;   // CG iteration this kernel belongs to (1-based)
     int pcg;  // 1: PCGLinearSolver bookkeeping (r.z, tolerance * b.b, no threshold test)
     int warm; // 1: CG warmStart (the solve starts from the previous solution)
+    int replace_every = 0;  // residual replacement: check every this many iterations (0: off)
 };
+
+// Residual replacement condition (van der Vorst and Ye, SIAM J. Sci. Comput.
+// 22(3), 2000, with their epsilon-hat = sqrt(u) for the FP32 unit roundoff
+// u = 2^-24): the residual is recomputed in FP64 only once the recurrence
+// residual has fallen below kReplaceEps times its largest norm since the
+// last replacement (the drift between recurrence and true residual then
+// matters), or when the recurrence says the solve has converged (the true
+// residual decides). A solve whose residual does not decrease -- a truncated
+// solve of a badly conditioned system -- is left to the FP32 recurrence, so
+// a replacement never perturbs a Krylov sequence that is still far from
+// converged.
+constexpr double kReplaceEps = 1.0 / 4096.0;
 
 // Last-block finish of a dot product: every block writes its partial; the
 // last block to arrive (integer ticket) adds the partials in block order and
@@ -943,6 +971,8 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         cg->normb = sqrt(total);
         cg->iters = 0;
         cg->last_err = 0.0;
+        cg->rmax = sqrt(total);
+        cg->replace_it = 0;
         if (cg->normb == 0.0) {
             cg->done = 1;
         } else {
@@ -968,6 +998,12 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         cg->beta = total / cg->rho_prev;
         double err = sqrt(total) / cg->normb;
         cg->last_err = err;
+        if (sc.replace_every > 0) {
+            const double nr = sqrt(total);
+            if (nr > cg->rmax) cg->rmax = nr;
+            if (sc.it % sc.replace_every == 0 && (nr <= kReplaceEps * cg->rmax || err <= sc.tol))
+                cg->replace_it = sc.it;
+        }
         if (err <= sc.tol) cg->done = 1;
     } else if (FIN == FIN_WARM_START) {
         // warmStart (CGLinearSolver.inl:95-99): r = b - A x; iteration 1
@@ -987,6 +1023,7 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
         double err = sqrt(total) / cg->normb;
         cg->last_err = err;
         cg->done = (err <= sc.tol) ? 1 : 0;
+        cg->rmax = sqrt(total);
     }
 }
 
@@ -1072,7 +1109,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R*
                                                            MassArgs ma, double mfac, int mass_first, double h,
                                                            const uint8_t* __restrict__ fixed, R* __restrict__ b,
                                                            R* __restrict__ r, R* __restrict__ xs, CgScalars* cg,
-                                                           double* terms, int N, SolveConsts sc)
+                                                           double* terms, int N, SolveConsts sc, int first_order = 0)
 {
     const R mm = (R)(mfac != 1.0 ? ma.vertex_mass * mfac : ma.vertex_mass);
     const R hr = (R)h;
@@ -1080,18 +1117,22 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R*
     if (blockIdx.x == 0 && threadIdx.x == 0) cg->done = 0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         R a[3] = {f[3 * (size_t)n], f[3 * (size_t)n + 1], f[3 * (size_t)n + 2]};
-        R vv[3] = {(R)v[3 * (size_t)n], (R)v[3 * (size_t)n + 1], (R)v[3 * (size_t)n + 2]};
-        if (mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
-        const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
-        for (int s = s0; s < s1; ++s) {
-            const R* c = eforce + 3 * (size_t)csr.slots[s];
-            a[0] -= c[0];
-            a[1] -= c[1];
-            a[2] -= c[2];
-        }
-        if (!mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+        if (!first_order) {
+            // b = h (f + (-rm M + (h + rs) K) v); firstOrder: b = f
+            // (EulerImplicitSolver.cpp:137-160)
+            R vv[3] = {(R)v[3 * (size_t)n], (R)v[3 * (size_t)n + 1], (R)v[3 * (size_t)n + 2]};
+            if (mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+            const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
+            for (int s = s0; s < s1; ++s) {
+                const R* c = eforce + 3 * (size_t)csr.slots[s];
+                a[0] -= c[0];
+                a[1] -= c[1];
+                a[2] -= c[2];
+            }
+            if (!mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) a[k] *= hr;
+            for (int k = 0; k < 3; ++k) a[k] *= hr;
+        }
         if (fixed[n]) a[0] = a[1] = a[2] = R(0);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -1311,20 +1352,26 @@ __global__ void __launch_bounds__(kNodeBlock) k_pcg_start(NodeCSR csr, const R* 
 
 // Euler update (MechanicalObject::vMultiOp fast path, MechanicalObject.inl:
 // 2206-2240): v += dv; x += v h; optional v *= exp(-h vdamping).
+// firstOrder (EulerImplicitSolver.cpp:200-224): v = dv, then x += v h.
+// project_velocity: FixedProjectiveConstraint::projectVelocity
+// (FixedProjectiveConstraint.inl:237-261), after the solve: fixed nodes'
+// velocities set to zero (their positions have moved with the unprojected v).
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict__ x, double* __restrict__ v,
                                                              const R* __restrict__ xs, double h, double vdamp,
-                                                             CgScalars* cg, int N)
+                                                             CgScalars* cg, int N, int first_order = 0,
+                                                             const uint8_t* __restrict__ project_fixed = nullptr)
 {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const bool zero_v = project_fixed && project_fixed[n];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const size_t i = 3 * (size_t)n + k;
-            double vv = v[i] + (double)xs[i];
+            double vv = first_order ? (double)xs[i] : v[i] + (double)xs[i];
             double t = vv * h;
             x[i] = x[i] + t;
             if (vdamp != 1.0) vv *= vdamp;
-            v[i] = vv;
+            v[i] = zero_v ? 0.0 : vv;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) cg->time_step_count += 1;
@@ -1583,12 +1630,13 @@ __global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv,
 
 // addDForce (MODE 0) as its own kernel so that it can carry its own register
 // cap: 128-thread CTAs, at least 10 per SM in FP32 (51 registers), measured
-// faster than the 64 the CG modes need. `gate`: run only if iteration
-// gate_it of that solve ran (residual replacement inside a captured step).
+// faster than the 64 the CG modes need. `gate`: run only if *gate equals
+// gate_it (residual replacement inside a captured step: the iteration a
+// replacement was decided for).
 template <typename R>
 __global__ void __launch_bounds__(kPatchThreads, sizeof(R) == 4 ? 10 : 1)
     k_patch_adddforce(PatchView pv, ElemView<R> ev, const R* __restrict__ dx, R kf, R* __restrict__ df,
-                      R* __restrict__ partials, const CgScalars* gate, int gate_it)
+                      R* __restrict__ partials, const int* gate, int gate_it)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* ef;
@@ -1596,246 +1644,233 @@ __global__ void __launch_bounds__(kPatchThreads, sizeof(R) == 4 ? 10 : 1)
     uint16_t* sl;
     int* lr;
     patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
-    if (gate && gate->iters != gate_it) return;
+    if (gate && *gate != gate_it) return;
     const PatchArgs<R> args{dx, nullptr, nullptr, R(0), kf, R(0), {nullptr, 0.0, {0.0, 0.0, 0.0}}, 1.0, nullptr, df,
                             partials, nullptr};
     for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) (void)patch_body<R, 0>(pv, ev, P, args, ef, lp, sl, lr);
 }
 
 // ------------------------------------------------------------------------
-// FP32 fused matvec with the element data staged by bulk copies. Phase 1 is
-// the only reader of a patch's element data (quaternion and three J/K
-// planes, 64 B per element, and the local connectivity, 8 B), which is
-// contiguous per patch. Right after phase 1 of patch i, one thread issues
-// the bulk copies (cp.async.bulk, completion counted on an mbarrier) of the
-// block's next patch into the same stage buffer; they land while the block
-// runs phase 2 of patch i and phase 0 of patch i+1, so the element stream
-// keeps DRAM busy across the block barriers. Every wait on the mbarrier is
-// bounded; a wait that runs out sets an error flag, waits (also bounded)
-// once more for the copies in flight and leaves the loop.
+// FP32 fused matvec, compact element format: per element only the rotation
+// Q = R0^T R (16 B) and the local connectivity; the strain-displacement
+// values are formed on the fly from the nodes' rest positions in the world
+// frame (float-float, staged per local node in phase 0 with the nodal
+// values). With node a's edges e_b, e_c, e_d (each formed from the
+// float-float positions and rounded once), computeStrainDisplacement
+// (TFEM.inl:134-209) on rest coordinates relative to node a gives
+// J_b = e_c x e_d, J_c = e_d x e_b, J_d = e_b x e_c, J_a = -(J_b + J_c + J_d),
+// and K(0,0) = s / (36 V) = s / (6 |e_b . J_b|): the kernel carries
+// J sqrt(K(0,0)) and the two ratios K(0,1)/K(0,0), K(3,3)/K(0,0), as the
+// stored FP32 format does. Element data drops from 64 to 16 bytes (32 with a
+// per-element material).
 // ------------------------------------------------------------------------
-constexpr int kStagedThreads = 128;
-constexpr long long kStageWaitTries = 1LL << 22;
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+__host__ __device__ __forceinline__ size_t patch_smem_size_c(int pe, int max_lnodes)
 {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    return sizeof(float) * 12 * (size_t)pe + 8 * (size_t)pe + ((4 * ((size_t)max_lnodes + 1) + 15) & ~(size_t)15) +
+           48 * (size_t)max_lnodes;
 }
 
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes)
+__device__ __forceinline__ void patch_smem_carve_c(unsigned char* base, int pe, int max_lnodes, float** ef,
+                                                   uint16_t** sl, int** lr, float4** lp, float4** rh, float4** rl)
 {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
+    unsigned char* p = base;
+    *ef = reinterpret_cast<float*>(p);
+    p += sizeof(float) * 12 * (size_t)pe;
+    *sl = reinterpret_cast<uint16_t*>(p);
+    p += 8 * (size_t)pe;
+    *lr = reinterpret_cast<int*>(p);
+    p += (4 * ((size_t)max_lnodes + 1) + 15) & ~(size_t)15;
+    *lp = reinterpret_cast<float4*>(p);
+    p += 16 * (size_t)max_lnodes;
+    *rh = reinterpret_cast<float4*>(p);
+    p += 16 * (size_t)max_lnodes;
+    *rl = reinterpret_cast<float4*>(p);
 }
 
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar)
+// J sqrt(K(0,0)) of an element from its nodes' float-float rest positions
+// and its material factors m = {sqrt(s/6), K(0,1)/K(0,0), K(3,3)/K(0,0)}.
+__device__ __forceinline__ void compact_strain_displacement(const float4 h[4], const float4 l[4], float4 m,
+                                                            float J[12], float K[3])
 {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
+    float eb[3], ec[3], ed[3];
+    eb[0] = (h[1].x - h[0].x) + (l[1].x - l[0].x);
+    eb[1] = (h[1].y - h[0].y) + (l[1].y - l[0].y);
+    eb[2] = (h[1].z - h[0].z) + (l[1].z - l[0].z);
+    ec[0] = (h[2].x - h[0].x) + (l[2].x - l[0].x);
+    ec[1] = (h[2].y - h[0].y) + (l[2].y - l[0].y);
+    ec[2] = (h[2].z - h[0].z) + (l[2].z - l[0].z);
+    ed[0] = (h[3].x - h[0].x) + (l[3].x - l[0].x);
+    ed[1] = (h[3].y - h[0].y) + (l[3].y - l[0].y);
+    ed[2] = (h[3].z - h[0].z) + (l[3].z - l[0].z);
+    J[3] = ec[1] * ed[2] - ec[2] * ed[1];
+    J[4] = ec[2] * ed[0] - ec[0] * ed[2];
+    J[5] = ec[0] * ed[1] - ec[1] * ed[0];
+    J[6] = ed[1] * eb[2] - ed[2] * eb[1];
+    J[7] = ed[2] * eb[0] - ed[0] * eb[2];
+    J[8] = ed[0] * eb[1] - ed[1] * eb[0];
+    J[9] = eb[1] * ec[2] - eb[2] * ec[1];
+    J[10] = eb[2] * ec[0] - eb[0] * ec[2];
+    J[11] = eb[0] * ec[1] - eb[1] * ec[0];
+    const float det = eb[0] * J[3] + eb[1] * J[4] + eb[2] * J[5];
+    const float sk = m.x * rsqrtf(fabsf(det));
+#pragma unroll
+    for (int i = 3; i < 12; ++i) J[i] *= sk;
+    J[0] = -(J[3] + J[6] + J[9]);
+    J[1] = -(J[4] + J[7] + J[10]);
+    J[2] = -(J[5] + J[8] + J[11]);
+    K[0] = 1.f;
+    K[1] = m.y;
+    K[2] = m.z;
 }
 
-// Bounded wait for the mbarrier phase with the given parity.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
+template <int MODE, int PC>
+__device__ __forceinline__ float patch_body_c(const PatchView& pv, const CompactView& cv, int P,
+                                              const PatchArgs<float>& a, float* ef, float4* lp, float4* rh,
+                                              float4* rl, uint16_t* sl, int* lr)
 {
-    for (long long i = 0; i < kStageWaitTries; ++i) {
-        unsigned ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(smem_addr(bar)), "r"(parity)
-            : "memory");
-        if (ok) return true;
+    float pen = 0.f;
+    const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
+    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
+        uint4* dst = reinterpret_cast<uint4*>(sl);
+        const int n16 = (8 * ne + 15) >> 4;
+        for (int k = threadIdx.x; k < n16; k += blockDim.x) dst[k] = src[k];
+        for (int l = threadIdx.x; l <= nn; l += blockDim.x) lr[l] = pv.lrow[n0 + l] - 4 * e0;
     }
-    return false;
-}
-
-// Shared memory of the staged kernel: an mbarrier (16 B), the stage
-// (q[pe] float4, jk[3][pe] float4, lc[pe] ushort4: 72 B per element), then
-// the regions of the plain patch kernel.
-inline size_t staged_smem_bytes(int pe, int max_lnodes)
-{
-    return 16 + 72 * (size_t)pe + patch_smem_size<float>(pe, max_lnodes);
-}
-
-// Issued by one thread: the element data of patch P into the stage. Global
-// addresses are 16-byte aligned (patches start at even element positions,
-// the arrays are 256-byte aligned); the connectivity copy is rounded up to
-// 16 bytes, which the array's two padding entries cover.
-__device__ __forceinline__ void stage_elements(unsigned char* stage, uint64_t* bar, const ElemView<float>& ev,
-                                               const ushort4* lconn, int e0, int ne, int pe)
-{
-    const float4* q = reinterpret_cast<const float4*>(ev.rot);
-    const float4* J = reinterpret_cast<const float4*>(ev.J);
-    const size_t En = (size_t)ev.n_tets;
-    const unsigned qb = 16u * (unsigned)ne;
-    const unsigned lb = (8u * (unsigned)ne + 15u) & ~15u;
-    fence_async_shared();
-    mbar_expect_tx(bar, 4 * qb + lb);
-    bulk_load(stage, q + e0, qb, bar);
-    for (int k = 0; k < 3; ++k) bulk_load(stage + 16u * pe * (1 + k), J + k * En + e0, qb, bar);
-    bulk_load(stage + 64u * pe, lconn + e0, lb, bar);
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
-    PatchView pv, ElemView<float> ev, const float* __restrict__ rin, const float* __restrict__ pold,
-    float* __restrict__ pnew, CgScalars* cg, float kf, MassArgs ma, double mf, const uint8_t* __restrict__ fixed,
-    float* __restrict__ qout, float* __restrict__ partials, SolveConsts sc, int* err)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int pe = pv.pe;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    unsigned char* stage = smem_raw + 16;
-    const float4* sq = reinterpret_cast<const float4*>(stage);
-    const float4* sj = reinterpret_cast<const float4*>(stage + 16u * pe);
-    const ushort4* slc = reinterpret_cast<const ushort4*>(stage + 64u * pe);
-    float *ef, *lp;
-    uint16_t* sl;
-    int* lr;
-    patch_smem_carve<float>(stage + 72u * pe, pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
-    if (MODE != 0 && cg->done) return;
-    const float beta = (MODE == 2) ? (float)cg->beta : 0.f;
-    const float mmu = (float)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        mbar_fence_init();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int g = pv.lnode_gid[n0 + l];
+        rh[l] = cv.nrest_hi[g];
+        rl[l] = cv.nrest_lo[g];
+        float v[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float rv = a.rin[3 * (size_t)g + k];
+            if constexpr (PC != 0) rv = a.dinv[3 * (size_t)g + k] * rv;
+            v[k] = (MODE == 2) ? cg_dir(rv, a.pold[3 * (size_t)g + k], a.beta) : rv;
+        }
+        lp[l] = make_float4(v[0], v[1], v[2], 0.f);
+        if (MODE != 0) {
+            const int info = pv.lnode_info[n0 + l];
+            if (info < 0 || (info & 1)) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) a.pnew[3 * (size_t)g + k] = v[k];
+            }
+        }
     }
     __syncthreads();
-    const int G = gridDim.x, NP = pv.n_patches;
-    int P = blockIdx.x;
-    if (threadIdx.x == 0 && P < NP)
-        stage_elements(stage, bar, ev, pv.lconn, pv.elem_start[P], pv.elem_start[P + 1] - pv.elem_start[P], pe);
-    double energy = 0.0;
-    bool failed = false;
-    unsigned parity = 0;
-    for (; P < NP; P += G, parity ^= 1u) {
-        const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
-        const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
-        float pen = 0.f;
-        // phase 0: slot lists and row starts, then the nodal values
+    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+        const size_t e = (size_t)(e0 + le);
+        const ushort4 c = pv.lconn[e];
+        float Qm[9], K[3], J[12];
+        quat_to_rot(cv.rotq[e], Qm);
         {
-            const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
-            uint4* dst = reinterpret_cast<uint4*>(sl);
-            const int n16 = (8 * ne + 15) >> 4;
-            for (int k = threadIdx.x; k < n16; k += blockDim.x) dst[k] = src[k];
-            for (int l = threadIdx.x; l <= nn; l += blockDim.x) lr[l] = pv.lrow[n0 + l] - 4 * e0;
+            const float4 h[4] = {rh[c.x], rh[c.y], rh[c.z], rh[c.w]};
+            const float4 l[4] = {rl[c.x], rl[c.y], rl[c.z], rl[c.w]};
+            compact_strain_displacement(h, l, cv.emat ? cv.emat[e] : cv.mat, J, K);
         }
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const int g = pv.lnode_gid[n0 + l];
-            float v[3];
+        const float4 v0 = lp[c.x], v1 = lp[c.y], v2 = lp[c.z], v3 = lp[c.w];
+        const float xr[4][3] = {{0.f, 0.f, 0.f},
+                                {v1.x - v0.x, v1.y - v0.y, v1.z - v0.z},
+                                {v2.x - v0.x, v2.y - v0.y, v2.z - v0.z},
+                                {v3.x - v0.x, v3.y - v0.y, v3.z - v0.z}};
+        float X[12], F[12];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                X[3 * i + k] = Qm[3 * k] * xr[i][0] + Qm[3 * k + 1] * xr[i][1] + Qm[3 * k + 2] * xr[i][2];
+        element_force(F, X, K, J, a.kf);
+        float en = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float rv = rin[3 * (size_t)g + k];
-                v[k] = (MODE == 2) ? cg_dir(rv, pold[3 * (size_t)g + k], beta) : rv;
-                lp[3 * l + k] = v[k];
+                const float ck = Qm[k] * F[3 * i] + Qm[3 + k] * F[3 * i + 1] + Qm[6 + k] * F[3 * i + 2];
+                ef[(3 * i + k) * pv.pe + le] = ck;
+                en += xr[i][k] * ck;
             }
-            if (MODE != 0) {
-                const int info = pv.lnode_info[n0 + l];
-                if (info < 0 || (info & 1)) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) pnew[3 * (size_t)g + k] = v[k];
-                }
-            }
-        }
-        const bool ok = mbar_wait(bar, parity);
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        // phase 1 from the stage
-        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
-            float Rm[9], K[3], J[12];
-            quat_to_rot(sq[le], Rm);
-            const float4 a = sj[le], b = sj[pe + le], d = sj[2 * pe + le];
-            J[3] = a.x;
-            J[4] = a.y;
-            J[5] = a.z;
-            J[6] = a.w;
-            J[7] = b.x;
-            J[8] = b.y;
-            J[9] = b.z;
-            J[10] = b.w;
-            J[11] = d.x;
-            J[0] = -(J[3] + J[6] + J[9]);
-            J[1] = -(J[4] + J[7] + J[10]);
-            J[2] = -(J[5] + J[8] + J[11]);
-            K[0] = 1.f;
-            K[1] = d.y;
-            K[2] = d.z;
-            patch_element<float, MODE>(le, slc[le], Rm, K, J, kf, pe, lp, ef, pen);
-        }
-        __syncthreads();
-        // the stage is free: the next patch's element data streams in now
-        const int Pn = P + G;
-        if (threadIdx.x == 0 && Pn < NP)
-            stage_elements(stage, bar, ev, pv.lconn, pv.elem_start[Pn], pv.elem_start[Pn + 1] - pv.elem_start[Pn],
-                           pe);
-        // phase 2: per local node, its slots in element order
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const int s0 = lr[l], s1 = lr[l + 1];
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-            for (int k = s0; k < s1; ++k) {
-                const int slot = sl[k];
-                const int le = slot >> 2, cc = slot & 3;
-                a0 += ef[(3 * cc + 0) * pe + le];
-                a1 += ef[(3 * cc + 1) * pe + le];
-                a2 += ef[(3 * cc + 2) * pe + le];
-            }
-            const int g = pv.lnode_gid[n0 + l];
-            const int info = pv.lnode_info[n0 + l];
-            if (info >= 0) {
-                float* o = partials + 3 * (size_t)(info >> 1);
-                o[0] = a0;
-                o[1] = a1;
-                o[2] = a2;
-            }
-            const size_t g3 = 3 * (size_t)g;
-            if (MODE == 0) {
-                if (info < 0) {
-                    qout[g3] -= a0;
-                    qout[g3 + 1] -= a1;
-                    qout[g3 + 2] -= a2;
-                }
-            } else if (info < 0 || (info & 1)) {
-                const float p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
-                const float mm = ma.node_mass ? (float)(ma.node_mass[g] * mf) : mmu;
-                pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
-                if (info < 0) {
-                    float q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
-                    if (fixed[g]) q0 = q1 = q2 = 0.f;
-                    qout[g3] = q0;
-                    qout[g3 + 1] = q1;
-                    qout[g3 + 2] = q2;
-                }
-            }
-        }
-        energy += (double)pen;
-        __syncthreads();
+        if (MODE != 0) pen -= en;
     }
-    if (failed) {
-        if (threadIdx.x == 0) {
-            *err = 1;
-            if (MODE != 0) {
-                cg->status |= 2;
-                cg->done = 1;
+    __syncthreads();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int s0 = lr[l], s1 = lr[l + 1];
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int s = s0; s < s1; ++s) {
+            const int slot = sl[s];
+            const int le = slot >> 2, cc = slot & 3;
+            a0 += ef[(3 * cc + 0) * pv.pe + le];
+            a1 += ef[(3 * cc + 1) * pv.pe + le];
+            a2 += ef[(3 * cc + 2) * pv.pe + le];
+        }
+        const int g = pv.lnode_gid[n0 + l];
+        const int info = pv.lnode_info[n0 + l];
+        if (info >= 0) {
+            float* o = a.partials + 3 * (size_t)(info >> 1);
+            o[0] = a0;
+            o[1] = a1;
+            o[2] = a2;
+        }
+        if (MODE == 0) {
+            if (info < 0) {
+                a.qout[3 * (size_t)g] -= a0;
+                a.qout[3 * (size_t)g + 1] -= a1;
+                a.qout[3 * (size_t)g + 2] -= a2;
+            }
+        } else if (info < 0 || (info & 1)) {
+            const float4 pl = lp[l];
+            const float mm = a.ma.node_mass ? (float)(a.ma.node_mass[g] * a.mf) : a.mmu;
+            pen += mm * (pl.x * pl.x + pl.y * pl.y + pl.z * pl.z);
+            if (info < 0) {
+                float q0 = mm * pl.x - a0, q1 = mm * pl.y - a1, q2 = mm * pl.z - a2;
+                if (a.fixed[g]) q0 = q1 = q2 = 0.f;
+                a.qout[3 * (size_t)g] = q0;
+                a.qout[3 * (size_t)g + 1] = q1;
+                a.qout[3 * (size_t)g + 2] = q2;
             }
         }
-        // the copies of the current patch must land before the block exits
-        mbar_wait(bar, parity);
-        return;
     }
-    if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
+    __syncthreads();
+    return pen;
+}
+
+template <int MODE, int PC>
+__global__ void __launch_bounds__(kPatchThreads, 8)
+    k_patch_matvec_c(PatchView pv, CompactView cv, const float* __restrict__ rin, const float* __restrict__ pold,
+                     float* __restrict__ pnew, CgScalars* cg, float kf, MassArgs ma, double mf,
+                     const uint8_t* __restrict__ fixed, float* __restrict__ qout, float* __restrict__ partials,
+                     SolveConsts sc, const float* __restrict__ dinv)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* ef;
+    float4 *lp, *rh, *rl;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve_c(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp, &rh, &rl);
+    if (cg->done) return;
+    const float beta = (MODE == 2) ? (float)cg->beta : 0.f;
+    const float mmu = (float)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
+    const PatchArgs<float> args{rin, pold, pnew, beta, kf, mmu, ma, mf, fixed, qout, partials, dinv};
+    double energy = 0.0;
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
+        energy += (double)patch_body_c<MODE, PC>(pv, cv, P, args, ef, lp, rh, rl, sl, lr);
+    finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
+}
+
+__global__ void __launch_bounds__(kPatchThreads, 8)
+    k_patch_adddforce_c(PatchView pv, CompactView cv, const float* __restrict__ dx, float kf, float* __restrict__ df,
+                        float* __restrict__ partials)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* ef;
+    float4 *lp, *rh, *rl;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve_c(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp, &rh, &rl);
+    const PatchArgs<float> args{dx, nullptr, nullptr, 0.f, kf, 0.f, {nullptr, 0.0, {0.0, 0.0, 0.0}}, 1.0, nullptr, df,
+                                partials, nullptr};
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
+        (void)patch_body_c<0, 0>(pv, cv, P, args, ef, lp, rh, rl, sl, lr);
 }
 
 // C ABI addDForce, second pass: nodes shared by several patches subtract
@@ -1843,9 +1878,9 @@ __global__ void __launch_bounds__(kStagedThreads) k_patch_matvec_staged(
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restrict__ bnd_rowptr,
                                                             const R* __restrict__ partials, R* __restrict__ df, int N,
-                                                            const CgScalars* gate = nullptr, int gate_it = 0)
+                                                            const int* gate = nullptr, int gate_it = 0)
 {
-    if (gate && gate->iters != gate_it) return;
+    if (gate && *gate != gate_it) return;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
         if (b0 == b1) continue;
@@ -1860,6 +1895,11 @@ __global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restric
         df[3 * (size_t)n + 2] -= a2;
     }
 }
+
+// A node's r.r, with the roundings spelled out (two fused multiply-adds), so
+// that every kernel forming it gets the same bits.
+__device__ __forceinline__ float node_rr(const float r[3]) { return __fmaf_rn(r[2], r[2], __fmaf_rn(r[1], r[1], r[0] * r[0])); }
+__device__ __forceinline__ double node_rr(const double r[3]) { return __fma_rn(r[2], r[2], __fma_rn(r[1], r[1], r[0] * r[0])); }
 
 // CG update of one node after a patch matvec: completes q on a shared node
 // (mass term minus the patches' partial sums, projected), then x += alpha p,
@@ -1907,7 +1947,7 @@ __device__ __forceinline__ R cg_update1(size_t n, R* __restrict__ xs, R* __restr
         for (int k = 0; k < 3; ++k) zz[k] = dinv[i3 + k] * rr[k];
         return rr[0] * zz[0] + rr[1] * zz[1] + rr[2] * zz[2];
     }
-    return rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
+    return node_rr(rr);
 }
 
 __device__ __forceinline__ void ld12(const float* __restrict__ a, size_t n0, float v[12])
@@ -1999,6 +2039,60 @@ __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, 
     return (double)local;
 }
 
+// cg_update4 for the batch engine: the four nodes' r.r in t[0..3], each
+// formed as node_rr forms it (cg_update1 gives the same per node).
+__device__ __forceinline__ void cg_update4_terms(size_t n0, float* __restrict__ xs, float* __restrict__ r,
+                                                 const float* __restrict__ p, const float* __restrict__ q,
+                                                 const float* __restrict__ partials,
+                                                 const int* __restrict__ bnd_rowptr,
+                                                 const double* __restrict__ node_mass, float mmu, double mf,
+                                                 const uint8_t* __restrict__ fixed, float alpha, double t[4])
+{
+    float pp[12], qq[12], xx[12], rr[12];
+    ld12(p, n0, pp);
+    ld12(q, n0, qq);
+    ld12(xs, n0, xx);
+    ld12(r, n0, rr);
+    const int4 br = *reinterpret_cast<const int4*>(bnd_rowptr + n0);
+    const int bb[5] = {br.x, br.y, br.z, br.w, bnd_rowptr[n0 + 4]};
+    const uchar4 fx = *reinterpret_cast<const uchar4*>(fixed + n0);
+    const uint8_t ff[4] = {fx.x, fx.y, fx.z, fx.w};
+    float ps[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) ps[k] = 0.f;
+#pragma unroll 4
+    for (int b = bb[0]; b < bb[4]; ++b) {
+        const float v0 = partials[3 * (size_t)b], v1 = partials[3 * (size_t)b + 1], v2 = partials[3 * (size_t)b + 2];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (b >= bb[j] && b < bb[j + 1]) {
+                ps[3 * j] += v0;
+                ps[3 * j + 1] += v1;
+                ps[3 * j + 2] += v2;
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (bb[j + 1] > bb[j]) {
+            const float mm = node_mass ? (float)(node_mass[n0 + j] * mf) : mmu;
+            qq[3 * j] = mm * pp[3 * j] - ps[3 * j];
+            qq[3 * j + 1] = mm * pp[3 * j + 1] - ps[3 * j + 1];
+            qq[3 * j + 2] = mm * pp[3 * j + 2] - ps[3 * j + 2];
+            if (ff[j]) qq[3 * j] = qq[3 * j + 1] = qq[3 * j + 2] = 0.f;
+        }
+    }
+    const float nalpha = -alpha;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+        xx[k] = xx[k] + pp[k] * alpha;
+        rr[k] = rr[k] + qq[k] * nalpha;
+    }
+    st12(xs, n0, xx);
+    st12(r, n0, rr);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) t[j] = (double)node_rr(rr + 3 * j);
+}
+
 template <typename R, int PC>
 __device__ __forceinline__ double cg_update4g(size_t n0, R* xs, R* r, const R* p, const R* q, const R* partials,
                                               const int* bnd_rowptr, const double* node_mass, R mmu, double mf,
@@ -2070,12 +2164,12 @@ __global__ void __launch_bounds__(kNodeBlock) k_refine_start(const double* __res
     }
 }
 
-// x64 += xs32, xs32 = 0, if iteration `it` of the solve ran.
+// x64 += xs32, xs32 = 0, if a replacement was decided after iteration `it`.
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_refine_accumulate(double* __restrict__ x64, R* __restrict__ xs,
                                                                   const CgScalars* cg, int it, int N)
 {
-    if (cg->iters != it) return;
+    if (cg->replace_it != it) return;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 3 * (size_t)N;
          i += (size_t)gridDim.x * blockDim.x) {
         x64[i] += (double)xs[i];
@@ -2093,7 +2187,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_refine_residual(const double* __
                                                                 R* __restrict__ r, CgScalars* cg, int N,
                                                                 SolveConsts sc)
 {
-    if (cg->iters != sc.it) return;
+    if (cg->replace_it != sc.it) return;
     const double mmu = ma.vertex_mass * mf;
     double local = 0.0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
@@ -2116,9 +2210,11 @@ template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_euler_refined(double* __restrict__ x, double* __restrict__ v,
                                                               const double* __restrict__ x64,
                                                               const R* __restrict__ xs, double h, double vdamp,
-                                                              CgScalars* cg, int N)
+                                                              CgScalars* cg, int N,
+                                                              const uint8_t* __restrict__ project_fixed = nullptr)
 {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const bool zero_v = project_fixed && project_fixed[n];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const size_t i = 3 * (size_t)n + k;
@@ -2126,7 +2222,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_refined(double* __restrict
             double t = vv * h;
             x[i] = x[i] + t;
             if (vdamp != 1.0) vv *= vdamp;
-            v[i] = vv;
+            v[i] = zero_v ? 0.0 : vv;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) cg->time_step_count += 1;
@@ -2157,7 +2253,48 @@ ElemView<R> view(TfemMesh* m)
     ev.R0 = m->method == METHOD_SVD ? (const R*)m->R0 : nullptr;
     ev.n_tets = m->n_tets;
     ev.method = m->method;
+    if (m->compact) {
+        ev.rotq = m->rotq;
+        ev.R0rows = (const R*)m->R0;
+    }
     return ev;
+}
+
+inline CompactView compact_view(const TfemMesh* m)
+{
+    return CompactView{m->rotq, m->emat, m->nrest_hi, m->nrest_lo, m->cmat};
+}
+
+// Compact format at rest: Q = identity, per-element material factors when
+// the material varies, and the float-float rest positions of the nodes.
+__global__ void k_init_compact(const double* __restrict__ rest_pos, const int* __restrict__ elem_orig, int E, int N,
+                               const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
+                               int n_poisson, const double* __restrict__ lsf, int n_lsf, float4* __restrict__ rotq,
+                               float4* __restrict__ emat, float4* __restrict__ hi, float4* __restrict__ lo)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < E) {
+        rotq[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+        if (emat) {
+            // getVecRealInElement (BaseLinearElasticityFEMForceField.inl:114-132)
+            const int e = elem_orig[i];
+            double Ey = (n_young > e) ? young[e] : young[0];
+            const double nu = (n_poisson > e) ? poisson[e] : poisson[0];
+            const double f = (n_lsf > 0) ? lsf[(size_t)e * (size_t)n_lsf / (size_t)E] : 1.0;
+            emat[i] = compact_material(f * Ey, nu);
+        }
+    }
+    if (i < N) {
+        float h[3], l[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double x = rest_pos[3 * (size_t)i + k];
+            h[k] = (float)x;
+            l[k] = (float)(x - (double)h[k]);
+        }
+        hi[i] = make_float4(h[0], h[1], h[2], 0.f);
+        lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+    }
 }
 
 template <typename R>
@@ -2168,6 +2305,12 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
     k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
         m->rest_pos, m->tets, m->elem_orig, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K,
         (R*)m->J, (R*)m->rest, m->rest_ff, (R*)m->rot, (R*)m->A0inv, (R*)m->R0, vol);
+    if (m->compact) {
+        const int n = std::max(m->n_tets, m->n_nodes);
+        k_init_compact<<<(n + kElemBlock - 1) / kElemBlock, kElemBlock, 0, s>>>(
+            m->rest_pos, m->elem_orig, m->n_tets, m->n_nodes, young, ny, poisson, np, lsf, nl, m->rotq, m->emat,
+            m->nrest_hi, m->nrest_lo);
+    }
 }
 
 // Mixed precision: the per-element factor sqrt(K(0,0)) of the stored
@@ -2338,6 +2481,18 @@ size_t patch_smem_bytes(const TfemMesh* m)
     return patch_smem_size<R>(m->pl.pe, m->pl.max_lnodes);
 }
 
+// The compact FP32 matvec of CG iteration `it` (MODE 1 on the first).
+template <int PC, typename... A>
+void launch_matvec_c(const TfemMesh* m, int it, cudaStream_t s, const PatchView& pv, A... a)
+{
+    const size_t smem = patch_smem_size_c(m->pl.pe, m->pl.max_lnodes);
+    const CompactView cv = compact_view(m);
+    if (it == 1)
+        k_patch_matvec_c<1, PC><<<m->patch_grid_c, kPatchThreads, smem, s>>>(pv, cv, a...);
+    else
+        k_patch_matvec_c<2, PC><<<m->patch_grid_c, kPatchThreads, smem, s>>>(pv, cv, a...);
+}
+
 // The CG update with the register cap chosen at preparation (MINB resident
 // CTAs of kNodeBlock threads per SM).
 template <typename R, int PC = 0, typename... A>
@@ -2349,6 +2504,18 @@ void launch_cg_update(const TfemMesh* m, int grid, cudaStream_t s, A... a)
         k_cg_update_patch<R, 3, PC><<<grid, kNodeBlock, 0, s>>>(a...);
     else
         k_cg_update_patch<R, 4, PC><<<grid, kNodeBlock, 0, s>>>(a...);
+}
+
+template <typename K>
+int resident_grid(K kernel, int threads, size_t smem, int sms, int n_patches)
+{
+    int nb = 0;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem);
+    long long g = (long long)(nb < 1 ? 1 : nb) * sms;
+    if (g > kMaxDotBlocks) g = kMaxDotBlocks;
+    if (g > n_patches) g = n_patches;
+    return (int)(g < 1 ? 1 : g);
 }
 
 // Sets the shared-memory attribute of the patch kernels and returns the grid
@@ -2414,35 +2581,16 @@ int prepare_patch(TfemMesh* m)
         if (ga > m->pl.n_patches) ga = m->pl.n_patches;
         m->adddforce_grid = (int)(ga < 1 ? 1 : ga);
     }
-    m->staged = false;
     if constexpr (is_mixed<R>::value) {
-        // FP32: the bulk-copy staged kernels when their shared memory fits
-        // (even pe: every patch but the last starts on a 16-byte element
-        // boundary; the device error flag exists)
-        const char* env = getenv("SGB_PATCH_STAGING");
-        if (env && env[0] == '1' && (m->pl.pe % 2) == 0 && m->dev_flags) {
-            const size_t ss = staged_smem_bytes(m->pl.pe, m->pl.max_lnodes);
-            int s0 = 0, s1 = 0, s2 = 0;
-            if (cudaFuncSetAttribute(k_patch_matvec_staged<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
-                    cudaSuccess &&
-                cudaFuncSetAttribute(k_patch_matvec_staged<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
-                    cudaSuccess &&
-                cudaFuncSetAttribute(k_patch_matvec_staged<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss) ==
-                    cudaSuccess) {
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s0, k_patch_matvec_staged<0>, kStagedThreads, ss);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s1, k_patch_matvec_staged<1>, kStagedThreads, ss);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s2, k_patch_matvec_staged<2>, kStagedThreads, ss);
-                int sb = s0 < s1 ? s0 : s1;
-                sb = sb < s2 ? sb : s2;
-                if (sb >= 1) {
-                    long long sg = (long long)sb * sms;
-                    if (sg > kMaxDotBlocks) sg = kMaxDotBlocks;
-                    if (sg > m->pl.n_patches) sg = m->pl.n_patches;
-                    m->staged = true;
-                    m->staged_grid = (int)sg;
-                }
-            }
-            cudaGetLastError();
+        if (m->compact) {
+            const size_t sc = patch_smem_size_c(m->pl.pe, m->pl.max_lnodes);
+            const int np = m->pl.n_patches;
+            int gc = resident_grid(k_patch_matvec_c<1, 0>, kPatchThreads, sc, sms, np);
+            gc = std::min(gc, resident_grid(k_patch_matvec_c<2, 0>, kPatchThreads, sc, sms, np));
+            gc = std::min(gc, resident_grid(k_patch_matvec_c<1, 1>, kPatchThreads, sc, sms, np));
+            gc = std::min(gc, resident_grid(k_patch_matvec_c<2, 1>, kPatchThreads, sc, sms, np));
+            m->patch_grid_c = gc;
+            m->adddforce_grid_c = resident_grid(k_patch_adddforce_c, kPatchThreads, sc, sms, np);
         }
     }
     return (int)g;
@@ -2468,11 +2616,10 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
         SolveConsts sc{0.0, 0.0, 0};
         bool done = false;
         if constexpr (is_mixed<R>::value) {
-            if (m->staged) {
-                k_patch_matvec_staged<0>
-                    <<<m->staged_grid, kStagedThreads, staged_smem_bytes(m->pl.pe, m->pl.max_lnodes), s>>>(
-                        pv, view<R>(m), dx, nullptr, nullptr, nullptr, kfactor, ma, 1.0, nullptr, df,
-                        (R*)m->pl.partials, sc, m->dev_flags);
+            if (m->compact) {
+                k_patch_adddforce_c<<<m->adddforce_grid_c, kPatchThreads,
+                                      patch_smem_size_c(m->pl.pe, m->pl.max_lnodes), s>>>(
+                    pv, compact_view(m), dx, kfactor, df, (R*)m->pl.partials);
                 done = true;
             }
         }
@@ -2559,14 +2706,15 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     // f = F(x)
     launch_elem_force<R>(m, sc->x, s);
     k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
-    // b = h (f - (h+rs) K v - rm M v)
-    const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
-    launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)kf_rhs, s);
+    // b = h (f - (h+rs) K v - rm M v); firstOrder: b = f
+    const StepFactors F = step_factors(P);
+    if (!P.first_order) launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)F.kf_rhs, s);
     k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass, mass_first,
-                                              h, sc->fixed, b, r, xs, sc->cg, dot_terms, N, cons);
-    // CG (or PCG) on (mF M + kF K) dv = b
-    const double mf = 1 + 1.0 * h * P.rayleigh_mass;
-    const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+                                              h, sc->fixed, b, r, xs, sc->cg, dot_terms, N, cons, P.first_order);
+    // CG (or PCG) on (mF M + kF K) dv = b, each component with its own
+    // Rayleigh term folded into its factor
+    const double mf = F.mf_mass;
+    const double kf = F.kf_ff;
     if (pcg || P.warm_start) pcg_begin<R>(sc, mass_first, mf, kf, cons, dot_terms, s);
     for (int it = 1; it <= P.cg_iterations; ++it) {
         cons.it = it;
@@ -2595,7 +2743,8 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
             k_cg_update<R><<<ng, kNodeBlock, 0, s>>>(xs, r, p, q, sc->cg, dot_terms, N, cons);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
-    k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);
+    k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N, P.first_order,
+                                                P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
 }
 
 // The same step with the fused patch matvec: two launches per CG iteration
@@ -2625,12 +2774,12 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0, P.warm_start};
     launch_elem_force<R>(m, sc->x, s);
     k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
-    const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
-    launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)kf_rhs, s);
+    const StepFactors F = step_factors(P);
+    if (!P.first_order) launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)F.kf_rhs, s);
     k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass, mass_first,
-                                              h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons);
-    const double mf = 1 + 1.0 * h * P.rayleigh_mass;
-    const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+                                              h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons, P.first_order);
+    const double mf = F.mf_mass;
+    const double kf = F.kf_ff;
     if (pcg || P.warm_start) pcg_begin<R>(sc, mass_first, mf, kf, cons, nullptr, s);
     PatchView pv = patch_view(m);
     ElemView<R> ev = view<R>(m);
@@ -2642,7 +2791,17 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
         if (dinv) {
-            if (it == 1)
+            bool pdone = false;
+            if constexpr (is_mixed<R>::value) {
+                if (m->compact) {
+                    launch_matvec_c<1>(m, it, s, pv, (const float*)r, (const float*)pold, pnew, sc->cg, (R)kf, ma,
+                                       mf, (const uint8_t*)sc->fixed, q, partials, cons, (const float*)dinv);
+                    pdone = true;
+                }
+            }
+            if (pdone)
+                ;
+            else if (it == 1)
                 k_patch_matvec<R, 1, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
                     pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch,
                     dinv);
@@ -2657,16 +2816,9 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
         }
         bool done = false;
         if constexpr (is_mixed<R>::value) {
-            if (m->staged) {
-                const size_t ss = staged_smem_bytes(m->pl.pe, m->pl.max_lnodes);
-                if (it == 1)
-                    k_patch_matvec_staged<1><<<m->staged_grid, kStagedThreads, ss, s>>>(
-                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons,
-                        m->dev_flags);
-                else
-                    k_patch_matvec_staged<2><<<m->staged_grid, kStagedThreads, ss, s>>>(
-                        pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons,
-                        m->dev_flags);
+            if (m->compact) {
+                launch_matvec_c<0>(m, it, s, pv, (const float*)r, (const float*)pold, pnew, sc->cg, (R)kf, ma, mf,
+                                   (const uint8_t*)sc->fixed, q, partials, cons, (const float*)nullptr);
                 done = true;
             }
         }
@@ -2683,7 +2835,8 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
                             m->update_vec4);
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
-    k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N);
+    k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N, P.first_order,
+                                                P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
 }
 
 // The FP32 patch step with residual replacement every sc->replace_every CG
@@ -2705,22 +2858,22 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
     R* q = (R*)sc->q;
     R* xs = (R*)sc->xs;
     R* partials = (R*)m->pl.partials;
-    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1};
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, 0, 0, sc->replace_every};
     // FP64: f = F(x) and b = h (f - (h+rs) K v - rm M v) on the FP64 operator
     NodeCSR csr64{sh->rowptr, sh->slots};
     launch_elem_force<double>(sh, sc->x, s);
     k_gather_force<double><<<ng, kNodeBlock, 0, s>>>(csr64, (const double*)sh->eforce, sc->ext64, ma, mass_first,
                                                      sc->w64, N);
-    const double kf_rhs = h * 1.0 + P.rayleigh_stiffness;
-    launch_elem_dforce<double, double, 0>(sh, sc->v, nullptr, sc->cg, kf_rhs, s);
+    const StepFactors F = step_factors(P);
+    launch_elem_dforce<double, double, 0>(sh, sc->v, nullptr, sc->cg, F.kf_rhs, s);
     k_gather_rhs<double><<<ng, kNodeBlock, 0, s>>>(csr64, (const double*)sh->eforce, sc->w64, sc->v, ma,
                                                    -P.rayleigh_mass, mass_first, h, sc->fixed, sc->b64, sc->r64,
                                                    sc->x64, sc->cg, nullptr, N, cons);
     // FP32: the element rotations at x, r = b, xs = 0
     launch_elem_force<R>(m, sc->x, s);
     k_refine_start<R><<<ng3, kNodeBlock, 0, s>>>(sc->b64, r, xs, N);
-    const double mf = 1 + 1.0 * h * P.rayleigh_mass;
-    const double kf = -1.0 * h * (1.0 * h + P.rayleigh_stiffness);
+    const double mf = F.mf_mass;
+    const double kf = F.kf_ff;
     PatchView pv = patch_view(m);
     ElemView<R> ev = view<R>(m);
     const size_t smem = patch_smem_bytes<R>(m);
@@ -2730,7 +2883,11 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
         cons.it = it;
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
-        if (it == 1)
+        if (m->compact)
+            launch_matvec_c<0>(m, it, s, pv, (const float*)r, (const float*)pold, (float*)pnew, sc->cg, (float)kf,
+                               ma, mf, (const uint8_t*)sc->fixed, (float*)q, (float*)partials, cons,
+                               (const float*)nullptr);
+        else if (it == 1)
             k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
                 pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
         else
@@ -2743,15 +2900,17 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
             k_refine_accumulate<R><<<ng3, kNodeBlock, 0, s>>>(sc->x64, xs, sc->cg, it, N);
             cudaMemsetAsync(sc->w64, 0, sizeof(double) * 3 * (size_t)N, s);
             k_patch_adddforce<double><<<sh->patch_grid, kPatchThreads, patch_smem_bytes<double>(sh), s>>>(
-                patch_view(sh), view<double>(sh), sc->x64, kf, sc->w64, (double*)sh->pl.partials, sc->cg, it);
+                patch_view(sh), view<double>(sh), sc->x64, kf, sc->w64, (double*)sh->pl.partials,
+                &sc->cg->replace_it, it);
             k_patch_fixup<double><<<ng, kNodeBlock, 0, s>>>(sh->pl.bnd_rowptr, (const double*)sh->pl.partials,
-                                                            sc->w64, N, sc->cg, it);
+                                                            sc->w64, N, &sc->cg->replace_it, it);
             k_refine_residual<R><<<ng, kNodeBlock, 0, s>>>(sc->b64, sc->x64, sc->w64, ma, mf, sc->fixed, r, sc->cg,
                                                            N, cons);
         }
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
-    k_euler_refined<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, sc->x64, xs, h, vd, sc->cg, N);
+    k_euler_refined<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, sc->x64, xs, h, vd, sc->cg, N,
+                                                 P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
 }
 
 }  // namespace SGB_NS

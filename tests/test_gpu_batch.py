@@ -116,3 +116,54 @@ def test_external_force_and_per_mesh_iterations(capi):
     y1 = b.state(s1)[0][tip, 1].mean()
     y2 = b.state(s2)[0][tip, 1].mean()
     assert y2 < y1  # the traction pulls the tip further down
+
+
+TILES = [dict(matvec_ctas_per_sm=8, update_nodes_per_thread=1, update_ctas_per_sm=2, elem_ctas_per_sm=8, prefetch=1),
+         dict(matvec_ctas_per_sm=5, update_nodes_per_thread=2, update_ctas_per_sm=8, elem_ctas_per_sm=2, prefetch=0)]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64_fma"])
+def test_tiles_are_rounding_neutral(capi, precision):
+    """Every launch tile the tuner can pick gives the same bits: the mix with
+    non-default tiles equals each mesh run alone with the default tiles."""
+    meshes = [(topo.beam(n, 0.5, 0.05, seed), E, nu, m) for n, seed, E, nu, m in MESHES]
+    alone = []
+    for mesh, E, nu, m in meshes:
+        b = capi.Batch(precision, budget_bytes=64 << 20, max_meshes=4)
+        s = b.add_mesh(mesh.positions, mesh.tetrahedra, **beam_kw(mesh, E, nu, m))
+        b.step(15)
+        alone.append(b.state(s)[0])
+        b.close()
+    for tiles in TILES:
+        b = capi.Batch(precision, budget_bytes=256 << 20, max_meshes=8)
+        slots = [b.add_mesh(mesh.positions, mesh.tetrahedra, **beam_kw(mesh, E, nu, m))
+                 for mesh, E, nu, m in meshes]
+        b.set_tiles(**tiles)
+        b.step(15)
+        for s, xa in zip(slots, alone):
+            assert np.array_equal(b.state(s)[0], xa), tiles
+        b.close()
+
+
+def test_tuner_keeps_state_and_results(capi):
+    """sgb_batch_tune times whole steps but restores every mesh's state: a
+    batch tuned after 5 steps and stepped 5 more equals one stepped 10."""
+    meshes = [(topo.beam(n, 0.5, 0.05, seed), E, nu, m) for n, seed, E, nu, m in MESHES]
+    res = []
+    for tune in (False, True):
+        b = capi.Batch("mixed", budget_bytes=256 << 20, max_meshes=8)
+        slots = [b.add_mesh(mesh.positions, mesh.tetrahedra, **beam_kw(mesh, E, nu, m))
+                 for mesh, E, nu, m in meshes]
+        b.step(5)
+        if tune:
+            info = b.tune(steps_per_trial=2, use_cache=False)
+            assert info["trials"] >= 10 and info["tuned_ms_per_step"] > 0
+            assert info["tuned_ms_per_step"] <= info["default_ms_per_step"]
+            assert all(b.stats(s)[2] == 5 for s in slots)  # step counters restored
+            again = b.tune(use_cache=True)  # the same mix: answered by the cache
+            assert again["trials"] == 0
+        b.step(5)
+        res.append([b.state(s) for s in slots])
+        b.close()
+    for (xa, va), (xb, vb) in zip(*res):
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)

@@ -181,3 +181,70 @@ def test_cg_warm_start_scene_file_against_oracle(capi, oracle):
     osc.step(30)
     xo, _ = osc.state()
     assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+
+
+@pytest.mark.parametrize("edit,opts", [
+    (("<TetrahedronFEMForceField name=\"FEM\"", "<TetrahedronFEMForceField rayleighStiffness=\"0.05\" name=\"FEM\""),
+     dict(ff_rayleigh_stiffness=0.05)),
+    (("<DiagonalMass name=\"mass\"", "<DiagonalMass rayleighMass=\"0.2\" name=\"mass\""),
+     dict(mass_rayleigh_mass=0.2)),
+    (("<EulerImplicitSolver />", "<EulerImplicitSolver firstOrder=\"1\" />"), dict(first_order=True)),
+    (("name=\"fixC\"", "name=\"fixC\" activate_projectVelocity=\"1\""), dict(project_velocity=True)),
+])
+def test_grid_scene_file_with_component_options(capi, oracle, edit, opts):
+    """The grid scene with the force field's rayleighStiffness, the mass's
+    rayleighMass, the solver's firstOrder or the constraint's
+    activate_projectVelocity set: loaded through the component layer, 30
+    steps within 1e-10 of the oracle configured the same way."""
+    text = _read("grid_fem_4x10x4.scn")
+    assert edit[0] in text
+    s = capi.SofaScene(text.replace(edit[0], edit[1], 1))
+    s.animate(30)
+    x = s.positions(0)
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+    osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01, cg_iterations=20,
+                             cg_tolerance=1e-5, cg_threshold=1e-6)
+    osc.set_options(**opts)
+    osc.step(30)
+    xo, _ = osc.state()
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+
+
+def test_reset_and_unload(capi, oracle):
+    """SofaPhysicsAPI-style lifecycle. After reset the scene is back at its
+    initial state and time 0, and 10 more steps match the oracle run through
+    the same history (7 steps, the state put back, 10 steps: the solver keeps
+    its time-step count across the reset, as the reference's CGLinearSolver
+    does). unload frees the device; the next animate starts over from the
+    initial state, bit-identical to a fresh load."""
+    text = _read("grid_fem_4x10x4.scn")
+    fresh = capi.SofaScene(text)
+    fresh.animate(10)
+    x_fresh = fresh.positions(0)
+    s = capi.SofaScene(text)
+    x0 = s.positions(0)
+    s.animate(7)
+    s.reset()
+    assert s.time == 0.0
+    assert np.array_equal(s.positions(0), x0)
+    s.animate(10)
+    x_reset = s.positions(0)
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+    osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01, cg_iterations=20,
+                             cg_tolerance=1e-5, cg_threshold=1e-6)
+    osc.step(7)
+    osc.set_state(pos, np.zeros_like(pos))
+    osc.step(10)
+    xo, _ = osc.state()
+    assert np.max(np.abs(x_reset - xo)) <= 1e-10 * np.max(np.abs(xo))
+    s.unload()
+    assert s.time == 0.0
+    assert np.array_equal(s.positions(0), x0)  # no device objects: the initial positions
+    s.animate(10)
+    assert np.array_equal(s.positions(0), x_fresh)  # a fresh start: bit-identical to the fresh load
