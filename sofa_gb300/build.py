@@ -19,7 +19,11 @@ LIB = os.path.join(HERE, "libsofa_gb300.so")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# -ffp-contract=off for the host compiler: host-side factor arithmetic (the
+# implicit-Euler factors, the components' Rayleigh terms) rounds each a*b+c
+# twice, as the reference does on a target without fused multiply-add; the
+# Arm hosts' gcc would otherwise fuse it. Device code is governed by -fmad.
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 # translation unit -> extra flags

@@ -123,10 +123,6 @@ static void free_mesh(TfemMesh& m)
     cudaFree(m.pl.bnd_rowptr);
     cudaFree(m.pl.partials);
     cudaFree(m.dev_flags);
-    cudaFree(m.rotq);
-    cudaFree(m.emat);
-    cudaFree(m.nrest_hi);
-    cudaFree(m.nrest_lo);
     m = TfemMesh();
 }
 
@@ -244,20 +240,6 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     if ((ce = cudaMemsetAsync(m.dev_flags, 0, sizeof(int), h->stream)) != cudaSuccess) {
         rc = cuda_fail(ce, "cudaMemsetAsync");
         goto fail_out;
-    }
-    // compact FP32 matvec (mixed large / polar with patches; SGB_MATVEC_COMPACT=0
-    // keeps the stored 64-byte element format in the matvec)
-    if (precision == SGB_PRECISION_MIXED && !L.elem_start.empty() &&
-        (method == SGB_METHOD_LARGE || method == SGB_METHOD_POLAR)) {
-        const char* e = getenv("SGB_MATVEC_COMPACT");
-        m.compact = (e && e[0] == '0') ? 0 : 1;
-    }
-    if (m.compact) {
-        const bool uniform = E_h.size() == 1 && nu_h.size() == 1 && n_lsf == 0;
-        if ((rc = dev_alloc(&m.rotq, E, acc)) || (rc = dev_alloc(&m.nrest_hi, (size_t)n_nodes, acc)) ||
-            (rc = dev_alloc(&m.nrest_lo, (size_t)n_nodes, acc)) || (!uniform && (rc = dev_alloc(&m.emat, E, acc))))
-            goto fail_out;
-        if (uniform) m.cmat = compact_material(E_h[0], nu_h[0]);
     }
     if (!L.elem_start.empty()) {
         PatchLayout& pl = m.pl;

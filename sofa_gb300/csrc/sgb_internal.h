@@ -38,10 +38,6 @@ struct ElemView {
     const R* R0;            // svd: initial rotation rows, 9 rows (or null)
     int n_tets;
     int method;
-    // compact FP32 matvec (or null): the force kernel also writes the
-    // quaternion of Q = R0^T R, from the initial rotation rows R0rows
-    float4* rotq = nullptr;
-    const R* R0rows = nullptr;
 };
 
 // Compact FP32 element format of the matvec: per element only the rotation
@@ -50,23 +46,6 @@ struct ElemView {
 // nodes' rest positions in the world frame (float-float, per node) -- for an
 // isotropic material K_e(R0 p) = R0 K_e(p) R0^T, so the rotated rest frame
 // of the reference and the world frame give the same stiffness.
-// The compact matvec's material factors of one element: sqrt(s / 6) with s
-// the isotropic scale of computeMaterialStiffness (TFEM.inl:256-291), so that
-// sqrt(K(0,0)) = sqrt(s / 6) / sqrt(|det|) for K(0,0) = s / (36 V), and the
-// ratios K(0,1)/K(0,0), K(3,3)/K(0,0).
-__host__ __device__ inline float4 compact_material(double Ey, double nu)
-{
-    const double sc = (Ey * (1 - nu)) / ((1 + nu) * (1 - 2 * nu));
-    return make_float4((float)sqrt(sc / 6.0), (float)(nu / (1 - nu)), (float)((1 - 2 * nu) / (2 * (1 - nu))), 0.f);
-}
-
-struct CompactView {
-    const float4* rotq;      // per element: quaternion of Q
-    const float4* emat;      // per element {sqrt(s/6), K(0,1)/K(0,0), K(3,3)/K(0,0), 0}, or null: uniform
-    const float4* nrest_hi;  // per node: rest position, high float parts
-    const float4* nrest_lo;  // per node: rest position, low float parts
-    float4 mat;              // the uniform material factors
-};
 
 // Node -> (element*4 + corner) incidence in CSR form, each row sorted by slot.
 struct NodeCSR {
@@ -141,14 +120,6 @@ struct TfemMesh {
     int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads
     int update_minb = 4;      // CG update: resident CTAs per SM the register cap is set for
     int update_grid = 0;      // CG update grid; 0: one thread per group of four nodes
-    // compact FP32 matvec (mixed large / polar meshes with patches)
-    int compact = 0;
-    float4* rotq = nullptr;      // per element: quaternion of Q = R0^T R
-    float4* emat = nullptr;      // per element material factors (null when uniform)
-    float4* nrest_hi = nullptr;  // per node: rest position as float-float, high parts
-    float4* nrest_lo = nullptr;  // low parts
-    float4 cmat = {0.f, 0.f, 0.f, 0.f};  // uniform material factors
-    int patch_grid_c = 0, adddforce_grid_c = 0;  // CTAs of the compact kernels
     int* dev_flags = nullptr; // sticky device error flag: 1 = a bounded device wait ran out
     double rest_volume = 0.0;
     // plasticity (plasticMaxThreshold > 0): 6 plastic strain rows per

@@ -655,20 +655,6 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
         }
     }
     store_rot(ev, (size_t)e, Rm);
-    if constexpr (is_mixed<R>::value) {
-        if (ev.rotq) {
-            // Q = R0^T R for the compact matvec
-            float R0m[9], Q[9];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) R0m[i] = ev.R0rows[i * En + e];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    Q[3 * i + j] = R0m[i] * Rm[j] + R0m[3 + i] * Rm[3 + j] + R0m[6 + i] * Rm[6 + j];
-            ev.rotq[e] = rot_to_quat(Q);
-        }
-    }
     addforce_element(F, D, K, J, pl, (size_t)e, En);
     // f[node] += rotations[e] * F_node, rotations[e] = R^T
 #pragma unroll
@@ -1650,229 +1636,6 @@ __global__ void __launch_bounds__(kPatchThreads, sizeof(R) == 4 ? 10 : 1)
     for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) (void)patch_body<R, 0>(pv, ev, P, args, ef, lp, sl, lr);
 }
 
-// ------------------------------------------------------------------------
-// FP32 fused matvec, compact element format: per element only the rotation
-// Q = R0^T R (16 B) and the local connectivity; the strain-displacement
-// values are formed on the fly from the nodes' rest positions in the world
-// frame (float-float, staged per local node in phase 0 with the nodal
-// values). With node a's edges e_b, e_c, e_d (each formed from the
-// float-float positions and rounded once), computeStrainDisplacement
-// (TFEM.inl:134-209) on rest coordinates relative to node a gives
-// J_b = e_c x e_d, J_c = e_d x e_b, J_d = e_b x e_c, J_a = -(J_b + J_c + J_d),
-// and K(0,0) = s / (36 V) = s / (6 |e_b . J_b|): the kernel carries
-// J sqrt(K(0,0)) and the two ratios K(0,1)/K(0,0), K(3,3)/K(0,0), as the
-// stored FP32 format does. Element data drops from 64 to 16 bytes (32 with a
-// per-element material).
-// ------------------------------------------------------------------------
-__host__ __device__ __forceinline__ size_t patch_smem_size_c(int pe, int max_lnodes)
-{
-    return sizeof(float) * 12 * (size_t)pe + 8 * (size_t)pe + ((4 * ((size_t)max_lnodes + 1) + 15) & ~(size_t)15) +
-           48 * (size_t)max_lnodes;
-}
-
-__device__ __forceinline__ void patch_smem_carve_c(unsigned char* base, int pe, int max_lnodes, float** ef,
-                                                   uint16_t** sl, int** lr, float4** lp, float4** rh, float4** rl)
-{
-    unsigned char* p = base;
-    *ef = reinterpret_cast<float*>(p);
-    p += sizeof(float) * 12 * (size_t)pe;
-    *sl = reinterpret_cast<uint16_t*>(p);
-    p += 8 * (size_t)pe;
-    *lr = reinterpret_cast<int*>(p);
-    p += (4 * ((size_t)max_lnodes + 1) + 15) & ~(size_t)15;
-    *lp = reinterpret_cast<float4*>(p);
-    p += 16 * (size_t)max_lnodes;
-    *rh = reinterpret_cast<float4*>(p);
-    p += 16 * (size_t)max_lnodes;
-    *rl = reinterpret_cast<float4*>(p);
-}
-
-// J sqrt(K(0,0)) of an element from its nodes' float-float rest positions
-// and its material factors m = {sqrt(s/6), K(0,1)/K(0,0), K(3,3)/K(0,0)}.
-__device__ __forceinline__ void compact_strain_displacement(const float4 h[4], const float4 l[4], float4 m,
-                                                            float J[12], float K[3])
-{
-    float eb[3], ec[3], ed[3];
-    eb[0] = (h[1].x - h[0].x) + (l[1].x - l[0].x);
-    eb[1] = (h[1].y - h[0].y) + (l[1].y - l[0].y);
-    eb[2] = (h[1].z - h[0].z) + (l[1].z - l[0].z);
-    ec[0] = (h[2].x - h[0].x) + (l[2].x - l[0].x);
-    ec[1] = (h[2].y - h[0].y) + (l[2].y - l[0].y);
-    ec[2] = (h[2].z - h[0].z) + (l[2].z - l[0].z);
-    ed[0] = (h[3].x - h[0].x) + (l[3].x - l[0].x);
-    ed[1] = (h[3].y - h[0].y) + (l[3].y - l[0].y);
-    ed[2] = (h[3].z - h[0].z) + (l[3].z - l[0].z);
-    J[3] = ec[1] * ed[2] - ec[2] * ed[1];
-    J[4] = ec[2] * ed[0] - ec[0] * ed[2];
-    J[5] = ec[0] * ed[1] - ec[1] * ed[0];
-    J[6] = ed[1] * eb[2] - ed[2] * eb[1];
-    J[7] = ed[2] * eb[0] - ed[0] * eb[2];
-    J[8] = ed[0] * eb[1] - ed[1] * eb[0];
-    J[9] = eb[1] * ec[2] - eb[2] * ec[1];
-    J[10] = eb[2] * ec[0] - eb[0] * ec[2];
-    J[11] = eb[0] * ec[1] - eb[1] * ec[0];
-    const float det = eb[0] * J[3] + eb[1] * J[4] + eb[2] * J[5];
-    const float sk = m.x * rsqrtf(fabsf(det));
-#pragma unroll
-    for (int i = 3; i < 12; ++i) J[i] *= sk;
-    J[0] = -(J[3] + J[6] + J[9]);
-    J[1] = -(J[4] + J[7] + J[10]);
-    J[2] = -(J[5] + J[8] + J[11]);
-    K[0] = 1.f;
-    K[1] = m.y;
-    K[2] = m.z;
-}
-
-template <int MODE, int PC>
-__device__ __forceinline__ float patch_body_c(const PatchView& pv, const CompactView& cv, int P,
-                                              const PatchArgs<float>& a, float* ef, float4* lp, float4* rh,
-                                              float4* rl, uint16_t* sl, int* lr)
-{
-    float pen = 0.f;
-    const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
-    const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
-    {
-        const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
-        uint4* dst = reinterpret_cast<uint4*>(sl);
-        const int n16 = (8 * ne + 15) >> 4;
-        for (int k = threadIdx.x; k < n16; k += blockDim.x) dst[k] = src[k];
-        for (int l = threadIdx.x; l <= nn; l += blockDim.x) lr[l] = pv.lrow[n0 + l] - 4 * e0;
-    }
-    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int g = pv.lnode_gid[n0 + l];
-        rh[l] = cv.nrest_hi[g];
-        rl[l] = cv.nrest_lo[g];
-        float v[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float rv = a.rin[3 * (size_t)g + k];
-            if constexpr (PC != 0) rv = a.dinv[3 * (size_t)g + k] * rv;
-            v[k] = (MODE == 2) ? cg_dir(rv, a.pold[3 * (size_t)g + k], a.beta) : rv;
-        }
-        lp[l] = make_float4(v[0], v[1], v[2], 0.f);
-        if (MODE != 0) {
-            const int info = pv.lnode_info[n0 + l];
-            if (info < 0 || (info & 1)) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) a.pnew[3 * (size_t)g + k] = v[k];
-            }
-        }
-    }
-    __syncthreads();
-    for (int le = threadIdx.x; le < ne; le += blockDim.x) {
-        const size_t e = (size_t)(e0 + le);
-        const ushort4 c = pv.lconn[e];
-        float Qm[9], K[3], J[12];
-        quat_to_rot(cv.rotq[e], Qm);
-        {
-            const float4 h[4] = {rh[c.x], rh[c.y], rh[c.z], rh[c.w]};
-            const float4 l[4] = {rl[c.x], rl[c.y], rl[c.z], rl[c.w]};
-            compact_strain_displacement(h, l, cv.emat ? cv.emat[e] : cv.mat, J, K);
-        }
-        const float4 v0 = lp[c.x], v1 = lp[c.y], v2 = lp[c.z], v3 = lp[c.w];
-        const float xr[4][3] = {{0.f, 0.f, 0.f},
-                                {v1.x - v0.x, v1.y - v0.y, v1.z - v0.z},
-                                {v2.x - v0.x, v2.y - v0.y, v2.z - v0.z},
-                                {v3.x - v0.x, v3.y - v0.y, v3.z - v0.z}};
-        float X[12], F[12];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                X[3 * i + k] = Qm[3 * k] * xr[i][0] + Qm[3 * k + 1] * xr[i][1] + Qm[3 * k + 2] * xr[i][2];
-        element_force(F, X, K, J, a.kf);
-        float en = 0.f;
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float ck = Qm[k] * F[3 * i] + Qm[3 + k] * F[3 * i + 1] + Qm[6 + k] * F[3 * i + 2];
-                ef[(3 * i + k) * pv.pe + le] = ck;
-                en += xr[i][k] * ck;
-            }
-        if (MODE != 0) pen -= en;
-    }
-    __syncthreads();
-    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int s0 = lr[l], s1 = lr[l + 1];
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        for (int s = s0; s < s1; ++s) {
-            const int slot = sl[s];
-            const int le = slot >> 2, cc = slot & 3;
-            a0 += ef[(3 * cc + 0) * pv.pe + le];
-            a1 += ef[(3 * cc + 1) * pv.pe + le];
-            a2 += ef[(3 * cc + 2) * pv.pe + le];
-        }
-        const int g = pv.lnode_gid[n0 + l];
-        const int info = pv.lnode_info[n0 + l];
-        if (info >= 0) {
-            float* o = a.partials + 3 * (size_t)(info >> 1);
-            o[0] = a0;
-            o[1] = a1;
-            o[2] = a2;
-        }
-        if (MODE == 0) {
-            if (info < 0) {
-                a.qout[3 * (size_t)g] -= a0;
-                a.qout[3 * (size_t)g + 1] -= a1;
-                a.qout[3 * (size_t)g + 2] -= a2;
-            }
-        } else if (info < 0 || (info & 1)) {
-            const float4 pl = lp[l];
-            const float mm = a.ma.node_mass ? (float)(a.ma.node_mass[g] * a.mf) : a.mmu;
-            pen += mm * (pl.x * pl.x + pl.y * pl.y + pl.z * pl.z);
-            if (info < 0) {
-                float q0 = mm * pl.x - a0, q1 = mm * pl.y - a1, q2 = mm * pl.z - a2;
-                if (a.fixed[g]) q0 = q1 = q2 = 0.f;
-                a.qout[3 * (size_t)g] = q0;
-                a.qout[3 * (size_t)g + 1] = q1;
-                a.qout[3 * (size_t)g + 2] = q2;
-            }
-        }
-    }
-    __syncthreads();
-    return pen;
-}
-
-template <int MODE, int PC>
-__global__ void __launch_bounds__(kPatchThreads, 8)
-    k_patch_matvec_c(PatchView pv, CompactView cv, const float* __restrict__ rin, const float* __restrict__ pold,
-                     float* __restrict__ pnew, CgScalars* cg, float kf, MassArgs ma, double mf,
-                     const uint8_t* __restrict__ fixed, float* __restrict__ qout, float* __restrict__ partials,
-                     SolveConsts sc, const float* __restrict__ dinv)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* ef;
-    float4 *lp, *rh, *rl;
-    uint16_t* sl;
-    int* lr;
-    patch_smem_carve_c(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp, &rh, &rl);
-    if (cg->done) return;
-    const float beta = (MODE == 2) ? (float)cg->beta : 0.f;
-    const float mmu = (float)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
-    const PatchArgs<float> args{rin, pold, pnew, beta, kf, mmu, ma, mf, fixed, qout, partials, dinv};
-    double energy = 0.0;
-    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
-        energy += (double)patch_body_c<MODE, PC>(pv, cv, P, args, ef, lp, rh, rl, sl, lr);
-    finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
-}
-
-__global__ void __launch_bounds__(kPatchThreads, 8)
-    k_patch_adddforce_c(PatchView pv, CompactView cv, const float* __restrict__ dx, float kf, float* __restrict__ df,
-                        float* __restrict__ partials)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* ef;
-    float4 *lp, *rh, *rl;
-    uint16_t* sl;
-    int* lr;
-    patch_smem_carve_c(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp, &rh, &rl);
-    const PatchArgs<float> args{dx, nullptr, nullptr, 0.f, kf, 0.f, {nullptr, 0.0, {0.0, 0.0, 0.0}}, 1.0, nullptr, df,
-                                partials, nullptr};
-    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x)
-        (void)patch_body_c<0, 0>(pv, cv, P, args, ef, lp, rh, rl, sl, lr);
-}
-
 // C ABI addDForce, second pass: nodes shared by several patches subtract
 // their partial sums in patch order.
 template <typename R>
@@ -2152,18 +1915,6 @@ __global__ void __launch_bounds__(kNodeBlock, MINB) k_cg_update_patch(R* __restr
 // copy of the operator.
 // ------------------------------------------------------------------------
 
-// r32 = b64 (rounded), xs32 = 0: the FP32 solve starts from the FP64 RHS.
-template <typename R>
-__global__ void __launch_bounds__(kNodeBlock) k_refine_start(const double* __restrict__ b64, R* __restrict__ r,
-                                                             R* __restrict__ xs, int N)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 3 * (size_t)N;
-         i += (size_t)gridDim.x * blockDim.x) {
-        r[i] = (R)b64[i];
-        xs[i] = R(0);
-    }
-}
-
 // x64 += xs32, xs32 = 0, if a replacement was decided after iteration `it`.
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_refine_accumulate(double* __restrict__ x64, R* __restrict__ xs,
@@ -2253,48 +2004,7 @@ ElemView<R> view(TfemMesh* m)
     ev.R0 = m->method == METHOD_SVD ? (const R*)m->R0 : nullptr;
     ev.n_tets = m->n_tets;
     ev.method = m->method;
-    if (m->compact) {
-        ev.rotq = m->rotq;
-        ev.R0rows = (const R*)m->R0;
-    }
     return ev;
-}
-
-inline CompactView compact_view(const TfemMesh* m)
-{
-    return CompactView{m->rotq, m->emat, m->nrest_hi, m->nrest_lo, m->cmat};
-}
-
-// Compact format at rest: Q = identity, per-element material factors when
-// the material varies, and the float-float rest positions of the nodes.
-__global__ void k_init_compact(const double* __restrict__ rest_pos, const int* __restrict__ elem_orig, int E, int N,
-                               const double* __restrict__ young, int n_young, const double* __restrict__ poisson,
-                               int n_poisson, const double* __restrict__ lsf, int n_lsf, float4* __restrict__ rotq,
-                               float4* __restrict__ emat, float4* __restrict__ hi, float4* __restrict__ lo)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < E) {
-        rotq[i] = make_float4(0.f, 0.f, 0.f, 1.f);
-        if (emat) {
-            // getVecRealInElement (BaseLinearElasticityFEMForceField.inl:114-132)
-            const int e = elem_orig[i];
-            double Ey = (n_young > e) ? young[e] : young[0];
-            const double nu = (n_poisson > e) ? poisson[e] : poisson[0];
-            const double f = (n_lsf > 0) ? lsf[(size_t)e * (size_t)n_lsf / (size_t)E] : 1.0;
-            emat[i] = compact_material(f * Ey, nu);
-        }
-    }
-    if (i < N) {
-        float h[3], l[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const double x = rest_pos[3 * (size_t)i + k];
-            h[k] = (float)x;
-            l[k] = (float)(x - (double)h[k]);
-        }
-        hi[i] = make_float4(h[0], h[1], h[2], 0.f);
-        lo[i] = make_float4(l[0], l[1], l[2], 0.f);
-    }
 }
 
 template <typename R>
@@ -2305,12 +2015,6 @@ void launch_init(TfemMesh* m, const double* young, int ny, const double* poisson
     k_init_elements<R><<<elem_grid(m->n_tets), kElemBlock, 0, s>>>(
         m->rest_pos, m->tets, m->elem_orig, m->n_tets, m->method, young, ny, poisson, np, lsf, nl, (R*)m->K,
         (R*)m->J, (R*)m->rest, m->rest_ff, (R*)m->rot, (R*)m->A0inv, (R*)m->R0, vol);
-    if (m->compact) {
-        const int n = std::max(m->n_tets, m->n_nodes);
-        k_init_compact<<<(n + kElemBlock - 1) / kElemBlock, kElemBlock, 0, s>>>(
-            m->rest_pos, m->elem_orig, m->n_tets, m->n_nodes, young, ny, poisson, np, lsf, nl, m->rotq, m->emat,
-            m->nrest_hi, m->nrest_lo);
-    }
 }
 
 // Mixed precision: the per-element factor sqrt(K(0,0)) of the stored
@@ -2481,18 +2185,6 @@ size_t patch_smem_bytes(const TfemMesh* m)
     return patch_smem_size<R>(m->pl.pe, m->pl.max_lnodes);
 }
 
-// The compact FP32 matvec of CG iteration `it` (MODE 1 on the first).
-template <int PC, typename... A>
-void launch_matvec_c(const TfemMesh* m, int it, cudaStream_t s, const PatchView& pv, A... a)
-{
-    const size_t smem = patch_smem_size_c(m->pl.pe, m->pl.max_lnodes);
-    const CompactView cv = compact_view(m);
-    if (it == 1)
-        k_patch_matvec_c<1, PC><<<m->patch_grid_c, kPatchThreads, smem, s>>>(pv, cv, a...);
-    else
-        k_patch_matvec_c<2, PC><<<m->patch_grid_c, kPatchThreads, smem, s>>>(pv, cv, a...);
-}
-
 // The CG update with the register cap chosen at preparation (MINB resident
 // CTAs of kNodeBlock threads per SM).
 template <typename R, int PC = 0, typename... A>
@@ -2581,18 +2273,6 @@ int prepare_patch(TfemMesh* m)
         if (ga > m->pl.n_patches) ga = m->pl.n_patches;
         m->adddforce_grid = (int)(ga < 1 ? 1 : ga);
     }
-    if constexpr (is_mixed<R>::value) {
-        if (m->compact) {
-            const size_t sc = patch_smem_size_c(m->pl.pe, m->pl.max_lnodes);
-            const int np = m->pl.n_patches;
-            int gc = resident_grid(k_patch_matvec_c<1, 0>, kPatchThreads, sc, sms, np);
-            gc = std::min(gc, resident_grid(k_patch_matvec_c<2, 0>, kPatchThreads, sc, sms, np));
-            gc = std::min(gc, resident_grid(k_patch_matvec_c<1, 1>, kPatchThreads, sc, sms, np));
-            gc = std::min(gc, resident_grid(k_patch_matvec_c<2, 1>, kPatchThreads, sc, sms, np));
-            m->patch_grid_c = gc;
-            m->adddforce_grid_c = resident_grid(k_patch_adddforce_c, kPatchThreads, sc, sms, np);
-        }
-    }
     return (int)g;
 }
 
@@ -2614,17 +2294,7 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
         PatchView pv = patch_view(m);
         MassArgs ma{nullptr, 0.0, {0.0, 0.0, 0.0}};
         SolveConsts sc{0.0, 0.0, 0};
-        bool done = false;
-        if constexpr (is_mixed<R>::value) {
-            if (m->compact) {
-                k_patch_adddforce_c<<<m->adddforce_grid_c, kPatchThreads,
-                                      patch_smem_size_c(m->pl.pe, m->pl.max_lnodes), s>>>(
-                    pv, compact_view(m), dx, kfactor, df, (R*)m->pl.partials);
-                done = true;
-            }
-        }
-        if (!done)
-            k_patch_adddforce<R><<<m->adddforce_grid, kPatchThreads, patch_smem_bytes<R>(m), s>>>(
+        k_patch_adddforce<R><<<m->adddforce_grid, kPatchThreads, patch_smem_bytes<R>(m), s>>>(
                 pv, view<R>(m), dx, kfactor, df, (R*)m->pl.partials, nullptr, 0);
         k_patch_fixup<R><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(m->pl.bnd_rowptr, (const R*)m->pl.partials, df,
                                                                       m->n_nodes);
@@ -2791,17 +2461,7 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
         if (dinv) {
-            bool pdone = false;
-            if constexpr (is_mixed<R>::value) {
-                if (m->compact) {
-                    launch_matvec_c<1>(m, it, s, pv, (const float*)r, (const float*)pold, pnew, sc->cg, (R)kf, ma,
-                                       mf, (const uint8_t*)sc->fixed, q, partials, cons, (const float*)dinv);
-                    pdone = true;
-                }
-            }
-            if (pdone)
-                ;
-            else if (it == 1)
+            if (it == 1)
                 k_patch_matvec<R, 1, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
                     pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch,
                     dinv);
@@ -2814,17 +2474,7 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
                                    m->update_vec4, dinv);
             continue;
         }
-        bool done = false;
-        if constexpr (is_mixed<R>::value) {
-            if (m->compact) {
-                launch_matvec_c<0>(m, it, s, pv, (const float*)r, (const float*)pold, pnew, sc->cg, (R)kf, ma, mf,
-                                   (const uint8_t*)sc->fixed, q, partials, cons, (const float*)nullptr);
-                done = true;
-            }
-        }
-        if (done)
-            ;
-        else if (it == 1)
+        if (it == 1)
             k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
                 pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
         else
@@ -2852,7 +2502,6 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
     const double h = P.dt;
     MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
     const int ng = node_grid(N);
-    const int ng3 = node_grid(3 * N);
     R* r = (R*)sc->r;
     R* pb[2] = {(R*)sc->p, (R*)sc->p2};
     R* q = (R*)sc->q;
@@ -2869,9 +2518,18 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
     k_gather_rhs<double><<<ng, kNodeBlock, 0, s>>>(csr64, (const double*)sh->eforce, sc->w64, sc->v, ma,
                                                    -P.rayleigh_mass, mass_first, h, sc->fixed, sc->b64, sc->r64,
                                                    sc->x64, sc->cg, nullptr, N, cons);
-    // FP32: the element rotations at x, r = b, xs = 0
+    // FP32: the plain mixed step's forces and right-hand side (b, r = b,
+    // xs = 0); its CG start replaces the FP64 one's, so that a step whose
+    // solve never meets the replacement condition is the plain mixed step,
+    // bit for bit; b64 is used only by the replacements
+    NodeCSR csr{m->rowptr, m->slots};
     launch_elem_force<R>(m, sc->x, s);
-    k_refine_start<R><<<ng3, kNodeBlock, 0, s>>>(sc->b64, r, xs, N);
+    k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first,
+                                                (R*)sc->f, N);
+    launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)F.kf_rhs, s);
+    k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->f, sc->v, ma,
+                                              -P.rayleigh_mass, mass_first, h, sc->fixed, (R*)sc->b, r, xs, sc->cg,
+                                              nullptr, N, cons);
     const double mf = F.mf_mass;
     const double kf = F.kf_ff;
     PatchView pv = patch_view(m);
@@ -2883,11 +2541,7 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
         cons.it = it;
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
-        if (m->compact)
-            launch_matvec_c<0>(m, it, s, pv, (const float*)r, (const float*)pold, (float*)pnew, sc->cg, (float)kf,
-                               ma, mf, (const uint8_t*)sc->fixed, (float*)q, (float*)partials, cons,
-                               (const float*)nullptr);
-        else if (it == 1)
+        if (it == 1)
             k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
                 pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
         else
@@ -2897,7 +2551,7 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
                             (const R*)q, (const R*)partials, (const int*)m->pl.bnd_rowptr, ma, mf,
                             (const uint8_t*)sc->fixed, sc->cg, N, cons, m->update_vec4);
         if (k > 0 && it % k == 0 && it < P.cg_iterations) {
-            k_refine_accumulate<R><<<ng3, kNodeBlock, 0, s>>>(sc->x64, xs, sc->cg, it, N);
+            k_refine_accumulate<R><<<node_grid(3 * N), kNodeBlock, 0, s>>>(sc->x64, xs, sc->cg, it, N);
             cudaMemsetAsync(sc->w64, 0, sizeof(double) * 3 * (size_t)N, s);
             k_patch_adddforce<double><<<sh->patch_grid, kPatchThreads, patch_smem_bytes<double>(sh), s>>>(
                 patch_view(sh), view<double>(sh), sc->x64, kf, sc->w64, (double*)sh->pl.partials,

@@ -54,13 +54,22 @@ def test_residual_replacement_reaches_fp64_accuracy(capi):
     assert err_r <= 0.1 * err_m, (err_r, err_m)
 
 
-def test_residual_replacement_runs_on_the_stiff_inclusion(capi):
+def test_residual_replacement_no_worse_on_the_stiff_inclusion(capi):
     """The ill-conditioned inclusion beam (E 1e6 in 1e3, nu 0.49) truncated at
-    CG 200: every variant stays finite; the errors against FP64 are reported
-    by the benchmark, not bounded here (none of the solves converges)."""
+    CG 200: replacements happen only when the recurrence residual has dropped
+    by 2^-12 below its largest value (van der Vorst and Ye), so on solves that
+    are far from converged the replaced run is no further from FP64 than the
+    plain mixed run -- and equal to it bit for bit when no replacement
+    happens."""
     ib = topo.inclusion_beam((8, 8, 25), seed=3)
+    x64, _, _ = _run(capi, ib.mesh, ib.young, 0.49, "fp64_fma", 0, 5, 200, ib.tip_force)
     xr, ir, rr = _run(capi, ib.mesh, ib.young, 0.49, "mixed", 20, 5, 200, ib.tip_force)
-    assert np.all(np.isfinite(xr)) and np.isfinite(rr) and ir == 200
+    xm, im, rm = _run(capi, ib.mesh, ib.young, 0.49, "mixed", 0, 5, 200, ib.tip_force)
+    assert np.all(np.isfinite(xr)) and np.isfinite(rr)
+    d = np.linalg.norm(x64 - ib.mesh.positions)
+    err_r = np.linalg.norm(xr - x64) / d
+    err_m = np.linalg.norm(xm - x64) / d
+    assert np.array_equal(xr, xm) or err_r <= 1.05 * err_m, (err_r, err_m)
 
 
 def test_residual_replacement_rejected_for_fp64(capi):
