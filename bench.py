@@ -254,6 +254,11 @@ def run_batched(torch, capi, args, plain_best):
     nodes = sum(m.n_nodes for m, _ in beams)
     threads = min(16, host_threads())
     b = capi.Batch("mixed", budget_bytes=int(60e9), max_meshes=args.beams + 8, max_cg_iterations=25)
+    # elements per patch picked by timing a sample of the population (every
+    # 16th beam) before admission
+    t0 = time.perf_counter()
+    pe, pe_ms = b.tune_patch_size([(m.positions, m.tetrahedra, kw) for m, kw in beams[::16]], steps_per_trial=2)
+    pe_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     slots = b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=threads)
     admit_s = time.perf_counter() - t0
@@ -293,7 +298,9 @@ def run_batched(torch, capi, args, plain_best):
     return {"workload": f"{len(beams)} beams, {nodes} nodes, {tets} tets, mixed precision, one launch per phase, "
                         "CUDA-graph steps", "tet_steps_per_s": value, "ms_per_step": t / k * 1e3, "steps": k,
             "admission_s": admit_s, "budget_used_bytes": info["budget_used"],
-            "tiles": dict(tuning, tuning_s=tune_s),
+            "tiles": dict(tuning, tuning_s=tune_s,
+                          patch_size_sample_ms_per_step={str(k): v for k, v in pe_ms.items()},
+                          patch_size_tuning_s=pe_s),
             "speedup_vs_plain_fp64_single_mesh": value / plain_best,
             "position_error": {"steps": args.warmup + k, "beams_checked": len(beams),
                                "rel_l2_position_max": max(errs), "rel_l2_position_median": float(np.median(errs)),

@@ -419,6 +419,17 @@ void* sgb_batch_stream(sgb_batch_t* batch);
  * (elements per patch: 512 mixed, 256 FP64), because it fixes each node's
  * gather order. Synchronous. */
 int sgb_batch_tune(sgb_batch_t* batch, int steps_per_trial, int use_cache);
+/* Elements per patch (the matvec's elements per CTA) picked before any mesh is
+ * admitted, by timing a sample of the workload: for each candidate (256, 384,
+ * 512 in mixed precision; 128, 192, 256 in FP64) the sample meshes are
+ * admitted with that patch size, stepped steps_per_trial times after one
+ * warm-up step, and removed. The fastest candidate is kept for the batch's
+ * lifetime (it fixes every mesh's gather order, so results depend on it,
+ * deterministically). chosen (may be NULL): the patch size kept;
+ * ms_per_step (may be NULL): the three candidates' step times.
+ * SGB_ERR_NOT_SUPPORTED when meshes are admitted already. Synchronous. */
+int sgb_batch_tune_patch_size(sgb_batch_t* batch, const sgb_mesh_desc* sample, int n, int steps_per_trial,
+                              int* chosen, double* ms_per_step);
 /* tiles: matvec CTAs per SM, update nodes per thread, update CTAs per SM,
  * element CTAs per SM, prefetch (0 / 1). */
 int sgb_batch_set_tiles(sgb_batch_t* batch, const int tiles[5]);

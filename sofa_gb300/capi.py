@@ -183,6 +183,8 @@ def load():
                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
         "sgb_batch_stream": (_vp, [_vp]),
         "sgb_batch_tune": (c_int, [_vp, c_int, c_int]),
+        "sgb_batch_tune_patch_size": (c_int, [_vp, ctypes.POINTER(MeshDesc), c_int, c_int, ctypes.POINTER(c_int),
+                                              _dp]),
         "sgb_batch_set_tiles": (c_int, [_vp, ctypes.POINTER(c_int)]),
         "sgb_batch_get_tiles": (c_int, [_vp, ctypes.POINTER(c_int), _dp, _dp, ctypes.POINTER(c_int)]),
         "sgb_server_create": (c_int, [ctypes.POINTER(_vp), c_int, ctypes.c_size_t, c_int, c_int, c_int, c_int]),
@@ -634,6 +636,23 @@ class Batch:
         (state is restored; results do not change)."""
         check(load().sgb_batch_tune(self._h, int(steps_per_trial), int(use_cache)))
         return self.tuning()
+
+    def tune_patch_size(self, sample, steps_per_trial=2):
+        """Elements per patch picked by timing `sample` ([(positions,
+        tetrahedra, kwargs), ...]) at each candidate size; call before
+        admitting meshes. Returns (chosen, {size: ms per step})."""
+        descs = (MeshDesc * len(sample))()
+        keep = []
+        for i, (pos, tets, kw) in enumerate(sample):
+            d, k = self.mesh_desc(pos, tets, **kw)
+            descs[i] = d
+            keep.append(k)
+        chosen = ctypes.c_int()
+        ms = (ctypes.c_double * 3)()
+        check(load().sgb_batch_tune_patch_size(self._h, descs, len(sample), int(steps_per_trial),
+                                               ctypes.byref(chosen), ms))
+        cands = (256, 384, 512) if self.precision == "mixed" else (128, 192, 256)
+        return chosen.value, {c: ms[i] for i, c in enumerate(cands)}
 
     def set_tiles(self, matvec_ctas_per_sm=6, update_nodes_per_thread=4, update_ctas_per_sm=4,
                   elem_ctas_per_sm=4, prefetch=0):

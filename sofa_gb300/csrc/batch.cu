@@ -783,6 +783,62 @@ int valid_tiles(const BatchTiles& t)
 
 }  // namespace
 
+int sgb_batch_tune_patch_size(sgb_batch_t* B, const sgb_mesh_desc* sample, int n, int steps_per_trial,
+                              int* chosen, double* ms_per_step)
+{
+    if (!B || !sample || n <= 0 || steps_per_trial < 1)
+        return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_tune_patch_size: invalid argument");
+    for (auto& m : B->slots)
+        if (m.active)
+            return bfail(SGB_ERR_NOT_SUPPORTED, "sgb_batch_tune_patch_size: the patch size is chosen before any "
+                                                "mesh is admitted (it fixes each mesh's gather order)");
+    // elements per patch: 256, 384, 512 (FP32); 128, 192, 256 (FP64)
+    const int cand[3] = {B->rs == 4 ? 256 : 128, B->rs == 4 ? 384 : 192, B->rs == 4 ? 512 : 256};
+    const int start = B->pe;
+    cudaEvent_t e0, e1;
+    BTRY(cudaEventCreate(&e0));
+    BTRY(cudaEventCreate(&e1));
+    std::vector<int> slots((size_t)n, -1);
+    int best = start, rc = SGB_OK;
+    double best_ms = 0.0;
+    for (int c = 0; c < 3 && rc == SGB_OK; ++c) {
+        B->pe = cand[c];
+        B->sms = B->ops->batch_prepare(B->pe, B->grid_patch_v);
+        B->graph_valid = false;
+        if (B->sms <= 0) {
+            rc = bfail(SGB_ERR_CUDA, "sgb_batch_tune_patch_size: kernel attributes");
+            break;
+        }
+        rc = sgb_batch_add_meshes(B, sample, n, slots.data(), 8);
+        if (rc == SGB_OK) rc = sgb_batch_step(B, 1);  // records the graph; warms up
+        float f = 0.f;
+        if (rc == SGB_OK) {
+            cudaError_t ce;
+            if ((ce = cudaEventRecord(e0, B->stream)) != cudaSuccess) rc = bcuda(ce, "cudaEventRecord");
+            if (rc == SGB_OK) rc = sgb_batch_step(B, steps_per_trial);
+            if (rc == SGB_OK && ((ce = cudaEventRecord(e1, B->stream)) != cudaSuccess ||
+                                 (ce = cudaEventSynchronize(e1)) != cudaSuccess ||
+                                 (ce = cudaEventElapsedTime(&f, e0, e1)) != cudaSuccess))
+                rc = bcuda(ce, "timing");
+        }
+        for (int i = 0; i < n; ++i)
+            if (slots[(size_t)i] >= 0) sgb_batch_remove_mesh(B, slots[(size_t)i]);
+        const double ms = (double)f / steps_per_trial;
+        if (ms_per_step) ms_per_step[c] = ms;
+        if (rc == SGB_OK && (c == 0 || ms < best_ms)) {
+            best = cand[c];
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->pe = rc == SGB_OK ? best : start;
+    B->sms = B->ops->batch_prepare(B->pe, B->grid_patch_v);
+    B->graph_valid = false;
+    if (chosen) *chosen = B->pe;
+    return rc;
+}
+
 int sgb_batch_set_tiles(sgb_batch_t* B, const int tiles[5])
 {
     if (!B || !tiles) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_set_tiles: NULL argument");

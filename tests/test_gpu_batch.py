@@ -167,3 +167,30 @@ def test_tuner_keeps_state_and_results(capi):
         b.close()
     for (xa, va), (xb, vb) in zip(*res):
         assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+def test_patch_size_tuning(capi, monkeypatch):
+    """Elements per patch chosen by timing a sample before admission: the
+    choice is one of the candidates, a batch admits and steps with it exactly
+    as a batch created with that patch size, and the choice is refused once
+    meshes are admitted."""
+    meshes = [(topo.beam(n, 0.5, 0.05, seed), E, nu, m) for n, seed, E, nu, m in MESHES]
+    sample = [(mesh.positions, mesh.tetrahedra, beam_kw(mesh, E, nu, m)) for mesh, E, nu, m in meshes]
+    b = capi.Batch("mixed", budget_bytes=256 << 20, max_meshes=8)
+    chosen, ms = b.tune_patch_size(sample, steps_per_trial=2)
+    assert chosen in (256, 384, 512) and sorted(ms) == [256, 384, 512] and all(v > 0 for v in ms.values())
+    assert b.tuning()["elements_per_patch"] == chosen
+    slots = [b.add_mesh(*m) for m in sample]
+    b.step(10)
+    got = [b.state(s)[0] for s in slots]
+    with pytest.raises(capi.SgbError) as e:
+        b.tune_patch_size(sample)
+    assert e.value.code == -4
+    b.close()
+    monkeypatch.setenv("SGB_BATCH_PE", str(chosen))
+    ref = capi.Batch("mixed", budget_bytes=256 << 20, max_meshes=8)
+    rslots = [ref.add_mesh(*m) for m in sample]
+    ref.step(10)
+    for s, x in zip(rslots, got):
+        assert np.array_equal(ref.state(s)[0], x)
+    ref.close()
