@@ -285,6 +285,11 @@ typedef struct sgb_scene_params {
      * of the fixed nodes is set to zero (DefaultAnimationLoop's
      * projectPositionAndVelocity, DefaultAnimationLoop.cpp:228-233, 293). */
     int project_velocity;
+    /* EulerImplicitSolver trapezoidalScheme (EulerImplicitSolver.cpp:117-171):
+     * the factor tr = 0.5 on h in the right-hand side's stiffness factor
+     * (h tr + rs) and in the system factors mF = 1 + tr h rm, bF = -tr h,
+     * kF = -tr h (tr h + rs) (first order: kF = -h tr). */
+    int trapezoidal_scheme;
 } sgb_scene_params;
 
 #define SGB_SOLVER_CG 0
@@ -369,7 +374,8 @@ int sgb_batch_destroy(sgb_batch_t* batch);
  * Euler scheme, so a mesh whose params ask for PCG, a preconditioner,
  * warmStart, residual replacement, serial dots, firstOrder or
  * project_velocity is refused with SGB_ERR_NOT_SUPPORTED, here and at
- * admission. The components' Rayleigh coefficients are supported. */
+ * admission. The components' Rayleigh coefficients and trapezoidalScheme are
+ * supported. */
 int sgb_batch_mesh_bytes(const sgb_batch_t* batch, const sgb_mesh_desc* mesh, size_t* bytes);
 /* Admission: SGB_ERR_BUDGET when the mesh does not fit or no slot is free.
  * Synchronous; positions start at rest, velocities at zero. */

@@ -68,6 +68,7 @@ def _load():
     lib.orc_scene_set_solver.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orc_scene_set_warm_start.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_set_options.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+    lib.orc_scene_set_trapezoidal.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_jacobi.argtypes = [vp, _dp]
     lib.orc_scene_compute_force.argtypes = [vp, _dp]
     lib.orc_scene_last_iterations.restype = ctypes.c_int
@@ -262,12 +263,14 @@ class OracleScene:
         _load().orc_scene_set_warm_start(self._h, int(on))
 
     def set_options(self, ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0, first_order=False,
-                    project_velocity=False):
+                    project_velocity=False, trapezoidal_scheme=False):
         """The force field's and the mass's own Rayleigh coefficients,
-        EulerImplicitSolver firstOrder, FixedProjectiveConstraint
-        activate_projectVelocity."""
-        _load().orc_scene_set_options(self._h, float(ff_rayleigh_stiffness), float(mass_rayleigh_mass),
-                                      int(first_order), int(project_velocity))
+        EulerImplicitSolver firstOrder and trapezoidalScheme,
+        FixedProjectiveConstraint activate_projectVelocity."""
+        lib = _load()
+        lib.orc_scene_set_options(self._h, float(ff_rayleigh_stiffness), float(mass_rayleigh_mass),
+                                  int(first_order), int(project_velocity))
+        lib.orc_scene_set_trapezoidal(self._h, int(trapezoidal_scheme))
 
     def set_solver(self, solver="cg", preconditioner=None, rate=1):
         """solver "cg" (CGLinearSolver) or "pcg" (PCGLinearSolver, warm start);

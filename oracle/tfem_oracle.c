@@ -1193,7 +1193,7 @@ typedef struct orc_scene {
      * mass rayleighMass), EulerImplicitSolver firstOrder,
      * FixedProjectiveConstraint activate_projectVelocity */
     double ff_rs, mass_rm;
-    int first_order, project_velocity;
+    int first_order, project_velocity, trapezoidal;
     double cur_bf; /* bFactor of the matrix being applied (0 for the right-hand side) */
 } orc_scene;
 
@@ -1646,6 +1646,9 @@ void orc_scene_set_solver(orc_scene* s, int solver, int precond, int precond_rat
 /* CGLinearSolver warmStart: each CG solve starts from the previous solution. */
 void orc_scene_set_warm_start(orc_scene* s, int on) { s->warm_start = on ? 1 : 0; }
 
+/* EulerImplicitSolver trapezoidalScheme. */
+void orc_scene_set_trapezoidal(orc_scene* s, int on) { s->trapezoidal = on ? 1 : 0; }
+
 /* The components' own Rayleigh coefficients, EulerImplicitSolver firstOrder and
  * FixedProjectiveConstraint activate_projectVelocity. */
 void orc_scene_set_options(orc_scene* s, double ff_rayleigh_stiffness, double mass_rayleigh_mass, int first_order,
@@ -1689,7 +1692,8 @@ static void scene_compute_force(orc_scene* s)
 static void euler_step(orc_scene* s)
 {
     const long n3 = 3L * s->n;
-    const double h = s->dt, tr = 1.0;
+    /* trapezoidalScheme: tr = 0.5 on some uses of h (EulerImplicitSolver.cpp:117-123) */
+    const double h = s->dt, tr = s->trapezoidal ? 0.5 : 1.0;
     scene_compute_force(s);
     memcpy(s->b, s->f, sizeof(double) * (size_t)n3);
     if (!s->first_order) {

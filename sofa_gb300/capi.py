@@ -61,6 +61,7 @@ class SceneParams(ctypes.Structure):
         ("mass_rayleigh_mass", ctypes.c_double),
         ("first_order", ctypes.c_int),
         ("project_velocity", ctypes.c_int),
+        ("trapezoidal_scheme", ctypes.c_int),
     ]
 
 
@@ -369,7 +370,7 @@ class Scene:
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
                  serial_dots=False, residual_replacement=0, linear_solver="cg", preconditioner=None,
                  preconditioner_rate=1, warm_start=False, ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0,
-                 first_order=False, project_velocity=False):
+                 first_order=False, project_velocity=False, trapezoidal_scheme=False):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -404,6 +405,7 @@ class Scene:
         p.mass_rayleigh_mass = float(mass_rayleigh_mass)
         p.first_order = int(first_order)
         p.project_velocity = int(project_velocity)
+        p.trapezoidal_scheme = int(trapezoidal_scheme)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now
@@ -477,7 +479,7 @@ class Scene:
 def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.0, cg_iterations=25,
                  cg_tolerance=1e-5, cg_threshold=1e-5, gravity=(0.0, -9.81, 0.0), vertex_mass=1.0,
                  node_masses=None, fixed=(), fix_all=False, keep=None, linear_solver="cg", preconditioner=None,
-                 ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0):
+                 ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0, trapezoidal_scheme=False):
     """A filled SceneParams; `keep` collects the numpy buffers it points to.
     linear_solver "cg" or "pcg"; preconditioner None or "jacobi" (PCG)."""
     lib = load()
@@ -506,6 +508,7 @@ def scene_params(dt=0.01, rayleigh_stiffness=0.0, rayleigh_mass=0.0, vdamping=0.
     p.preconditioner = {None: 0, "jacobi": 1}[preconditioner]
     p.ff_rayleigh_stiffness = float(ff_rayleigh_stiffness)
     p.mass_rayleigh_mass = float(mass_rayleigh_mass)
+    p.trapezoidal_scheme = int(trapezoidal_scheme)
     return p
 
 

@@ -509,6 +509,7 @@ int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot_out)
     sp.rayleigh_mass = P.rayleigh_mass;
     sp.ff_rs = P.ff_rayleigh_stiffness;
     sp.mass_rm = P.mass_rayleigh_mass;
+    sp.trapezoidal = P.trapezoidal_scheme ? 1 : 0;
     const StepFactors F = step_factors(sp);
     d.kf_rhs = F.kf_rhs;
     d.rm_factor = -P.rayleigh_mass;

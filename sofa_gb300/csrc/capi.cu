@@ -858,6 +858,7 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     s.prm.mass_rm = P.mass_rayleigh_mass;
     s.prm.first_order = P.first_order ? 1 : 0;
     s.prm.project_velocity = P.project_velocity ? 1 : 0;
+    s.prm.trapezoidal = P.trapezoidal_scheme ? 1 : 0;
     s.stream = fem->stream;
     sc->fem = fem;
     sc->ops = fem->ops;

@@ -717,9 +717,8 @@ int Scene::init_host(std::string* err)
         const int fallback = precision_of(fem->template_name, SGB_PRECISION_FP64);
         b.precision = precision_override >= 0 ? precision_override : precision_of(mo->template_name, fallback);
         // EulerImplicitSolver + CGLinearSolver
-        if (euler->get_bool(*this, "trapezoidalScheme"))
-            return unsupported(err, where + "trapezoidalScheme is not supported");
         sgb_scene_params_default(&b.params);
+        b.params.trapezoidal_scheme = euler->get_bool(*this, "trapezoidalScheme") ? 1 : 0;
         b.params.dt = dt;
         b.params.first_order = euler->get_bool(*this, "firstOrder") ? 1 : 0;
         // the force field's own rayleighStiffness (BaseForceField.cpp:34): its

@@ -170,10 +170,12 @@ struct SceneParams {
     double mass_rm = 0.0;  // the mass's own rayleighMass
     int first_order = 0;   // EulerImplicitSolver firstOrder
     int project_velocity = 0;  // FixedProjectiveConstraint activate_projectVelocity
+    int trapezoidal = 0;       // EulerImplicitSolver trapezoidalScheme (tr = 0.5)
 };
 
-// Factors of one EulerImplicitSolver step (EulerImplicitSolver.cpp:138-171,
-// trapezoidal factor tr = 1): the system matrix mF M + bF B + kF K, with the
+// Factors of one EulerImplicitSolver step (EulerImplicitSolver.cpp:117-171,
+// trapezoidal factor tr = 0.5 with trapezoidalScheme, else 1): the system
+// matrix mF M + bF B + kF K, with the
 // components' Rayleigh terms folded into the factors each component applies
 // (MechanicalParams::k/mFactorIncludingRayleighDamping, MechanicalParams.h:
 // 62-64), and the right-hand side's stiffness factor h + rs (bF = 0 there).
@@ -186,7 +188,7 @@ struct StepFactors {
 
 inline StepFactors step_factors(const SceneParams& P)
 {
-    const double h = P.dt, tr = 1.0;
+    const double h = P.dt, tr = P.trapezoidal ? 0.5 : 1.0;
     StepFactors f;
     if (P.first_order) {
         f.mf = 1;

@@ -180,7 +180,7 @@ def test_patch_size_tuning(capi, monkeypatch):
     chosen, ms = b.tune_patch_size(sample, steps_per_trial=2)
     assert chosen in (256, 384, 512) and sorted(ms) == [256, 384, 512] and all(v > 0 for v in ms.values())
     assert b.tuning()["elements_per_patch"] == chosen
-    slots = [b.add_mesh(*m) for m in sample]
+    slots = [b.add_mesh(pos, tets, **kw) for pos, tets, kw in sample]
     b.step(10)
     got = [b.state(s)[0] for s in slots]
     with pytest.raises(capi.SgbError) as e:
@@ -189,7 +189,7 @@ def test_patch_size_tuning(capi, monkeypatch):
     b.close()
     monkeypatch.setenv("SGB_BATCH_PE", str(chosen))
     ref = capi.Batch("mixed", budget_bytes=256 << 20, max_meshes=8)
-    rslots = [ref.add_mesh(*m) for m in sample]
+    rslots = [ref.add_mesh(pos, tets, **kw) for pos, tets, kw in sample]
     ref.step(10)
     for s, x in zip(rslots, got):
         assert np.array_equal(ref.state(s)[0], x)

@@ -1,5 +1,6 @@
 """GPU parity of the components' Rayleigh coefficients, EulerImplicitSolver
-firstOrder and FixedProjectiveConstraint activate_projectVelocity against
+firstOrder and trapezoidalScheme, and FixedProjectiveConstraint
+activate_projectVelocity against
 the oracle (tests/test_oracle_options.py pins the oracle's semantics).
 
 Tolerances: FP64 reference rounding with serial dots bit-identical after 20
@@ -30,7 +31,8 @@ OPTIONS = {
     "component_rayleigh": dict(ff_rayleigh_stiffness=0.05, mass_rayleigh_mass=0.03),
     "first_order": dict(first_order=True),
     "project_velocity": dict(project_velocity=True),
-    "all": dict(ff_rayleigh_stiffness=0.02, mass_rayleigh_mass=0.2, project_velocity=True),
+    "trapezoidal": dict(trapezoidal_scheme=True),
+    "all": dict(ff_rayleigh_stiffness=0.02, mass_rayleigh_mass=0.2, project_velocity=True, trapezoidal_scheme=True),
 }
 
 
@@ -88,13 +90,14 @@ def test_batch_component_rayleigh_matches_scene(capi):
     mesh = cases.beam_mesh()
     kw = dict(young=5000.0, poisson=0.45, method="large", dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1,
               cg_iterations=25, cg_tolerance=1e-9, cg_threshold=1e-9, total_mass=1.0, fixed=mesh.fixed,
-              ff_rayleigh_stiffness=0.05, mass_rayleigh_mass=0.03)
+              ff_rayleigh_stiffness=0.05, mass_rayleigh_mass=0.03, trapezoidal_scheme=1)
     b = capi.Batch("fp64_fma", budget_bytes=64 << 20, max_meshes=2)
     s = b.add_mesh(mesh.positions, mesh.tetrahedra, **kw)
     b.step(20)
     xb, _ = b.state(s)
     b.close()
-    sc = cases.gpu_scene(capi, mesh, "large", "fp64_fma", ff_rayleigh_stiffness=0.05, mass_rayleigh_mass=0.03)
+    sc = cases.gpu_scene(capi, mesh, "large", "fp64_fma", ff_rayleigh_stiffness=0.05, mass_rayleigh_mass=0.03,
+                         trapezoidal_scheme=True)
     sc.step(20)
     x, _ = sc.state()
     assert cases.rel_err(xb, x) <= 1e-10

@@ -189,6 +189,7 @@ def test_cg_warm_start_scene_file_against_oracle(capi, oracle):
     (("<DiagonalMass name=\"mass\"", "<DiagonalMass rayleighMass=\"0.2\" name=\"mass\""),
      dict(mass_rayleigh_mass=0.2)),
     (("<EulerImplicitSolver />", "<EulerImplicitSolver firstOrder=\"1\" />"), dict(first_order=True)),
+    (("<EulerImplicitSolver />", "<EulerImplicitSolver trapezoidalScheme=\"1\" />"), dict(trapezoidal_scheme=True)),
     (("name=\"fixC\"", "name=\"fixC\" activate_projectVelocity=\"1\""), dict(project_velocity=True)),
 ])
 def test_grid_scene_file_with_component_options(capi, oracle, edit, opts):

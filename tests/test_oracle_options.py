@@ -96,3 +96,26 @@ def test_project_velocity_zeroes_fixed_nodes(oracle):
     free = np.setdiff1d(np.arange(mesh.n_nodes), fx)
     assert np.array_equal(v_on[free], v_off[free])
     np.testing.assert_allclose(x_on[fx], mesh.positions[fx] + 0.01 * v0[fx], rtol=0, atol=1e-15)
+
+
+def test_trapezoidal_spring_recurrence(oracle):
+    """trapezoidalScheme (EulerImplicitSolver.cpp:117-171): tr = 0.5 on h in
+    the right-hand side's stiffness factor and the system factors. One node
+    of mass m held by a spring k: (m + (tr h)^2 k) dv = h (-k x - tr h k v),
+    v += dv, x += h v."""
+    m, k, h, tr = 0.5, 40.0, 0.01, 0.5
+    x = np.array([0.3, -0.3, 0.6])
+    v = np.array([0.1, 0.0, -0.2])
+    sc = oracle.OracleScene(None, n_nodes=1, vertex_mass=m, gravity=(0.0, 0.0, 0.0), dt=h, cg_iterations=10,
+                            cg_tolerance=1e-30, cg_threshold=1e-30)
+    sc.set_springs(k, np.zeros((1, 3)))
+    sc.set_state(x[None], v[None])
+    sc.set_options(trapezoidal_scheme=True)
+    for _ in range(6):
+        dv = h * (-k * x - tr * h * k * v) / (m + (tr * h) ** 2 * k)
+        v = v + dv
+        x = x + h * v
+    sc.step(6)
+    xo, vo = sc.state()
+    np.testing.assert_allclose(xo[0], x, rtol=1e-12)
+    np.testing.assert_allclose(vo[0], v, rtol=1e-12)

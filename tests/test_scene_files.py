@@ -155,7 +155,6 @@ def test_scene_errors(capi, case):
 @pytest.mark.parametrize("edit,msg", [
     (('method="large"', 'method="large" updateStiffnessMatrix="1"'), "updateStiffnessMatrix"),
     (('<DiagonalMass name="mass" massDensity="1.0" />', ''), "mass"),
-    (('<EulerImplicitSolver />', '<EulerImplicitSolver trapezoidalScheme="1" />'), "trapezoidalScheme"),
     (('name="fixC"', 'name="fixC" activate_projectVelocity="1"'
       ' />\n        <FixedProjectiveConstraint name="fix2" indices="0"'), "activate_projectVelocity"),
     (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="3" name="FEM"'),
