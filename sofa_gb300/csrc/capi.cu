@@ -197,10 +197,12 @@ int sgb_tfem_create(sgb_tfem_t** out, int n_nodes, const double* rest_positions_
     // the fused variants; the reference-rounding variant keeps the caller's
     // element order
     HostLayout L;
-    // elements per patch: 256 (measured best for FP32 on GB300 among 128..512
-    // with 64..256 threads) and 256 for FP64; SGB_PATCH_PE overrides the FP32
-    // value (an even count in [32, 1024])
-    int pe = 256;
+    // elements per patch: 320 for FP32 (the fastest implicit step on a
+    // GB300 among 256..512: 10.42 ms per step of the 64x64x257 beam against
+    // 10.75 at 256, where fewer shared nodes make the CG update cheaper; a
+    // lone addDForce call is 2 % faster at 256) and 256 for FP64;
+    // SGB_PATCH_PE overrides the FP32 value (an even count in [32, 1024])
+    int pe = ops->real_size == 4 ? 320 : 256;
     if (ops->real_size == 4)
         if (const char* e = getenv("SGB_PATCH_PE")) {
             const int v = atoi(e);
@@ -706,16 +708,22 @@ int sgb_patch_layout_check(int n_nodes, const double* rest_positions_host, int n
     build_patch_layout(n_nodes, n_tets, tetrahedra_host, rest_positions_host, elements_per_patch,
                        max_nodes_per_patch, L);
     const int P = (int)L.elem_start.size() - 1;
+    // patches with elements first, then the patches of nodes of no element
+    int P_elem = 0;
+    while (P_elem < P && L.elem_start[P_elem + 1] > L.elem_start[P_elem]) ++P_elem;
     // every (element, corner) is gathered exactly once, by the patch that
     // holds the element, at the local node that is that corner's node
     std::vector<int> seen((size_t)n_tets * 4, 0);
     std::vector<int> owners((size_t)n_nodes, 0), touched((size_t)n_nodes, 0);
     for (int p = 0; p < P; ++p) {
         const int e0 = L.elem_start[p], e1 = L.elem_start[p + 1];
-        if (e1 - e0 > elements_per_patch || e1 <= e0) return fail(SGB_ERR_NUMERICAL, "patch element range");
-        if (p + 1 < P && ((e1 - e0) & 1)) return fail(SGB_ERR_NUMERICAL, "odd element count before the last patch");
+        if (e1 - e0 > elements_per_patch || (p < P_elem ? e1 <= e0 : (e0 != n_tets || e1 != n_tets)))
+            return fail(SGB_ERR_NUMERICAL, "patch element range");
+        if (p + 1 < P_elem && ((e1 - e0) & 1))
+            return fail(SGB_ERR_NUMERICAL, "odd element count before the last patch");
         const int n0 = L.node_start[p], n1 = L.node_start[p + 1];
-        if (n1 - n0 > max_nodes_per_patch) return fail(SGB_ERR_NUMERICAL, "patch node count");
+        if (n1 - n0 > max_nodes_per_patch || (p >= P_elem && (n1 <= n0 || n1 - n0 > L.max_lnodes)))
+            return fail(SGB_ERR_NUMERICAL, "patch node count");
         for (int l = n0; l < n1; ++l) {
             const int g = L.lnode_gid[(size_t)l];
             if (l > n0 && g <= L.lnode_gid[(size_t)l - 1]) return fail(SGB_ERR_NUMERICAL, "local nodes not sorted");
@@ -746,7 +754,8 @@ int sgb_patch_layout_check(int n_nodes, const double* rest_positions_host, int n
     int boundary = 0;
     for (int n = 0; n < n_nodes; ++n) {
         const int cnt = L.bnd_rowptr[(size_t)n + 1] - L.bnd_rowptr[(size_t)n];
-        if (touched[(size_t)n] > 0 && owners[(size_t)n] != 1) return fail(SGB_ERR_NUMERICAL, "node owner count");
+        if ((P > 0 && touched[(size_t)n] == 0) || (touched[(size_t)n] > 0 && owners[(size_t)n] != 1))
+            return fail(SGB_ERR_NUMERICAL, "node owner count");
         if (touched[(size_t)n] > 1 ? cnt != touched[(size_t)n] : cnt != 0)
             return fail(SGB_ERR_NUMERICAL, "partial slot count");
         boundary += cnt > 0;

@@ -117,6 +117,24 @@ void build_patch_layout(int N, int E, const int32_t* tets, const double* pos, in
         L.node_start.push_back((int)L.lnode_gid.size());
         L.max_lnodes = std::max(L.max_lnodes, (int)nodes.size());
     }
+    // nodes of no element (a MechanicalObject with unused points) go into
+    // trailing patches without elements, at most max_lnodes each: the patch
+    // kernels then form their mass rows (and CG directions) like any other
+    // node's, with an empty stiffness sum
+    if (P > 0) {
+        std::vector<int> lone;
+        for (int n = 0; n < N; ++n)
+            if (patch_count[(size_t)n] == 0) lone.push_back(n);
+        const size_t chunk = (size_t)std::max(L.max_lnodes, 1);
+        for (size_t i = 0; i < lone.size(); i += chunk) {
+            const size_t j = std::min(lone.size(), i + chunk);
+            for (size_t k = i; k < j; ++k) patch_count[(size_t)lone[k]] = 1;
+            L.lnode_gid.insert(L.lnode_gid.end(), lone.begin() + (long)i, lone.begin() + (long)j);
+            L.node_start.push_back((int)L.lnode_gid.size());
+            L.elem_start.push_back(E);
+        }
+    }
+    const int P_all = (int)L.elem_start.size() - 1;
 
     // 4. boundary nodes: one partial slot per touching patch, in patch order;
     //    the first patch owns the node
@@ -130,7 +148,7 @@ void build_patch_layout(int N, int E, const int32_t* tets, const double* pos, in
     L.n_partials = L.bnd_rowptr[(size_t)N];
     std::vector<int> next(L.bnd_rowptr.begin(), L.bnd_rowptr.end() - 1);
     L.lnode_info.resize(L.lnode_gid.size());
-    for (int p = 0; p < P; ++p)
+    for (int p = 0; p < P_all; ++p)
         for (int l = L.node_start[p]; l < L.node_start[p + 1]; ++l) {
             const int g = L.lnode_gid[(size_t)l];
             if (patch_count[(size_t)g] <= 1) {

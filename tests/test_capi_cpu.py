@@ -109,6 +109,34 @@ def test_patch_layout_random_soup(capi):
     assert rc == 0, capi.last_error()
 
 
+def test_patch_layout_nodes_of_no_element(capi):
+    """Nodes that no tetrahedron uses go into trailing patches without
+    elements (each node owned once, no partial slots), so the patch kernels
+    form their mass rows; the checker counts every node as touched."""
+    from sofa_gb300 import topology as topo
+
+    mesh = topo.beam((6, 6, 20), spacing=0.5, jitter=0.05, seed=2)
+    n_old = mesh.n_nodes
+    # interleave unused nodes: old node i -> 2 i
+    pos = np.zeros((2 * n_old, 3))
+    pos[0::2] = mesh.positions
+    pos[1::2] = mesh.positions + 0.1
+    tets = np.ascontiguousarray(2 * mesh.tetrahedra, dtype=np.int32)
+    stats = (ctypes.c_int * 5)()
+    lib = capi.load()
+    lib.sgb_patch_layout_check.argtypes = [ctypes.c_int, capi._dp, ctypes.c_int, capi._ip, ctypes.c_int,
+                                           ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    for pe, pn in ((64, 64), (256, 1024)):
+        rc = lib.sgb_patch_layout_check(2 * n_old, np.ascontiguousarray(pos).ctypes.data_as(capi._dp),
+                                        mesh.n_tets, tets.ctypes.data_as(capi._ip), pe, pn, stats)
+        assert rc == 0, capi.last_error()
+        patches, max_ln, total_ln, boundary, partials = list(stats)
+        # the unused nodes appear exactly once each, in patches of at most
+        # max_ln nodes
+        assert patches >= -(-n_old // max_ln) + mesh.n_tets // pe
+        assert total_ln >= 2 * n_old
+
+
 @pytest.mark.parametrize("field,value", [("linear_solver", 1), ("preconditioner", 1), ("warm_start", 1),
                                          ("residual_replacement", 20), ("serial_dots", 1)])
 def test_batch_admission_refuses_solver_options_it_does_not_run(capi, field, value):

@@ -372,6 +372,55 @@ def test_ragged_materials_and_isolated_nodes(torch_cuda, capi, oracle, method, p
         assert cases.rel_err(f, f_ref) <= tol and cases.rel_err(df, df_ref) <= tol
 
 
+@pytest.mark.parametrize("method", ["large", "polar"])
+def test_scene_with_nodes_of_no_element(torch_cuda, capi, oracle, method):
+    """A scene whose MechanicalObject has points that no tetrahedron uses:
+    those points fall under gravity with their own mass rows. The mixed
+    step (fused patch kernels, where such nodes sit in element-free
+    patches) against the oracle over 10 steps, the batch engine's mixed step
+    beside it, and FP64 with serial dots bit-identical."""
+    mesh = cases.beam_mesh((4, 4, 13), seed=5)
+    n0 = mesh.n_nodes
+    pos = np.zeros((2 * n0, 3))
+    pos[0::2] = mesh.positions
+    pos[1::2] = mesh.positions + np.array([0.0, 3.0, 0.0])
+    tets = 2 * mesh.tetrahedra
+    fixed = 2 * np.asarray(mesh.fixed)
+    cfg = cases.BEAM_SMALL
+    kw = dict(dt=cfg["dt"], rayleigh_stiffness=cfg["rs"], rayleigh_mass=cfg["rm"], cg_iterations=cfg["cg_iterations"],
+              cg_tolerance=cfg["cg_tolerance"], cg_threshold=cfg["cg_threshold"], gravity=cfg["gravity"])
+    vm = cfg["total_mass"] / (2 * n0)
+    steps = 10
+    ofem = oracle.OracleFEM(pos, tets, cfg["young"], cfg["poisson"], method)
+    osc = oracle.OracleScene(ofem, vertex_mass=vm, fixed=fixed, **kw)
+    osc.step(steps)
+    xr, vr = osc.state()
+    it_ref = osc.last_iterations
+    d = np.linalg.norm(xr - pos)
+    for precision in ("fp64", "mixed"):
+        fem = capi.TetrahedronFEM(pos, tets, cfg["young"], cfg["poisson"], method, precision)
+        sc = capi.Scene(fem, vertex_mass=vm, fixed=fixed, serial_dots=precision == "fp64", **kw)
+        sc.step(steps)
+        it, _ = sc.sync()
+        x, v = sc.state()
+        sc.close()
+        if precision == "fp64":
+            assert it == it_ref
+            assert np.array_equal(x, xr) and np.array_equal(v, vr)
+        else:
+            assert np.linalg.norm(x - xr) / d <= 1e-4, np.linalg.norm(x - xr) / d
+            # the free points: x0 + the FP64 trajectory of a free mass
+            np.testing.assert_allclose(x[1::2], xr[1::2], rtol=0, atol=1e-6)
+    b = capi.Batch("mixed", budget_bytes=64 << 20, max_meshes=2)
+    s = b.add_mesh(pos, tets, young=cfg["young"], poisson=cfg["poisson"], method=method, total_mass=cfg["total_mass"],
+                   fixed=fixed, **kw)
+    b.step(steps)
+    x = b.state(s)[0]
+    b.close()
+    assert np.linalg.norm(x - xr) / d <= 1e-4
+    np.testing.assert_allclose(x[1::2], xr[1::2], rtol=0, atol=1e-6)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp64_fma", "mixed"])
 def test_fixed_constraint_constant_force_known_answer(torch_cuda, capi, precision):
     """The reference's FixedProjectiveConstraint_test known answer on the GPU
