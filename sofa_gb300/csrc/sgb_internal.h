@@ -115,6 +115,7 @@ struct TfemMesh {
     void* eforce = nullptr;   // scratch: 12 reals per element (corner forces)
     int patch_grid = 0;       // CTAs of the persistent patch kernels
     int patch_threads = 128;  // threads per CTA of the patch kernels
+    int matvec_minb = 1;      // CG matvec register cap: resident CTAs per SM it is set for (1: none)
     int adddforce_grid = 0;   // CTAs of the addDForce patch kernel (128 threads)
     int patch_prefetch = 0;   // 1: each CTA prefetches its next patch into L2
     int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads

@@ -1581,8 +1581,12 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
     return pen;
 }
 
-template <typename R, int MODE, int PC = 0>
-__global__ void __launch_bounds__(kPatchMaxThreads) k_patch_matvec(PatchView pv, ElemView<R> ev,
+// MINB > 1: 128-thread CTAs with the register cap for MINB resident CTAs
+// per SM (FP32 only; 9 gives 56 registers without spills); MINB = 1: no cap,
+// 64, 128 or 256 threads.
+template <typename R, int MODE, int PC = 0, int MINB = 1>
+__global__ void __launch_bounds__(MINB > 1 ? kPatchThreads : kPatchMaxThreads, sizeof(R) == 4 && MINB > 1 ? MINB : 0)
+    k_patch_matvec(PatchView pv, ElemView<R> ev,
                                                                    const R* __restrict__ rin,
                                                                    const R* __restrict__ pold, R* __restrict__ pnew,
                                                                    CgScalars* cg, R kf, MassArgs ma, double mf,
@@ -2198,6 +2202,16 @@ void launch_cg_update(const TfemMesh* m, int grid, cudaStream_t s, A... a)
         k_cg_update_patch<R, 4, PC><<<grid, kNodeBlock, 0, s>>>(a...);
 }
 
+// The CG matvec with the register cap chosen at preparation.
+template <typename R, int MODE, int PC = 0, typename... A>
+void launch_patch_matvec(const TfemMesh* m, size_t smem, cudaStream_t s, A... a)
+{
+    if (m->matvec_minb == 9)
+        k_patch_matvec<R, MODE, PC, 9><<<m->patch_grid, m->patch_threads, smem, s>>>(a...);
+    else
+        k_patch_matvec<R, MODE, PC, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(a...);
+}
+
 template <typename K>
 int resident_grid(K kernel, int threads, size_t smem, int sms, int n_patches)
 {
@@ -2208,6 +2222,16 @@ int resident_grid(K kernel, int threads, size_t smem, int sms, int n_patches)
     if (g > kMaxDotBlocks) g = kMaxDotBlocks;
     if (g > n_patches) g = n_patches;
     return (int)(g < 1 ? 1 : g);
+}
+
+// Dynamic shared memory of a patch matvec kernel, with the largest
+// shared-memory carve-out so that its resident CTAs are bounded by
+// registers rather than by the L1 split.
+template <typename K>
+void patch_matvec_attrs(K kernel, size_t smem)
+{
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 }
 
 // Sets the shared-memory attribute of the patch kernels and returns the grid
@@ -2252,12 +2276,29 @@ int prepare_patch(TfemMesh* m)
             m->update_grid = (int)gu;
         }
     }
-    cudaFuncSetAttribute(k_patch_matvec<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_patch_matvec<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_patch_matvec<R, 1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_patch_matvec<R, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, threads, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, threads, smem);
+    // CG matvec register cap: 9 resident 128-thread CTAs per SM (56
+    // registers) or none (64 registers, 8 per SM); SGB_MATVEC_MINB = 1 or 9
+    m->matvec_minb = 1;
+    if (const char* e = getenv("SGB_MATVEC_MINB")) {
+        const int v = atoi(e);
+        if (v == 1 || v == 9) m->matvec_minb = v;
+    }
+    if (sizeof(R) != 4 || threads != kPatchThreads) m->matvec_minb = 1;
+    if (m->matvec_minb == 9) {
+        patch_matvec_attrs(k_patch_matvec<R, 1, 0, 9>, smem);
+        patch_matvec_attrs(k_patch_matvec<R, 2, 0, 9>, smem);
+        patch_matvec_attrs(k_patch_matvec<R, 1, 1, 9>, smem);
+        patch_matvec_attrs(k_patch_matvec<R, 2, 1, 9>, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1, 0, 9>, threads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2, 0, 9>, threads, smem);
+    } else {
+        patch_matvec_attrs(k_patch_matvec<R, 1>, smem);
+        patch_matvec_attrs(k_patch_matvec<R, 2>, smem);
+        patch_matvec_attrs(k_patch_matvec<R, 1, 1>, smem);
+        patch_matvec_attrs(k_patch_matvec<R, 2, 1>, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1>, threads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2>, threads, smem);
+    }
     int nb = nb1;
     nb = nb < nb2 ? nb : nb2;
     if (nb < 1) nb = 1;
@@ -2292,8 +2333,6 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
 {
     if (m->pl.n_patches > 0 && m->method != METHOD_SMALL) {
         PatchView pv = patch_view(m);
-        MassArgs ma{nullptr, 0.0, {0.0, 0.0, 0.0}};
-        SolveConsts sc{0.0, 0.0, 0};
         k_patch_adddforce<R><<<m->adddforce_grid, kPatchThreads, patch_smem_bytes<R>(m), s>>>(
                 pv, view<R>(m), dx, kfactor, df, (R*)m->pl.partials, nullptr, 0);
         k_patch_fixup<R><<<node_grid(m->n_nodes), kNodeBlock, 0, s>>>(m->pl.bnd_rowptr, (const R*)m->pl.partials, df,
@@ -2462,24 +2501,24 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
         R* pnew = pb[(it + 1) & 1];
         if (dinv) {
             if (it == 1)
-                k_patch_matvec<R, 1, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
-                    pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch,
-                    dinv);
+                launch_patch_matvec<R, 1, 1>(m, smem, s, pv, ev, (const R*)r, (const R*)pold, pnew, sc->cg, (R)kf,
+                                             ma, mf, (const uint8_t*)sc->fixed, q, partials, cons,
+                                             m->patch_prefetch, (const R*)dinv);
             else
-                k_patch_matvec<R, 2, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
-                    pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch,
-                    dinv);
+                launch_patch_matvec<R, 2, 1>(m, smem, s, pv, ev, (const R*)r, (const R*)pold, pnew, sc->cg, (R)kf,
+                                             ma, mf, (const uint8_t*)sc->fixed, q, partials, cons,
+                                             m->patch_prefetch, (const R*)dinv);
             launch_cg_update<R, 1>(m, gu, s, xs, r, (const R*)pnew, (const R*)q, (const R*)partials,
                                    (const int*)m->pl.bnd_rowptr, ma, mf, (const uint8_t*)sc->fixed, sc->cg, N, cons,
                                    m->update_vec4, dinv);
             continue;
         }
         if (it == 1)
-            k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
-                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+            launch_patch_matvec<R, 1>(m, smem, s, pv, ev, (const R*)r, (const R*)pold, pnew, sc->cg, (R)kf, ma, mf,
+                                      (const uint8_t*)sc->fixed, q, partials, cons, m->patch_prefetch);
         else
-            k_patch_matvec<R, 2><<<m->patch_grid, m->patch_threads, smem, s>>>(
-                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+            launch_patch_matvec<R, 2>(m, smem, s, pv, ev, (const R*)r, (const R*)pold, pnew, sc->cg, (R)kf, ma, mf,
+                                      (const uint8_t*)sc->fixed, q, partials, cons, m->patch_prefetch);
         launch_cg_update<R>(m, gu, s, xs, r, (const R*)pnew, (const R*)q, (const R*)partials,
                             (const int*)m->pl.bnd_rowptr, ma, mf, (const uint8_t*)sc->fixed, sc->cg, N, cons,
                             m->update_vec4);
@@ -2542,11 +2581,11 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
         R* pold = pb[it & 1];
         R* pnew = pb[(it + 1) & 1];
         if (it == 1)
-            k_patch_matvec<R, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(
-                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+            launch_patch_matvec<R, 1>(m, smem, s, pv, ev, (const R*)r, (const R*)pold, pnew, sc->cg, (R)kf, ma, mf,
+                                      (const uint8_t*)sc->fixed, q, partials, cons, m->patch_prefetch);
         else
-            k_patch_matvec<R, 2><<<m->patch_grid, m->patch_threads, smem, s>>>(
-                pv, ev, r, pold, pnew, sc->cg, (R)kf, ma, mf, sc->fixed, q, partials, cons, m->patch_prefetch);
+            launch_patch_matvec<R, 2>(m, smem, s, pv, ev, (const R*)r, (const R*)pold, pnew, sc->cg, (R)kf, ma, mf,
+                                      (const uint8_t*)sc->fixed, q, partials, cons, m->patch_prefetch);
         launch_cg_update<R>(m, m->update_grid > 0 ? m->update_grid : ng_update, s, xs, r, (const R*)pnew,
                             (const R*)q, (const R*)partials, (const int*)m->pl.bnd_rowptr, ma, mf,
                             (const uint8_t*)sc->fixed, sc->cg, N, cons, m->update_vec4);

@@ -62,6 +62,20 @@ def test_create_rejects_bad_indices_before_touching_the_gpu(capi):
     rc = lib.sgb_tfem_create(ctypes.byref(h), 0, pos.ctypes.data_as(capi._dp), 0, None, None, 0, None, 0, None, 0,
                              1, 0)
     assert rc == -1
+    # the largest mesh: 12 corner terms per tetrahedron must index with 32
+    # bits; one more tetrahedron is refused before the array is read
+    too_many = 0x7FFFFFFF // 12 + 1
+    rc = lib.sgb_tfem_create(ctypes.byref(h), 4, pos.ctypes.data_as(capi._dp), too_many,
+                             tets.ctypes.data_as(capi._ip), y.ctypes.data_as(capi._dp), 1,
+                             nu.ctypes.data_as(capi._dp), 1, None, 0, 1, 0)
+    assert rc == -1 and "too many tetrahedra" in capi.last_error()
+    # non-finite rest positions are refused
+    bad = pos.copy()
+    bad[2, 1] = np.nan
+    tets_ok = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    rc = lib.sgb_tfem_create(ctypes.byref(h), 4, bad.ctypes.data_as(capi._dp), 1, tets_ok.ctypes.data_as(capi._ip),
+                             y.ctypes.data_as(capi._dp), 1, nu.ctypes.data_as(capi._dp), 1, None, 0, 1, 0)
+    assert rc == -1 and "non-finite" in capi.last_error()
 
 
 def test_scene_params_defaults_match_reference_data(capi):
