@@ -721,9 +721,11 @@ def main():
         except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None
 
-    # per step: element force, force gather, RHS element pass, RHS gather,
-    # CG iterations x (matvec + update), Euler update
-    launches_per_step = 5 + 2 * cfg["cg_iterations"]
+    # per step: the force and right-hand side element pass and node pass
+    # (four kernels with SGB_FUSED_RHS=0), CG iterations x (matvec + update),
+    # Euler update
+    fused_rhs = os.environ.get("SGB_FUSED_RHS", "1") != "0"
+    launches_per_step = (3 if fused_rhs else 5) + 2 * cfg["cg_iterations"]
     line = {
         "metric": "tet-steps/s", "value": value, "unit": "tet-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,

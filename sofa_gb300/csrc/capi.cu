@@ -802,6 +802,7 @@ static void free_scene(sgb_scene* sc)
     cudaFree(s.p2);
     cudaFree(s.q);
     cudaFree(s.r);
+    cudaFree(s.eforce_v);
     cudaFree(s.cg);
     cudaFree(sc->dot_terms);
     cudaFree(s.b64);
@@ -892,6 +893,13 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     if (P.node_masses_host && (rc = dev_alloc(&s.node_mass, (size_t)N, acc))) goto fail_out;
     if (P.serial_dots && (rc = dev_alloc(&sc->dot_terms, (size_t)N, acc))) goto fail_out;
     if (P.preconditioner == SGB_PRECOND_JACOBI && (rc = dev_alloc_bytes(&s.dinv, rs * 3 * N, acc))) goto fail_out;
+    // the patch step's second corner-term buffer (FP32 large / polar / svd),
+    // for its fused force and right-hand side passes; SGB_FUSED_RHS=0 leaves
+    // it out and the step runs the four separate kernels (the same values)
+    if (fem->m.precision == SGB_PRECISION_MIXED && fem->m.pl.n_patches > 0 && fem->m.method != SGB_METHOD_SMALL &&
+        !(getenv("SGB_FUSED_RHS") && getenv("SGB_FUSED_RHS")[0] == '0') &&
+        (rc = dev_alloc_bytes(&s.eforce_v, rs * 12 * std::max<size_t>((size_t)fem->m.n_tets, 1), acc)))
+        goto fail_out;
     if (P.residual_replacement > 0) {
         // the FP64 copy of the operator, created from the force field's
         // inputs (rest positions and tetrahedra read back, caller order)

@@ -227,6 +227,7 @@ struct Scene {
     void* q = nullptr;
     void* r = nullptr;
     void* dinv = nullptr;          // PCG + Jacobi: inverse diagonal of the system (3 per node)
+    void* eforce_v = nullptr;      // patch step: the right-hand side's K v corner terms (12 per element)
     CgScalars* cg = nullptr;
     CgScalars* cg_h = nullptr;  // pinned mirror for reads
     cudaStream_t stream = nullptr;

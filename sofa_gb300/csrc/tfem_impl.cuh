@@ -502,10 +502,13 @@ __device__ __forceinline__ void addforce_element(R F[12], const R D[12], const R
 // addForce element part: accumulateForceSmall / Large / Polar
 // (TFEM.inl:534-623, 870-986, 1025-1079). Writes rotations and the corner
 // forces R^T F (method=small: F).
-template <typename R, int METHOD>
+// KEEP: also hands the rotation (before packing), K and J to the caller
+// (rotated methods only).
+template <typename R, int METHOD, bool KEEP = false>
 __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, const double* __restrict__ x,
                                                 const double* __restrict__ rest_pos, R* __restrict__ eforce,
-                                                const PlasticArgs<R>& pl = PlasticArgs<R>{})
+                                                const PlasticArgs<R>& pl = PlasticArgs<R>{}, R* keep_rot = nullptr,
+                                                R* keep_K = nullptr, R* keep_J = nullptr)
 {
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
@@ -667,6 +670,14 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
             c[3 * i + k] = acc;
         }
     store_eforce(eforce, e, c);
+    if constexpr (KEEP) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) keep_rot[i] = Rm[i];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) keep_K[i] = K[i];
+#pragma unroll
+        for (int i = 0; i < 12; ++i) keep_J[i] = J[i];
+    }
 }
 
 template <typename R, int METHOD>
@@ -690,18 +701,13 @@ __device__ __forceinline__ R cg_dir(R r, R pold, R beta)
     return t + r;
 }
 
-// addDForce element part: applyStiffnessSmall / applyStiffnessCorotational
-// (TFEM.inl:721-749, 1193-1237). Writes the corner terms R K (R^T dx) fact
-// that the gather subtracts.
+// addDForce element inputs: the four nodes' values of dx (DIR 0), of the
+// CG direction p = r (DIR 1) or p = p_old*beta + r (DIR 2).
 template <typename R, typename VIN, int METHOD, int DIR, int PC = 0>
-__device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, const VIN* __restrict__ dx,
-                                                 const R* __restrict__ pold, R beta, R fact,
-                                                 R* __restrict__ eforce, const R* __restrict__ dinv = nullptr)
+__device__ __forceinline__ void dforce_inputs(const int node[4], const VIN* __restrict__ dx,
+                                              const R* __restrict__ pold, R beta, const R* __restrict__ dinv,
+                                              R xin[4][3])
 {
-    const size_t En = (size_t)ev.n_tets;
-    const int4 t = ev.tets[e];
-    const int node[4] = {t.x, t.y, t.z, t.w};
-    R xin[4][3];
     VIN v0[3];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -742,9 +748,17 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
 #pragma unroll
             for (int k = 0; k < 3; ++k) xin[i][k] -= xin[0][k];
     }
-    R K[3], J[12];
-    load_KJ(ev, (size_t)e, K, J);
-    R X[12], F[12], c[12];
+}
+
+// addDForce corner terms of one element from its inputs:
+// applyStiffnessSmall / applyStiffnessCorotational (TFEM.inl:721-749,
+// 1193-1237), c = R K (R^T x) fact, which the gather subtracts. Rm is
+// unused for method small.
+template <typename R, int METHOD>
+__device__ __forceinline__ void dforce_terms(const R xin[4][3], const R Rm[9], const R K[3], const R J[12], R fact,
+                                             R c[12])
+{
+    R X[12], F[12];
     if (METHOD == METHOD_SMALL) {
 #pragma unroll
         for (int i = 0; i < 4; ++i)
@@ -753,11 +767,8 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
         element_force(F, X, K, J, fact);
 #pragma unroll
         for (int i = 0; i < 12; ++i) c[i] = F[i];
-        store_eforce(eforce, e, c);
         return;
     }
-    R Rm[9];
-    load_rot(ev, (size_t)e, Rm);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -777,6 +788,23 @@ __device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, c
             acc += Rm[6 + k] * F[3 * i + 2];
             c[3 * i + k] = acc;
         }
+}
+
+// addDForce element part: the inputs, the element's stored rotation and
+// stiffness, the corner terms into eforce.
+template <typename R, typename VIN, int METHOD, int DIR, int PC = 0>
+__device__ __forceinline__ void elem_dforce_body(const ElemView<R>& ev, int e, const VIN* __restrict__ dx,
+                                                 const R* __restrict__ pold, R beta, R fact,
+                                                 R* __restrict__ eforce, const R* __restrict__ dinv = nullptr)
+{
+    const int4 t = ev.tets[e];
+    const int node[4] = {t.x, t.y, t.z, t.w};
+    R xin[4][3];
+    dforce_inputs<R, VIN, METHOD, DIR, PC>(node, dx, pold, beta, dinv, xin);
+    R K[3], J[12], Rm[9], c[12];
+    load_KJ(ev, (size_t)e, K, J);
+    if (METHOD != METHOD_SMALL) load_rot(ev, (size_t)e, Rm);
+    dforce_terms<R, METHOD>(xin, Rm, K, J, fact, c);
     store_eforce(eforce, e, c);
 }
 
@@ -791,6 +819,39 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, cons
     if (e >= ev.n_tets) return;
     const R beta = (DIR == 2) ? (R)cg->beta : R(0);
     elem_dforce_body<R, VIN, METHOD, DIR, PC>(ev, e, dx, pold, beta, fact, eforce, dinv);
+}
+
+// addForce and the right-hand side's stiffness term of one implicit step in
+// one pass over the elements (rotated methods): the force corner terms as
+// k_elem_force forms them into eforce, then the terms (h + rs) K v of
+// EulerImplicitSolver's right-hand side (EulerImplicitSolver.cpp:137-160) into
+// eforce_v, with the rotation as the stored copy gives it back and K, J from
+// registers; the values are those of k_elem_force followed by k_elem_dforce
+// on v.
+template <typename R, int METHOD>
+__global__ void __launch_bounds__(kElemBlock) k_elem_force_rhs(ElemView<R> ev, const double* __restrict__ x,
+                                                               const double* __restrict__ rest_pos,
+                                                               R* __restrict__ eforce, PlasticArgs<R> pl,
+                                                               const double* __restrict__ v, R kf_rhs,
+                                                               R* __restrict__ eforce_v)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ev.n_tets) return;
+    R Rm[9], K[3], J[12];
+    elem_force_body<R, METHOD, true>(ev, e, x, rest_pos, eforce, pl, Rm, K, J);
+    R Rq[9];
+    if constexpr (is_mixed<R>::value) {
+        quat_to_rot(rot_to_quat(Rm), Rq);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rq[i] = Rm[i];
+    }
+    const int4 t = ev.tets[e];
+    const int node[4] = {t.x, t.y, t.z, t.w};
+    R xin[4][3], c[12];
+    dforce_inputs<R, double, METHOD_LARGE, 0>(node, v, nullptr, R(0), nullptr, xin);
+    dforce_terms<R, METHOD_LARGE>(xin, Rq, K, J, kf_rhs, c);
+    store_eforce(eforce_v, e, c);
 }
 
 // ------------------------------------------------------------------------
@@ -1131,6 +1192,84 @@ __global__ void __launch_bounds__(kNodeBlock) k_gather_rhs(NodeCSR csr, const R*
         local += d;
     }
     finish_dot<FIN_RHS>(local, cg, terms, N, sc);
+}
+
+// computeForce and the right-hand side in one pass over the nodes, with the
+// operations of k_gather_force followed by k_gather_rhs (f stays in
+// registers): eforce holds the force corner terms, eforce_v the (h + rs) K v
+// terms (unused with firstOrder).
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_gather_force_rhs(NodeCSR csr, const R* __restrict__ eforce,
+                                                                 const R* __restrict__ eforce_v,
+                                                                 const R* __restrict__ ext,
+                                                                 const double* __restrict__ v, MassArgs ma,
+                                                                 double mfac, int mass_first, double h,
+                                                                 const uint8_t* __restrict__ fixed,
+                                                                 R* __restrict__ b, R* __restrict__ r,
+                                                                 R* __restrict__ xs, CgScalars* cg, int N,
+                                                                 SolveConsts sc, int first_order)
+{
+    const R mg0 = (R)(ma.g[0] * ma.vertex_mass), mg1 = (R)(ma.g[1] * ma.vertex_mass),
+            mg2 = (R)(ma.g[2] * ma.vertex_mass);
+    const R mm = (R)(mfac != 1.0 ? ma.vertex_mass * mfac : ma.vertex_mass);
+    const R hr = (R)h;
+    double local = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) cg->done = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        R a0 = R(0), a1 = R(0), a2 = R(0);
+        if (ext) {
+            a0 += ext[3 * (size_t)n];
+            a1 += ext[3 * (size_t)n + 1];
+            a2 += ext[3 * (size_t)n + 2];
+        }
+        R m0 = mg0, m1 = mg1, m2 = mg2;
+        if (ma.node_mass) {
+            const double m = ma.node_mass[n];
+            m0 = (R)(ma.g[0] * m);
+            m1 = (R)(ma.g[1] * m);
+            m2 = (R)(ma.g[2] * m);
+        }
+        if (mass_first) {
+            a0 += m0;
+            a1 += m1;
+            a2 += m2;
+        }
+        const int s0 = csr.rowptr[n], s1 = csr.rowptr[n + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* c = eforce + 3 * (size_t)csr.slots[s];
+            a0 += c[0];
+            a1 += c[1];
+            a2 += c[2];
+        }
+        if (!mass_first) {
+            a0 += m0;
+            a1 += m1;
+            a2 += m2;
+        }
+        R a[3] = {a0, a1, a2};
+        if (!first_order) {
+            R vv[3] = {(R)v[3 * (size_t)n], (R)v[3 * (size_t)n + 1], (R)v[3 * (size_t)n + 2]};
+            if (mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+            for (int s = s0; s < s1; ++s) {
+                const R* c = eforce_v + 3 * (size_t)csr.slots[s];
+                a[0] -= c[0];
+                a[1] -= c[1];
+                a[2] -= c[2];
+            }
+            if (!mass_first && mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] *= hr;
+        }
+        if (fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            b[3 * (size_t)n + k] = a[k];
+            r[3 * (size_t)n + k] = a[k];
+            if (!sc.pcg && !sc.warm) xs[3 * (size_t)n + k] = R(0);  // PCG / warmStart keep the previous solution
+        }
+        local += dot3(a, a);
+    }
+    finish_dot<FIN_RHS>(local, cg, nullptr, N, sc);
 }
 
 // q = A p for GraphScatteredMatrix::apply (GraphScatteredTypes.cpp:33-45):
@@ -2075,6 +2214,32 @@ void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
         k_elem_force<R, METHOD_POLAR><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
 }
 
+// k_elem_force_rhs for the rotated methods (the patch step's force field).
+template <typename R>
+void launch_elem_force_rhs(TfemMesh* m, const double* x, const double* v, R kf_rhs, R* eforce_v, cudaStream_t s)
+{
+    if (m->n_tets == 0) return;
+    ElemView<R> ev = view<R>(m);
+    const int g = elem_grid(m->n_tets);
+    PlasticArgs<R> pl;
+    if (m->plastic && m->plastic_max > 0.0) {
+        pl.strain = (R*)m->plastic;
+        pl.scale = (const R*)m->plastic_scale;
+        pl.max_threshold = (R)m->plastic_max;
+        pl.yield_threshold = (R)m->plastic_yield;
+        pl.creep = (R)m->plastic_creep;
+    }
+    if (m->method == METHOD_LARGE)
+        k_elem_force_rhs<R, METHOD_LARGE>
+            <<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl, v, kf_rhs, eforce_v);
+    else if (m->method == METHOD_SVD)
+        k_elem_force_rhs<R, METHOD_SVD>
+            <<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl, v, kf_rhs, eforce_v);
+    else
+        k_elem_force_rhs<R, METHOD_POLAR>
+            <<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl, v, kf_rhs, eforce_v);
+}
+
 template <typename R, typename VIN, int DIR>
 void launch_elem_dforce(TfemMesh* m, const VIN* dx, const R* pold, const CgScalars* cg, R fact, cudaStream_t s,
                         const R* dinv = nullptr)
@@ -2277,8 +2442,10 @@ int prepare_patch(TfemMesh* m)
         }
     }
     // CG matvec register cap: 9 resident 128-thread CTAs per SM (56
-    // registers) or none (64 registers, 8 per SM); SGB_MATVEC_MINB = 1 or 9
-    m->matvec_minb = 1;
+    // registers, no spills; 1.9 % faster steps on the 64x64x257 beam at 320
+    // tets per patch, slower at 256) or none (64 registers, 8 per SM);
+    // SGB_MATVEC_MINB = 1 or 9 overrides
+    m->matvec_minb = m->pl.pe >= 288 ? 9 : 1;
     if (const char* e = getenv("SGB_MATVEC_MINB")) {
         const int v = atoi(e);
         if (v == 1 || v == 9) m->matvec_minb = v;
@@ -2471,7 +2638,6 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     NodeCSR csr{m->rowptr, m->slots};
     MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
     const int ng = node_grid(N);
-    R* f = (R*)sc->f;
     R* b = (R*)sc->b;
     R* r = (R*)sc->r;
     R* pb[2] = {(R*)sc->p, (R*)sc->p2};
@@ -2481,12 +2647,28 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     const bool pcg = P.solver == 1;
     const R* dinv = pcg ? (const R*)sc->dinv : nullptr;
     SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0, P.warm_start};
-    launch_elem_force<R>(m, sc->x, s);
-    k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f, N);
     const StepFactors F = step_factors(P);
-    if (!P.first_order) launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)F.kf_rhs, s);
-    k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass, mass_first,
-                                              h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons, P.first_order);
+    // forces and the right-hand side: one pass over the elements (force
+    // terms and (h + rs) K v terms), one over the nodes; the same values as
+    // the four kernels of scene_step (sc->eforce_v null: those kernels)
+    if (sc->eforce_v) {
+        if (P.first_order)
+            launch_elem_force<R>(m, sc->x, s);
+        else
+            launch_elem_force_rhs<R>(m, sc->x, sc->v, (R)F.kf_rhs, (R*)sc->eforce_v, s);
+        k_gather_force_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->eforce_v,
+                                                        (const R*)sc->ext, sc->v, ma, -P.rayleigh_mass, mass_first,
+                                                        h, sc->fixed, b, r, xs, sc->cg, N, cons, P.first_order);
+    } else {
+        R* f = (R*)sc->f;
+        launch_elem_force<R>(m, sc->x, s);
+        k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first, f,
+                                                    N);
+        if (!P.first_order) launch_elem_dforce<R, double, 0>(m, sc->v, nullptr, sc->cg, (R)F.kf_rhs, s);
+        k_gather_rhs<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, f, sc->v, ma, -P.rayleigh_mass,
+                                                  mass_first, h, sc->fixed, b, r, xs, sc->cg, nullptr, N, cons,
+                                                  P.first_order);
+    }
     const double mf = F.mf_mass;
     const double kf = F.kf_ff;
     if (pcg || P.warm_start) pcg_begin<R>(sc, mass_first, mf, kf, cons, nullptr, s);

@@ -1,0 +1,87 @@
+"""The mixed patch step forms the forces and the right-hand side in two
+passes (k_elem_force_rhs, k_gather_force_rhs) instead of the four kernels of
+the element-order step (k_elem_force, k_gather_force, k_elem_dforce on v,
+k_gather_rhs). The fused kernels perform the same operations on the same
+values, so the trajectories are bit-identical; SGB_FUSED_RHS=0 at scene
+creation selects the four kernels. Checked over 8 steps for the rotated
+methods and the options that enter the right-hand side: the components'
+Rayleigh coefficients, firstOrder, trapezoidalScheme, projectVelocity,
+vdamping, per-node masses, mass_first, an external force, plasticity.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def capi():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from sofa_gb300 import build, capi
+
+    build.build()
+    capi.load()
+    return capi
+
+
+CASES = {
+    "plain": dict(),
+    "component_rayleigh": dict(ff_rayleigh_stiffness=0.05, mass_rayleigh_mass=0.03),
+    "first_order": dict(first_order=True),
+    "trapezoidal_project": dict(trapezoidal_scheme=True, project_velocity=True, vdamping=0.5),
+    "node_masses_mass_last": dict(node_masses="ramp", mass_first=False),
+    "external_force": dict(external="tip"),
+    "plasticity": dict(plastic=True),
+}
+
+
+def run(capi, mesh, method, case, fused, steps=8):
+    opts = dict(CASES[case])
+    ext = opts.pop("external", None)
+    plastic = opts.pop("plastic", False)
+    if opts.get("node_masses") == "ramp":
+        opts["node_masses"] = np.linspace(0.5, 1.5, mesh.n_nodes) / mesh.n_nodes
+    old = os.environ.get("SGB_FUSED_RHS")
+    os.environ["SGB_FUSED_RHS"] = "1" if fused else "0"
+    try:
+        fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, method, "mixed")
+        if plastic:
+            fem.set_plasticity(1e-2, 1e-6, 0.5)
+        sc = capi.Scene(fem, dt=0.01, rayleigh_stiffness=0.1, rayleigh_mass=0.1, cg_iterations=25,
+                        cg_tolerance=1e-9, cg_threshold=1e-9, gravity=(0.0, -9.81, 0.0),
+                        vertex_mass=1.0 / mesh.n_nodes, fixed=mesh.fixed, **opts)
+    finally:
+        if old is None:
+            del os.environ["SGB_FUSED_RHS"]
+        else:
+            os.environ["SGB_FUSED_RHS"] = old
+    v0 = np.random.default_rng(8).normal(scale=0.05, size=mesh.positions.shape)
+    sc.set_state(mesh.positions, v0)
+    if ext is not None:
+        f = np.zeros_like(mesh.positions)
+        tip = mesh.positions[:, 2] >= mesh.positions[:, 2].max() - 1e-9
+        f[tip] = (0.0, -2e-3, 1e-3)
+        sc.set_external_force(f)
+    sc.step(steps)
+    it, res = sc.sync()
+    x, v = sc.state()
+    sc.close()
+    return x, v, it, res
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("method", ["large", "polar", "svd"])
+def test_fused_force_and_rhs_bit_identical(capi, method, case):
+    mesh = cases.beam_mesh()
+    a = run(capi, mesh, method, case, fused=True)
+    b = run(capi, mesh, method, case, fused=False)
+    assert np.array_equal(a[0], b[0]), cases.rel_err(a[0], b[0])
+    assert np.array_equal(a[1], b[1])
+    assert a[2] == b[2] and a[3] == b[3]
+    assert np.linalg.norm(a[0] - mesh.positions) > 0  # the scene moved
