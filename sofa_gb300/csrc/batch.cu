@@ -136,6 +136,8 @@ static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool no
     d.rest_ff = nullptr;
     if (rs == sizeof(float)) c.add((float2**)&d.rest_ff, sizeof(float2) * 9 * E);
     c.add(&d.eforce, rs * 12 * E);
+    d.eforce_v = nullptr;
+    if (B->fused_rhs) c.add(&d.eforce_v, rs * 12 * E);
     c.add((int**)&d.rowptr, sizeof(int) * (N + 1));
     c.add((int**)&d.slots, sizeof(int) * 4 * (size_t)E);
     c.add((int**)&d.elem_start, sizeof(int) * (P + 1));
@@ -235,6 +237,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
             if (v >= 64 && v <= 512 && v % 2 == 0) B->pe = v;
         }
     if (const char* e = getenv("SGB_BATCH_PREFETCH")) B->tiles.prefetch = (e[0] == '1');
+    B->fused_rhs = fused_rhs_default();
     B->max_slots = max_meshes;
     B->max_iterations = max_cg_iterations;
     B->slots.resize((size_t)max_meshes);
@@ -327,7 +330,7 @@ int sgb_batch_mesh_bytes(const sgb_batch_t* B, const sgb_mesh_desc* m, size_t* b
     const int pe = B ? B->pe : 512;
     const size_t rs = B ? B->rs : sizeof(float);
     PreparedMesh pm;
-    int rc = prepare_mesh(m, pe, rs, pm);
+    int rc = prepare_mesh(m, pe, rs, pm, B ? B->fused_rhs : fused_rhs_default());
     if (rc) return rc;
     *bytes = pm.bytes;
     return SGB_OK;
@@ -338,7 +341,7 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
     if (!B || !slot_out) return bfail(SGB_ERR_INVALID_ARGUMENT, "sgb_batch_add_mesh: NULL argument");
     *slot_out = -1;
     PreparedMesh pm;
-    int rc = prepare_mesh(m, B->pe, B->rs, pm);
+    int rc = prepare_mesh(m, B->pe, B->rs, pm, B->fused_rhs);
     if (rc) return rc;
     return admit_prepared(B, pm, slot_out);
 }
@@ -350,7 +353,15 @@ namespace sgb {
 // Host-only part of admission: validation, material checks like the
 // reference (BaseLinearElasticityFEMForceField.inl:53-85), element order,
 // patch layout, gather tables and the byte count. Safe on any thread.
-int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm)
+// SGB_FUSED_RHS=0: the batch runs the force and right-hand side as four
+// passes (the same operations) and its meshes carry no eforce_v.
+int fused_rhs_default()
+{
+    const char* e = getenv("SGB_FUSED_RHS");
+    return !(e && e[0] == '0');
+}
+
+int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm, int fused_rhs)
 {
     int rc = validate_mesh(m);
     if (rc) return rc;
@@ -391,6 +402,7 @@ int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm)
     int* eo;
     sgb_batch tmp;
     tmp.rs = rs;
+    tmp.fused_rhs = fused_rhs;
     pm.bytes = align_up(mesh_plan(&tmp, N, E, pm.L, !pm.node_mass.empty(), !pm.ext.empty(), c, d, &y, &p, &eo,
                                   pm.Eh.size(), pm.nuh.size()));
     return SGB_OK;
@@ -557,7 +569,7 @@ int sgb_batch_add_meshes(sgb_batch_t* B, const sgb_mesh_desc* meshes, int n, int
     for (int t = 0; t < threads; ++t)
         pool.emplace_back([&, t] {
             for (int i = t; i < n; i += threads) {
-                rcs[(size_t)i] = prepare_mesh(&meshes[i], B->pe, B->rs, pms[(size_t)i]);
+                rcs[(size_t)i] = prepare_mesh(&meshes[i], B->pe, B->rs, pms[(size_t)i], B->fused_rhs);
                 if (rcs[(size_t)i]) errs[(size_t)i] = sgb_last_error();
             }
         });
@@ -610,6 +622,7 @@ int sgb_batch_step(sgb_batch_t* B, int n_steps)
         L.pe = B->pe;
         L.max_iterations = B->max_iterations;
         L.prefetch = T.prefetch;
+        L.fused_rhs = B->fused_rhs;
         L.err = B->d_err;
         cudaGraph_t g;
         BTRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));

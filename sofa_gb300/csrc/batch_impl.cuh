@@ -268,6 +268,107 @@ __global__ void __launch_bounds__(kBatchThreads) kb_rhs_gather(BMeshDesc* M, con
     }
 }
 
+// ---- forces and right-hand side in one element pass and one node pass ------
+// The operations of kb_force_elem + kb_rhs_elem (force terms into eforce, the
+// (h + rs) K v terms into eforce_v) and of kb_force_gather + kb_rhs_gather
+// (f kept in registers): the same operations in two launches instead of
+// four (FMA contraction may differ between the kernels: equal to rounding).
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_force_rhs_elem(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                                   const int* __restrict__ counts)
+{
+    const int L = counts[WL_ELEM];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        const BMeshDesc& m = M[it.slot];
+        const ElemView<R> ev = bm_elem_view<R>(m);
+        R* ef = (R*)m.eforce;
+        R* efv = (R*)m.eforce_v;
+        const R kf = (R)m.kf_rhs;
+        for (int e = it.a + threadIdx.x; e < it.b; e += blockDim.x) {
+            R Rm[9], K[3], J[12];
+            if (m.method == METHOD_LARGE)
+                elem_force_body<R, METHOD_LARGE, true>(ev, e, m.x, m.rest_pos, ef, PlasticArgs<R>{}, Rm, K, J);
+            else
+                elem_force_body<R, METHOD_POLAR, true>(ev, e, m.x, m.rest_pos, ef, PlasticArgs<R>{}, Rm, K, J);
+            rhs_v_terms(ev, e, m.v, Rm, K, J, kf, efv);
+        }
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_force_rhs_gather(BMeshDesc* M,
+                                                                     const WorkItem* __restrict__ items,
+                                                                     const int* __restrict__ counts)
+{
+    const int L = counts[WL_NODE];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        BMeshDesc& m = M[it.slot];
+        const R* ef = (const R*)m.eforce;
+        const R* efv = (const R*)m.eforce_v;
+        const R* ext = (const R*)m.ext;
+        R* b = (R*)m.b;
+        R* r = (R*)m.r;
+        R* xs = (R*)m.xs;
+        const R mg0 = (R)(m.g[0] * m.vertex_mass), mg1 = (R)(m.g[1] * m.vertex_mass),
+                mg2 = (R)(m.g[2] * m.vertex_mass);
+        const double rmf = m.rm_factor;  // -rm
+        const R mmu = (R)(rmf != 1.0 ? m.vertex_mass * rmf : m.vertex_mass);
+        const R hr = (R)m.h;
+        double dlocal = 0.0;
+        for (int n = it.a + threadIdx.x; n < it.b; n += blockDim.x) {
+            R a0 = R(0), a1 = R(0), a2 = R(0);
+            if (ext) {
+                a0 += ext[3 * (size_t)n];
+                a1 += ext[3 * (size_t)n + 1];
+                a2 += ext[3 * (size_t)n + 2];
+            }
+            if (m.node_mass) {
+                const double mm = m.node_mass[n];
+                a0 += (R)(m.g[0] * mm);
+                a1 += (R)(m.g[1] * mm);
+                a2 += (R)(m.g[2] * mm);
+            } else {
+                a0 += mg0;
+                a1 += mg1;
+                a2 += mg2;
+            }
+            const int s0 = m.rowptr[n], s1 = m.rowptr[n + 1];
+            for (int s = s0; s < s1; ++s) {
+                const R* c = ef + 3 * (size_t)m.slots[s];
+                a0 += c[0];
+                a1 += c[1];
+                a2 += c[2];
+            }
+            R a[3] = {a0, a1, a2};
+            const R vv[3] = {(R)m.v[3 * (size_t)n], (R)m.v[3 * (size_t)n + 1], (R)m.v[3 * (size_t)n + 2]};
+            if (rmf != 0.0) {
+                const R mm = m.node_mass ? (R)(m.node_mass[n] * rmf) : mmu;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) a[k] += vv[k] * mm;
+            }
+            for (int s = s0; s < s1; ++s) {
+                const R* c = efv + 3 * (size_t)m.slots[s];
+                a[0] -= c[0];
+                a[1] -= c[1];
+                a[2] -= c[2];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] *= hr;
+            if (m.fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                b[3 * (size_t)n + k] = a[k];
+                r[3 * (size_t)n + k] = a[k];
+                xs[3 * (size_t)n + k] = R(0);
+            }
+            dlocal += (double)(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        }
+        rhs_done(m, it.c, dlocal);  // the chunk's partial at its own index
+    }
+}
+
 // ---- CG matvec over patches ------------------------------------------------
 // MINB: resident CTAs per SM the register cap is set for (a tile of the
 // tuner; the arithmetic is the same for every value)
@@ -542,10 +643,15 @@ void batch_record_step(const BatchLaunch& B, cudaStream_t s)
 {
     const WorkItem* eit = B.items[WL_ELEM];
     const WorkItem* nit = B.items[WL_NODE];
-    kb_force_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
-    kb_force_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
-    kb_rhs_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
-    kb_rhs_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+    if (B.fused_rhs) {
+        kb_force_rhs_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
+        kb_force_rhs_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+    } else {
+        kb_force_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
+        kb_force_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+        kb_rhs_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
+        kb_rhs_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+    }
     const size_t smem = batch_patch_smem<R>(B.pe);
     for (int it = 1; it <= B.max_iterations; ++it) {
         if (it == 1)

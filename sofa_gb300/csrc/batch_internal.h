@@ -56,6 +56,7 @@ struct sgb_batch {
     int precision = 0;
     size_t rs = 4;
     int pe = 512;  // elements per patch (shared-memory stride of the batch matvec)
+    int fused_rhs = 1;  // forces and right-hand side in two passes (each mesh carries eforce_v)
     int max_slots = 0;
     int max_iterations = 0;
     sgb::Arena arena;
@@ -80,6 +81,7 @@ struct sgb_batch {
 
 
 namespace sgb {
-int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& out);
+int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& out, int fused_rhs);
+int fused_rhs_default();
 int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot);
 }  // namespace sgb

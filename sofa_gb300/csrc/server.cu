@@ -121,7 +121,7 @@ static void prep_worker(sgb_server* S)
             S->incoming.pop_front();
             p->in_worker = true;
         }
-        const int rc = prepare_mesh(&p->req.mesh, S->batch->pe, S->batch->rs, p->pm);
+        const int rc = prepare_mesh(&p->req.mesh, S->batch->pe, S->batch->rs, p->pm, S->batch->fused_rhs);
         std::string err = rc ? std::string(sgb_last_error()) : std::string();
         bool drop = false;
         {

@@ -276,6 +276,7 @@ struct BMeshDesc {
     const void* rest;
     const float2* rest_ff;
     void* eforce;
+    void* eforce_v;  // the right-hand side's K v corner terms (fused force / right-hand side passes)
     // node -> (element*4+corner) gather table
     const int* rowptr;
     const int* slots;
@@ -342,6 +343,7 @@ struct BatchLaunch {
     int pe;
     int max_iterations;
     int prefetch;  // FP32 matvec: prefetch the block's next patch into L2
+    int fused_rhs;  // forces and right-hand side in two launches (the meshes carry eforce_v)
     int* err;    // sticky device error flag of the batch
 };
 

@@ -821,6 +821,30 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, cons
     elem_dforce_body<R, VIN, METHOD, DIR, PC>(ev, e, dx, pold, beta, fact, eforce, dinv);
 }
 
+// The right-hand side's (h + rs) K v corner terms of element e (rotated
+// methods) from the rotation elem_force_body formed (Rm, before packing) and
+// its K, J: the rotation as the packed copy gives it back, then the
+// operations of elem_dforce_body on the FP64 velocities.
+template <typename R>
+__device__ __forceinline__ void rhs_v_terms(const ElemView<R>& ev, int e, const double* __restrict__ v,
+                                            const R Rm[9], const R K[3], const R J[12], R kf_rhs,
+                                            R* __restrict__ eforce_v)
+{
+    R Rq[9];
+    if constexpr (is_mixed<R>::value) {
+        quat_to_rot(rot_to_quat(Rm), Rq);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Rq[i] = Rm[i];
+    }
+    const int4 t = ev.tets[e];
+    const int node[4] = {t.x, t.y, t.z, t.w};
+    R xin[4][3], c[12];
+    dforce_inputs<R, double, METHOD_LARGE, 0>(node, v, nullptr, R(0), nullptr, xin);
+    dforce_terms<R, METHOD_LARGE>(xin, Rq, K, J, kf_rhs, c);
+    store_eforce(eforce_v, e, c);
+}
+
 // addForce and the right-hand side's stiffness term of one implicit step in
 // one pass over the elements (rotated methods): the force corner terms as
 // k_elem_force forms them into eforce, then the terms (h + rs) K v of
@@ -839,19 +863,7 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_force_rhs(ElemView<R> ev, c
     if (e >= ev.n_tets) return;
     R Rm[9], K[3], J[12];
     elem_force_body<R, METHOD, true>(ev, e, x, rest_pos, eforce, pl, Rm, K, J);
-    R Rq[9];
-    if constexpr (is_mixed<R>::value) {
-        quat_to_rot(rot_to_quat(Rm), Rq);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Rq[i] = Rm[i];
-    }
-    const int4 t = ev.tets[e];
-    const int node[4] = {t.x, t.y, t.z, t.w};
-    R xin[4][3], c[12];
-    dforce_inputs<R, double, METHOD_LARGE, 0>(node, v, nullptr, R(0), nullptr, xin);
-    dforce_terms<R, METHOD_LARGE>(xin, Rq, K, J, kf_rhs, c);
-    store_eforce(eforce_v, e, c);
+    rhs_v_terms(ev, e, v, Rm, K, J, kf_rhs, eforce_v);
 }
 
 // ------------------------------------------------------------------------
@@ -2408,12 +2420,12 @@ int prepare_patch(TfemMesh* m)
     int dev = 0, sms = 0, nb1 = 0, nb2 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // launch-shape knobs: threads per CTA (64/128/256), L2 prefetch of the
+    // launch-shape knobs: threads per CTA (a multiple of 32 in [64, 256]), L2 prefetch of the
     // next patch, vectorised FP32 update
     int threads = 128;
     if (const char* e = getenv("SGB_PATCH_THREADS")) {
         const int t = atoi(e);
-        if (t == 64 || t == 128 || t == 256) threads = t;
+        if (t >= 64 && t <= kPatchMaxThreads && t % 32 == 0) threads = t;
     }
     m->patch_threads = threads;
     if (const char* e = getenv("SGB_PATCH_PREFETCH")) m->patch_prefetch = (e[0] == '1');
@@ -2649,8 +2661,10 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0, P.warm_start};
     const StepFactors F = step_factors(P);
     // forces and the right-hand side: one pass over the elements (force
-    // terms and (h + rs) K v terms), one over the nodes; the same values as
-    // the four kernels of scene_step (sc->eforce_v null: those kernels)
+    // terms and (h + rs) K v terms), one over the nodes; the operations of
+    // the four kernels of scene_step, which this library's FP32 build
+    // contracts alike, so the values agree bit for bit (sc->eforce_v null:
+    // those four kernels)
     if (sc->eforce_v) {
         if (P.first_order)
             launch_elem_force<R>(m, sc->x, s);

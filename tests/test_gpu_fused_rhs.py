@@ -2,8 +2,9 @@
 passes (k_elem_force_rhs, k_gather_force_rhs) instead of the four kernels of
 the element-order step (k_elem_force, k_gather_force, k_elem_dforce on v,
 k_gather_rhs). The fused kernels perform the same operations on the same
-values, so the trajectories are bit-identical; SGB_FUSED_RHS=0 at scene
-creation selects the four kernels. Checked over 8 steps for the rotated
+values, and for the single-mesh kernels the build contracts them alike, so
+the trajectories are bit-identical; SGB_FUSED_RHS=0 at scene creation
+selects the four kernels. Checked over 8 steps for the rotated
 methods and the options that enter the right-hand side: the components'
 Rayleigh coefficients, firstOrder, trapezoidalScheme, projectVelocity,
 vdamping, per-node masses, mass_first, an external force, plasticity.
@@ -85,3 +86,39 @@ def test_fused_force_and_rhs_bit_identical(capi, method, case):
     assert np.array_equal(a[1], b[1])
     assert a[2] == b[2] and a[3] == b[3]
     assert np.linalg.norm(a[0] - mesh.positions) > 0  # the scene moved
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-5), ("fp64_fma", 1e-12)])
+def test_batch_fused_force_and_rhs(capi, precision, tol):
+    """The batch engine's two passes (kb_force_rhs_elem, kb_force_rhs_gather)
+    against its four (SGB_FUSED_RHS=0 at batch creation), on beams of the
+    batched workload's population (both methods), 5 steps. The passes do the
+    same operations, but in these FMA-contracting builds the compiler fuses
+    multiply-adds per kernel, and the batch's fused element pass (both
+    methods and the right-hand side in one kernel) comes out with other
+    contractions than its two separate passes: the trajectories agree to the
+    rounding of the element terms (displacement-relative difference within
+    `tol`), not bit for bit."""
+    from sofa_gb300 import workloads as wl
+
+    beams = wl.beam_population(64, seed=5, members=range(0, 64, 8))
+    out = []
+    for fused in (True, False):
+        old = os.environ.get("SGB_FUSED_RHS")
+        os.environ["SGB_FUSED_RHS"] = "1" if fused else "0"
+        try:
+            b = capi.Batch(precision, budget_bytes=4 << 30, max_meshes=len(beams) + 1)
+        finally:
+            if old is None:
+                del os.environ["SGB_FUSED_RHS"]
+            else:
+                os.environ["SGB_FUSED_RHS"] = old
+        slots = b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=8)
+        b.step(5)
+        out.append([b.state(s) for s in slots])
+        b.close()
+    worst = 0.0
+    for (m, _), (xa, _), (xb, _) in zip(beams, *out):
+        d = np.linalg.norm(xb - m.positions)
+        worst = max(worst, float(np.linalg.norm(xa - xb) / d))
+    assert worst <= tol, worst
