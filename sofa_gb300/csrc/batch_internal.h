@@ -82,6 +82,5 @@ struct sgb_batch {
 
 namespace sgb {
 int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& out, int fused_rhs);
-int fused_rhs_default();
 int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot);
 }  // namespace sgb

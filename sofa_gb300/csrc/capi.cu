@@ -897,7 +897,7 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     // for its fused force and right-hand side passes; SGB_FUSED_RHS=0 leaves
     // it out and the step runs the four separate kernels (the same operations)
     if (fem->m.precision == SGB_PRECISION_MIXED && fem->m.pl.n_patches > 0 && fem->m.method != SGB_METHOD_SMALL &&
-        !(getenv("SGB_FUSED_RHS") && getenv("SGB_FUSED_RHS")[0] == '0') &&
+        fused_rhs_default() &&
         (rc = dev_alloc_bytes(&s.eforce_v, rs * 12 * std::max<size_t>((size_t)fem->m.n_tets, 1), acc)))
         goto fail_out;
     if (P.residual_replacement > 0) {

@@ -347,6 +347,11 @@ struct BatchLaunch {
     int* err;    // sticky device error flag of the batch
 };
 
+// Forces and right-hand side of the FP32 patch step and of the batch in two
+// passes (1), or in the four passes of the element-order step (0:
+// SGB_FUSED_RHS=0); batch.cu.
+int fused_rhs_default();
+
 // von Mises stress (von_mises.cu): per-element lambda and mu, then the
 // per-element values (caller's order) and the per-node means.
 void launch_lame(const TfemMesh* m, const double* young, int ny, const double* poisson, int np, const double* lsf,

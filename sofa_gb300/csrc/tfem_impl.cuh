@@ -2454,10 +2454,15 @@ int prepare_patch(TfemMesh* m)
         }
     }
     // CG matvec register cap: 9 resident 128-thread CTAs per SM (56
-    // registers, no spills; 1.9 % faster steps on the 64x64x257 beam at 320
-    // tets per patch, slower at 256) or none (64 registers, 8 per SM);
-    // SGB_MATVEC_MINB = 1 or 9 overrides
-    m->matvec_minb = m->pl.pe >= 288 ? 9 : 1;
+    // registers, no spills) or none (64 registers, 8 per SM). More warps pay
+    // where the element data streams from DRAM: the 5.08 M-tet beam (0.4 GB of
+    // element data, 3x L2) steps 2 % faster with the cap at 320 tets per
+    // patch, while the 2.12 M-tet block (1.3x L2) and 256-tet patches step
+    // slower. Hence the cap from 288 tets per patch and at least twice L2 of
+    // element data (80 B per tet); SGB_MATVEC_MINB = 1 or 9 overrides.
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    m->matvec_minb = (m->pl.pe >= 288 && (double)m->n_tets * 80.0 >= 2.0 * (double)l2) ? 9 : 1;
     if (const char* e = getenv("SGB_MATVEC_MINB")) {
         const int v = atoi(e);
         if (v == 1 || v == 9) m->matvec_minb = v;
