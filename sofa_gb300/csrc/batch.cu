@@ -379,7 +379,7 @@ int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm, in
         if (!(y >= 0)) y = 5000.0;
     for (double& v : pm.nuh)
         if (!(v >= 0 && v < 0.5)) v = 0.45;
-    build_patch_layout(N, E, m->tetrahedra_host, m->rest_positions_host, pe, kBatchMaxLocalNodes, pm.L);
+    build_patch_layout(N, E, m->tetrahedra_host, m->rest_positions_host, pe, batch_max_lnodes(pe), pm.L);
     int maxval = 0;
     build_node_csr(N, E, m->tetrahedra_host, pm.L.inv, pm.rowptr, pm.slots, maxval);
     pm.tets_store.resize((size_t)E * 4);

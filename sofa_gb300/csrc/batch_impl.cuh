@@ -51,7 +51,7 @@ __device__ __forceinline__ PatchView bm_patch_view(const BMeshDesc& m, int pe)
     pv.bnd_rowptr = m.bnd_rowptr;
     pv.n_patches = m.n_patches;
     pv.pe = pe;
-    pv.max_lnodes = kBatchMaxLocalNodes;
+    pv.max_lnodes = batch_max_lnodes(pe);
     return pv;
 }
 
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(kPatchThreads, MINB) kb_matvec(BMeshDesc* M, c
     R* lp;
     uint16_t* sl;
     int* lr;
-    patch_smem_carve<R>(smem_raw, pe, kBatchMaxLocalNodes, &ef, &sl, &lr, &lp);
+    patch_smem_carve<R>(smem_raw, pe, batch_max_lnodes(pe), &ef, &sl, &lr, &lp);
     // the open mesh's views and operands, read where they are used
     __shared__ PatchView spv;
     __shared__ ElemView<R> sev;
@@ -576,7 +576,7 @@ __global__ void __launch_bounds__(kBatchThreads) kb_euler(BMeshDesc* M, const Wo
 template <typename R>
 size_t batch_patch_smem(int pe)
 {
-    return patch_smem_size<R>(pe, kBatchMaxLocalNodes);
+    return patch_smem_size<R>(pe, batch_max_lnodes(pe));
 }
 
 // Kernel attributes of the batch step; grid_patch[i]: resident matvec CTAs

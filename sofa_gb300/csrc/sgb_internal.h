@@ -264,6 +264,14 @@ constexpr int kBatchElemChunk = 1024;
 constexpr int kBatchNodeChunk = 1024;
 constexpr int kBatchMaxLocalNodes = 512;
 
+// Local nodes of one batch patch at most: as many as the patch has elements
+// (a 5-tet split of a grid gives about half as many), at most
+// kBatchMaxLocalNodes; the matvec's shared memory is sized by it.
+__host__ __device__ inline int batch_max_lnodes(int pe)
+{
+    return pe < kBatchMaxLocalNodes ? pe : kBatchMaxLocalNodes;
+}
+
 // Device-resident descriptor of one admitted mesh: its arrays (inside the
 // batch's HBM arena), its solver parameters and its CG scalars. Kernels read
 // it through the slot index of a work item; reductions update its scalars.
