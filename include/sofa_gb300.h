@@ -119,6 +119,20 @@ int sgb_tfem_get_rotations(sgb_tfem_t* fem, double* rotations_host, double* init
  * turns it off and keeps the strain. Thresholds are 2-norms of the 6-vector
  * strain. Synchronous on the handle's stream when first turned on. */
 int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_threshold, double creep);
+
+/* Data updateStiffnessMatrix of TetrahedronFEMForceField
+ * (TetrahedronFEMForceField.inl:49): on (1), every add_force call (and every
+ * scene step) rebuilds each element's strain-displacement matrix from its
+ * deformed positions in its current frame before forming the force
+ * (accumulateForcePolar :1063-1067, accumulateForceSVD :1174-1177), and the
+ * later addDForce / CG products use it. Methods polar and svd; method small
+ * ignores the flag, as the reference does. Method large returns
+ * SGB_ERR_NOT_SUPPORTED: the reference's large update (:908-921) writes only
+ * one of the entries J(3i,0) = J(3i+1,3) = J(3i+2,5) (and the like) that it
+ * builds equal, which this library stores once. Off (0) keeps the last
+ * rebuilt matrix, as the reference does. Synchronous on the handle's stream
+ * when first turned on (mixed precision computes a per-element scale). */
+int sgb_tfem_set_update_stiffness(sgb_tfem_t* fem, int on);
 /* von Mises stress (TetrahedronFEMForceField::computeVonMisesStress,
  * TetrahedronFEMForceField.inl:2197-2374; Data computeVonMisesStress,
  * vonMisesPerElement, vonMisesPerNode) at positions x_dev (n_nodes xyz

@@ -45,6 +45,7 @@ def _load():
     lib.orc_fem_rest_volume.restype = ctypes.c_double
     lib.orc_fem_rest_volume.argtypes = [vp]
     lib.orc_fem_set_plasticity.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.orc_fem_set_update_stiffness.argtypes = [vp, ctypes.c_int]
     lib.orc_fem_plastic_strain.argtypes = [vp, _dp]
     lib.orc_fem_von_mises.restype = ctypes.c_int
     lib.orc_fem_von_mises.argtypes = [vp, ctypes.c_int, _dp, _dp, _dp]
@@ -173,6 +174,10 @@ class OracleFEM:
     def set_plasticity(self, max_threshold, yield_threshold=1e-4, creep=0.9):
         """plasticMaxThreshold / plasticYieldThreshold / plasticCreep."""
         _load().orc_fem_set_plasticity(self._h, max_threshold, yield_threshold, creep)
+
+    def set_update_stiffness(self, on=True):
+        """updateStiffnessMatrix (methods polar and svd)."""
+        _load().orc_fem_set_update_stiffness(self._h, int(bool(on)))
 
     def von_mises(self, x, mode):
         """computeVonMisesStress at x: (per element, per node)."""

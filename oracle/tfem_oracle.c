@@ -592,6 +592,7 @@ typedef struct orc_fem {
     double* ebuf;      /* exact parallel mode: 12 corner terms per element */
     int32_t* nrow;     /* exact parallel mode: node -> (element*4 + corner) CSR, */
     int32_t* nslot;    /* rows in increasing order */
+    int update_stiffness; /* Data updateStiffnessMatrix (polar, svd) */
 } orc_fem;
 
 /* BaseLinearElasticityFEMForceField::getVecRealInElement
@@ -773,6 +774,11 @@ static void element_force_terms(orc_fem* m, int e, const double* p, double out[1
         D[11] = rr[11] - def[11];
     } else {
         for (int i = 0; i < 12; ++i) D[i] = rr[i] - def[i];
+        /* updateStiffnessMatrix: computeStrainDisplacement on the deformed
+         * positions in the element frame before the force
+         * (accumulateForcePolar TFEM.inl:1063-1067, accumulateForceSVD
+         * :1174-1177) */
+        if (m->update_stiffness) strain_displacement(&def[0], &def[3], &def[6], &def[9], &m->J3[12 * e]);
     }
     compute_force_pl(F, D, K3, J3, 0, 0.0, m->plastic ? &m->plastic[6 * e] : NULL, &m->pl);
     for (int i = 0; i < 4; ++i) mat_vec(rot, &F[3 * i], &out[3 * i]);
@@ -986,6 +992,14 @@ void orc_fem_element(const orc_fem* m, int e, double* out)
 }
 
 double orc_fem_rest_volume(const orc_fem* m) { return m->rest_volume; }
+
+/* updateStiffnessMatrix (TFEM.inl:49) for methods polar and svd: every
+ * addForce rebuilds J from the deformed element (see element_force_terms).
+ * The large method's partial rebuild (:908-921) is not restated. */
+void orc_fem_set_update_stiffness(orc_fem* m, int on)
+{
+    m->update_stiffness = (on && (m->method == ORC_POLAR || m->method == ORC_SVD)) ? 1 : 0;
+}
 
 /* plasticMaxThreshold / plasticYieldThreshold / plasticCreep; the plastic
  * strain starts at zero when plasticity is first turned on. */

@@ -150,6 +150,7 @@ def load():
         "sgb_tfem_add_dforce_f32": (c_int, [_vp, _vp, _vp, c_float, _vp]),
         "sgb_tfem_get_rotations": (c_int, [_vp, _dp, _dp]),
         "sgb_tfem_set_plasticity": (c_int, [_vp, c_double, c_double, c_double]),
+        "sgb_tfem_set_update_stiffness": (c_int, [_vp, c_int]),
         "sgb_tfem_reset_plasticity": (c_int, [_vp]),
         "sgb_tfem_get_plastic_strain": (c_int, [_vp, _dp]),
         "sgb_tfem_stiffness_bsr": (c_int, [_vp, ctypes.POINTER(c_int), _ip, _ip, _dp]),
@@ -329,6 +330,11 @@ class TetrahedronFEM:
         max_threshold > 0 every addForce updates the per-element plastic
         strain (TetrahedronFEMForceField::computeForce)."""
         check(load().sgb_tfem_set_plasticity(self._h, float(max_threshold), float(yield_threshold), float(creep)))
+
+    def set_update_stiffness(self, on=True):
+        """updateStiffnessMatrix: every addForce rebuilds the strain-displacement
+        matrices from the deformed elements (methods polar and svd)."""
+        check(load().sgb_tfem_set_update_stiffness(self._h, int(bool(on))))
 
     def von_mises(self, x_dev, mode, per_element_dev, per_node_dev=None, stream=None):
         """computeVonMisesStress at positions x_dev (device pointers, FP64)."""

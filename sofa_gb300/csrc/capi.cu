@@ -550,6 +550,51 @@ static cudaError_t upload_materials(const TfemMesh& m, double** d_y, double** d_
     return ce;
 }
 
+// Mixed precision: the per-element sqrt(K(0,0)) the packed J carries,
+// computed once (plasticity and updateStiffnessMatrix share it).
+static int ensure_k_scale(sgb_tfem_t* fem)
+{
+    TfemMesh& m = fem->m;
+    const size_t E = (size_t)m.n_tets;
+    if (m.real_size != sizeof(float) || m.plastic_scale || E == 0) return SGB_OK;
+    SGB_CUDA_TRY(cudaStreamSynchronize(fem->stream));
+    SGB_CUDA_TRY(cudaMalloc(&m.plastic_scale, sizeof(float) * E));
+    m.device_bytes += sizeof(float) * E;
+    double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr;
+    cudaError_t ce = upload_materials(m, &d_y, &d_p, &d_l);
+    if (ce == cudaSuccess) {
+        fem->ops->plastic_scale(&m, d_y, (int)m.young_h.size(), d_p, (int)m.poisson_h.size(), d_l,
+                                (int)m.lsf_h.size(), fem->stream);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(fem->stream);
+    cudaFree(d_y);
+    cudaFree(d_p);
+    cudaFree(d_l);
+    if (ce != cudaSuccess) return cuda_fail(ce, "per-element strain scale");
+    return SGB_OK;
+}
+
+int sgb_tfem_set_update_stiffness(sgb_tfem_t* fem, int on)
+{
+    if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_set_update_stiffness: NULL handle");
+    TfemMesh& m = fem->m;
+    if (on && m.method == METHOD_LARGE)
+        return fail(SGB_ERR_NOT_SUPPORTED,
+                    "sgb_tfem_set_update_stiffness: method large (the reference rebuilds only some of the "
+                    "strain-displacement entries it builds equal)");
+    if (on && m.method != METHOD_SMALL) {
+        int rc = ensure_k_scale(fem);
+        if (rc) return rc;
+    }
+    const int v = (on && m.method != METHOD_SMALL) ? 1 : 0;
+    if (v != m.update_j) {
+        m.update_j = v;
+        m.plastic_version++;  // captured steps re-record with the new force kernel arguments
+    }
+    return SGB_OK;
+}
+
 int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_threshold, double creep)
 {
     if (!fem) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_tfem_set_plasticity: NULL handle");
@@ -565,22 +610,8 @@ int sgb_tfem_set_plasticity(sgb_tfem_t* fem, double max_threshold, double yield_
         SGB_CUDA_TRY(cudaMalloc(&m.plastic, m.real_size * 6 * E));
         m.device_bytes += m.real_size * 6 * E;
         SGB_CUDA_TRY(cudaMemsetAsync(m.plastic, 0, m.real_size * 6 * E, fem->stream));
-        if (m.real_size == sizeof(float)) {
-            SGB_CUDA_TRY(cudaMalloc(&m.plastic_scale, sizeof(float) * E));
-            m.device_bytes += sizeof(float) * E;
-            double *d_y = nullptr, *d_p = nullptr, *d_l = nullptr;
-            cudaError_t ce = upload_materials(m, &d_y, &d_p, &d_l);
-            if (ce == cudaSuccess) {
-                fem->ops->plastic_scale(&m, d_y, (int)m.young_h.size(), d_p, (int)m.poisson_h.size(), d_l,
-                                        (int)m.lsf_h.size(), fem->stream);
-                ce = cudaGetLastError();
-            }
-            if (ce == cudaSuccess) ce = cudaStreamSynchronize(fem->stream);
-            cudaFree(d_y);
-            cudaFree(d_p);
-            cudaFree(d_l);
-            if (ce != cudaSuccess) return cuda_fail(ce, "sgb_tfem_set_plasticity");
-        }
+        int rc = ensure_k_scale(fem);
+        if (rc) return rc;
     }
     m.plastic_max = max_threshold;
     m.plastic_yield = yield_threshold;

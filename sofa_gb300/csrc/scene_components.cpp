@@ -698,9 +698,15 @@ int Scene::init_host(std::string* err)
         else return unsupported(err, where + "TetrahedronFEMForceField method '" + method + "' is not supported");
         if (fem->get_bool(*this, "computeGlobalMatrix") || fem->get_bool(*this, "assembling"))
             return unsupported(err, where + "computeGlobalMatrix=true (assembled matrix) is not supported");
-        if (b.method != SGB_METHOD_SMALL && fem->get_bool(*this, "updateStiffnessMatrix"))
-            return unsupported(err, where + "updateStiffnessMatrix=true (strain-displacement rebuilt every step, "
-                                            "TetrahedronFEMForceField.inl:908, 1063, 1174) is not supported");
+        // updateStiffnessMatrix: polar and svd rebuild J at every addForce
+        // (TetrahedronFEMForceField.inl:1063, 1174); small ignores it; the
+        // large rebuild (:908-921) writes only some of the entries it builds
+        // equal, which the library stores once
+        b.update_stiffness = fem->get_bool(*this, "updateStiffnessMatrix") && b.method != SGB_METHOD_SMALL;
+        if (b.update_stiffness && b.method == SGB_METHOD_LARGE)
+            return unsupported(err, where + "updateStiffnessMatrix=true with method large (the reference rebuilds "
+                                            "only part of the strain-displacement entries, "
+                                            "TetrahedronFEMForceField.inl:908-921) is not supported");
         b.plastic_max = fem->get_real(*this, "plasticMaxThreshold");
         b.plastic_yield = fem->get_real(*this, "plasticYieldThreshold");
         b.plastic_creep = fem->get_real(*this, "plasticCreep");
@@ -803,8 +809,9 @@ int Scene::init_device(std::string* err)
             *err = sgb_last_error();
             return rc;
         }
-        if (b.plastic_max > 0.0 &&
-            (rc = sgb_tfem_set_plasticity(fem, b.plastic_max, b.plastic_yield, b.plastic_creep))) {
+        if ((b.plastic_max > 0.0 &&
+             (rc = sgb_tfem_set_plasticity(fem, b.plastic_max, b.plastic_yield, b.plastic_creep))) ||
+            (b.update_stiffness && (rc = sgb_tfem_set_update_stiffness(fem, 1)))) {
             *err = sgb_last_error();
             sgb_tfem_destroy(fem);
             return rc;

@@ -133,6 +133,7 @@ struct Body {
     std::vector<int32_t> tets;  // E x 4
     std::vector<double> young, poisson;
     double plastic_max = 0.0, plastic_yield = 1e-4, plastic_creep = 0.9;  // TetrahedronFEMForceField plasticity
+    bool update_stiffness = false;  // TetrahedronFEMForceField updateStiffnessMatrix (polar, svd)
     int von_mises_mode = 0;  // computeVonMisesStress: 0 off, 1 corotational, 2 Green strain
     int method = SGB_METHOD_LARGE;
     int precision = SGB_PRECISION_FP64;

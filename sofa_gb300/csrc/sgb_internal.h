@@ -129,6 +129,7 @@ struct TfemMesh {
     void* plastic_scale = nullptr;
     double plastic_max = 0.0, plastic_yield = 1e-4, plastic_creep = 0.9;
     int plastic_version = 0;  // bumped by every change of the settings (a captured step re-records)
+    int update_j = 0;         // updateStiffnessMatrix (polar, svd): J rebuilt at every addForce
     double* vm_lame = nullptr;  // von Mises: lambda, mu per element (2 rows, computed on first use)
     std::vector<double> young_h, poisson_h;  // as given (for inspection)
     std::vector<double> lsf_h;               // localStiffnessFactor as given

@@ -441,6 +441,11 @@ struct PlasticArgs {
     R* strain = nullptr;         // 6 rows x n_tets; null: plasticity off
     const R* scale = nullptr;    // mixed: sqrt(K(0,0)) per element; null for FP64
     R max_threshold = R(0), yield_threshold = R(0), creep = R(0);
+    // updateStiffnessMatrix (polar, svd): the element's strain-displacement
+    // values rebuilt from its deformed positions in its current frame at
+    // every addForce (TFEM.inl:1063-1067, 1174-1177) and stored here (the
+    // mesh's J array; mixed: scaled by `scale`); null: J stays as built
+    R* update_J = nullptr;
 };
 
 // computeForce's plastic step (TFEM.inl:357-370): the elastic part of the
@@ -502,6 +507,31 @@ __device__ __forceinline__ void addforce_element(R F[12], const R D[12], const R
 // addForce element part: accumulateForceSmall / Large / Polar
 // (TFEM.inl:534-623, 870-986, 1025-1079). Writes rotations and the corner
 // forces R^T F (method=small: F).
+// updateStiffnessMatrix, FP32: J from the element's deformed edges in its
+// frame (node a at the origin: the cofactors are translation invariant, and
+// relative coordinates keep them accurate in FP32), scaled by sqrt(K(0,0))
+// and packed as the init kernel packs it; J (registers) takes the new
+// values, node a's as minus the sum of the others like load_KJ.
+template <typename R>
+__device__ __forceinline__ void update_j_mixed(const float ew[3][3], float sk, const R K[3], R J[12], R* Jout,
+                                               size_t e, size_t En)
+{
+    if constexpr (is_mixed<R>::value) {
+        const float o[3] = {0.f, 0.f, 0.f};
+        float Jn[12];
+        strain_displacement(o, ew[0], ew[1], ew[2], Jn);
+#pragma unroll
+        for (int i = 3; i < 12; ++i) J[i] = sk * Jn[i];
+        J[0] = -(J[3] + J[6] + J[9]);
+        J[1] = -(J[4] + J[7] + J[10]);
+        J[2] = -(J[5] + J[8] + J[11]);
+        float4* P = reinterpret_cast<float4*>(Jout);
+        P[e] = make_float4(J[3], J[4], J[5], J[6]);
+        P[En + e] = make_float4(J[7], J[8], J[9], J[10]);
+        P[2 * En + e] = make_float4(J[11], K[1], K[2], 0.f);
+    }
+}
+
 // KEEP: also hands the rotation (before packing), K and J to the caller
 // (rotated methods only).
 template <typename R, int METHOD, bool KEEP = false>
@@ -562,6 +592,16 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
                 acc += Rm[3 * k + 2] * (R)p[i][2];
                 def[3 * i + k] = acc;
             }
+        if constexpr (METHOD == METHOD_POLAR || METHOD == METHOD_SVD) {
+            // updateStiffnessMatrix: computeStrainDisplacement on the
+            // deformed positions in the element frame (absolute, as the
+            // reference passes them)
+            if (pl.update_J) {
+                strain_displacement(&def[0], &def[3], &def[6], &def[9], J);
+#pragma unroll
+                for (int i = 0; i < 12; ++i) pl.update_J[i * En + e] = J[i];
+            }
+        }
         if (METHOD == METHOD_LARGE) {
             def[3] -= def[0];
             def[6] -= def[0];
@@ -615,6 +655,7 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
 #pragma unroll
             for (int i = 0; i < 9; ++i) Rm[i] = X[i] + dX[i];
             D[0] = D[1] = D[2] = R(0);
+            float ew[3][3];  // the edges in the element frame (updateStiffnessMatrix)
 #pragma unroll
             for (int i = 1; i < 4; ++i)
 #pragma unroll
@@ -631,7 +672,10 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
                     lo += dr[0] * ei[0].h + dr[1] * ei[1].h + dr[2] * ei[2].h;
                     const float2 rv = ev.rest_ff[(size_t)(3 * (i - 1) + k) * En + e];
                     D[3 * i + k] = (rv.x - s.h) + (rv.y - lo);
+                    ew[i - 1][k] = s.h + lo;
                 }
+            if constexpr (METHOD == METHOD_POLAR || METHOD == METHOD_SVD)
+                if (pl.update_J) update_j_mixed(ew, pl.scale[e], K, J, pl.update_J, (size_t)e, En);
         } else {
             // mixed without float-float rest coordinates: edges formed in FP64
             // and rounded once, the strain in FP32 on positions relative to node a
@@ -647,14 +691,18 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
                 if (!(METHOD == METHOD_SVD && svd_frame_elem(ev, (size_t)e, A, Rm))) polar3(A, Rm);
             }
             D[0] = D[1] = D[2] = R(0);
+            float ew[3][3];  // the edges in the element frame (updateStiffnessMatrix)
 #pragma unroll
             for (int i = 1; i < 4; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     R d = Rm[3 * k] * ed[i - 1][0] + Rm[3 * k + 1] * ed[i - 1][1] + Rm[3 * k + 2] * ed[i - 1][2];
                     D[3 * i + k] = rr[3 * i + k] - d;
+                    ew[i - 1][k] = (float)d;
                 }
             if (METHOD == METHOD_LARGE) D[4] = D[5] = D[8] = R(0);
+            if constexpr (METHOD == METHOD_POLAR || METHOD == METHOD_SVD)
+                if (pl.update_J) update_j_mixed(ew, pl.scale[e], K, J, pl.update_J, (size_t)e, En);
         }
     }
     store_rot(ev, (size_t)e, Rm);
@@ -2216,6 +2264,10 @@ void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
         pl.yield_threshold = (R)m->plastic_yield;
         pl.creep = (R)m->plastic_creep;
     }
+    if (m->update_j) {
+        pl.update_J = (R*)m->J;
+        pl.scale = (const R*)m->plastic_scale;
+    }
     if (m->method == METHOD_SMALL)
         k_elem_force<R, METHOD_SMALL><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
     else if (m->method == METHOD_LARGE)
@@ -2240,6 +2292,10 @@ void launch_elem_force_rhs(TfemMesh* m, const double* x, const double* v, R kf_r
         pl.max_threshold = (R)m->plastic_max;
         pl.yield_threshold = (R)m->plastic_yield;
         pl.creep = (R)m->plastic_creep;
+    }
+    if (m->update_j) {
+        pl.update_J = (R*)m->J;
+        pl.scale = (const R*)m->plastic_scale;
     }
     if (m->method == METHOD_LARGE)
         k_elem_force_rhs<R, METHOD_LARGE>
@@ -2667,9 +2723,9 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     const StepFactors F = step_factors(P);
     // forces and the right-hand side: one pass over the elements (force
     // terms and (h + rs) K v terms), one over the nodes; the operations of
-    // the four kernels of scene_step, which this library's FP32 build
-    // contracts alike, so the values agree bit for bit (sc->eforce_v null:
-    // those four kernels)
+    // the four kernels of scene_step (sc->eforce_v null: those four
+    // kernels), equal to rounding (the FP32 build may contract multiply-adds
+    // differently in the fused kernel)
     if (sc->eforce_v) {
         if (P.first_order)
             launch_elem_force<R>(m, sc->x, s);
