@@ -1697,6 +1697,11 @@ __device__ __forceinline__ void cp_async16(void* dst_smem, const void* src)
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void* dst_smem, const void* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all()
 {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
@@ -1713,8 +1718,8 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
     // phase 0: the patch's slot lists (4 per element, from slot 4*e0; e0 is
     // even, so the 16-byte copies start on a 16-byte boundary and may read 8
     // bytes of padding past the end; a patch without elements copies
-    // nothing) and row starts into shared memory, so that the gather of
-    // phase 2 runs on shared memory only
+    // nothing) and row starts (global offsets; phase 2 subtracts 4*e0) into
+    // shared memory, so that the gather of phase 2 runs on shared memory only
     {
         const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
         uint4* dst = reinterpret_cast<uint4*>(sl);
@@ -1722,7 +1727,7 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         // asynchronous copies: the node loads below go out without waiting
         // for them (0.35 % faster CG steps than copies through registers)
         for (int k = threadIdx.x; k < n16; k += blockDim.x) cp_async16(dst + k, src + k);
-        for (int l = threadIdx.x; l <= nn; l += blockDim.x) lr[l] = pv.lrow[n0 + l] - 4 * e0;
+        for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(lr + l, pv.lrow + n0 + l);
     }
     // phase 0: nodal values of the patch
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
@@ -1756,7 +1761,7 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
     __syncthreads();
     // phase 2: per local node, its slots in element order
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int s0 = lr[l], s1 = lr[l + 1];
+        const int s0 = lr[l] - 4 * e0, s1 = lr[l + 1] - 4 * e0;
         R a0 = R(0), a1 = R(0), a2 = R(0);
         for (int s = s0; s < s1; ++s) {
             const int slot = sl[s];
