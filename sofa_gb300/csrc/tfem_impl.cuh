@@ -1759,8 +1759,25 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         patch_element<R, MODE>(le, pv.lconn[e], Rm, K, J, a.kf, pv.pe, lp, ef, pen);
     }
     __syncthreads();
-    // phase 2: per local node, its slots in element order
+    // phase 2: per local node, its slots in element order. The node's
+    // global loads (id, layout word, then what its finish reads: df for
+    // addDForce, mass and fixed flag for the CG modes) go out before the
+    // shared-memory sum, so that they arrive while it runs.
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int g = pv.lnode_gid[n0 + l];
+        const int info = pv.lnode_info[n0 + l];
+        R d0 = R(0), d1 = R(0), d2 = R(0), mm = a.mmu;
+        bool fx = false;
+        if (MODE == 0) {
+            if (info < 0) {
+                d0 = a.qout[3 * (size_t)g];
+                d1 = a.qout[3 * (size_t)g + 1];
+                d2 = a.qout[3 * (size_t)g + 2];
+            }
+        } else if (info < 0 || (info & 1)) {
+            if (a.ma.node_mass) mm = (R)(a.ma.node_mass[g] * a.mf);
+            if (info < 0) fx = a.fixed[g] != 0;
+        }
         const int s0 = lr[l] - 4 * e0, s1 = lr[l + 1] - 4 * e0;
         R a0 = R(0), a1 = R(0), a2 = R(0);
         for (int s = s0; s < s1; ++s) {
@@ -1770,8 +1787,6 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
             a1 += ef[(3 * cc + 1) * pv.pe + le];
             a2 += ef[(3 * cc + 2) * pv.pe + le];
         }
-        const int g = pv.lnode_gid[n0 + l];
-        const int info = pv.lnode_info[n0 + l];
         if (info >= 0) {
             R* o = a.partials + 3 * (size_t)(info >> 1);
             o[0] = a0;
@@ -1780,17 +1795,16 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         }
         if (MODE == 0) {
             if (info < 0) {
-                a.qout[3 * (size_t)g] -= a0;
-                a.qout[3 * (size_t)g + 1] -= a1;
-                a.qout[3 * (size_t)g + 2] -= a2;
+                a.qout[3 * (size_t)g] = d0 - a0;
+                a.qout[3 * (size_t)g + 1] = d1 - a1;
+                a.qout[3 * (size_t)g + 2] = d2 - a2;
             }
         } else if (info < 0 || (info & 1)) {
             const R p0 = lp[3 * l], p1 = lp[3 * l + 1], p2 = lp[3 * l + 2];
-            const R mm = a.ma.node_mass ? (R)(a.ma.node_mass[g] * a.mf) : a.mmu;
             pen += mm * (p0 * p0 + p1 * p1 + p2 * p2);
             if (info < 0) {
                 R q0 = mm * p0 - a0, q1 = mm * p1 - a1, q2 = mm * p2 - a2;
-                if (a.fixed[g]) q0 = q1 = q2 = R(0);
+                if (fx) q0 = q1 = q2 = R(0);
                 a.qout[3 * (size_t)g] = q0;
                 a.qout[3 * (size_t)g + 1] = q1;
                 a.qout[3 * (size_t)g + 2] = q2;
