@@ -304,6 +304,14 @@ typedef struct sgb_scene_params {
      * (h tr + rs) and in the system factors mF = 1 + tr h rm, bF = -tr h,
      * kF = -tr h (tr h + rs) (first order: kF = -h tr). */
     int trapezoidal_scheme;
+    /* EulerImplicitSolver computeResidual (EulerImplicitSolver.cpp:48-49,
+     * 314-338): after each step the squared norm of r = M (v_new - v_old) -
+     * dt F(x_new), projected, is kept (sgb_scene_residual). In the animation
+     * loop's call v_new and v_old are the same vector, so r = -dt F(x_new);
+     * the extra force computation runs the force field again (its plastic
+     * strains and, with updateStiffnessMatrix, its strain-displacement
+     * matrices see it, as in the reference). */
+    int compute_residual;
 } sgb_scene_params;
 
 #define SGB_SOLVER_CG 0
@@ -329,6 +337,10 @@ int sgb_scene_step(sgb_scene_t* scene, int n_steps);
  * run, last relative residual |r|/|b|, and SGB_ERR_NUMERICAL if a
  * non-finite value was met. */
 int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual);
+/* The Data `residual` of EulerImplicitSolver after the last step: r.r of the
+ * residual above (scene created with compute_residual). Synchronises the
+ * scene's stream. SGB_ERR_INVALID_ARGUMENT when compute_residual is off. */
+int sgb_scene_residual(sgb_scene_t* scene, double* residual);
 
 /* von Mises stress of the scene's force field at its current positions
  * (sgb_tfem_von_mises; TetrahedronFEMForceField computes it at the end of

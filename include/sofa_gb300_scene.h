@@ -99,6 +99,12 @@ int sgb_sofa_scene_get_positions(sgb_sofa_scene_t* scene, int body, double* x_ho
 int sgb_sofa_scene_get_von_mises(sgb_sofa_scene_t* scene, int body, double* per_element_host,
                                  double* per_node_host);
 
+/* The Data `residual` of a body's EulerImplicitSolver with computeResidual
+ * set (EulerImplicitSolver.cpp:48-49, 314-338): r.r of the last step's
+ * residual. SGB_ERR_INVALID_ARGUMENT when computeResidual is 0 or the device
+ * is not initialised yet. Synchronous. */
+int sgb_sofa_scene_get_residual(sgb_sofa_scene_t* scene, int body, double* residual);
+
 /* Simulated time (steps x dt). */
 int sgb_sofa_scene_time(const sgb_sofa_scene_t* scene, double* t);
 

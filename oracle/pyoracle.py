@@ -70,6 +70,9 @@ def _load():
     lib.orc_scene_set_warm_start.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_set_options.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
     lib.orc_scene_set_trapezoidal.argtypes = [vp, ctypes.c_int]
+    lib.orc_scene_set_compute_residual.argtypes = [vp, ctypes.c_int]
+    lib.orc_scene_residual.restype = ctypes.c_double
+    lib.orc_scene_residual.argtypes = [vp]
     lib.orc_scene_jacobi.argtypes = [vp, _dp]
     lib.orc_scene_compute_force.argtypes = [vp, _dp]
     lib.orc_scene_last_iterations.restype = ctypes.c_int
@@ -305,6 +308,15 @@ class OracleScene:
     @property
     def last_error(self):
         return _load().orc_scene_last_error(self._h)
+
+    def set_compute_residual(self, on=True):
+        """EulerImplicitSolver computeResidual."""
+        _load().orc_scene_set_compute_residual(self._h, int(bool(on)))
+
+    @property
+    def residual(self):
+        """EulerImplicitSolver's Data `residual` after the last step."""
+        return _load().orc_scene_residual(self._h)
 
 
 def ref_math_lib():

@@ -1209,6 +1209,8 @@ typedef struct orc_scene {
     double ff_rs, mass_rm;
     int first_order, project_velocity, trapezoidal;
     double cur_bf; /* bFactor of the matrix being applied (0 for the right-hand side) */
+    int compute_residual; /* EulerImplicitSolver computeResidual */
+    double residual;      /* its Data `residual` after the last step */
 } orc_scene;
 
 orc_scene* orc_scene_create(orc_fem* fem, int n_nodes, int mass_kind, double vertex_mass,
@@ -1750,12 +1752,26 @@ static void euler_step(orc_scene* s)
         const double d = exp(-h * s->vdamping);
         for (long i = 0; i < n3; ++i) s->v[i] *= d;
     }
+    if (s->compute_residual) {
+        /* computeResidual (EulerImplicitSolver.cpp:314-338): r = 0;
+         * r += M (newVel - vel), zero, the animation loop passing the
+         * state's velocity as both; f = computeForce at the new state (the
+         * force field runs again, plastic strains and rebuilt J included);
+         * r += f (-dt); projectResponse(r); residual = r.r (vDot) */
+        scene_compute_force(s);
+        for (long i = 0; i < n3; ++i) s->r[i] = 0.0 + s->f[i] * (-h);
+        project_response(s, s->r);
+        s->residual = vdot(s->r, s->r, s->n);
+    }
     /* DefaultAnimationLoop::projectPositionAndVelocity (DefaultAnimationLoop.cpp:
      * 228-233, 293): FixedProjectiveConstraint::projectVelocity
      * (FixedProjectiveConstraint.inl:237-261) zeroes the fixed nodes' velocity
      * when activate_projectVelocity is set; projectPosition does nothing */
     if (s->project_velocity) project_response(s, s->v);
 }
+
+void orc_scene_set_compute_residual(orc_scene* s, int on) { s->compute_residual = on ? 1 : 0; }
+double orc_scene_residual(const orc_scene* s) { return s->residual; }
 
 void orc_scene_step(orc_scene* s, int n_steps)
 {

@@ -62,6 +62,7 @@ class SceneParams(ctypes.Structure):
         ("first_order", ctypes.c_int),
         ("project_velocity", ctypes.c_int),
         ("trapezoidal_scheme", ctypes.c_int),
+        ("compute_residual", ctypes.c_int),
     ]
 
 
@@ -162,6 +163,7 @@ def load():
         "sgb_scene_destroy": (c_int, [_vp]),
         "sgb_scene_step": (c_int, [_vp, c_int]),
         "sgb_scene_sync": (c_int, [_vp, ctypes.POINTER(c_int), _dp]),
+        "sgb_scene_residual": (c_int, [_vp, _dp]),
         "sgb_scene_von_mises": (c_int, [_vp, c_int, _dp, _dp]),
         "sgb_tfem_von_mises": (c_int, [_vp, c_int, _vp, _vp, _vp, _vp]),
         "sgb_scene_get_state": (c_int, [_vp, _dp, _dp]),
@@ -214,6 +216,7 @@ def load():
         "sgb_sofa_scene_animate": (c_int, [_vp, c_int]),
         "sgb_sofa_scene_get_positions": (c_int, [_vp, c_int, _dp]),
         "sgb_sofa_scene_get_von_mises": (c_int, [_vp, c_int, _dp, _dp]),
+        "sgb_sofa_scene_get_residual": (c_int, [_vp, c_int, _dp]),
         "sgb_sofa_scene_time": (c_int, [_vp, _dp]),
         "sgb_object_factory_new": (_vp, []),
         "sgb_object_factory_delete": (None, [_vp]),
@@ -376,7 +379,7 @@ class Scene:
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
                  serial_dots=False, residual_replacement=0, linear_solver="cg", preconditioner=None,
                  preconditioner_rate=1, warm_start=False, ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0,
-                 first_order=False, project_velocity=False, trapezoidal_scheme=False):
+                 first_order=False, project_velocity=False, trapezoidal_scheme=False, compute_residual=False):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -412,6 +415,7 @@ class Scene:
         p.first_order = int(first_order)
         p.project_velocity = int(project_velocity)
         p.trapezoidal_scheme = int(trapezoidal_scheme)
+        p.compute_residual = int(compute_residual)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now
@@ -447,6 +451,13 @@ class Scene:
         res = ctypes.c_double()
         check(load().sgb_scene_sync(self._h, ctypes.byref(it), ctypes.byref(res)))
         return it.value, res.value
+
+    def residual(self):
+        """EulerImplicitSolver's Data `residual` after the last step
+        (scene created with compute_residual=True)."""
+        r = ctypes.c_double()
+        check(load().sgb_scene_residual(self._h, ctypes.byref(r)))
+        return r.value
 
     def state(self):
         x = np.zeros((self.n_nodes, 3))
@@ -852,6 +863,13 @@ class SofaScene:
         check(load().sgb_sofa_scene_get_von_mises(self._h, int(body), e.ctypes.data_as(_dp),
                                                   n.ctypes.data_as(_dp)))
         return e, n
+
+    def residual(self, body=0):
+        """The Data `residual` of a body's EulerImplicitSolver with
+        computeResidual set, after the last step."""
+        r = ctypes.c_double()
+        check(load().sgb_sofa_scene_get_residual(self._h, int(body), ctypes.byref(r)))
+        return r.value
 
     @property
     def time(self) -> float:

@@ -316,6 +316,8 @@ static int validate_mesh(const sgb_mesh_desc* m)
     if (p.serial_dots)
         return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes sum dot products per block, not serially (serial_dots)");
     if (p.first_order) return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes run the second-order Euler scheme");
+    if (p.compute_residual)
+        return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not compute EulerImplicitSolver's residual");
     if (p.project_velocity)
         return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not support activate_projectVelocity");
     if (!std::isfinite(p.ff_rayleigh_stiffness) || !std::isfinite(p.mass_rayleigh_mass))

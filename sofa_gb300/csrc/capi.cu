@@ -900,6 +900,7 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     s.prm.first_order = P.first_order ? 1 : 0;
     s.prm.project_velocity = P.project_velocity ? 1 : 0;
     s.prm.trapezoidal = P.trapezoidal_scheme ? 1 : 0;
+    s.prm.compute_residual = P.compute_residual ? 1 : 0;
     s.stream = fem->stream;
     sc->fem = fem;
     sc->ops = fem->ops;
@@ -1062,6 +1063,18 @@ int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual)
     if (cg_residual) *cg_residual = s.cg_h->last_err;
     if (s.cg_h->status & 1) return fail(SGB_ERR_NUMERICAL, "non-finite value in the CG solve");
     if (s.cg_h->status & 2) return fail(SGB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait ran out in the CG solve");
+    return SGB_OK;
+}
+
+int sgb_scene_residual(sgb_scene_t* scene, double* residual)
+{
+    if (!scene || !residual) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_residual: NULL argument");
+    Scene& s = scene->s;
+    if (!s.prm.compute_residual)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_scene_residual: the scene was created without compute_residual");
+    SGB_CUDA_TRY(cudaMemcpyAsync(s.cg_h, s.cg, offsetof(CgScalars, partials), cudaMemcpyDeviceToHost, s.stream));
+    SGB_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    *residual = s.cg_h->residual;
     return SGB_OK;
 }
 

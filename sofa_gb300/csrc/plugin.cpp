@@ -195,6 +195,18 @@ int sgb_sofa_scene_get_von_mises(sgb_sofa_scene_t* scene, int body, double* per_
     return sgb_scene_von_mises(b.scene, b.von_mises_mode, per_element_host, per_node_host);
 }
 
+int sgb_sofa_scene_get_residual(sgb_sofa_scene_t* scene, int body, double* residual)
+{
+    if (!scene || !residual || body < 0 || body >= (int)scene->scene.bodies.size())
+        return fail(SGB_ERR_NOT_FOUND, "sgb_sofa_scene_get_residual: no such body");
+    sgb::scn::Body& b = scene->scene.bodies[(size_t)body];
+    if (!b.params.compute_residual)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_get_residual: computeResidual is 0");
+    if (!b.scene)
+        return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_get_residual: the device is not initialised yet");
+    return sgb_scene_residual(b.scene, residual);
+}
+
 int sgb_sofa_scene_time(const sgb_sofa_scene_t* scene, double* t)
 {
     if (!scene || !t) return fail(SGB_ERR_INVALID_ARGUMENT, "sgb_sofa_scene_time: NULL argument");

@@ -727,6 +727,7 @@ int Scene::init_host(std::string* err)
         b.params.trapezoidal_scheme = euler->get_bool(*this, "trapezoidalScheme") ? 1 : 0;
         b.params.dt = dt;
         b.params.first_order = euler->get_bool(*this, "firstOrder") ? 1 : 0;
+        b.params.compute_residual = euler->get_bool(*this, "computeResidual") ? 1 : 0;
         // the force field's own rayleighStiffness (BaseForceField.cpp:34): its
         // addDForce factor is kFactorIncludingRayleighDamping
         b.params.ff_rayleigh_stiffness = fem->get_real(*this, "rayleighStiffness");

@@ -155,6 +155,7 @@ struct CgScalars {
     double rmax;
     int replace_it;
     int pad3;
+    double residual;  // EulerImplicitSolver computeResidual: r.r after the last step
     double partials[kMaxDotBlocks];
 };
 
@@ -173,6 +174,7 @@ struct SceneParams {
     int first_order = 0;   // EulerImplicitSolver firstOrder
     int project_velocity = 0;  // FixedProjectiveConstraint activate_projectVelocity
     int trapezoidal = 0;       // EulerImplicitSolver trapezoidalScheme (tr = 0.5)
+    int compute_residual = 0;  // EulerImplicitSolver computeResidual
 };
 
 // Factors of one EulerImplicitSolver step (EulerImplicitSolver.cpp:117-171,

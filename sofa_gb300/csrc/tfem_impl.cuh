@@ -981,7 +981,15 @@ __device__ __forceinline__ double dot3(const A a[3], const B b[3])
     return r;
 }
 
-enum Finish { FIN_RHS = 0, FIN_DEN = 1, FIN_RHO = 2, FIN_REPLACE = 3, FIN_PCG_START = 4, FIN_WARM_START = 5 };
+enum Finish {
+    FIN_RHS = 0,
+    FIN_DEN = 1,
+    FIN_RHO = 2,
+    FIN_REPLACE = 3,
+    FIN_PCG_START = 4,
+    FIN_WARM_START = 5,
+    FIN_RESIDUAL = 6
+};
 
 struct SolveConsts {
     double tol, threshold;
@@ -1036,6 +1044,10 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
     }
     if (threadIdx.x != 0) return;
     cg->ticket = 0;
+    if (FIN == FIN_RESIDUAL) {  // the Data `residual` only; the solve is over
+        cg->residual = total;
+        return;
+    }
     if (!isfinite(total)) {
         cg->status |= 1;
         cg->done = 1;
@@ -1541,6 +1553,28 @@ __global__ void __launch_bounds__(kNodeBlock) k_pcg_start(NodeCSR csr, const R* 
 // project_velocity: FixedProjectiveConstraint::projectVelocity
 // (FixedProjectiveConstraint.inl:237-261), after the solve: fixed nodes'
 // velocities set to zero (their positions have moved with the unprojected v).
+// EulerImplicitSolver computeResidual (EulerImplicitSolver.cpp:314-338),
+// after the step: r = 0; r += M (v_new - v_old), zero because the animation
+// loop passes the state's own velocity as both; r += f (-dt) with f the
+// scene's force at the new state (computeForce, just formed into f); r
+// projected; r.r (MechanicalObject::vDot, serial with `terms`).
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_residual_dot(const R* __restrict__ f,
+                                                             const uint8_t* __restrict__ fixed, double dt,
+                                                             CgScalars* cg, double* terms, int N, SolveConsts sc)
+{
+    double local = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        double r[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r[k] = fixed[n] ? 0.0 : (double)f[3 * (size_t)n + k] * (-dt);
+        const double d = dot3(r, r);
+        if (terms) terms[n] = d;
+        local += d;
+    }
+    finish_dot<FIN_RESIDUAL>(local, cg, terms, N, sc);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict__ x, double* __restrict__ v,
                                                              const R* __restrict__ xs, double h, double vdamp,
@@ -2663,6 +2697,26 @@ void pcg_begin(Scene* sc, int mass_first, double mf, double kf, const SolveConst
                                              mass_first, sc->fixed, dinv, (R*)sc->r, sc->cg, dot_terms, N, cons);
 }
 
+// computeResidual at the end of a step: the scene's force at the new state
+// (the force field runs again, with its side effects on plastic strains
+// and rebuilt strain-displacement matrices, as the reference's computeForce
+// does), then the residual's r.r into cg->residual.
+template <typename R>
+void launch_step_residual(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
+{
+    TfemMesh* m = sc->mesh;
+    const int N = sc->n;
+    const SceneParams& P = sc->prm;
+    NodeCSR csr{m->rowptr, m->slots};
+    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const int ng = node_grid(N);
+    SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, 0, 0};
+    launch_elem_force<R>(m, sc->x, s);
+    k_gather_force<R><<<ng, kNodeBlock, 0, s>>>(csr, (const R*)m->eforce, (const R*)sc->ext, ma, mass_first,
+                                                (R*)sc->f, N);
+    k_residual_dot<R><<<ng, kNodeBlock, 0, s>>>((const R*)sc->f, sc->fixed, P.dt, sc->cg, dot_terms, N, cons);
+}
+
 // One implicit Euler step of a scene (EulerImplicitSolver::solve,
 // Sofa/Component/ODESolver/Backward/src/sofa/component/odesolver/backward/
 // EulerImplicitSolver.cpp:83-341) as a fixed sequence of launches: the CG
@@ -2729,6 +2783,7 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N, P.first_order,
                                                 P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
+    if (P.compute_residual) launch_step_residual<R>(sc, dot_terms, mass_first, s);
 }
 
 // The same step with the fused patch matvec: two launches per CG iteration
@@ -2818,6 +2873,7 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N, P.first_order,
                                                 P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
+    if (P.compute_residual) launch_step_residual<R>(sc, nullptr, mass_first, s);
 }
 
 // The FP32 patch step with residual replacement every sc->replace_every CG
@@ -2896,6 +2952,7 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_refined<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, sc->x64, xs, h, vd, sc->cg, N,
                                                  P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
+    if (P.compute_residual) launch_step_residual<R>(sc, nullptr, mass_first, s);
 }
 
 }  // namespace SGB_NS

@@ -152,7 +152,8 @@ def test_patch_layout_nodes_of_no_element(capi):
 
 
 @pytest.mark.parametrize("field,value", [("linear_solver", 1), ("preconditioner", 1), ("warm_start", 1),
-                                         ("residual_replacement", 20), ("serial_dots", 1)])
+                                         ("residual_replacement", 20), ("serial_dots", 1),
+                                         ("compute_residual", 1)])
 def test_batch_admission_refuses_solver_options_it_does_not_run(capi, field, value):
     """The batch engine runs cold-start CG with block-ordered dots; a mesh
     that asks for PCG, a preconditioner, warmStart, residual replacement or
