@@ -702,6 +702,15 @@ int Scene::init_host(std::string* err)
         // (TetrahedronFEMForceField.inl:1063, 1174); small ignores it; the
         // large rebuild (:908-921) writes only some of the entries it builds
         // equal, which the library stores once
+        // initialPoints replaces the force field's rest positions
+        // (TetrahedronFEMForceField::init); only the default (empty, or equal
+        // to the MechanicalObject's rest positions) is supported
+        {
+            const std::vector<double> ip = fem->get_reals(*this, "initialPoints");
+            if (!ip.empty() && ip != b.rest)
+                return unsupported(err, where + "TetrahedronFEMForceField initialPoints other than the rest "
+                                                "positions is not supported");
+        }
         b.update_stiffness = fem->get_bool(*this, "updateStiffnessMatrix") && b.method != SGB_METHOD_SMALL;
         if (b.update_stiffness && b.method == SGB_METHOD_LARGE)
             return unsupported(err, where + "updateStiffnessMatrix=true with method large (the reference rebuilds "
@@ -761,6 +770,14 @@ int Scene::init_host(std::string* err)
         // the mass's own rayleighMass (BaseMass.cpp:33-34): its addMDx factor
         // is mFactorIncludingRayleighDamping
         b.params.mass_rayleigh_mass = mass->get_real(*this, "rayleighMass");
+        // separateGravity moves gravity out of the force into a velocity
+        // increment after the position update (UniformMass::addGravityToV,
+        // EulerImplicitSolver.cpp:296), which the step does not run
+        if (mass->get_bool(*this, "separateGravity"))
+            return unsupported(err, where + mass->class_name() + " separateGravity=true is not supported");
+        if (mass->class_name() == "UniformMass" && !mass->get_ints(*this, "indices").empty())
+            return unsupported(err, where + "UniformMass indices (a mass on a subset of the points) is not "
+                                            "supported");
         if (mass->class_name() == "UniformMass") {
             // UniformMass::init: totalMass wins over vertexMass when both are
             // set; neither set is an error (UniformMass.inl:233-268)

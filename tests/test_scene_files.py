@@ -159,6 +159,9 @@ def test_scene_errors(capi, case):
       ' />\n        <FixedProjectiveConstraint name="fix2" indices="0"'), "activate_projectVelocity"),
     (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="3" name="FEM"'),
      "computeVonMisesStress"),
+    (('<DiagonalMass name="mass"', '<DiagonalMass separateGravity="1" name="mass"'), "separateGravity"),
+    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField initialPoints="0 0 0" name="FEM"'),
+     "initialPoints"),
 ])
 def test_unsupported_component_settings(capi, edit, msg):
     xml = _read("grid_fem_4x10x4.scn").replace(*edit)
