@@ -312,6 +312,12 @@ typedef struct sgb_scene_params {
      * strains and, with updateStiffnessMatrix, its strain-displacement
      * matrices see it, as in the reference). */
     int compute_residual;
+    /* The mass's separateGravity (UniformMass / DiagonalMass; UniformMass.inl:
+     * 450-475): the mass adds no weight to the force, and after the position
+     * update the step adds g dt to every velocity (EulerImplicitSolver.cpp:
+     * 296), before the velocity damping; the fixed points get it too, as in
+     * the reference. */
+    int separate_gravity;
 } sgb_scene_params;
 
 #define SGB_SOLVER_CG 0
@@ -334,8 +340,9 @@ int sgb_scene_destroy(sgb_scene_t* scene);
 int sgb_scene_step(sgb_scene_t* scene, int n_steps);
 
 /* Waits for the scene's stream and reports the last CG solve: iterations
- * run, last relative residual |r|/|b|, and SGB_ERR_NUMERICAL if a
- * non-finite value was met. */
+ * run (the matrix-vector products, including that of an iteration ended by
+ * the denominator threshold), last relative residual |r|/|b|, and
+ * SGB_ERR_NUMERICAL if a non-finite value was met. */
 int sgb_scene_sync(sgb_scene_t* scene, int* cg_iterations, double* cg_residual);
 /* The Data `residual` of EulerImplicitSolver after the last step: r.r of the
  * residual above (scene created with compute_residual). Synchronises the

@@ -71,6 +71,7 @@ def _load():
     lib.orc_scene_set_options.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
     lib.orc_scene_set_trapezoidal.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_set_compute_residual.argtypes = [vp, ctypes.c_int]
+    lib.orc_scene_set_separate_gravity.argtypes = [vp, ctypes.c_int]
     lib.orc_scene_residual.restype = ctypes.c_double
     lib.orc_scene_residual.argtypes = [vp]
     lib.orc_scene_jacobi.argtypes = [vp, _dp]
@@ -308,6 +309,10 @@ class OracleScene:
     @property
     def last_error(self):
         return _load().orc_scene_last_error(self._h)
+
+    def set_separate_gravity(self, on=True):
+        """The mass's separateGravity."""
+        _load().orc_scene_set_separate_gravity(self._h, int(bool(on)))
 
     def set_compute_residual(self, on=True):
         """EulerImplicitSolver computeResidual."""

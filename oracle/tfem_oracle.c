@@ -1211,6 +1211,7 @@ typedef struct orc_scene {
     double cur_bf; /* bFactor of the matrix being applied (0 for the right-hand side) */
     int compute_residual; /* EulerImplicitSolver computeResidual */
     double residual;      /* its Data `residual` after the last step */
+    int separate_gravity; /* the mass's separateGravity */
 } orc_scene;
 
 orc_scene* orc_scene_create(orc_fem* fem, int n_nodes, int mass_kind, double vertex_mass,
@@ -1374,6 +1375,9 @@ static void vop_run(int kind, double* out, const double* a, double f, long n3, d
  * (DiagonalMass.inl:1393-1413): f += m g. */
 static void mass_add_force(const orc_scene* s, double* f)
 {
+    /* separateGravity: UniformMass::addForce returns at once
+     * (UniformMass.inl:471-475), DiagonalMass::addForce likewise */
+    if (s->separate_gravity) return;
     if (s->mass_kind == 0) {
         double mg[3] = {s->g[0] * s->vertex_mass, s->g[1] * s->vertex_mass, s->g[2] * s->vertex_mass};
         for (int i = 0; i < s->n; ++i)
@@ -1748,6 +1752,13 @@ static void euler_step(orc_scene* s)
         /* vMultiOp fast path (MechanicalObject.inl:2206-2240): v += dv; x += v h */
         vop_run(VOP_INTEGRATE, s->v, s->xs, h, n3, s->x);
     }
+    if (s->separate_gravity) {
+        /* addSeparateGravity (EulerImplicitSolver.cpp:296; UniformMass::
+         * addGravityToV, UniformMass.inl:450-468): v += g dt, every point */
+        double hg[3];
+        for (int k = 0; k < 3; ++k) hg[k] = s->g[k] * h;
+        for (long i = 0; i < n3; ++i) s->v[i] += hg[i % 3];
+    }
     if (s->vdamping != 0.0) {
         const double d = exp(-h * s->vdamping);
         for (long i = 0; i < n3; ++i) s->v[i] *= d;
@@ -1771,6 +1782,7 @@ static void euler_step(orc_scene* s)
 }
 
 void orc_scene_set_compute_residual(orc_scene* s, int on) { s->compute_residual = on ? 1 : 0; }
+void orc_scene_set_separate_gravity(orc_scene* s, int on) { s->separate_gravity = on ? 1 : 0; }
 double orc_scene_residual(const orc_scene* s) { return s->residual; }
 
 void orc_scene_step(orc_scene* s, int n_steps)

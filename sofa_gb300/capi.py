@@ -63,6 +63,7 @@ class SceneParams(ctypes.Structure):
         ("project_velocity", ctypes.c_int),
         ("trapezoidal_scheme", ctypes.c_int),
         ("compute_residual", ctypes.c_int),
+        ("separate_gravity", ctypes.c_int),
     ]
 
 
@@ -379,7 +380,8 @@ class Scene:
                  vertex_mass=None, total_mass=None, node_masses=None, fixed=(), fix_all=False, mass_first=True,
                  serial_dots=False, residual_replacement=0, linear_solver="cg", preconditioner=None,
                  preconditioner_rate=1, warm_start=False, ff_rayleigh_stiffness=0.0, mass_rayleigh_mass=0.0,
-                 first_order=False, project_velocity=False, trapezoidal_scheme=False, compute_residual=False):
+                 first_order=False, project_velocity=False, trapezoidal_scheme=False, compute_residual=False,
+                 separate_gravity=False):
         lib = load()
         p = SceneParams()
         lib.sgb_scene_params_default(ctypes.byref(p))
@@ -416,6 +418,7 @@ class Scene:
         p.project_velocity = int(project_velocity)
         p.trapezoidal_scheme = int(trapezoidal_scheme)
         p.compute_residual = int(compute_residual)
+        p.separate_gravity = int(separate_gravity)
         h = _vp()
         check(lib.sgb_scene_create(ctypes.byref(h), fem.handle, ctypes.byref(p)))
         fem._owned = False  # the scene owns the force field now

@@ -318,6 +318,7 @@ static int validate_mesh(const sgb_mesh_desc* m)
     if (p.first_order) return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes run the second-order Euler scheme");
     if (p.compute_residual)
         return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not compute EulerImplicitSolver's residual");
+    if (p.separate_gravity) return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes add gravity as a force");
     if (p.project_velocity)
         return bfail(SGB_ERR_NOT_SUPPORTED, "batched meshes do not support activate_projectVelocity");
     if (!std::isfinite(p.ff_rayleigh_stiffness) || !std::isfinite(p.mass_rayleigh_mass))

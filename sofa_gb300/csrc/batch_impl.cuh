@@ -521,12 +521,15 @@ __global__ void __launch_bounds__(kBatchThreads) kb_cg_scalars(BMeshDesc* M, int
                     m.status |= 1;
                     m.done = 1;
                 } else if (total != 0.0) {
-                    if (fabs(total) <= m.thr && !first_of_first)
+                    if (fabs(total) <= m.thr && !first_of_first) {
                         m.done = 1;
-                    else
+                        m.iters = it;  // the matvecs run, as the single-mesh count
+                    } else {
                         m.alpha = m.rho / total;
+                    }
                 } else {
                     m.done = 1;
+                    m.iters = it;
                 }
             } else {
                 m.rho_prev = m.rho;

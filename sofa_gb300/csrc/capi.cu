@@ -901,6 +901,7 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     s.prm.project_velocity = P.project_velocity ? 1 : 0;
     s.prm.trapezoidal = P.trapezoidal_scheme ? 1 : 0;
     s.prm.compute_residual = P.compute_residual ? 1 : 0;
+    s.prm.separate_gravity = P.separate_gravity ? 1 : 0;
     s.stream = fem->stream;
     sc->fem = fem;
     sc->ops = fem->ops;

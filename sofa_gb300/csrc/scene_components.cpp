@@ -772,9 +772,8 @@ int Scene::init_host(std::string* err)
         b.params.mass_rayleigh_mass = mass->get_real(*this, "rayleighMass");
         // separateGravity moves gravity out of the force into a velocity
         // increment after the position update (UniformMass::addGravityToV,
-        // EulerImplicitSolver.cpp:296), which the step does not run
-        if (mass->get_bool(*this, "separateGravity"))
-            return unsupported(err, where + mass->class_name() + " separateGravity=true is not supported");
+        // EulerImplicitSolver.cpp:296)
+        b.params.separate_gravity = mass->get_bool(*this, "separateGravity") ? 1 : 0;
         if (mass->class_name() == "UniformMass" && !mass->get_ints(*this, "indices").empty())
             return unsupported(err, where + "UniformMass indices (a mass on a subset of the points) is not "
                                             "supported");

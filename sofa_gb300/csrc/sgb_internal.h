@@ -175,6 +175,7 @@ struct SceneParams {
     int project_velocity = 0;  // FixedProjectiveConstraint activate_projectVelocity
     int trapezoidal = 0;       // EulerImplicitSolver trapezoidalScheme (tr = 0.5)
     int compute_residual = 0;  // EulerImplicitSolver computeResidual
+    int separate_gravity = 0;  // the mass's separateGravity
 };
 
 // Factors of one EulerImplicitSolver step (EulerImplicitSolver.cpp:117-171,

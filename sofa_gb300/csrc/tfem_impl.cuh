@@ -1100,15 +1100,19 @@ __device__ void finish_dot(double local, CgScalars* cg, const double* terms, int
             cg->done = (err <= sc.tol && !first_of_first) ? 1 : 0;
         }
     } else if (FIN == FIN_DEN) {
+        // a break here comes after iteration sc.it's matvec: the iteration
+        // count is that of the matvecs run (the update is skipped)
         cg->den = total;
         if (total != 0.0) {
             if (fabs(total) <= sc.threshold && !first_of_first) {
                 cg->done = 1;
+                cg->iters = sc.it;
             } else {
                 cg->alpha = cg->rho / total;
             }
         } else {
             cg->done = 1;
+            cg->iters = sc.it;
         }
     } else if (FIN == FIN_RHO) {
         cg->rho_prev = cg->rho;
@@ -1575,11 +1579,20 @@ __global__ void __launch_bounds__(kNodeBlock) k_residual_dot(const R* __restrict
     finish_dot<FIN_RESIDUAL>(local, cg, terms, N, sc);
 }
 
+// EulerImplicitSolver's addSeparateGravity (EulerImplicitSolver.cpp:296;
+// UniformMass::addGravityToV, UniformMass.inl:450-468): v += g dt after the
+// position update, before the velocity damping.
+struct SepGravity {
+    double hg[3];
+    int on;
+};
+
 template <typename R>
 __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict__ x, double* __restrict__ v,
                                                              const R* __restrict__ xs, double h, double vdamp,
                                                              CgScalars* cg, int N, int first_order = 0,
-                                                             const uint8_t* __restrict__ project_fixed = nullptr)
+                                                             const uint8_t* __restrict__ project_fixed = nullptr,
+                                                             SepGravity sg = SepGravity{{0.0, 0.0, 0.0}, 0})
 {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         const bool zero_v = project_fixed && project_fixed[n];
@@ -1589,6 +1602,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_update(double* __restrict_
             double vv = first_order ? (double)xs[i] : v[i] + (double)xs[i];
             double t = vv * h;
             x[i] = x[i] + t;
+            if (sg.on) vv = vv + sg.hg[k];
             if (vdamp != 1.0) vv *= vdamp;
             v[i] = zero_v ? 0.0 : vv;
         }
@@ -2234,7 +2248,8 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_refined(double* __restrict
                                                               const double* __restrict__ x64,
                                                               const R* __restrict__ xs, double h, double vdamp,
                                                               CgScalars* cg, int N,
-                                                              const uint8_t* __restrict__ project_fixed = nullptr)
+                                                              const uint8_t* __restrict__ project_fixed = nullptr,
+                                                              SepGravity sg = SepGravity{{0.0, 0.0, 0.0}, 0})
 {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         const bool zero_v = project_fixed && project_fixed[n];
@@ -2244,6 +2259,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_euler_refined(double* __restrict
             double vv = v[i] + (x64[i] + (double)xs[i]);
             double t = vv * h;
             x[i] = x[i] + t;
+            if (sg.on) vv = vv + sg.hg[k];
             if (vdamp != 1.0) vv *= vdamp;
             v[i] = zero_v ? 0.0 : vv;
         }
@@ -2660,6 +2676,29 @@ void api_add_dforce(TfemMesh* m, const R* dx, R* df, R kfactor, cudaStream_t s)
 // the previous step's solution and r.z. CG with warmStart
 // (CGLinearSolver.inl:95-99): the same start with r.r. Element-order
 // kernels: once per step.
+
+// The scene's mass operands. With separateGravity (UniformMass::addForce,
+// UniformMass.inl:471-475) the mass adds no weight to the force; gravity
+// enters the velocity after the position update instead (k_euler_update).
+inline MassArgs scene_mass_args(const Scene* sc)
+{
+    const SceneParams& P = sc->prm;
+    const double z = 0.0;
+    return MassArgs{sc->node_mass, P.vertex_mass,
+                    {P.separate_gravity ? z : P.gravity[0], P.separate_gravity ? z : P.gravity[1],
+                     P.separate_gravity ? z : P.gravity[2]}};
+}
+
+
+inline SepGravity scene_sep_gravity(const Scene* sc)
+{
+    const SceneParams& P = sc->prm;
+    SepGravity sg{{0.0, 0.0, 0.0}, P.separate_gravity ? 1 : 0};
+    if (sg.on)
+        for (int k = 0; k < 3; ++k) sg.hg[k] = P.gravity[k] * P.dt;
+    return sg;
+}
+
 template <typename R>
 void pcg_begin(Scene* sc, int mass_first, double mf, double kf, const SolveConsts& cons, double* dot_terms,
                cudaStream_t s)
@@ -2668,7 +2707,7 @@ void pcg_begin(Scene* sc, int mass_first, double mf, double kf, const SolveConst
     const int N = sc->n;
     const SceneParams& P = sc->prm;
     NodeCSR csr{m->rowptr, m->slots};
-    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const MassArgs ma = scene_mass_args(sc);
     const int ng = node_grid(N);
     R* dinv = (R*)sc->dinv;  // null: no preconditioner
     if (P.solver != 1) {
@@ -2708,7 +2747,7 @@ void launch_step_residual(Scene* sc, double* dot_terms, int mass_first, cudaStre
     const int N = sc->n;
     const SceneParams& P = sc->prm;
     NodeCSR csr{m->rowptr, m->slots};
-    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const MassArgs ma = scene_mass_args(sc);
     const int ng = node_grid(N);
     SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, 0, 0};
     launch_elem_force<R>(m, sc->x, s);
@@ -2730,7 +2769,7 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     const SceneParams& P = sc->prm;
     const double h = P.dt;
     NodeCSR csr{m->rowptr, m->slots};
-    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const MassArgs ma = scene_mass_args(sc);
     const int ng = node_grid(N);
     R* f = (R*)sc->f;
     R* b = (R*)sc->b;
@@ -2782,7 +2821,8 @@ void scene_step(Scene* sc, double* dot_terms, int mass_first, cudaStream_t s)
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N, P.first_order,
-                                                P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
+                                                P.project_velocity ? (const uint8_t*)sc->fixed : nullptr,
+                                                scene_sep_gravity(sc));
     if (P.compute_residual) launch_step_residual<R>(sc, dot_terms, mass_first, s);
 }
 
@@ -2799,7 +2839,7 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     const SceneParams& P = sc->prm;
     const double h = P.dt;
     NodeCSR csr{m->rowptr, m->slots};
-    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const MassArgs ma = scene_mass_args(sc);
     const int ng = node_grid(N);
     R* b = (R*)sc->b;
     R* r = (R*)sc->r;
@@ -2872,7 +2912,8 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_update<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, xs, h, vd, sc->cg, N, P.first_order,
-                                                P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
+                                                P.project_velocity ? (const uint8_t*)sc->fixed : nullptr,
+                                                scene_sep_gravity(sc));
     if (P.compute_residual) launch_step_residual<R>(sc, nullptr, mass_first, s);
 }
 
@@ -2887,7 +2928,7 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
     const int N = sc->n;
     const SceneParams& P = sc->prm;
     const double h = P.dt;
-    MassArgs ma{sc->node_mass, P.vertex_mass, {P.gravity[0], P.gravity[1], P.gravity[2]}};
+    const MassArgs ma = scene_mass_args(sc);
     const int ng = node_grid(N);
     R* r = (R*)sc->r;
     R* pb[2] = {(R*)sc->p, (R*)sc->p2};
@@ -2951,7 +2992,8 @@ void scene_step_refined(Scene* sc, int mass_first, cudaStream_t s)
     }
     const double vd = (P.vdamping != 0.0) ? exp(-h * P.vdamping) : 1.0;
     k_euler_refined<R><<<ng, kNodeBlock, 0, s>>>(sc->x, sc->v, sc->x64, xs, h, vd, sc->cg, N,
-                                                 P.project_velocity ? (const uint8_t*)sc->fixed : nullptr);
+                                                 P.project_velocity ? (const uint8_t*)sc->fixed : nullptr,
+                                                 scene_sep_gravity(sc));
     if (P.compute_residual) launch_step_residual<R>(sc, nullptr, mass_first, s);
 }
 

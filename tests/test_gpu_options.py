@@ -101,3 +101,29 @@ def test_batch_component_rayleigh_matches_scene(capi):
     sc.step(20)
     x, _ = sc.state()
     assert cases.rel_err(xb, x) <= 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fma", "mixed"])
+@pytest.mark.parametrize("method", ["large", "polar"])
+def test_separate_gravity_against_oracle(capi, oracle, precision, method):
+    """The mass's separateGravity: no weight in the force, v += g dt after the
+    position update (the fixed points too). 20 steps against the oracle."""
+    mesh = cases.beam_mesh()
+    _, osc = cases.oracle_scene(oracle, mesh, method)
+    osc.set_separate_gravity(True)
+    osc.step(20)
+    xr, vr = osc.state()
+    sc = cases.gpu_scene(capi, mesh, method, precision, serial_dots=(precision == "fp64"), separate_gravity=True)
+    sc.step(20)
+    it, _ = sc.sync()
+    x, v = sc.state()
+    sc.close()
+    if precision == "fp64":
+        assert np.array_equal(x, xr), cases.rel_err(x, xr)
+        assert np.array_equal(v, vr)
+        assert it == osc.last_iterations
+    elif precision == "fp64_fma":
+        assert cases.rel_err(x, xr) <= 1e-10
+    else:
+        assert cases.rel_err(x, xr) <= 1e-4
+    assert np.any(x[mesh.fixed] != mesh.positions[mesh.fixed])  # the reference's drift of the fixed points

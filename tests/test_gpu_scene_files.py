@@ -241,6 +241,26 @@ def test_grid_scene_file_with_update_stiffness_matrix(capi, oracle):
     assert np.max(np.abs(plain.state()[0] - xo)) > 1e-8 * np.max(np.abs(xo))
 
 
+def test_grid_scene_file_with_separate_gravity(capi, oracle):
+    """The grid scene with the mass's separateGravity="1": 30 steps within
+    1e-10 of the oracle configured the same way."""
+    text = _read("grid_fem_4x10x4.scn")
+    assert '<DiagonalMass name="mass"' in text
+    s = capi.SofaScene(text.replace('<DiagonalMass name="mass"', '<DiagonalMass separateGravity="1" name="mass"', 1))
+    s.animate(30)
+    x = s.positions(0)
+    pos, hexa = topo.regular_grid((4, 10, 4), (0, 0, 20), (10, 40, 30))
+    tets = topo.hexa_to_tetra6(hexa, (3, 9))
+    _, masses, fixed = s.body_arrays(0)
+    fem = oracle.OracleFEM(pos, tets, 600.0, 0.3, "large")
+    osc = oracle.OracleScene(fem, node_masses=masses, gravity=(0, 10, 0), fixed=fixed, dt=0.01, cg_iterations=20,
+                             cg_tolerance=1e-5, cg_threshold=1e-6)
+    osc.set_separate_gravity(True)
+    osc.step(30)
+    xo, _ = osc.state()
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+
+
 def test_reset_and_unload(capi, oracle):
     """SofaPhysicsAPI-style lifecycle. After reset the scene is back at its
     initial state and time 0, and 10 more steps match the oracle run through

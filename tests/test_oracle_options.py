@@ -119,3 +119,45 @@ def test_trapezoidal_spring_recurrence(oracle):
     xo, vo = sc.state()
     np.testing.assert_allclose(xo[0], x, rtol=1e-12)
     np.testing.assert_allclose(vo[0], v, rtol=1e-12)
+
+
+def test_separate_gravity_free_particle(oracle):
+    """separateGravity (UniformMass.inl:450-475, EulerImplicitSolver.cpp:296):
+    the mass adds no weight; after the position update v += g dt. A free
+    particle then lags the plain scheme by one step: x_{n+1} = x_n + h v_n,
+    v_{n+1} = v_n + g h, bit for bit."""
+    m, h = 0.5, 0.01
+    g = np.array([0.0, -9.81, 1.5])
+    sc = oracle.OracleScene(None, n_nodes=1, vertex_mass=m, gravity=tuple(g), dt=h, cg_iterations=10,
+                            cg_tolerance=1e-30, cg_threshold=1e-30)
+    sc.set_separate_gravity(True)
+    x = np.array([0.3, 1.0, -2.0])
+    v = np.array([0.2, 0.0, 0.1])
+    sc.set_state(x[None, :], v[None, :])
+    sc.step(6)
+    hg = [float(g[k]) * h for k in range(3)]
+    xs, vs = [float(c) for c in x], [float(c) for c in v]
+    for _ in range(6):
+        for k in range(3):
+            vv = vs[k] + 0.0  # the solve gives dv = 0: no force
+            xs[k] = xs[k] + vv * h
+            vs[k] = vv + hg[k]
+    xo, vo = sc.state()
+    assert np.array_equal(xo[0], np.array(xs)) and np.array_equal(vo[0], np.array(vs))
+
+
+def test_separate_gravity_fixed_points_drift(oracle):
+    """With separateGravity every point's velocity takes g dt, the fixed
+    points' too (addGravityToV has no projection), so without
+    activate_projectVelocity they move from the second step on, as in the
+    reference; with it they stay."""
+    mesh = cases.beam_mesh()
+    res = {}
+    for pv in (False, True):
+        sc = scene(oracle, mesh, rs=0.1, rm=0.1, project_velocity=pv)
+        sc.set_separate_gravity(True)
+        sc.step(3)
+        res[pv] = sc.state()[0]
+    fx = mesh.fixed
+    assert np.any(res[False][fx] != mesh.positions[fx])
+    assert np.array_equal(res[True][fx], mesh.positions[fx])

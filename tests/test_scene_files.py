@@ -159,7 +159,6 @@ def test_scene_errors(capi, case):
       ' />\n        <FixedProjectiveConstraint name="fix2" indices="0"'), "activate_projectVelocity"),
     (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="3" name="FEM"'),
      "computeVonMisesStress"),
-    (('<DiagonalMass name="mass"', '<DiagonalMass separateGravity="1" name="mass"'), "separateGravity"),
     (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField initialPoints="0 0 0" name="FEM"'),
      "initialPoints"),
 ])
