@@ -702,15 +702,10 @@ int Scene::init_host(std::string* err)
         // (TetrahedronFEMForceField.inl:1063, 1174); small ignores it; the
         // large rebuild (:908-921) writes only some of the entries it builds
         // equal, which the library stores once
-        // initialPoints replaces the force field's rest positions
-        // (TetrahedronFEMForceField::init); only the default (empty, or equal
-        // to the MechanicalObject's rest positions) is supported
-        {
-            const std::vector<double> ip = fem->get_reals(*this, "initialPoints");
-            if (!ip.empty() && ip != b.rest)
-                return unsupported(err, where + "TetrahedronFEMForceField initialPoints other than the rest "
-                                                "positions is not supported");
-        }
+        // initialPoints is accepted and, as in the reference, replaced by the
+        // MechanicalObject's rest positions when the force field initialises
+        // (TetrahedronFEMForceField::reinit, TetrahedronFEMForceField.inl:
+        // 1411-1412)
         b.update_stiffness = fem->get_bool(*this, "updateStiffnessMatrix") && b.method != SGB_METHOD_SMALL;
         if (b.update_stiffness && b.method == SGB_METHOD_LARGE)
             return unsupported(err, where + "updateStiffnessMatrix=true with method large (the reference rebuilds "

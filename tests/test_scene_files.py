@@ -159,14 +159,25 @@ def test_scene_errors(capi, case):
       ' />\n        <FixedProjectiveConstraint name="fix2" indices="0"'), "activate_projectVelocity"),
     (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField computeVonMisesStress="3" name="FEM"'),
      "computeVonMisesStress"),
-    (('<TetrahedronFEMForceField name="FEM"', '<TetrahedronFEMForceField initialPoints="0 0 0" name="FEM"'),
-     "initialPoints"),
 ])
 def test_unsupported_component_settings(capi, edit, msg):
     xml = _read("grid_fem_4x10x4.scn").replace(*edit)
     with pytest.raises(capi.SgbError) as e:
         capi.SofaScene(xml)
     assert e.value.code == -4 and msg in str(e.value)
+
+
+def test_initial_points_are_replaced_by_the_rest_positions(capi):
+    """TetrahedronFEMForceField initialPoints is accepted and, as in the
+    reference, replaced by the MechanicalObject's rest positions at init
+    (TetrahedronFEMForceField.inl:1411-1412): the body's rest configuration is
+    the one without it."""
+    text = _read("grid_fem_4x10x4.scn")
+    plain = capi.SofaScene(text)
+    with_ip = capi.SofaScene(text.replace('<TetrahedronFEMForceField name="FEM"',
+                                          '<TetrahedronFEMForceField initialPoints="0 0 0 1 1 1" name="FEM"', 1))
+    assert np.array_equal(plain.positions(0), with_ip.positions(0))
+    assert np.array_equal(plain.body_arrays(0)[1], with_ip.body_arrays(0)[1])
 
 
 PCG_SCENE = ('<CGLinearSolver iterations="20" tolerance="1e-5" threshold="1e-6" />',
