@@ -2037,6 +2037,11 @@ __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, 
     const int bb[5] = {br.x, br.y, br.z, br.w, bnd_rowptr[n0 + 4]};
     const uchar4 fx = *reinterpret_cast<const uchar4*>(fixed + n0);
     const uint8_t ff[4] = {fx.x, fx.y, fx.z, fx.w};
+    // x needs no partial sum: advanced and stored first, which frees its
+    // registers before the partial loop
+#pragma unroll
+    for (int k = 0; k < 12; ++k) xx[k] = xx[k] + pp[k] * alpha;
+    st12(xs, n0, xx);
     // the group's partial slots are one contiguous range (node-major CSR):
     // one unrolled loop over it, each slot added to its node in slot order,
     // so the loads of several slots are in flight together
@@ -2066,11 +2071,7 @@ __device__ __forceinline__ double cg_update4(size_t n0, float* __restrict__ xs, 
     }
     const float nalpha = -alpha;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) {
-        xx[k] = xx[k] + pp[k] * alpha;
-        rr[k] = rr[k] + qq[k] * nalpha;
-    }
-    st12(xs, n0, xx);
+    for (int k = 0; k < 12; ++k) rr[k] = rr[k] + qq[k] * nalpha;
     st12(r, n0, rr);
     float zz[12];
     if constexpr (PC != 0) {
