@@ -721,9 +721,9 @@ def main():
         except (OSError, ValueError, KeyError, ZeroDivisionError):
             traffic = None
 
-    # per step: the force and right-hand side element pass and node pass
-    # (four kernels with SGB_FUSED_RHS=0), CG iterations x (matvec + update),
-    # Euler update
+    # per step: the force and right-hand side patch pass (element pass with
+    # SGB_PATCH_RHS=0) and node pass (four kernels with SGB_FUSED_RHS=0), CG
+    # iterations x (matvec + update), Euler update
     fused_rhs = os.environ.get("SGB_FUSED_RHS", "1") != "0"
     launches_per_step = (3 if fused_rhs else 5) + 2 * cfg["cg_iterations"]
     line = {

@@ -137,7 +137,7 @@ static size_t mesh_plan(sgb_batch* B, int N, int E, const HostLayout& L, bool no
     if (rs == sizeof(float)) c.add((float2**)&d.rest_ff, sizeof(float2) * 9 * E);
     c.add(&d.eforce, rs * 12 * E);
     d.eforce_v = nullptr;
-    if (B->fused_rhs) c.add(&d.eforce_v, rs * 12 * E);
+    if (B->fused_rhs == 1) c.add(&d.eforce_v, rs * 12 * E);
     c.add((int**)&d.rowptr, sizeof(int) * (N + 1));
     c.add((int**)&d.slots, sizeof(int) * 4 * (size_t)E);
     c.add((int**)&d.elem_start, sizeof(int) * (P + 1));
@@ -237,7 +237,7 @@ int sgb_batch_create(sgb_batch_t** out, int precision, size_t hbm_budget_bytes, 
             if (v >= 64 && v <= 512 && v % 2 == 0) B->pe = v;
         }
     if (const char* e = getenv("SGB_BATCH_PREFETCH")) B->tiles.prefetch = (e[0] == '1');
-    B->fused_rhs = fused_rhs_default();
+    B->fused_rhs = batch_rhs_form(fused_rhs_default(), B->rs);
     B->max_slots = max_meshes;
     B->max_iterations = max_cg_iterations;
     B->slots.resize((size_t)max_meshes);
@@ -353,16 +353,24 @@ int sgb_batch_add_mesh(sgb_batch_t* B, const sgb_mesh_desc* m, int* slot_out)
 
 namespace sgb {
 
-// Host-only part of admission: validation, material checks like the
-// reference (BaseLinearElasticityFEMForceField.inl:53-85), element order,
-// patch layout, gather tables and the byte count. Safe on any thread.
-// SGB_FUSED_RHS=0: the batch runs the force and right-hand side as four
-// passes (the same operations) and its meshes carry no eforce_v.
+// SGB_FUSED_RHS=0: the force and right-hand side run as four passes (the
+// same operations); SGB_PATCH_RHS=0: as one pass over the elements (the
+// meshes carry eforce_v) and one over the nodes; else by patches.
 int fused_rhs_default()
 {
     const char* e = getenv("SGB_FUSED_RHS");
-    return !(e && e[0] == '0');
+    if (e && e[0] == '0') return 0;
+    const char* p = getenv("SGB_PATCH_RHS");
+    return (p && p[0] == '0') ? 1 : 2;
 }
+
+// The batch's form of those passes: by patches in mixed precision only (the
+// FP64 batch keeps the element-order pair).
+int batch_rhs_form(int fused_rhs, size_t rs) { return (fused_rhs == 2 && rs != sizeof(float)) ? 1 : fused_rhs; }
+
+// Host-only part of admission: validation, material checks like the
+// reference (BaseLinearElasticityFEMForceField.inl:53-85), element order,
+// patch layout, gather tables and the byte count. Safe on any thread.
 
 int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm, int fused_rhs)
 {
@@ -405,7 +413,7 @@ int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& pm, in
     int* eo;
     sgb_batch tmp;
     tmp.rs = rs;
-    tmp.fused_rhs = fused_rhs;
+    tmp.fused_rhs = batch_rhs_form(fused_rhs, rs);
     pm.bytes = align_up(mesh_plan(&tmp, N, E, pm.L, !pm.node_mass.empty(), !pm.ext.empty(), c, d, &y, &p, &eo,
                                   pm.Eh.size(), pm.nuh.size()));
     return SGB_OK;
@@ -626,6 +634,7 @@ int sgb_batch_step(sgb_batch_t* B, int n_steps)
         L.max_iterations = B->max_iterations;
         L.prefetch = T.prefetch;
         L.fused_rhs = B->fused_rhs;
+        L.grid_force = B->grid_patch_v[3];
         L.err = B->d_err;
         cudaGraph_t g;
         BTRY(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));

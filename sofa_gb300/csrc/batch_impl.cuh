@@ -369,6 +369,173 @@ __global__ void __launch_bounds__(kBatchThreads) kb_force_rhs_gather(BMeshDesc* 
     }
 }
 
+// ---- forces and right-hand side by patches (mixed precision) ---------------
+// The operations of kb_force_rhs_elem + kb_force_rhs_gather with each
+// element's force terms less its (h + rs) K v terms summed per local node in
+// shared memory, as k_patch_force_rhs does for one mesh: interior nodes into
+// the mesh's q, shared nodes into their partial slots; kb_rhs_finish_patch
+// then forms b per node chunk. Every sum belongs to one patch or one node
+// chunk, so the results do not depend on the other meshes of the batch.
+template <typename R>
+struct BRhsArgs {
+    const double* x;
+    const double* rest_pos;
+    const double* v;
+    R kf;
+    int method;
+    R* own;
+    R* partials;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(kPatchThreads) kb_force_rhs_patch(BMeshDesc* M, const WorkItem* __restrict__ items,
+                                                                    const int* __restrict__ counts, int pe)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* ef;
+    R* lp;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve<R>(smem_raw, pe, batch_max_lnodes(pe), &ef, &sl, &lr, &lp);
+    // the open mesh's views and operands, read where they are used
+    __shared__ PatchView spv;
+    __shared__ ElemView<R> sev;
+    __shared__ BRhsArgs<R> sa;
+    const int L = counts[WL_PATCH];
+    int open_slot = -1;
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem wi = items[w];
+        if (open_slot != wi.slot) {
+            open_slot = wi.slot;
+            // the previous patch ended with a block barrier
+            if (threadIdx.x == 0) {
+                const BMeshDesc& m = M[wi.slot];
+                spv = bm_patch_view(m, pe);
+                sev = bm_elem_view<R>(m);
+                sa = BRhsArgs<R>{m.x, m.rest_pos, m.v, (R)m.kf_rhs, m.method, (R*)m.q, (R*)m.partials};
+            }
+            __syncthreads();
+        }
+        const int e0 = spv.elem_start[wi.a], ne = spv.elem_start[wi.a + 1] - e0;
+        const int n0 = spv.node_start[wi.a], nn = spv.node_start[wi.a + 1] - n0;
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(spv.lslots + 4 * (size_t)e0);
+            uint4* dst = reinterpret_cast<uint4*>(sl);
+            const int n16 = (8 * ne + 15) >> 4;
+            for (int k = threadIdx.x; k < n16; k += blockDim.x) cp_async16(dst + k, src + k);
+            for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(lr + l, spv.lrow + n0 + l);
+        }
+        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+            const int e = e0 + le;
+            R Rm[9], K[3], J[12], c[12], cv[12];
+            if (sa.method == METHOD_LARGE)
+                elem_force_body<R, METHOD_LARGE, true>(sev, e, sa.x, sa.rest_pos, nullptr, PlasticArgs<R>{}, Rm, K, J,
+                                                       c);
+            else
+                elem_force_body<R, METHOD_POLAR, true>(sev, e, sa.x, sa.rest_pos, nullptr, PlasticArgs<R>{}, Rm, K, J,
+                                                       c);
+            rhs_v_terms_c(sev, e, sa.v, Rm, K, J, sa.kf, cv);
+#pragma unroll
+            for (int i = 0; i < 12; ++i) ef[i * pe + le] = c[i] - cv[i];
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int g = spv.lnode_gid[n0 + l];
+            const int info = spv.lnode_info[n0 + l];
+            const int s0 = lr[l] - 4 * e0, s1 = lr[l + 1] - 4 * e0;
+            R a0 = R(0), a1 = R(0), a2 = R(0);
+            for (int s = s0; s < s1; ++s) {
+                const int slot = sl[s];
+                const int le = slot >> 2, cc = slot & 3;
+                a0 += ef[(3 * cc + 0) * pe + le];
+                a1 += ef[(3 * cc + 1) * pe + le];
+                a2 += ef[(3 * cc + 2) * pe + le];
+            }
+            R* o = info >= 0 ? sa.partials + 3 * (size_t)(info >> 1) : sa.own + 3 * (size_t)g;
+            o[0] = a0;
+            o[1] = a1;
+            o[2] = a2;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) kb_rhs_finish_patch(BMeshDesc* M,
+                                                                     const WorkItem* __restrict__ items,
+                                                                     const int* __restrict__ counts)
+{
+    const int L = counts[WL_NODE];
+    for (int w = blockIdx.x; w < L; w += gridDim.x) {
+        const WorkItem it = items[w];
+        BMeshDesc& m = M[it.slot];
+        const R* own = (const R*)m.q;
+        const R* part = (const R*)m.partials;
+        const R* ext = (const R*)m.ext;
+        R* b = (R*)m.b;
+        R* r = (R*)m.r;
+        R* xs = (R*)m.xs;
+        const R mg0 = (R)(m.g[0] * m.vertex_mass), mg1 = (R)(m.g[1] * m.vertex_mass),
+                mg2 = (R)(m.g[2] * m.vertex_mass);
+        const double rmf = m.rm_factor;  // -rm
+        const R mmu = (R)(rmf != 1.0 ? m.vertex_mass * rmf : m.vertex_mass);
+        const R hr = (R)m.h;
+        double dlocal = 0.0;
+        for (int n = it.a + threadIdx.x; n < it.b; n += blockDim.x) {
+            const int b0 = m.bnd_rowptr[n], b1 = m.bnd_rowptr[n + 1];
+            R s0 = R(0), s1 = R(0), s2 = R(0);
+            if (b0 == b1) {
+                s0 = own[3 * (size_t)n];
+                s1 = own[3 * (size_t)n + 1];
+                s2 = own[3 * (size_t)n + 2];
+            } else {
+                for (int k = b0; k < b1; ++k) {
+                    s0 += part[3 * (size_t)k];
+                    s1 += part[3 * (size_t)k + 1];
+                    s2 += part[3 * (size_t)k + 2];
+                }
+            }
+            R a[3] = {R(0), R(0), R(0)};
+            if (ext) {
+                a[0] += ext[3 * (size_t)n];
+                a[1] += ext[3 * (size_t)n + 1];
+                a[2] += ext[3 * (size_t)n + 2];
+            }
+            if (m.node_mass) {
+                const double mm = m.node_mass[n];
+                a[0] += (R)(m.g[0] * mm);
+                a[1] += (R)(m.g[1] * mm);
+                a[2] += (R)(m.g[2] * mm);
+            } else {
+                a[0] += mg0;
+                a[1] += mg1;
+                a[2] += mg2;
+            }
+            a[0] += s0;
+            a[1] += s1;
+            a[2] += s2;
+            if (rmf != 0.0) {
+                const R mm = m.node_mass ? (R)(m.node_mass[n] * rmf) : mmu;
+                const R vv[3] = {(R)m.v[3 * (size_t)n], (R)m.v[3 * (size_t)n + 1], (R)m.v[3 * (size_t)n + 2]};
+#pragma unroll
+                for (int k = 0; k < 3; ++k) a[k] += vv[k] * mm;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] *= hr;
+            if (m.fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                b[3 * (size_t)n + k] = a[k];
+                r[3 * (size_t)n + k] = a[k];
+                xs[3 * (size_t)n + k] = R(0);
+            }
+            dlocal += (double)(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        }
+        rhs_done(m, it.c, dlocal);  // the chunk's partial at its own index
+    }
+}
+
 // ---- CG matvec over patches ------------------------------------------------
 // MINB: resident CTAs per SM the register cap is set for (a tile of the
 // tuner; the arithmetic is the same for every value)
@@ -611,6 +778,17 @@ int batch_prepare(int pe, int* grid_patch)
     grid_patch[1] = matvec_grid<R, kBatchMatvecMinb[1]>(smem, sms);
     grid_patch[2] = matvec_grid<R, kBatchMatvecMinb[2]>(smem, sms);
     if (grid_patch[0] < 0 || grid_patch[1] < 0 || grid_patch[2] < 0) return -1;
+    // grid_patch[3]: resident CTAs of the patch force / right-hand side pass
+    // (mixed precision)
+    grid_patch[3] = 0;
+    if constexpr (is_mixed<R>::value) {
+        if (cudaFuncSetAttribute(kb_force_rhs_patch<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return -1;
+        int nf = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, kb_force_rhs_patch<R>, kPatchThreads, smem);
+        grid_patch[3] = (nf < 1 ? 1 : nf) * sms;
+    }
     return sms;
 }
 
@@ -646,7 +824,13 @@ void batch_record_step(const BatchLaunch& B, cudaStream_t s)
 {
     const WorkItem* eit = B.items[WL_ELEM];
     const WorkItem* nit = B.items[WL_NODE];
-    if (B.fused_rhs) {
+    if (B.fused_rhs == 2) {
+        if constexpr (is_mixed<R>::value) {
+            kb_force_rhs_patch<R><<<B.grid_force, kPatchThreads, batch_patch_smem<R>(B.pe), s>>>(
+                B.meshes, B.items[WL_PATCH], B.counts, B.pe);
+            kb_rhs_finish_patch<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
+        }
+    } else if (B.fused_rhs) {
         kb_force_rhs_elem<R><<<B.grid_elem, kBatchThreads, 0, s>>>(B.meshes, eit, B.counts);
         kb_force_rhs_gather<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
     } else {

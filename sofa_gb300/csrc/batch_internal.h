@@ -56,7 +56,7 @@ struct sgb_batch {
     int precision = 0;
     size_t rs = 4;
     int pe = 512;  // elements per patch (shared-memory stride of the batch matvec)
-    int fused_rhs = 1;  // forces and right-hand side in two passes (each mesh carries eforce_v)
+    int fused_rhs = 2;  // forces and right-hand side: 2 by patches, 1 by elements (eforce_v), 0 four passes
     int max_slots = 0;
     int max_iterations = 0;
     sgb::Arena arena;
@@ -72,7 +72,8 @@ struct sgb_batch {
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     int sms = 152;
-    int grid_patch_v[3] = {152, 152, 152};  // resident matvec CTAs per register-cap variant (kBatchMatvecMinb)
+    int grid_patch_v[4] = {152, 152, 152, 0};  // resident matvec CTAs per register-cap variant (kBatchMatvecMinb),
+                                               // then those of the patch force / right-hand side pass
     sgb::BatchTiles tiles;                  // launch tiles (set by sgb_batch_tune / sgb_batch_set_tiles)
     double tune_default_ms = 0.0, tune_best_ms = 0.0;  // last tuning: step time of the default and chosen tiles
     int tune_trials = 0;                    // configurations timed by the last tuning (0: from the cache)
@@ -82,5 +83,6 @@ struct sgb_batch {
 
 namespace sgb {
 int prepare_mesh(const sgb_mesh_desc* m, int pe, size_t rs, PreparedMesh& out, int fused_rhs);
+int batch_rhs_form(int fused_rhs, size_t rs);
 int admit_prepared(sgb_batch* B, PreparedMesh& pm, int* slot);
 }  // namespace sgb

@@ -926,13 +926,20 @@ int sgb_scene_create(sgb_scene_t** out, sgb_tfem_t* fem, const sgb_scene_params*
     if (P.node_masses_host && (rc = dev_alloc(&s.node_mass, (size_t)N, acc))) goto fail_out;
     if (P.serial_dots && (rc = dev_alloc(&sc->dot_terms, (size_t)N, acc))) goto fail_out;
     if (P.preconditioner == SGB_PRECOND_JACOBI && (rc = dev_alloc_bytes(&s.dinv, rs * 3 * N, acc))) goto fail_out;
-    // the patch step's second corner-term buffer (FP32 large / polar / svd),
-    // for its fused force and right-hand side passes; SGB_FUSED_RHS=0 leaves
-    // it out and the step runs the four separate kernels (the same operations)
+    // the patch step's force and right-hand side passes (FP32 large / polar /
+    // svd): by patches where the force field set that kernel up, else over
+    // the elements with a second corner-term buffer; SGB_FUSED_RHS=0 runs
+    // the four separate kernels (the same operations)
     if (fem->m.precision == SGB_PRECISION_MIXED && fem->m.pl.n_patches > 0 && fem->m.method != SGB_METHOD_SMALL &&
-        fused_rhs_default() &&
-        (rc = dev_alloc_bytes(&s.eforce_v, rs * 12 * std::max<size_t>((size_t)fem->m.n_tets, 1), acc)))
-        goto fail_out;
+        fused_rhs_default()) {
+        if (fem->m.force_patch_grid > 0) {
+            s.rhs_form = 2;
+        } else {
+            if ((rc = dev_alloc_bytes(&s.eforce_v, rs * 12 * std::max<size_t>((size_t)fem->m.n_tets, 1), acc)))
+                goto fail_out;
+            s.rhs_form = 1;
+        }
+    }
     if (P.residual_replacement > 0) {
         // the FP64 copy of the operator, created from the force field's
         // inputs (rest positions and tetrahedra read back, caller order)

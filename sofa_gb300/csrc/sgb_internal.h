@@ -117,6 +117,7 @@ struct TfemMesh {
     int patch_threads = 128;  // threads per CTA of the patch kernels
     int matvec_minb = 1;      // CG matvec register cap: resident CTAs per SM it is set for (1: none)
     int adddforce_grid = 0;   // CTAs of the addDForce patch kernel (128 threads)
+    int force_patch_grid = 0; // CTAs of the patch force / right-hand side kernel (0: not used)
     int patch_prefetch = 0;   // 1: each CTA prefetches its next patch into L2
     int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads
     int update_minb = 4;      // CG update: resident CTAs per SM the register cap is set for
@@ -232,6 +233,10 @@ struct Scene {
     void* r = nullptr;
     void* dinv = nullptr;          // PCG + Jacobi: inverse diagonal of the system (3 per node)
     void* eforce_v = nullptr;      // patch step: the right-hand side's K v corner terms (12 per element)
+    // the patch step's force and right-hand side passes: 2 one pass over the
+    // patches and one over the nodes, 1 one over the elements (eforce_v) and
+    // one over the nodes, 0 the four kernels of the element-order step
+    int rhs_form = 0;
     CgScalars* cg = nullptr;
     CgScalars* cg_h = nullptr;  // pinned mirror for reads
     cudaStream_t stream = nullptr;
@@ -355,13 +360,17 @@ struct BatchLaunch {
     int pe;
     int max_iterations;
     int prefetch;  // FP32 matvec: prefetch the block's next patch into L2
-    int fused_rhs;  // forces and right-hand side in two launches (the meshes carry eforce_v)
+    // forces and right-hand side: 2 by patches and by node chunks (mixed),
+    // 1 by elements (the meshes carry eforce_v) and by node chunks, 0 the
+    // four passes of the element-order step
+    int fused_rhs;
+    int grid_force;  // CTAs of the patch force / right-hand side pass
     int* err;    // sticky device error flag of the batch
 };
 
 // Forces and right-hand side of the FP32 patch step and of the batch in two
-// passes (1), or in the four passes of the element-order step (0:
-// SGB_FUSED_RHS=0); batch.cu.
+// passes, by patches (2) or by elements (1: SGB_PATCH_RHS=0), or in the four
+// passes of the element-order step (0: SGB_FUSED_RHS=0); batch.cu.
 int fused_rhs_default();
 
 // von Mises stress (von_mises.cu): per-element lambda and mu, then the

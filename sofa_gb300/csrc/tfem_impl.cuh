@@ -533,12 +533,13 @@ __device__ __forceinline__ void update_j_mixed(const float ew[3][3], float sk, c
 }
 
 // KEEP: also hands the rotation (before packing), K and J to the caller
+// and, with eforce null, the corner terms in keep_c instead of storing them
 // (rotated methods only).
 template <typename R, int METHOD, bool KEEP = false>
 __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, const double* __restrict__ x,
                                                 const double* __restrict__ rest_pos, R* __restrict__ eforce,
                                                 const PlasticArgs<R>& pl = PlasticArgs<R>{}, R* keep_rot = nullptr,
-                                                R* keep_K = nullptr, R* keep_J = nullptr)
+                                                R* keep_K = nullptr, R* keep_J = nullptr, R* keep_c = nullptr)
 {
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
@@ -717,8 +718,12 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
             acc += Rm[6 + k] * F[3 * i + 2];
             c[3 * i + k] = acc;
         }
-    store_eforce(eforce, e, c);
+    if (eforce) store_eforce(eforce, e, c);
     if constexpr (KEEP) {
+        if (!eforce) {
+#pragma unroll
+            for (int i = 0; i < 12; ++i) keep_c[i] = c[i];
+        }
 #pragma unroll
         for (int i = 0; i < 9; ++i) keep_rot[i] = Rm[i];
 #pragma unroll
@@ -874,9 +879,8 @@ __global__ void __launch_bounds__(kElemBlock) k_elem_dforce(ElemView<R> ev, cons
 // its K, J: the rotation as the packed copy gives it back, then the
 // operations of elem_dforce_body on the FP64 velocities.
 template <typename R>
-__device__ __forceinline__ void rhs_v_terms(const ElemView<R>& ev, int e, const double* __restrict__ v,
-                                            const R Rm[9], const R K[3], const R J[12], R kf_rhs,
-                                            R* __restrict__ eforce_v)
+__device__ __forceinline__ void rhs_v_terms_c(const ElemView<R>& ev, int e, const double* __restrict__ v,
+                                              const R Rm[9], const R K[3], const R J[12], R kf_rhs, R c[12])
 {
     R Rq[9];
     if constexpr (is_mixed<R>::value) {
@@ -887,9 +891,18 @@ __device__ __forceinline__ void rhs_v_terms(const ElemView<R>& ev, int e, const 
     }
     const int4 t = ev.tets[e];
     const int node[4] = {t.x, t.y, t.z, t.w};
-    R xin[4][3], c[12];
+    R xin[4][3];
     dforce_inputs<R, double, METHOD_LARGE, 0>(node, v, nullptr, R(0), nullptr, xin);
     dforce_terms<R, METHOD_LARGE>(xin, Rq, K, J, kf_rhs, c);
+}
+
+template <typename R>
+__device__ __forceinline__ void rhs_v_terms(const ElemView<R>& ev, int e, const double* __restrict__ v,
+                                            const R Rm[9], const R K[3], const R J[12], R kf_rhs,
+                                            R* __restrict__ eforce_v)
+{
+    R c[12];
+    rhs_v_terms_c(ev, e, v, Rm, K, J, kf_rhs, c);
     store_eforce(eforce_v, e, c);
 }
 
@@ -1945,6 +1958,143 @@ __global__ void __launch_bounds__(kNodeBlock) k_patch_fixup(const int* __restric
     }
 }
 
+// computeForce and the right-hand side's stiffness term by patches (mixed
+// precision, rotated methods): each element's force corner terms, less its
+// (h + rs) K v terms (firstOrder: the force terms alone), go to shared
+// memory as in the matvec's phase 1; each local node sums its slots there,
+// interior nodes into own[], nodes shared by several patches into their
+// partial slot. k_rhs_finish_patch then forms b. The same operations as
+// k_elem_force_rhs and k_gather_force_rhs, summed per patch instead of in
+// element order, with no corner-term buffers in HBM.
+template <typename R, int METHOD>
+__global__ void __launch_bounds__(kPatchThreads) k_patch_force_rhs(PatchView pv, ElemView<R> ev,
+                                                                   const double* __restrict__ x,
+                                                                   const double* __restrict__ rest_pos,
+                                                                   PlasticArgs<R> pl, const double* __restrict__ v,
+                                                                   R kf_rhs, int first_order, R* __restrict__ own,
+                                                                   R* __restrict__ partials)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* ef;
+    R* lp;
+    uint16_t* sl;
+    int* lr;
+    patch_smem_carve<R>(smem_raw, pv.pe, pv.max_lnodes, &ef, &sl, &lr, &lp);
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
+        const int e0 = pv.elem_start[P], ne = pv.elem_start[P + 1] - e0;
+        const int n0 = pv.node_start[P], nn = pv.node_start[P + 1] - n0;
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(pv.lslots + 4 * (size_t)e0);
+            uint4* dst = reinterpret_cast<uint4*>(sl);
+            const int n16 = (8 * ne + 15) >> 4;
+            for (int k = threadIdx.x; k < n16; k += blockDim.x) cp_async16(dst + k, src + k);
+            for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(lr + l, pv.lrow + n0 + l);
+        }
+        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
+            const int e = e0 + le;
+            R Rm[9], K[3], J[12], c[12];
+            elem_force_body<R, METHOD, true>(ev, e, x, rest_pos, nullptr, pl, Rm, K, J, c);
+            if (!first_order) {
+                R cv[12];
+                rhs_v_terms_c(ev, e, v, Rm, K, J, kf_rhs, cv);
+#pragma unroll
+                for (int i = 0; i < 12; ++i) c[i] -= cv[i];
+            }
+#pragma unroll
+            for (int i = 0; i < 12; ++i) ef[i * pv.pe + le] = c[i];
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int g = pv.lnode_gid[n0 + l];
+            const int info = pv.lnode_info[n0 + l];
+            const int s0 = lr[l] - 4 * e0, s1 = lr[l + 1] - 4 * e0;
+            R a0 = R(0), a1 = R(0), a2 = R(0);
+            for (int s = s0; s < s1; ++s) {
+                const int slot = sl[s];
+                const int le = slot >> 2, cc = slot & 3;
+                a0 += ef[(3 * cc + 0) * pv.pe + le];
+                a1 += ef[(3 * cc + 1) * pv.pe + le];
+                a2 += ef[(3 * cc + 2) * pv.pe + le];
+            }
+            R* o = info >= 0 ? partials + 3 * (size_t)(info >> 1) : own + 3 * (size_t)g;
+            o[0] = a0;
+            o[1] = a1;
+            o[2] = a2;
+        }
+        __syncthreads();
+    }
+}
+
+// The right-hand side per node after k_patch_force_rhs: the element sum
+// (own[] or the node's partial sums in patch order), external and gravity
+// forces, the Rayleigh mass term on v, times h; projected; b = r, x = 0
+// (cold start) and |b|^2 as k_gather_force_rhs forms them.
+template <typename R>
+__global__ void __launch_bounds__(kNodeBlock) k_rhs_finish_patch(const R* __restrict__ own,
+                                                                 const R* __restrict__ partials,
+                                                                 const int* __restrict__ bnd_rowptr,
+                                                                 const R* __restrict__ ext,
+                                                                 const double* __restrict__ v, MassArgs ma,
+                                                                 double mfac, double h,
+                                                                 const uint8_t* __restrict__ fixed,
+                                                                 R* __restrict__ b, R* __restrict__ r,
+                                                                 R* __restrict__ xs, CgScalars* cg, int N,
+                                                                 SolveConsts sc, int first_order)
+{
+    const R mg0 = (R)(ma.g[0] * ma.vertex_mass), mg1 = (R)(ma.g[1] * ma.vertex_mass),
+            mg2 = (R)(ma.g[2] * ma.vertex_mass);
+    const R mm = (R)(mfac != 1.0 ? ma.vertex_mass * mfac : ma.vertex_mass);
+    const R hr = (R)h;
+    double local = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) cg->done = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const int b0 = bnd_rowptr[n], b1 = bnd_rowptr[n + 1];
+        R s0 = R(0), s1 = R(0), s2 = R(0);
+        if (b0 == b1) {
+            s0 = own[3 * (size_t)n];
+            s1 = own[3 * (size_t)n + 1];
+            s2 = own[3 * (size_t)n + 2];
+        } else {
+            for (int k = b0; k < b1; ++k) {
+                s0 += partials[3 * (size_t)k];
+                s1 += partials[3 * (size_t)k + 1];
+                s2 += partials[3 * (size_t)k + 2];
+            }
+        }
+        R a[3] = {mg0, mg1, mg2};
+        if (ma.node_mass) {
+            const double m = ma.node_mass[n];
+            a[0] = (R)(ma.g[0] * m);
+            a[1] = (R)(ma.g[1] * m);
+            a[2] = (R)(ma.g[2] * m);
+        }
+        if (ext) {
+            a[0] += ext[3 * (size_t)n];
+            a[1] += ext[3 * (size_t)n + 1];
+            a[2] += ext[3 * (size_t)n + 2];
+        }
+        a[0] += s0;
+        a[1] += s1;
+        a[2] += s2;
+        if (!first_order) {
+            R vv[3] = {(R)v[3 * (size_t)n], (R)v[3 * (size_t)n + 1], (R)v[3 * (size_t)n + 2]};
+            if (mfac != 0.0) add_mdx(a, vv, ma, mfac, mm, n);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a[k] *= hr;
+        }
+        if (fixed[n]) a[0] = a[1] = a[2] = R(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            b[3 * (size_t)n + k] = a[k];
+            r[3 * (size_t)n + k] = a[k];
+            if (!sc.pcg && !sc.warm) xs[3 * (size_t)n + k] = R(0);  // PCG / warmStart keep the previous solution
+        }
+        local += dot3(a, a);
+    }
+    finish_dot<FIN_RHS>(local, cg, nullptr, N, sc);
+}
+
 // A node's r.r, with the roundings spelled out (two fused multiply-adds), so
 // that every kernel forming it gets the same bits.
 __device__ __forceinline__ float node_rr(const float r[3]) { return __fmaf_rn(r[2], r[2], __fmaf_rn(r[1], r[1], r[0] * r[0])); }
@@ -2336,12 +2486,10 @@ void launch_plastic_scale(TfemMesh* m, const double* young, int ny, const double
                                                                    (R*)m->plastic_scale);
 }
 
+// The force kernels' plasticity and updateStiffnessMatrix operands.
 template <typename R>
-void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
+PlasticArgs<R> plastic_args(TfemMesh* m)
 {
-    if (m->n_tets == 0) return;
-    ElemView<R> ev = view<R>(m);
-    const int g = elem_grid(m->n_tets);
     PlasticArgs<R> pl;
     if (m->plastic && m->plastic_max > 0.0) {
         pl.strain = (R*)m->plastic;
@@ -2354,6 +2502,16 @@ void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
         pl.update_J = (R*)m->J;
         pl.scale = (const R*)m->plastic_scale;
     }
+    return pl;
+}
+
+template <typename R>
+void launch_elem_force(TfemMesh* m, const double* x, cudaStream_t s)
+{
+    if (m->n_tets == 0) return;
+    ElemView<R> ev = view<R>(m);
+    const int g = elem_grid(m->n_tets);
+    const PlasticArgs<R> pl = plastic_args<R>(m);
     if (m->method == METHOD_SMALL)
         k_elem_force<R, METHOD_SMALL><<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl);
     else if (m->method == METHOD_LARGE)
@@ -2371,18 +2529,7 @@ void launch_elem_force_rhs(TfemMesh* m, const double* x, const double* v, R kf_r
     if (m->n_tets == 0) return;
     ElemView<R> ev = view<R>(m);
     const int g = elem_grid(m->n_tets);
-    PlasticArgs<R> pl;
-    if (m->plastic && m->plastic_max > 0.0) {
-        pl.strain = (R*)m->plastic;
-        pl.scale = (const R*)m->plastic_scale;
-        pl.max_threshold = (R)m->plastic_max;
-        pl.yield_threshold = (R)m->plastic_yield;
-        pl.creep = (R)m->plastic_creep;
-    }
-    if (m->update_j) {
-        pl.update_J = (R*)m->J;
-        pl.scale = (const R*)m->plastic_scale;
-    }
+    const PlasticArgs<R> pl = plastic_args<R>(m);
     if (m->method == METHOD_LARGE)
         k_elem_force_rhs<R, METHOD_LARGE>
             <<<g, kElemBlock, 0, s>>>(ev, x, m->rest_pos, (R*)m->eforce, pl, v, kf_rhs, eforce_v);
@@ -2553,6 +2700,30 @@ void patch_matvec_attrs(K kernel, size_t smem)
     cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 }
 
+// k_patch_force_rhs for the rotated methods (mixed precision; the grid is
+// set by prepare_patch).
+template <typename R>
+void launch_patch_force_rhs(TfemMesh* m, const double* x, const double* v, R kf_rhs, int first_order, R* own,
+                            R* partials, cudaStream_t s)
+{
+    if constexpr (is_mixed<R>::value) {
+        const PlasticArgs<R> pl = plastic_args<R>(m);
+        const PatchView pv = patch_view(m);
+        const ElemView<R> ev = view<R>(m);
+        const size_t smem = patch_smem_bytes<R>(m);
+        const int g = m->force_patch_grid;
+        if (m->method == METHOD_LARGE)
+            k_patch_force_rhs<R, METHOD_LARGE><<<g, kPatchThreads, smem, s>>>(pv, ev, x, m->rest_pos, pl, v, kf_rhs,
+                                                                              first_order, own, partials);
+        else if (m->method == METHOD_SVD)
+            k_patch_force_rhs<R, METHOD_SVD><<<g, kPatchThreads, smem, s>>>(pv, ev, x, m->rest_pos, pl, v, kf_rhs,
+                                                                            first_order, own, partials);
+        else
+            k_patch_force_rhs<R, METHOD_POLAR><<<g, kPatchThreads, smem, s>>>(pv, ev, x, m->rest_pos, pl, v, kf_rhs,
+                                                                              first_order, own, partials);
+    }
+}
+
 // Sets the shared-memory attribute of the patch kernels and returns the grid
 // (CTAs resident at once, capped by the dot-product partial array).
 template <typename R>
@@ -2632,6 +2803,31 @@ int prepare_patch(TfemMesh* m)
     if (g > kMaxDotBlocks) g = kMaxDotBlocks;
     if (g > m->pl.n_patches) g = m->pl.n_patches;
     if (g < 1) g = 1;
+    // the patch force / right-hand side pass (mixed precision, rotated
+    // methods; SGB_PATCH_RHS=0 keeps the element-order pair of kernels)
+    m->force_patch_grid = 0;
+    if constexpr (is_mixed<R>::value) {
+        const char* e = getenv("SGB_PATCH_RHS");
+        if (m->method != METHOD_SMALL && !(e && e[0] == '0')) {
+            int nf = 0;
+            if (m->method == METHOD_LARGE) {
+                patch_matvec_attrs(k_patch_force_rhs<R, METHOD_LARGE>, smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, k_patch_force_rhs<R, METHOD_LARGE>, kPatchThreads,
+                                                              smem);
+            } else if (m->method == METHOD_SVD) {
+                patch_matvec_attrs(k_patch_force_rhs<R, METHOD_SVD>, smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, k_patch_force_rhs<R, METHOD_SVD>, kPatchThreads,
+                                                              smem);
+            } else {
+                patch_matvec_attrs(k_patch_force_rhs<R, METHOD_POLAR>, smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, k_patch_force_rhs<R, METHOD_POLAR>, kPatchThreads,
+                                                              smem);
+            }
+            long long gf = (long long)(nf < 1 ? 1 : nf) * sms;
+            if (gf > m->pl.n_patches) gf = m->pl.n_patches;
+            m->force_patch_grid = (int)(gf < 1 ? 1 : gf);
+        }
+    }
     {
         int na = 0;
         cudaFuncSetAttribute(k_patch_adddforce<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -2852,12 +3048,19 @@ void scene_step_patch(Scene* sc, int mass_first, cudaStream_t s)
     const R* dinv = pcg ? (const R*)sc->dinv : nullptr;
     SolveConsts cons{P.cg_tolerance, P.cg_threshold, 1, pcg ? 1 : 0, P.warm_start};
     const StepFactors F = step_factors(P);
-    // forces and the right-hand side: one pass over the elements (force
-    // terms and (h + rs) K v terms), one over the nodes; the operations of
-    // the four kernels of scene_step (sc->eforce_v null: those four
-    // kernels), equal to rounding (the FP32 build may contract multiply-adds
-    // differently in the fused kernel)
-    if (sc->eforce_v) {
+    // forces and the right-hand side (sc->rhs_form): one pass over the
+    // patches (element force and (h + rs) K v terms summed per patch in
+    // shared memory) and one over the nodes; or one pass over the elements
+    // (eforce_v) and one over the nodes in element order; or the four
+    // kernels of scene_step. The same operations, equal to rounding
+    // (summation order; the FP32 build may contract multiply-adds
+    // differently in the fused kernels).
+    if (sc->rhs_form == 2) {
+        launch_patch_force_rhs<R>(m, sc->x, sc->v, (R)F.kf_rhs, P.first_order, q, partials, s);
+        k_rhs_finish_patch<R><<<ng, kNodeBlock, 0, s>>>(q, partials, (const int*)m->pl.bnd_rowptr, (const R*)sc->ext,
+                                                        sc->v, ma, -P.rayleigh_mass, h, sc->fixed, b, r, xs, sc->cg,
+                                                        N, cons, P.first_order);
+    } else if (sc->rhs_form == 1) {
         if (P.first_order)
             launch_elem_force<R>(m, sc->x, s);
         else

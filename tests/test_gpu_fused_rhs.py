@@ -1,15 +1,20 @@
 """The mixed patch step forms the forces and the right-hand side in two
-passes (k_elem_force_rhs, k_gather_force_rhs) instead of the four kernels of
-the element-order step (k_elem_force, k_gather_force, k_elem_dforce on v,
-k_gather_rhs); SGB_FUSED_RHS=0 at scene creation selects the four kernels.
-The fused kernels perform the same operations on the same values, but in the
-FMA-contracting FP32 build the compiler fuses multiply-adds per kernel, and
-the fused element pass can come out with other contractions than the
-separate ones (it did for polar and svd once the updateStiffnessMatrix path
-joined the force kernel): the trajectories agree to the rounding of the
-element terms (displacement-relative difference within 1e-4 after 8 steps,
-the bar of the mixed path against FP64; measured up to 1.6e-5, with the
-velocity projection and vdamping), not necessarily bit for bit. Checked over 8 steps for the rotated
+passes instead of the four kernels of the element-order step (k_elem_force,
+k_gather_force, k_elem_dforce on v, k_gather_rhs): by default one pass over
+the patches that sums each element's force and (h + rs) K v terms per local
+node in shared memory (k_patch_force_rhs) and one over the nodes
+(k_rhs_finish_patch); with SGB_PATCH_RHS=0 one pass over the elements and
+one over the nodes in element order (k_elem_force_rhs, k_gather_force_rhs);
+SGB_FUSED_RHS=0 at creation selects the four kernels. All three perform the
+same operations on the same values, but the patch form sums in patch order,
+and in the FMA-contracting FP32 build the compiler fuses multiply-adds per
+kernel, so the fused element passes can come out with other contractions
+than the separate ones (they did for polar and svd once the
+updateStiffnessMatrix path joined the force kernel): the trajectories agree
+to the rounding of the element terms (displacement-relative difference
+within 1e-4 after 8 steps, the bar of the mixed path against FP64; measured
+up to 1.6e-5 for the element-order pair, with the velocity projection and
+vdamping), not necessarily bit for bit. Checked over 8 steps for the rotated
 methods and the options that enter the right-hand side: the components'
 Rayleigh coefficients, firstOrder, trapezoidalScheme, projectVelocity,
 vdamping, per-node masses, mass_first, an external force, plasticity.
@@ -47,14 +52,21 @@ CASES = {
 }
 
 
-def run(capi, mesh, method, case, fused, steps=8):
+# the three forms of the force and right-hand side passes: the
+# environment at creation
+FORMS = {"patch": {"SGB_FUSED_RHS": "1", "SGB_PATCH_RHS": "1"},
+         "element": {"SGB_FUSED_RHS": "1", "SGB_PATCH_RHS": "0"},
+         "four": {"SGB_FUSED_RHS": "0", "SGB_PATCH_RHS": "0"}}
+
+
+def run(capi, mesh, method, case, form, steps=8):
     opts = dict(CASES[case])
     ext = opts.pop("external", None)
     plastic = opts.pop("plastic", False)
     if opts.get("node_masses") == "ramp":
         opts["node_masses"] = np.linspace(0.5, 1.5, mesh.n_nodes) / mesh.n_nodes
-    old = os.environ.get("SGB_FUSED_RHS")
-    os.environ["SGB_FUSED_RHS"] = "1" if fused else "0"
+    old = {k: os.environ.get(k) for k in FORMS[form]}
+    os.environ.update(FORMS[form])
     try:
         fem = capi.TetrahedronFEM(mesh.positions, mesh.tetrahedra, 5000.0, 0.45, method, "mixed")
         if plastic:
@@ -63,10 +75,11 @@ def run(capi, mesh, method, case, fused, steps=8):
                         cg_tolerance=1e-9, cg_threshold=1e-9, gravity=(0.0, -9.81, 0.0),
                         vertex_mass=1.0 / mesh.n_nodes, fixed=mesh.fixed, **opts)
     finally:
-        if old is None:
-            del os.environ["SGB_FUSED_RHS"]
-        else:
-            os.environ["SGB_FUSED_RHS"] = old
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
     v0 = np.random.default_rng(8).normal(scale=0.05, size=mesh.positions.shape)
     sc.set_state(mesh.positions, v0)
     if ext is not None:
@@ -85,44 +98,50 @@ def run(capi, mesh, method, case, fused, steps=8):
 @pytest.mark.parametrize("method", ["large", "polar", "svd"])
 def test_fused_force_and_rhs(capi, method, case):
     mesh = cases.beam_mesh()
-    a = run(capi, mesh, method, case, fused=True)
-    b = run(capi, mesh, method, case, fused=False)
+    b = run(capi, mesh, method, case, "four")
     d = np.linalg.norm(b[0] - mesh.positions)
     assert d > 0  # the scene moved
-    assert np.linalg.norm(a[0] - b[0]) / d <= 1e-4, np.linalg.norm(a[0] - b[0]) / d
+    for form in ("patch", "element"):
+        a = run(capi, mesh, method, case, form)
+        assert np.linalg.norm(a[0] - b[0]) / d <= 1e-4, (form, np.linalg.norm(a[0] - b[0]) / d)
 
 
 @pytest.mark.parametrize("precision,tol", [("mixed", 1e-4), ("fp64_fma", 1e-12)])
 def test_batch_fused_force_and_rhs(capi, precision, tol):
-    """The batch engine's two passes (kb_force_rhs_elem, kb_force_rhs_gather)
-    against its four (SGB_FUSED_RHS=0 at batch creation), on beams of the
-    batched workload's population (both methods), 5 steps. The passes do the
-    same operations, but in these FMA-contracting builds the compiler fuses
-    multiply-adds per kernel, and the batch's fused element pass (both
-    methods and the right-hand side in one kernel) comes out with other
-    contractions than its two separate passes: the trajectories agree to the
-    rounding of the element terms (displacement-relative difference within
-    `tol`), not bit for bit."""
+    """The batch engine's two passes against its four (SGB_FUSED_RHS=0 at
+    batch creation), on beams of the batched workload's population (both
+    methods), 5 steps: by patches (kb_force_rhs_patch, kb_rhs_finish_patch;
+    mixed precision only, the FP64 batch keeps the element-order pair) and by
+    elements (kb_force_rhs_elem, kb_force_rhs_gather; SGB_PATCH_RHS=0). The
+    passes do the same operations, but the patch form sums in patch order,
+    and in these FMA-contracting builds the compiler fuses multiply-adds per
+    kernel, so the batch's fused element pass (both methods and the
+    right-hand side in one kernel) comes out with other contractions than
+    its two separate passes: the trajectories agree to the rounding of the
+    element terms (displacement-relative difference within `tol`), not bit
+    for bit."""
     from sofa_gb300 import workloads as wl
 
     beams = wl.beam_population(64, seed=5, members=range(0, 64, 8))
-    out = []
-    for fused in (True, False):
-        old = os.environ.get("SGB_FUSED_RHS")
-        os.environ["SGB_FUSED_RHS"] = "1" if fused else "0"
+    out = {}
+    for form in ("four", "element", "patch"):
+        old = {k: os.environ.get(k) for k in FORMS[form]}
+        os.environ.update(FORMS[form])
         try:
             b = capi.Batch(precision, budget_bytes=4 << 30, max_meshes=len(beams) + 1)
         finally:
-            if old is None:
-                del os.environ["SGB_FUSED_RHS"]
-            else:
-                os.environ["SGB_FUSED_RHS"] = old
+            for k, v in old.items():
+                if v is None:
+                    del os.environ[k]
+                else:
+                    os.environ[k] = v
         slots = b.add_meshes([(m.positions, m.tetrahedra, kw) for m, kw in beams], threads=8)
         b.step(5)
-        out.append([b.state(s) for s in slots])
+        out[form] = [b.state(s) for s in slots]
         b.close()
-    worst = 0.0
-    for (m, _), (xa, _), (xb, _) in zip(beams, *out):
-        d = np.linalg.norm(xb - m.positions)
-        worst = max(worst, float(np.linalg.norm(xa - xb) / d))
-    assert worst <= tol, worst
+    for form in ("element", "patch"):
+        worst = 0.0
+        for (m, _), (xa, _), (xb, _) in zip(beams, out[form], out["four"]):
+            d = np.linalg.norm(xb - m.positions)
+            worst = max(worst, float(np.linalg.norm(xa - xb) / d))
+        assert worst <= tol, (form, worst)
