@@ -379,13 +379,18 @@ __global__ void __launch_bounds__(kBatchThreads) kb_force_rhs_gather(BMeshDesc* 
 template <typename R>
 struct BRhsArgs {
     const double* x;
-    const double* rest_pos;
     const double* v;
     R kf;
     int method;
     R* own;
     R* partials;
 };
+
+template <typename R>
+size_t batch_force_smem(int pe)
+{
+    return force_patch_smem_size<R>(pe, batch_max_lnodes(pe));
+}
 
 template <typename R>
 __global__ void __launch_bounds__(kPatchThreads) kb_force_rhs_patch(BMeshDesc* M, const WorkItem* __restrict__ items,
@@ -397,6 +402,7 @@ __global__ void __launch_bounds__(kPatchThreads) kb_force_rhs_patch(BMeshDesc* M
     uint16_t* sl;
     int* lr;
     patch_smem_carve<R>(smem_raw, pe, batch_max_lnodes(pe), &ef, &sl, &lr, &lp);
+    float2* lv = reinterpret_cast<float2*>(lp);
     // the open mesh's views and operands, read where they are used
     __shared__ PatchView spv;
     __shared__ ElemView<R> sev;
@@ -412,52 +418,16 @@ __global__ void __launch_bounds__(kPatchThreads) kb_force_rhs_patch(BMeshDesc* M
                 const BMeshDesc& m = M[wi.slot];
                 spv = bm_patch_view(m, pe);
                 sev = bm_elem_view<R>(m);
-                sa = BRhsArgs<R>{m.x, m.rest_pos, m.v, (R)m.kf_rhs, m.method, (R*)m.q, (R*)m.partials};
+                sa = BRhsArgs<R>{m.x, m.v, (R)m.kf_rhs, m.method, (R*)m.q, (R*)m.partials};
             }
             __syncthreads();
         }
-        const int e0 = spv.elem_start[wi.a], ne = spv.elem_start[wi.a + 1] - e0;
-        const int n0 = spv.node_start[wi.a], nn = spv.node_start[wi.a + 1] - n0;
-        {
-            const uint4* src = reinterpret_cast<const uint4*>(spv.lslots + 4 * (size_t)e0);
-            uint4* dst = reinterpret_cast<uint4*>(sl);
-            const int n16 = (8 * ne + 15) >> 4;
-            for (int k = threadIdx.x; k < n16; k += blockDim.x) cp_async16(dst + k, src + k);
-            for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(lr + l, spv.lrow + n0 + l);
-        }
-        for (int le = threadIdx.x; le < ne; le += blockDim.x) {
-            const int e = e0 + le;
-            R Rm[9], K[3], J[12], c[12], cv[12];
-            if (sa.method == METHOD_LARGE)
-                elem_force_body<R, METHOD_LARGE, true>(sev, e, sa.x, sa.rest_pos, nullptr, PlasticArgs<R>{}, Rm, K, J,
-                                                       c);
-            else
-                elem_force_body<R, METHOD_POLAR, true>(sev, e, sa.x, sa.rest_pos, nullptr, PlasticArgs<R>{}, Rm, K, J,
-                                                       c);
-            rhs_v_terms_c(sev, e, sa.v, Rm, K, J, sa.kf, cv);
-#pragma unroll
-            for (int i = 0; i < 12; ++i) ef[i * pe + le] = c[i] - cv[i];
-        }
-        cp_async_wait_all();
-        __syncthreads();
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const int g = spv.lnode_gid[n0 + l];
-            const int info = spv.lnode_info[n0 + l];
-            const int s0 = lr[l] - 4 * e0, s1 = lr[l + 1] - 4 * e0;
-            R a0 = R(0), a1 = R(0), a2 = R(0);
-            for (int s = s0; s < s1; ++s) {
-                const int slot = sl[s];
-                const int le = slot >> 2, cc = slot & 3;
-                a0 += ef[(3 * cc + 0) * pe + le];
-                a1 += ef[(3 * cc + 1) * pe + le];
-                a2 += ef[(3 * cc + 2) * pe + le];
-            }
-            R* o = info >= 0 ? sa.partials + 3 * (size_t)(info >> 1) : sa.own + 3 * (size_t)g;
-            o[0] = a0;
-            o[1] = a1;
-            o[2] = a2;
-        }
-        __syncthreads();
+        if (sa.method == METHOD_LARGE)
+            patch_force_rhs_body<R, METHOD_LARGE>(spv, sev, wi.a, sa.x, sa.v, PlasticArgs<R>{}, sa.kf, 0, sa.own,
+                                                  sa.partials, ef, lv, sl, lr);
+        else
+            patch_force_rhs_body<R, METHOD_POLAR>(spv, sev, wi.a, sa.x, sa.v, PlasticArgs<R>{}, sa.kf, 0, sa.own,
+                                                  sa.partials, ef, lv, sl, lr);
     }
 }
 
@@ -782,11 +752,12 @@ int batch_prepare(int pe, int* grid_patch)
     // (mixed precision)
     grid_patch[3] = 0;
     if constexpr (is_mixed<R>::value) {
-        if (cudaFuncSetAttribute(kb_force_rhs_patch<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        const size_t fsmem = batch_force_smem<R>(pe);
+        if (cudaFuncSetAttribute(kb_force_rhs_patch<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem) !=
             cudaSuccess)
             return -1;
         int nf = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, kb_force_rhs_patch<R>, kPatchThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, kb_force_rhs_patch<R>, kPatchThreads, fsmem);
         grid_patch[3] = (nf < 1 ? 1 : nf) * sms;
     }
     return sms;
@@ -826,7 +797,7 @@ void batch_record_step(const BatchLaunch& B, cudaStream_t s)
     const WorkItem* nit = B.items[WL_NODE];
     if (B.fused_rhs == 2) {
         if constexpr (is_mixed<R>::value) {
-            kb_force_rhs_patch<R><<<B.grid_force, kPatchThreads, batch_patch_smem<R>(B.pe), s>>>(
+            kb_force_rhs_patch<R><<<B.grid_force, kPatchThreads, batch_force_smem<R>(B.pe), s>>>(
                 B.meshes, B.items[WL_PATCH], B.counts, B.pe);
             kb_rhs_finish_patch<R><<<B.grid_node, kBatchThreads, 0, s>>>(B.meshes, nit, B.counts);
         }

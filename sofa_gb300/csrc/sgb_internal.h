@@ -118,6 +118,7 @@ struct TfemMesh {
     int matvec_minb = 1;      // CG matvec register cap: resident CTAs per SM it is set for (1: none)
     int adddforce_grid = 0;   // CTAs of the addDForce patch kernel (128 threads)
     int force_patch_grid = 0; // CTAs of the patch force / right-hand side kernel (0: not used)
+    int force_threads = 160;  // threads per CTA of that kernel
     int patch_prefetch = 0;   // 1: each CTA prefetches its next patch into L2
     int update_vec4 = 1;      // FP32 CG update: four nodes per thread with 16-byte loads
     int update_minb = 4;      // CG update: resident CTAs per SM the register cap is set for
