@@ -75,31 +75,34 @@ __device__ __forceinline__ float4 rot_to_quat(const float Rm[9])
 #pragma unroll
     for (int i = 0; i < 9; ++i) M[i] = sg * Rm[i];
     const float tr = M[0] + M[4] + M[8];
+    // with t = 2 sqrt(s): 0.25 t = 0.5 s / sqrt(s) and 1 / t = 0.5 / sqrt(s),
+    // from the approximate reciprocal square root (the normalisation below
+    // absorbs its error)
     float x, y, z, w;
     if (tr > 0.f) {
-        const float t = sqrtf(tr + 1.f) * 2.f;
-        w = 0.25f * t;
-        x = (M[7] - M[5]) / t;
-        y = (M[2] - M[6]) / t;
-        z = (M[3] - M[1]) / t;
+        const float sq = tr + 1.f, h = 0.5f * rsqrtf(sq);
+        w = sq * h;
+        x = (M[7] - M[5]) * h;
+        y = (M[2] - M[6]) * h;
+        z = (M[3] - M[1]) * h;
     } else if (M[0] > M[4] && M[0] > M[8]) {
-        const float t = sqrtf(1.f + M[0] - M[4] - M[8]) * 2.f;
-        w = (M[7] - M[5]) / t;
-        x = 0.25f * t;
-        y = (M[1] + M[3]) / t;
-        z = (M[2] + M[6]) / t;
+        const float sq = 1.f + M[0] - M[4] - M[8], h = 0.5f * rsqrtf(sq);
+        w = (M[7] - M[5]) * h;
+        x = sq * h;
+        y = (M[1] + M[3]) * h;
+        z = (M[2] + M[6]) * h;
     } else if (M[4] > M[8]) {
-        const float t = sqrtf(1.f + M[4] - M[0] - M[8]) * 2.f;
-        w = (M[2] - M[6]) / t;
-        x = (M[1] + M[3]) / t;
-        y = 0.25f * t;
-        z = (M[5] + M[7]) / t;
+        const float sq = 1.f + M[4] - M[0] - M[8], h = 0.5f * rsqrtf(sq);
+        w = (M[2] - M[6]) * h;
+        x = (M[1] + M[3]) * h;
+        y = sq * h;
+        z = (M[5] + M[7]) * h;
     } else {
-        const float t = sqrtf(1.f + M[8] - M[0] - M[4]) * 2.f;
-        w = (M[3] - M[1]) / t;
-        x = (M[2] + M[6]) / t;
-        y = (M[5] + M[7]) / t;
-        z = 0.25f * t;
+        const float sq = 1.f + M[8] - M[0] - M[4], h = 0.5f * rsqrtf(sq);
+        w = (M[3] - M[1]) * h;
+        x = (M[2] + M[6]) * h;
+        y = (M[5] + M[7]) * h;
+        z = sq * h;
     }
     const float n = rsqrtf(x * x + y * y + z * z + w * w);
     x *= n;

@@ -118,9 +118,21 @@ __device__ __forceinline__ void polar3(const T A[9], T Q[9], int max_iter = 64)
         T det = Mk[0] * Madj[0] + Mk[1] * Madj[1] + Mk[2] * Madj[2];
         if (det == T(0)) break;
         T a_one = one_norm3(Madj), a_inf = inf_norm3(Madj);
-        T gamma = sqrt(sqrt((a_one * a_inf) / (m_one * m_inf)) / fabs(det));
+        T gamma, g2;
+        if constexpr (std::is_same<T, float>::value) {
+            // FP32: the scale gamma only sets how fast the iteration
+            // converges, not where to, so it comes from the hardware's
+            // approximate reciprocal square root and quotient; an error e in
+            // 1/(gamma det) scales the converged factor by 1 + e/2, within
+            // FP32 rounding (the mixed path then makes the factor orthonormal
+            // to ~1e-14 in float-float)
+            gamma = rsqrtf(fabsf(det) * rsqrtf(__fdividef(a_one * a_inf, m_one * m_inf)));
+            g2 = __fdividef(0.5f, gamma * det);
+        } else {
+            gamma = sqrt(sqrt((a_one * a_inf) / (m_one * m_inf)) / fabs(det));
+            g2 = T(0.5) / (gamma * det);
+        }
         T g1 = gamma * T(0.5);
-        T g2 = T(0.5) / (gamma * det);
         T e_one = T(0);
         T colsum[3] = {T(0), T(0), T(0)};
 #pragma unroll
