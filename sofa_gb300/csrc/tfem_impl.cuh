@@ -551,7 +551,7 @@ __device__ __forceinline__ void strain_ff(const ElemView<R>& ev, int e, const ff
     if (METHOD == METHOD_LARGE) {
         const float eab[3] = {eg[0][0].h, eg[0][1].h, eg[0][2].h};
         const float eac[3] = {eg[1][0].h, eg[1][1].h, eg[1][2].h};
-        rotation_large(eab, eac, X);
+        rotation_large_fast(eab, eac, X);
     } else {
         float A[9] = {eg[0][0].h, eg[0][1].h, eg[0][2].h, eg[1][0].h, eg[1][1].h,
                       eg[1][2].h, eg[2][0].h, eg[2][1].h, eg[2][2].h};

@@ -66,6 +66,38 @@ __device__ __forceinline__ void rotation_large(const T eab[3], const T eac[3], T
     }
 }
 
+// rotation_large for the FP32 frame of the mixed path, which is made
+// orthonormal to ~1e-14 afterwards: the unit vectors from the approximate
+// reciprocal square root (an error of it turns the frame slightly, which
+// adds no first-order strain), the same epsilon threshold.
+__device__ __forceinline__ void normalize3_fast(float v[3])
+{
+    const float n2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    if (n2 > RealTraits<float>::eps() * RealTraits<float>::eps()) {
+        const float r = rsqrtf(n2);
+        v[0] *= r;
+        v[1] *= r;
+        v[2] *= r;
+    }
+}
+
+__device__ __forceinline__ void rotation_large_fast(const float eab[3], const float eac[3], float R[9])
+{
+    float ex[3] = {eab[0], eab[1], eab[2]};
+    normalize3_fast(ex);
+    float ez[3];
+    cross3(ex, eac, ez);
+    normalize3_fast(ez);
+    float ey[3];
+    cross3(ez, ex, ey);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        R[k] = ex[k];
+        R[3 + k] = ey[k];
+        R[6 + k] = ez[k];
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T one_norm3(const T a[9])
 {
