@@ -609,13 +609,12 @@ __device__ __forceinline__ void elem_force_edges(const ElemView<R>& ev, int e, c
 }
 
 // KEEP: also hands the rotation (before packing), K and J to the caller
-// and, with eforce null, the corner terms in keep_c instead of storing them
 // (rotated methods only).
 template <typename R, int METHOD, bool KEEP = false>
 __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, const double* __restrict__ x,
                                                 const double* __restrict__ rest_pos, R* __restrict__ eforce,
                                                 const PlasticArgs<R>& pl = PlasticArgs<R>{}, R* keep_rot = nullptr,
-                                                R* keep_K = nullptr, R* keep_J = nullptr, R* keep_c = nullptr)
+                                                R* keep_K = nullptr, R* keep_J = nullptr)
 {
     const size_t En = (size_t)ev.n_tets;
     const int4 t = ev.tets[e];
@@ -760,12 +759,8 @@ __device__ __forceinline__ void elem_force_body(const ElemView<R>& ev, int e, co
             acc += Rm[6 + k] * F[3 * i + 2];
             c[3 * i + k] = acc;
         }
-    if (eforce) store_eforce(eforce, e, c);
+    store_eforce(eforce, e, c);
     if constexpr (KEEP) {
-        if (!eforce) {
-#pragma unroll
-            for (int i = 0; i < 12; ++i) keep_c[i] = c[i];
-        }
 #pragma unroll
         for (int i = 0; i < 9; ++i) keep_rot[i] = Rm[i];
 #pragma unroll
