@@ -116,6 +116,7 @@ struct TfemMesh {
     int patch_grid = 0;       // CTAs of the persistent patch kernels
     int patch_threads = 128;  // threads per CTA of the patch kernels
     int matvec_minb = 1;      // CG matvec register cap: resident CTAs per SM it is set for (1: none)
+    int matvec_db = 0;        // CG matvec with two sets of per-patch tables and no tail barrier
     int adddforce_grid = 0;   // CTAs of the addDForce patch kernel (128 threads)
     int force_patch_grid = 0; // CTAs of the patch force / right-hand side kernel (0: not used)
     int force_threads = 160;  // threads per CTA of that kernel

@@ -1717,6 +1717,29 @@ __host__ __device__ __forceinline__ size_t patch_smem_size(int pe, int max_lnode
            sizeof(R) * 3 * (size_t)max_lnodes;
 }
 
+// Shared memory of the matvec with two sets of slot lists and node values
+// (no row starts): ef, set 1, then set 2 from the next 16-byte boundary (the
+// slot lists take 16-byte asynchronous copies).
+template <typename R>
+__host__ __device__ __forceinline__ size_t patch_smem_set_db(int pe, int max_lnodes)
+{
+    return (8 * (size_t)pe + sizeof(R) * 3 * (size_t)max_lnodes + 15) & ~(size_t)15;
+}
+template <typename R>
+__host__ __device__ __forceinline__ size_t patch_smem_size_db(int pe, int max_lnodes)
+{
+    return sizeof(R) * 12 * (size_t)pe + 2 * patch_smem_set_db<R>(pe, max_lnodes);
+}
+template <typename R>
+__device__ __forceinline__ void patch_smem_carve_db(unsigned char* base, int pe, int max_lnodes, int set, R** ef,
+                                                    uint16_t** sl, R** lp)
+{
+    *ef = reinterpret_cast<R*>(base);
+    unsigned char* p = base + sizeof(R) * 12 * (size_t)pe + (size_t)set * patch_smem_set_db<R>(pe, max_lnodes);
+    *sl = reinterpret_cast<uint16_t*>(p);
+    *lp = reinterpret_cast<R*>(p + 8 * (size_t)pe);
+}
+
 template <typename R>
 __device__ __forceinline__ void patch_smem_carve(unsigned char* base, int pe, int max_lnodes, R** ef, uint16_t** sl,
                                                  int** lr, R** lp)
@@ -1805,7 +1828,11 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
 
-template <typename R, int MODE, int PC = 0>
+// DB: the caller alternates two sets of slot lists and node values between
+// consecutive patches (patch_smem_carve_db); the row starts are read from
+// global memory and no barrier follows phase 2 (the next patch's phase-0
+// barrier orders its phase 1 after this phase 2's reads of ef).
+template <typename R, int MODE, int PC = 0, bool DB = false>
 __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& ev, int P, const PatchArgs<R>& a, R* ef,
                                         R* lp, uint16_t* sl, int* lr)
 {
@@ -1825,7 +1852,8 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
         // asynchronous copies: the node loads below go out without waiting
         // for them (0.35 % faster CG steps than copies through registers)
         for (int k = threadIdx.x; k < n16; k += blockDim.x) cp_async16(dst + k, src + k);
-        for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(lr + l, pv.lrow + n0 + l);
+        if constexpr (!DB)
+            for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(lr + l, pv.lrow + n0 + l);
     }
     // phase 0: nodal values of the patch
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
@@ -1876,7 +1904,14 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
             if (a.ma.node_mass) mm = (R)(a.ma.node_mass[g] * a.mf);
             if (info < 0) fx = a.fixed[g] != 0;
         }
-        const int s0 = lr[l] - 4 * e0, s1 = lr[l + 1] - 4 * e0;
+        int s0, s1;
+        if constexpr (DB) {
+            s0 = pv.lrow[n0 + l] - 4 * e0;
+            s1 = pv.lrow[n0 + l + 1] - 4 * e0;
+        } else {
+            s0 = lr[l] - 4 * e0;
+            s1 = lr[l + 1] - 4 * e0;
+        }
         R a0 = R(0), a1 = R(0), a2 = R(0);
         for (int s = s0; s < s1; ++s) {
             const int slot = sl[s];
@@ -1909,14 +1944,14 @@ __device__ __forceinline__ R patch_body(const PatchView& pv, const ElemView<R>& 
             }
         }
     }
-    __syncthreads();
+    if constexpr (!DB) __syncthreads();
     return pen;
 }
 
 // MINB > 1: 128-thread CTAs with the register cap for MINB resident CTAs
 // per SM (FP32 only; 9 gives 56 registers without spills); MINB = 1: no cap,
 // 64, 128 or 256 threads.
-template <typename R, int MODE, int PC = 0, int MINB = 1>
+template <typename R, int MODE, int PC = 0, int MINB = 1, bool DB = false>
 __global__ void __launch_bounds__(MINB > 1 ? kPatchThreads : kPatchMaxThreads, sizeof(R) == 4 && MINB > 1 ? MINB : 0)
     k_patch_matvec(PatchView pv, ElemView<R> ev,
                                                                    const R* __restrict__ rin,
@@ -1941,11 +1976,17 @@ __global__ void __launch_bounds__(MINB > 1 ? kPatchThreads : kPatchMaxThreads, s
     const R mmu = (R)(mf != 1.0 ? ma.vertex_mass * mf : ma.vertex_mass);
     const PatchArgs<R> args{rin, pold, pnew, beta, kf, mmu, ma, mf, fixed, qout, partials, dinv};
     double energy = 0.0;  // FP64 across patches; FP32 within one patch
-    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x) {
+    int k = 0;
+    for (int P = blockIdx.x; P < pv.n_patches; P += gridDim.x, ++k) {
         if constexpr (is_mixed<R>::value)
             if (prefetch && threadIdx.x == 0 && P + (int)gridDim.x < pv.n_patches)
                 prefetch_patch(pv, ev, P + gridDim.x);
-        energy += (double)patch_body<R, MODE, PC>(pv, ev, P, args, ef, lp, sl, lr);
+        if constexpr (DB) {
+            patch_smem_carve_db<R>(smem_raw, pv.pe, pv.max_lnodes, k & 1, &ef, &sl, &lp);
+            energy += (double)patch_body<R, MODE, PC, true>(pv, ev, P, args, ef, lp, sl, nullptr);
+        } else {
+            energy += (double)patch_body<R, MODE, PC>(pv, ev, P, args, ef, lp, sl, lr);
+        }
     }
     if (MODE != 0) finish_dot<FIN_DEN>(energy, cg, nullptr, 0, sc);
 }
@@ -2790,7 +2831,10 @@ void launch_cg_update(const TfemMesh* m, int grid, cudaStream_t s, A... a)
 template <typename R, int MODE, int PC = 0, typename... A>
 void launch_patch_matvec(const TfemMesh* m, size_t smem, cudaStream_t s, A... a)
 {
-    if (m->matvec_minb == 9)
+    if (m->matvec_db)
+        k_patch_matvec<R, MODE, PC, 9, true>
+            <<<m->patch_grid, m->patch_threads, patch_smem_size_db<R>(m->pl.pe, m->pl.max_lnodes), s>>>(a...);
+    else if (m->matvec_minb == 9)
         k_patch_matvec<R, MODE, PC, 9><<<m->patch_grid, m->patch_threads, smem, s>>>(a...);
     else
         k_patch_matvec<R, MODE, PC, 1><<<m->patch_grid, m->patch_threads, smem, s>>>(a...);
@@ -2905,7 +2949,21 @@ int prepare_patch(TfemMesh* m)
         if (v == 1 || v == 9) m->matvec_minb = v;
     }
     if (sizeof(R) != 4 || threads != kPatchThreads) m->matvec_minb = 1;
-    if (m->matvec_minb == 9) {
+    // with the 9-CTA cap: two sets of slot lists and node values and no
+    // barrier after phase 2 (24.4 KB per CTA at 320 tets still fits 9 per
+    // SM; 0.2 % faster steps); SGB_MATVEC_DB=0 keeps one set
+    m->matvec_db = m->matvec_minb == 9 ? 1 : 0;
+    if (const char* e = getenv("SGB_MATVEC_DB"))
+        if (e[0] == '0') m->matvec_db = 0;
+    if (m->matvec_db) {
+        const size_t sdb = patch_smem_size_db<R>(m->pl.pe, m->pl.max_lnodes);
+        patch_matvec_attrs(k_patch_matvec<R, 1, 0, 9, true>, sdb);
+        patch_matvec_attrs(k_patch_matvec<R, 2, 0, 9, true>, sdb);
+        patch_matvec_attrs(k_patch_matvec<R, 1, 1, 9, true>, sdb);
+        patch_matvec_attrs(k_patch_matvec<R, 2, 1, 9, true>, sdb);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_patch_matvec<R, 1, 0, 9, true>, threads, sdb);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_patch_matvec<R, 2, 0, 9, true>, threads, sdb);
+    } else if (m->matvec_minb == 9) {
         patch_matvec_attrs(k_patch_matvec<R, 1, 0, 9>, smem);
         patch_matvec_attrs(k_patch_matvec<R, 2, 0, 9>, smem);
         patch_matvec_attrs(k_patch_matvec<R, 1, 1, 9>, smem);
