@@ -568,8 +568,10 @@ __global__ void __launch_bounds__(kPatchThreads, MINB) kb_matvec(BMeshDesc* M, c
 }
 
 // ---- CG update: shared-node q, x += alpha p, r -= alpha q, rho -------------
+// NPT 4: a register cap for 4 resident CTAs per SM (64 registers, a few
+// spilled; without it 95 registers and 2 CTAs per SM, 2.4 % slower steps)
 template <typename R, int NPT>
-__global__ void __launch_bounds__(kBatchThreads) kb_update(BMeshDesc* M, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(kBatchThreads, NPT == 4 ? 4 : 1) kb_update(BMeshDesc* M, const WorkItem* __restrict__ items,
                                                            const int* __restrict__ counts, int it)
 {
     __shared__ double gsum[kBatchNodeChunk / 32];

@@ -2416,6 +2416,11 @@ __device__ __forceinline__ void cg_update4_terms(size_t n0, float* __restrict__ 
     const int bb[5] = {br.x, br.y, br.z, br.w, bnd_rowptr[n0 + 4]};
     const uchar4 fx = *reinterpret_cast<const uchar4*>(fixed + n0);
     const uint8_t ff[4] = {fx.x, fx.y, fx.z, fx.w};
+    // x needs no partial sum: advanced and stored first, which frees its
+    // registers before the partial loop
+#pragma unroll
+    for (int k = 0; k < 12; ++k) xx[k] = xx[k] + pp[k] * alpha;
+    st12(xs, n0, xx);
     float ps[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) ps[k] = 0.f;
@@ -2442,11 +2447,7 @@ __device__ __forceinline__ void cg_update4_terms(size_t n0, float* __restrict__ 
     }
     const float nalpha = -alpha;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) {
-        xx[k] = xx[k] + pp[k] * alpha;
-        rr[k] = rr[k] + qq[k] * nalpha;
-    }
-    st12(xs, n0, xx);
+    for (int k = 0; k < 12; ++k) rr[k] = rr[k] + qq[k] * nalpha;
     st12(r, n0, rr);
 #pragma unroll
     for (int j = 0; j < 4; ++j) t[j] = (double)node_rr(rr + 3 * j);
