@@ -392,8 +392,10 @@ size_t batch_force_smem(int pe)
     return force_patch_smem_size<R>(pe, batch_max_lnodes(pe));
 }
 
+// 80 registers (no spills): 6 resident CTAs of 128 threads per SM instead of
+// 5 at 96, 0.3 % faster batch steps
 template <typename R>
-__global__ void __launch_bounds__(kPatchThreads) kb_force_rhs_patch(BMeshDesc* M, const WorkItem* __restrict__ items,
+__global__ void __maxnreg__(80) kb_force_rhs_patch(BMeshDesc* M, const WorkItem* __restrict__ items,
                                                                     const int* __restrict__ counts, int pe)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

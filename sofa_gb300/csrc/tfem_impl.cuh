@@ -2167,8 +2167,10 @@ __device__ __forceinline__ void patch_force_rhs_body(const PatchView& pv, const 
 // k_elem_force_rhs and k_gather_force_rhs, summed per patch instead of in
 // element order, with no corner-term buffers in HBM; k_rhs_finish_patch
 // then forms b.
+// 64 registers (no spills for large and polar; svd keeps 80): 6 resident
+// CTAs of 160 threads per SM instead of 4, 0.2 % faster steps
 template <typename R, int METHOD>
-__global__ void __launch_bounds__(kPatchMaxThreads) k_patch_force_rhs(PatchView pv, ElemView<R> ev,
+__global__ void __maxnreg__(METHOD == METHOD_SVD ? 80 : 64) k_patch_force_rhs(PatchView pv, ElemView<R> ev,
                                                                    const double* __restrict__ x,
                                                                    PlasticArgs<R> pl, const double* __restrict__ v,
                                                                    R kf_rhs, int first_order, R* __restrict__ own,
